@@ -1,0 +1,361 @@
+#!/usr/bin/env python3
+"""Benchmark of the force-and-push path: particle-substeps/s at N = 1,048,576.
+
+Workload: the large plain Barnes-Hut configuration (2-D Plummer-like disk,
+scale radius 50, plus a 5 % uniform background over a 2000 x 2000 box;
+lognormal(0, 1) masses; gravity + Coulomb + Yukawa; theta 0.5; leaf
+capacity 4), synthetic and seeded.  One step = one Physics.update frame of
+dt = 1/60 (adaptive Boris substeps, each with a tree rebuild and a force
+pass).  The metric counts N x substeps per second.
+
+Arms:
+  default            the CUDA library (libgeon_cuda.so through the C ABI)
+  --impl reference   the reference CPU path on this machine's host cores:
+                     the FP64 restatement in oracle/ (the reference itself is
+                     browser JavaScript), on a bounded sample per step.
+
+Timing: CUDA events on the library's stream around exactly K frames after W
+warm-up frames; the working set (about 0.5 GB) is far larger than L2.  Under
+torchrun each rank runs an independent replica on its own GPU ("replicas
+only": the path does not shard); the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-substeps/s at N=1M: learned vs plain BH at equal 1e-3 force error"
+UNIT = "particle-substeps/s"
+# FLOPs per pair interaction (FMA = 2; rsqrt/rcp/ex2 = 1): gravity 20, Coulomb 6,
+# tidal torque 16, Yukawa 16.
+FLOP_PER_INTERACTION_GCY = 58
+STATE_KEYS = ("x", "y", "wx", "wy", "mass", "charge", "angw")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--theta", type=float, default=0.5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=8192, help="targets per CPU sample step")
+    return ap.parse_args()
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(ws, v: float) -> float:
+    if ws <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(ws, v: float) -> float:
+    if ws <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        return {}
+
+
+def cpu_sample(wl, threads: int, k: int, seed: int = 0):
+    """One bounded CPU sample of a substep: full tree build + the force walk
+    for k random targets, extrapolated to all N targets."""
+    from oracle.oracle import OracleSim
+    o = OracleSim(wl.params, threads=threads)
+    o.add(*[wl.state[key] for key in STATE_KEYS])
+    idx = np.random.default_rng(seed).choice(wl.n, size=min(k, wl.n), replace=False)
+    t0 = time.perf_counter()
+    o.build_tree()
+    t1 = time.perf_counter()
+    o.compute_forces_subset(idx)
+    t2 = time.perf_counter()
+    o.close()
+    substep_s = (t1 - t0) + (t2 - t1) * wl.n / len(idx)
+    return wl.n / substep_s, {"tree_s": t1 - t0, "walk_s": t2 - t1, "targets": int(len(idx))}
+
+
+def run_reference(args, ws, rank):
+    from physsim_gb300 import workloads as W
+    if rank != 0:
+        return
+    from oracle import oracle
+    threads = oracle.max_threads()
+    wl = W.plummer_disk(args.n, theta=args.theta)
+    vals = []
+    t0 = time.perf_counter()
+    for s in range(args.warmup + args.steps):
+        v, info = cpu_sample(wl, threads, args.cpu_sample, seed=s)
+        if s >= args.warmup:
+            vals.append(v)
+    elapsed = time.perf_counter() - t0
+    value = float(np.mean(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wl.n / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": wl.name, "n": wl.n, "theta": args.theta, "forces": "gravity+coulomb+yukawa",
+                   "dt": wl.dt, "leaf_capacity": 4},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"per step: full tree build of N={wl.n} plus the force walk of "
+                                   f"{min(args.cpu_sample, wl.n)} random targets, extrapolated to N targets "
+                                   "(FP64 restatement of the reference CPU path; the reference is browser JS)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": elapsed,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_native(args, ws, rank, local):
+    import torch
+    from physsim_gb300 import build, workloads as W
+    from physsim_gb300.system import GeonSystem
+
+    build()
+    torch.cuda.set_device(local)
+    wl = W.plummer_disk(args.n, theta=args.theta)
+    n = wl.n
+    g = GeonSystem(wl.params, n)
+    stream = torch.cuda.ExternalStream(g.stream_ptr())
+    host = {k: np.ascontiguousarray(wl.state[k], dtype=np.float32) for k in STATE_KEYS}
+    g.upload(*[host[k] for k in STATE_KEYS])
+
+    # ---- device-resident timing ----
+    for _ in range(args.warmup):
+        g.update(wl.dt)
+    g.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = g.launch_count()
+    g.profile(True)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    t0 = time.perf_counter()
+    substeps = 0
+    for _ in range(args.steps):
+        substeps += g.update(wl.dt)
+    ev1.record(stream)
+    ev1.synchronize()
+    wall = time.perf_counter() - t0
+    prof = g.profile(False)
+    launches = g.launch_count() - l0
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    barrier(ws)
+    dev_s = ev0.elapsed_time(ev1) / 1e3
+    t_max = allmax(ws, dev_s)
+    total_ps = allsum(ws, float(n * substeps))
+    value = total_ps / t_max
+
+    # ---- end-to-end through the C ABI with pinned host buffers ----
+    pin_in = torch.empty((7, n), dtype=torch.float32, pin_memory=True)
+    pin_in.numpy()[:] = np.stack([host[k] for k in STATE_KEYS])
+    pin_out = torch.empty((7, n), dtype=torch.float32, pin_memory=True)
+    from physsim_gb300 import _native as N
+    lib, h = g.lib, g._h
+    in_ptr = N.fptr(pin_in.numpy())
+    out_ptr = N.fptr(pin_out.numpy())
+    import ctypes as C
+    sub = C.c_int32()
+    cnt = C.c_int32()
+
+    def e2e_step():
+        N.check(lib, h, lib.geon_upload_state(h, n, in_ptr, 0.0))
+        N.check(lib, h, lib.geon_update(h, wl.dt, C.byref(sub)))
+        N.check(lib, h, lib.geon_download_state(h, out_ptr, 7, n, C.byref(cnt)))
+        return sub.value
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier(ws)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    esub = 0
+    for _ in range(args.steps):
+        esub += e2e_step()
+    e1.record(stream)
+    e1.synchronize()
+    e_s = allmax(ws, e0.elapsed_time(e1) / 1e3)
+    e_total = allsum(ws, float(n * esub))
+    e2e_value = e_total / e_s
+
+    # ---- roofline of the dominant kernel (the Barnes-Hut walk, FP32 pipe) ----
+    pk = peaks()
+    fp32_peak = measured_fp32_peak(g)
+    walk_ms = prof["force_ms"] / max(prof["force_count"], 1)
+    inter = prof["interactions"] / max(prof["force_count"], 1)
+    achieved = inter * FLOP_PER_INTERACTION_GCY / (walk_ms / 1e3) / 1e12
+    tree_ms = prof["tree_ms"] / max(prof["tree_count"], 1)
+    g.close()
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+        threads = oracle.max_threads()
+        v, info = cpu_sample(wl, threads, args.cpu_sample)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"one substep: full tree build of N={n} ({info['tree_s']:.2f} s) plus the force walk of "
+                         f"{info['targets']} random targets ({info['walk_s']:.2f} s), extrapolated to N targets; "
+                         "FP64 restatement of the reference CPU path"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": wl.name, "n": n, "theta": args.theta, "forces": "gravity+coulomb+yukawa+tidal",
+                   "method": "plain Barnes-Hut (learned correction not in this line)", "dt": wl.dt,
+                   "substeps_per_step": substeps / args.steps, "leaf_capacity": 4,
+                   "l2": "working set ~0.5 GB > 129 MB L2 (no flush needed)",
+                   "parallelism": "replicas" if ws > 1 else "single"},
+        "roofline": {"bound": "fp32", "kernel": "walkb_kernel (BH walk + pair forces)",
+                     "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak if fp32_peak else None,
+                     "traffic": None, "flop_per_interaction": FLOP_PER_INTERACTION_GCY,
+                     "interactions_per_launch": inter, "launch_ms": walk_ms,
+                     "peak_source": "project FP32 FMA microbenchmark on this GPU (MEASURED_PEAKS.json has no FP32 figure)"},
+        "tree_build": {"ms": tree_ms, "bound": "hbm",
+                       "algorithmic_bytes": None, "peak_gbs": pk.get("hbm_gbs")},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 7 * 4 * n, "d2h_bytes_per_step": 7 * 4 * n,
+                "note": "per step: upload state (re-bootstraps forces), one frame, download state"},
+        "clocks": clk,
+        "gpu_launches": launches,
+        "profile": {k: prof[k] for k in ("tree_ms", "force_ms", "onepn_ms", "push_ms", "tree_count", "force_count")},
+        "wall_s": wall,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+def measured_fp32_peak(g) -> float | None:
+    from physsim_gb300 import _native as N
+    import ctypes as C
+    fn = getattr(g.lib, "geon_fp32_peak", None)
+    if fn is None:
+        return None
+    out = C.c_double()
+    fn.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+    fn.restype = C.c_int
+    if fn(g._h, C.byref(out)) != 0:
+        return None
+    return out.value
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_native(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,310 @@
+/*
+ * geon.h — C ABI of the GB300 force-and-push library (libgeon_cuda.so).
+ *
+ * One handle owns one particle system resident in GPU memory: FP32 SoA
+ * particle state, the signal-delay history ring, the quadtree built from
+ * radix-sorted Morton keys, and the per-particle force/field accumulators.
+ * Every entry point returns an int status (GEON_OK == 0, negative on error);
+ * geon_last_error() returns a message for the last failure on that handle.
+ *
+ * Ownership: the library owns all device memory.  Host arrays passed in are
+ * caller-owned and copied; host arrays passed out are caller-allocated.
+ * Threading: one handle per host thread.  All work of a handle is ordered on
+ * the handle's own CUDA stream (geon_get_stream); calls return when the
+ * requested results are on the host.
+ *
+ * The reference (a9lim/physsim, "Geon") has no native interface; each entry
+ * point below names the JavaScript method whose contract it carries.  The
+ * JS-side binding a maintainer would add (N-API) is shown in INTEGRATION.md.
+ */
+#ifndef GEON_H
+#define GEON_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define GEON_OK              0
+#define GEON_ERR_ARG        -1   /* bad argument (null, out of range)          */
+#define GEON_ERR_FULL       -2   /* capacity exhausted (src/gpu/gpu-physics.js:1864 returns -1) */
+#define GEON_ERR_CUDA       -3   /* CUDA runtime error                           */
+#define GEON_ERR_OVERFLOW   -4   /* device-side overflow flag (walk stack, node pool) */
+#define GEON_ERR_TIMEOUT    -5   /* bounded device wait gave up                  */
+#define GEON_ERR_NOMEM      -6   /* device allocation failed                     */
+#define GEON_ERR_UNSUPPORTED -7  /* toggle combination outside this library     */
+
+/* ---- toggle bits: same layout as the reference's toggles0 word
+ *      (src/gpu/gpu-constants.js:265-280, packed by gpu-physics.js:1969-1985) */
+#define GEON_GRAVITY      (1u << 0)
+#define GEON_COULOMB      (1u << 1)
+#define GEON_MAGNETIC     (1u << 2)
+#define GEON_GRAVITOMAG   (1u << 3)
+#define GEON_ONE_PN       (1u << 4)
+#define GEON_RELATIVITY   (1u << 5)
+#define GEON_SPIN_ORBIT   (1u << 6)
+#define GEON_RADIATION    (1u << 7)   /* unsupported: radiation is off the path */
+#define GEON_BLACK_HOLE   (1u << 8)   /* unsupported */
+#define GEON_YUKAWA       (1u << 11)
+#define GEON_HIGGS        (1u << 12)  /* unsupported: scalar fields off the path */
+#define GEON_AXION        (1u << 13)  /* unsupported */
+#define GEON_BARNES_HUT   (1u << 14)
+
+/* boundary modes (src/config.js:16-18) and topologies (src/config.js:22-24) */
+#define GEON_BOUND_DESPAWN 0
+#define GEON_BOUND_BOUNCE  1
+#define GEON_BOUND_LOOP    2
+#define GEON_TORUS 0
+#define GEON_KLEIN 1
+#define GEON_RP2   2
+
+/* option flags (GeonParams.flags) */
+#define GEON_FLAG_PE          (1u << 0)  /* accumulate potential energy in force passes */
+#define GEON_FLAG_BREAKDOWN   (1u << 1)  /* keep per-type force vectors (force breakdown) */
+#define GEON_FLAG_NO_GHOSTS   (1u << 2)  /* periodic BH without image ghosts (min-image only) */
+#define GEON_FLAG_SIMPLE_WALK (1u << 3)  /* one node per warp iteration (cross-check of the batched walk) */
+
+/* Physics parameters.  Mirrors the Physics fields that Physics.update reads
+ * (src/integrator.js:65-107, :726-736) plus theta/softening, which the
+ * reference hard-codes (src/config.js:44,57) and this library takes at run time. */
+typedef struct GeonParams {
+    uint32_t toggles;          /* GEON_* toggle bits                                  */
+    uint32_t flags;            /* GEON_FLAG_* bits                                    */
+    int32_t  boundary_mode;    /* GEON_BOUND_*                                        */
+    int32_t  topology;         /* GEON_TORUS / GEON_KLEIN / GEON_RP2                  */
+    double   domain_w;         /* width, height: Physics.update(width, height)        */
+    double   domain_h;
+    double   off_x;            /* offX, offY                                          */
+    double   off_y;
+    double   theta;            /* Barnes-Hut opening angle (BH_THETA = 0.5)           */
+    double   softening;        /* SOFTENING (8): softeningSq = s^2, dtSafe = sqrt(s/a) */
+    double   yukawa_mu;        /* Physics.yukawaMu (DEFAULT_PION_MASS = 0.15)         */
+    double   bounce_friction;  /* Physics.bounceFriction (0.4)                        */
+    double   ext_gravity;      /* Physics.extGravity / extGravityAngle               */
+    double   ext_gravity_angle;
+    double   ext_electric;     /* Physics.extElectric / extElectricAngle             */
+    double   ext_electric_angle;
+    double   ext_bz;           /* Physics.extBz                                       */
+    int32_t  max_substeps;     /* MAX_SUBSTEPS (32)                                   */
+    int32_t  reserved;
+} GeonParams;
+
+/* Conserved quantities in FP64 (src/energy.js:11-62 passes 1-2, and the
+ * potential energy of the last force pass, src/forces.js:26). */
+typedef struct GeonStats {
+    double linear_ke, spin_ke, pe;
+    double px, py;
+    double orbital_ang_mom, spin_ang_mom;
+    double com_x, com_y, total_mass;
+    double sim_time;
+    int32_t alive_count;
+    int32_t last_substeps;
+} GeonStats;
+
+/* Tree summary of the last build. */
+typedef struct GeonTreeInfo {
+    int32_t n_points;      /* tree points: particles + periodic ghosts            */
+    int32_t n_ghosts;
+    int32_t n_dropped;     /* points outside the closed root box (quadtree.js:186) */
+    int32_t n_internal;    /* divided nodes                                        */
+    int32_t n_leaves;      /* non-empty undivided nodes                            */
+    int32_t max_level;     /* deepest leaf level                                   */
+    int32_t n_bucket;      /* leaves at the depth cap holding > 4 points           */
+    int32_t reserved;
+} GeonTreeInfo;
+
+/* Per-particle output rows of geon_download_forces (each row n floats). */
+#define GEON_OUT_FX          0
+#define GEON_OUT_FY          1
+#define GEON_OUT_BZ          2
+#define GEON_OUT_BGZ         3
+#define GEON_OUT_DBZDX       4
+#define GEON_OUT_DBZDY       5
+#define GEON_OUT_DBGZDX      6
+#define GEON_OUT_DBGZDY      7
+#define GEON_OUT_TIDAL       8   /* _tidalTorque     */
+#define GEON_OUT_FRAMEDRAG   9   /* _frameDragTorque */
+#define GEON_OUT_F1PN_X     10
+#define GEON_OUT_F1PN_Y     11
+#define GEON_OUT_PE         12   /* per-particle PE sum (global PE = half the sum)  */
+#define GEON_OUT_GRAV_X     13   /* per-type vectors (GEON_FLAG_BREAKDOWN)          */
+#define GEON_OUT_GRAV_Y     14
+#define GEON_OUT_COUL_X     15
+#define GEON_OUT_COUL_Y     16
+#define GEON_OUT_MAG_X      17
+#define GEON_OUT_MAG_Y      18
+#define GEON_OUT_GM_X       19
+#define GEON_OUT_GM_Y       20
+#define GEON_OUT_YUK_X      21
+#define GEON_OUT_YUK_Y      22
+#define GEON_OUT_EXT_X      23
+#define GEON_OUT_EXT_Y      24
+#define GEON_OUT_ROWS       25
+
+/* Rows of the packed particle state (geon_upload_state / download_state). */
+#define GEON_ST_X       0
+#define GEON_ST_Y       1
+#define GEON_ST_WX      2   /* proper velocity w = gamma v */
+#define GEON_ST_WY      3
+#define GEON_ST_MASS    4
+#define GEON_ST_CHARGE  5
+#define GEON_ST_ANGW    6   /* angular celerity */
+#define GEON_ST_VX      7   /* coordinate velocity (download only; derived on upload) */
+#define GEON_ST_VY      8
+#define GEON_ST_ANGVEL  9   /* download only */
+#define GEON_ST_ROWS_IN 7
+#define GEON_ST_ROWS   10
+
+typedef struct GeonHandle GeonHandle;
+
+/* new GPUPhysics(device, domainW, domainH) + init()
+ * (src/gpu/gpu-physics.js:155-160).  max_particles sizes every buffer once. */
+int geon_create(const GeonParams* params, int32_t max_particles, GeonHandle** out);
+
+/* GPUPhysics.destroy() (src/gpu/gpu-physics.js:4291). */
+int geon_destroy(GeonHandle* h);
+
+/* GPUPhysics.setToggles(physics) (src/gpu/gpu-physics.js:1969) together with
+ * the domain/boundary fields main.js writes before update().  Takes effect at
+ * the next call. */
+int geon_set_params(GeonHandle* h, const GeonParams* params);
+int geon_get_params(GeonHandle* h, GeonParams* out);
+
+/* GPUPhysics.addParticle({x,y,vx,vy,mass,charge,angw}) (src/gpu/gpu-physics.js:1857),
+ * batched.  `soa` holds GEON_ST_ROWS_IN rows of n floats (x, y, wx, wy, mass,
+ * charge, angw) with the proper velocity already formed (the host layer turns
+ * coordinate velocity into w as setVelocity does, src/relativity.js:15-25).
+ * creation_time is the simTime stamp of the batch (Particle.creationTime).
+ * Writes the first slot index; GEON_ERR_FULL when the batch does not fit. */
+int geon_add_particles(GeonHandle* h, int32_t n, const float* soa,
+                       double creation_time, int32_t* first_index);
+
+/* GPUPhysics.removeParticle(idx) (src/gpu/gpu-physics.js:1936): the slot is
+ * removed and later slots shift down by one, keeping the CPU path's array
+ * order (integrator.js:1799-1824 compacts the same way). */
+int geon_remove_particle(GeonHandle* h, int32_t index);
+
+/* GPUPhysics.deserialize(state) (src/gpu/gpu-physics.js:3886): replaces the
+ * whole state with n particles (soa as in geon_add_particles).  Resets forces,
+ * moments and history; the next geon_update bootstraps forces. */
+int geon_upload_state(GeonHandle* h, int32_t n, const float* soa, double sim_time);
+
+/* GPUPhysics.serialize() (src/gpu/gpu-physics.js:3749): copies
+ * min(n, capacity) particles out as `rows` (<= GEON_ST_ROWS) rows of
+ * `capacity` floats each.  Writes the particle count. */
+int geon_download_state(GeonHandle* h, float* soa, int32_t rows, int32_t capacity, int32_t* n);
+
+/* Stable particle ids, in current slot order (ids are assigned by
+ * geon_add_particles / geon_upload_state in order and travel with each
+ * particle through compaction).  Lets a host keep GPUPhysics-style handles
+ * (main.js stores p._gpuIdx) although slots shift on removal. */
+int geon_download_ids(GeonHandle* h, int32_t* ids, int32_t capacity, int32_t* n);
+
+/* Same as geon_download_state with FP64 rows; positions carry the low
+ * parts of the compensated drift sums. */
+int geon_download_state_f64(GeonHandle* h, double* soa, int32_t rows, int32_t capacity, int32_t* n);
+
+/* GPUPhysics.reset() (src/gpu/gpu-physics.js:3973). */
+int geon_reset(GeonHandle* h);
+
+/* GPUPhysics.getParticleCount() (src/gpu/gpu-physics.js:4287). */
+int geon_particle_count(GeonHandle* h, int32_t* n);
+
+/* Physics.update(particles, dt, ...) (src/integrator.js:726-1825), the
+ * in-scope part: force bootstrap on the first call, adaptive Boris substeps
+ * (<= max_substeps) with tree rebuild and force recompute, 1PN velocity-Verlet,
+ * history sampling every 64 calls, boundary handling.  `substeps` (may be
+ * NULL) receives the number of substeps taken. */
+int geon_update(GeonHandle* h, double dt, int32_t* substeps);
+
+/* Waits for all work enqueued on the handle's stream. */
+int geon_synchronize(GeonHandle* h);
+
+/* One force pass at the current state without advancing it: resetForces +
+ * tree build + computeAllForces (src/forces.js:31-154), i.e. the bootstrap of
+ * Physics.update (src/integrator.js:750-758).  Uses Barnes-Hut when the
+ * GEON_BARNES_HUT toggle is set, the O(N^2) pairwise sum otherwise. */
+int geon_compute_forces(GeonHandle* h);
+
+/* 1PN-only force pass (src/forces.js:578-610) at the current state; writes
+ * the GEON_OUT_F1PN_* rows. */
+int geon_compute_1pn(GeonHandle* h);
+
+/* Copies `rows` rows (GEON_OUT_*) of per-particle force data, each `capacity`
+ * floats, starting at row `first_row`. */
+int geon_download_forces(GeonHandle* h, int32_t first_row, int32_t rows,
+                         float* out, int32_t capacity);
+
+/* QuadTreePool.build (src/quadtree.js:412-419) at the current positions
+ * (with periodic ghosts, src/integrator.js:247-260).  Fills `info`. */
+int geon_build_tree(GeonHandle* h, GeonTreeInfo* info);
+
+/* Leaf membership of the last build, for exact comparison with the
+ * reference tree: leaf_of_point[i] is the leaf index of tree point i
+ * (particles first, then ghosts in generation order) or -1 if the point was
+ * dropped.  For each leaf: centre (bx, by), half-size bw (quadtree.js:52-59)
+ * and level.  Arrays are sized by the caller from GeonTreeInfo. */
+int geon_tree_leaves(GeonHandle* h, int32_t* leaf_of_point, int32_t n_points,
+                     double* leaf_bx, double* leaf_by, double* leaf_bw,
+                     int32_t* leaf_level, int32_t n_leaves);
+
+/* Interaction count of the last Barnes-Hut force pass (pair evaluations
+ * summed over particles), for the walk's work accounting. */
+int geon_interaction_count(GeonHandle* h, int64_t* count);
+
+/* FP64 conserved quantities (src/energy.js:11-62; PE from src/forces.js:26).
+ * GPUPhysics.requestStats/readStats (src/gpu/gpu-physics.js:4146/4234). */
+int geon_stats(GeonHandle* h, GeonStats* out);
+
+/* Signal-delay history (Particle.histX.. ring, src/particle.js:77-85,124-134).
+ * Uploads `count` (<= 256) samples per particle, oldest first: times[count]
+ * (shared by all particles, as Physics records them together,
+ * integrator.js:1549-1565) and five rows (x, y, vx, vy, angw) of
+ * n*count floats, particle-major.  Used to start from a warmed history. */
+int geon_upload_history(GeonHandle* h, int32_t n, int32_t count,
+                        const double* times, const float* samples);
+
+/* Simulation clock (Physics.simTime). */
+int geon_set_sim_time(GeonHandle* h, double sim_time);
+int geon_get_sim_time(GeonHandle* h, double* sim_time);
+
+/* Per-phase device time, measured with CUDA events recorded on the handle's
+ * stream around each phase while profiling is on. */
+typedef struct GeonProfile {
+    double tree_ms;          /* ghosts, keys, radix sort, node emission, aggregation */
+    double force_ms;         /* force passes (BH walk or pairwise sum)               */
+    double onepn_ms;         /* 1PN-only passes                                      */
+    double push_ms;          /* Boris push, VV kick, boundary                        */
+    int64_t tree_count, force_count, onepn_count, push_count;
+    int64_t interactions;    /* pair evaluations summed over the profiled force passes */
+    int64_t particle_substeps;
+} GeonProfile;
+
+/* enable = 1 clears the counters and starts recording; enable = 0 stops.
+ * `out` (may be NULL) receives the totals recorded so far (synchronises). */
+int geon_profile(GeonHandle* h, int32_t enable, GeonProfile* out);
+
+/* Measured FP32 FMA throughput of this GPU in TFLOP/s (FMA = 2 FLOP), from a
+ * short microbenchmark on the handle's stream: the roofline denominator for
+ * the FP32-bound force kernels.  Diagnostic; no reference counterpart. */
+int geon_fp32_peak(GeonHandle* h, double* tflops);
+
+/* The handle's CUDA stream (a cudaStream_t), for timing with events. */
+int geon_get_stream(GeonHandle* h, void** stream);
+
+/* Number of kernels this handle has launched since creation. */
+int geon_launch_count(GeonHandle* h, int64_t* count);
+
+/* Message for the last error on h (or a global message if h is NULL). */
+const char* geon_last_error(GeonHandle* h);
+
+/* Library version string. */
+const char* geon_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GEON_H */

@@ -1,0 +1,241 @@
+"""ctypes wrapper of the FP64 oracle (oracle/geon_oracle.cpp).
+
+Test infrastructure only: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, as the checker.  Its API mirrors
+physsim_gb300.system.GeonSystem so a test can drive both with one script.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+from physsim_gb300 import _native as N
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "geon_oracle.cpp"
+LIB = HERE / "libgeon_oracle.so"
+
+
+def build(force: bool = False) -> Path:
+    """Compiles the oracle with g++ (OpenMP for the threaded CPU baseline)."""
+    hdr = HERE.parent / "include" / "geon.h"
+    if not force and LIB.exists() and LIB.stat().st_mtime >= max(SRC.stat().st_mtime, hdr.stat().st_mtime):
+        return LIB
+    tmp = LIB.with_suffix(".so.tmp")
+    cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-shared", "-fPIC", "-o", str(tmp), str(SRC)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    build()
+    lib = C.CDLL(str(LIB))
+    P = C.POINTER
+    d, i, v = C.c_double, C.c_int, C.c_void_p
+    sig = {
+        "oracle_create": ([P(N.GeonParams)], v),
+        "oracle_destroy": ([v], None),
+        "oracle_set_params": ([v, P(N.GeonParams)], None),
+        "oracle_set_threads": ([v, i], None),
+        "oracle_max_threads": ([], i),
+        "oracle_add_particles": ([v, i] + [P(d)] * 7 + [d], i),
+        "oracle_count": ([v], i),
+        "oracle_set_sim_time": ([v, d], None),
+        "oracle_sim_time": ([v], d),
+        "oracle_last_substeps": ([v], i),
+        "oracle_interactions": ([v], C.c_longlong),
+        "oracle_pe": ([v], d),
+        "oracle_set_forces_init": ([v, i], None),
+        "oracle_update": ([v, d], i),
+        "oracle_compute_forces": ([v], None),
+        "oracle_compute_forces_no_build": ([v], None),
+        "oracle_compute_1pn": ([v], None),
+        "oracle_get_state": ([v, P(d), i], i),
+        "oracle_get_ids": ([v, P(C.c_int), i], None),
+        "oracle_get_forces": ([v, P(d), i], i),
+        "oracle_build_tree": ([v, P(C.c_int)], i),
+        "oracle_tree_overflow": ([v], i),
+        "oracle_tree_leaves": ([v, P(C.c_int), i, P(d), P(d), P(d), P(C.c_int), i], i),
+        "oracle_ghost_origins": ([v, P(C.c_int), i], i),
+        "oracle_tree_nodes": ([v, P(d), P(C.c_int), i], i),
+        "oracle_upload_history": ([v, i, i, P(d), P(d)], i),
+        "oracle_set_hist_stride": ([v, i], None),
+        "oracle_stats": ([v, P(N.GeonStats)], None),
+        "oracle_min_image": ([d, d, d, d, i, d, d, P(d)], None),
+        "oracle_delayed_state": ([v, i, d, d, P(d)], i),
+        "oracle_compute_forces_subset": ([v, P(C.c_int), i], C.c_longlong),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def max_threads() -> int:
+    return load().oracle_max_threads()
+
+
+def min_image(ox, oy, sx, sy, topology, W, H):
+    out = np.zeros(2)
+    load().oracle_min_image(ox, oy, sx, sy, topology, W, H, _dp(out))
+    return out
+
+
+class OracleSim:
+    """FP64 restatement of the reference's Physics + QuadTreePool."""
+
+    def __init__(self, params: N.GeonParams, threads: int = 1):
+        self.lib = load()
+        self.params = params
+        self._h = self.lib.oracle_create(C.byref(params))
+        self.lib.oracle_set_threads(self._h, threads)
+
+    def close(self):
+        if self._h:
+            self.lib.oracle_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params):
+        self.params = params
+        self.lib.oracle_set_params(self._h, C.byref(params))
+
+    def set_threads(self, n: int):
+        self.lib.oracle_set_threads(self._h, n)
+
+    def add(self, x, y, wx, wy, mass, charge, angw, creation_time=float("-inf")) -> int:
+        cols = [np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (x, y, wx, wy, mass, charge, angw)]
+        n = cols[0].size
+        return self.lib.oracle_add_particles(self._h, n, *[_dp(c) for c in cols], creation_time)
+
+    def count(self) -> int:
+        return self.lib.oracle_count(self._h)
+
+    def update(self, dt: float) -> int:
+        return self.lib.oracle_update(self._h, dt)
+
+    def compute_forces(self):
+        self.lib.oracle_compute_forces(self._h)
+
+    def compute_forces_subset(self, idx) -> int:
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        return self.lib.oracle_compute_forces_subset(self._h, _ip(idx), idx.size)
+
+    def compute_1pn(self):
+        self.lib.oracle_compute_1pn(self._h)
+
+    def state(self) -> dict:
+        n = self.count()
+        out = np.zeros((10, max(n, 1)))
+        self.lib.oracle_get_state(self._h, _dp(out), max(n, 1))
+        return {k: out[r, :n].copy() for r, k in enumerate(N.ST_NAMES)}
+
+    def ids(self) -> np.ndarray:
+        n = self.count()
+        out = np.zeros(max(n, 1), dtype=np.int32)
+        self.lib.oracle_get_ids(self._h, _ip(out), max(n, 1))
+        return out[:n]
+
+    def forces(self) -> dict:
+        n = self.count()
+        out = np.zeros((N.OUT_ROWS, max(n, 1)))
+        self.lib.oracle_get_forces(self._h, _dp(out), max(n, 1))
+        return {k: out[r, :n].copy() for r, k in enumerate(N.OUT_NAMES)}
+
+    def build_tree(self):
+        nn = C.c_int()
+        npts = self.lib.oracle_build_tree(self._h, C.byref(nn))
+        return npts, nn.value
+
+    def leaves(self, n_points: int):
+        cap = max(4 * n_points + 8, 8)
+        lop = np.zeros(max(n_points, 1), dtype=np.int32)
+        bx = np.zeros(cap); by = np.zeros(cap); bw = np.zeros(cap)
+        lv = np.zeros(cap, dtype=np.int32)
+        nl = self.lib.oracle_tree_leaves(self._h, _ip(lop), n_points, _dp(bx), _dp(by), _dp(bw), _ip(lv), cap)
+        return lop[:n_points], bx[:nl], by[:nl], bw[:nl], lv[:nl]
+
+    def ghost_origins(self) -> np.ndarray:
+        n = self.lib.oracle_ghost_origins(self._h, None, 0)
+        out = np.zeros(max(n, 1), dtype=np.int32)
+        self.lib.oracle_ghost_origins(self._h, _ip(out), n)
+        return out[:n]
+
+    def tree_nodes(self):
+        total = self.lib.oracle_tree_nodes(self._h, None, None, 0)
+        cap = max(total, 1)
+        out = np.zeros((12, cap))
+        meta = np.zeros((3, cap), dtype=np.int32)
+        self.lib.oracle_tree_nodes(self._h, _dp(out), _ip(meta), cap)
+        names = ["bx", "by", "bw", "mass", "charge", "mag", "angmom", "momx", "momy", "comx", "comy", "bh"]
+        d = {k: out[r, :total] for r, k in enumerate(names)}
+        d["divided"], d["count"], d["level"] = meta[0, :total], meta[1, :total], meta[2, :total]
+        return d
+
+    def upload_history(self, times, x, y, vx, vy, angw):
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        planes = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, vx, vy, angw)]
+        n, count = planes[0].shape
+        samples = np.ascontiguousarray(np.stack(planes))
+        rc = self.lib.oracle_upload_history(self._h, n, count, _dp(times), _dp(samples))
+        if rc != 0:
+            raise ValueError("history upload rejected")
+
+    def set_sim_time(self, t):
+        self.lib.oracle_set_sim_time(self._h, t)
+
+    def sim_time(self):
+        return self.lib.oracle_sim_time(self._h)
+
+    def last_substeps(self):
+        return self.lib.oracle_last_substeps(self._h)
+
+    def interactions(self):
+        return self.lib.oracle_interactions(self._h)
+
+    def pe(self):
+        return self.lib.oracle_pe(self._h)
+
+    def stats(self) -> dict:
+        s = N.GeonStats()
+        self.lib.oracle_stats(self._h, C.byref(s))
+        return s.as_dict()
+
+    def delayed_state(self, src: int, ox: float, oy: float):
+        out = np.zeros(5)
+        ok = self.lib.oracle_delayed_state(self._h, src, ox, oy, _dp(out))
+        return out if ok else None
+
+    def set_forces_init(self, v: bool):
+        self.lib.oracle_set_forces_init(self._h, 1 if v else 0)
+
+    def set_hist_stride(self, v: int):
+        self.lib.oracle_set_hist_stride(self._h, v)

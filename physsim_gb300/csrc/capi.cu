@@ -1,0 +1,937 @@
+// capi.cu — the C ABI (include/geon.h): handle lifetime, state upload and
+// download, and the frame driver that sequences the kernels of one
+// Physics.update (src/integrator.js:726-1825, in-scope part).
+//
+// Substep planning (integrator.js:810-875) runs on the host in FP64 from
+// max-reductions that the force pass leaves in device memory: the host reads
+// them back once per substep (one small copy), computes dtSub exactly as the
+// reference does, and enqueues the next substep.
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include <climits>
+#include <string>
+#include <vector>
+#include "force.cuh"
+#include "push.cuh"
+
+using namespace geon;
+
+#define GEON_VERSION_STRING "geon-gb300 1.0 (sm_103a)"
+
+namespace {
+
+thread_local std::string g_err;
+
+// Frees every pointer registered with it.
+struct DevArena {
+    std::vector<void*> ptrs;
+    bool failed = false;
+    template <class T> T* alloc(size_t count) {
+        if (count == 0) count = 1;
+        void* p = nullptr;
+        if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) { failed = true; return nullptr; }
+        ptrs.push_back(p);
+        return static_cast<T*>(p);
+    }
+    void free_all() {
+        for (void* p : ptrs) cudaFree(p);
+        ptrs.clear();
+    }
+};
+
+int lsb_exp(double v) {
+    if (v == 0.0) return INT_MAX;
+    int e;
+    double m = std::frexp(std::fabs(v), &e);
+    uint64_t M = (uint64_t)std::ldexp(m, 53);
+    return e - 53 + __builtin_ctzll(M);
+}
+
+// True when every grid value c - hw + j * hw / 2^30, j = 0 .. 2^31, is an exact
+// double, so the reference's centre recurrence never rounds.
+bool grid_exact(double c, double hw) {
+    if (!(hw > 0)) return false;
+    const int e = std::min(lsb_exp(c), lsb_exp(hw) - 30);
+    const double maxabs = std::fabs(c) + hw;
+    return std::ldexp(maxabs, -e) < 9007199254740992.0;
+}
+
+}  // namespace
+
+struct GeonHandle {
+    GeonParams prm{};
+    DevParams P{};
+    int n_cap = 0;
+    int n = 0;
+    cudaStream_t st = nullptr;
+    DevArena arena;         // state + control
+    DevArena tree_arena;    // tree buffers (reallocated when ghost capacity changes)
+    DevArena hist_arena;    // history rings (allocated when relativity is first enabled)
+    DevState S{}, S2{};
+    TreeBufs T{};
+    bool tree_periodic = false;
+    bool hist_alloc = false;
+    FrameCtl* ctl = nullptr;
+    FrameCtl* ctl_h = nullptr;     // pinned
+    int* d_root = nullptr;
+    double* hist_t = nullptr;
+    float* hist_age = nullptr;
+    float* hist_segdt = nullptr;
+    int* keep = nullptr;
+    int* dst = nullptr;
+    int* cscan_tmp = nullptr;
+    float* staging = nullptr;      // GEON_ST_ROWS x n_cap floats
+    double* staging_d = nullptr;   // GEON_ST_ROWS x n_cap doubles
+    double* stats_d = nullptr;
+    double* stats_h = nullptr;     // pinned
+    double simTime = 0.0;
+    bool forcesInit = false;
+    int histStride = 0;
+    long long histTotal = 0;
+    int lastSubsteps = 0;
+    int nextId = 0;
+    LaunchCounter lc;
+    std::string err;
+    // profiling
+    bool prof = false;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_ev;
+    std::vector<cudaEvent_t> ev_pool;
+    GeonProfile prof_acc{};
+};
+
+enum { PH_TREE = 0, PH_FORCE, PH_ONEPN, PH_PUSH };
+
+static cudaEvent_t get_event(GeonHandle* h) {
+    if (!h->ev_pool.empty()) { cudaEvent_t e = h->ev_pool.back(); h->ev_pool.pop_back(); return e; }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Records a start event for a phase; returns its slot (or -1 when profiling is off).
+static int prof_begin(GeonHandle* h, int phase) {
+    if (!h->prof) return -1;
+    cudaEvent_t a = get_event(h), b = get_event(h);
+    cudaEventRecord(a, h->st);
+    h->prof_ev.push_back({ phase, { a, b } });
+    return (int)h->prof_ev.size() - 1;
+}
+static void prof_end(GeonHandle* h, int slot) {
+    if (slot < 0) return;
+    cudaEventRecord(h->prof_ev[slot].second.second, h->st);
+}
+static void prof_collect(GeonHandle* h) {
+    if (h->prof_ev.empty()) return;
+    cudaStreamSynchronize(h->st);
+    for (auto& pe : h->prof_ev) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, pe.second.first, pe.second.second);
+        switch (pe.first) {
+            case PH_TREE: h->prof_acc.tree_ms += ms; h->prof_acc.tree_count++; break;
+            case PH_FORCE: h->prof_acc.force_ms += ms; h->prof_acc.force_count++; break;
+            case PH_ONEPN: h->prof_acc.onepn_ms += ms; h->prof_acc.onepn_count++; break;
+            default: h->prof_acc.push_ms += ms; h->prof_acc.push_count++; break;
+        }
+        h->ev_pool.push_back(pe.second.first);
+        h->ev_pool.push_back(pe.second.second);
+    }
+    h->prof_ev.clear();
+}
+
+static int set_err(GeonHandle* h, int code, const std::string& msg) {
+    if (h) h->err = msg; else g_err = msg;
+    return code;
+}
+
+static int cuda_check(GeonHandle* h, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return GEON_OK;
+    return set_err(h, GEON_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(call) do { int _r = cuda_check(h, (call), #call); if (_r) return _r; } while (0)
+#define CKL() do { int _r = cuda_check(h, cudaGetLastError(), "kernel launch"); if (_r) return _r; } while (0)
+
+static int validate_params(GeonHandle* h, const GeonParams& p) {
+    const uint32_t unsupported = GEON_BLACK_HOLE | GEON_HIGGS | GEON_AXION;
+    if (p.toggles & unsupported) return set_err(h, GEON_ERR_UNSUPPORTED, "black-hole mode, Higgs and axion fields are not part of this library");
+    if (!(p.domain_w > 0) || !(p.domain_h > 0)) return set_err(h, GEON_ERR_ARG, "domain_w and domain_h must be positive");
+    if (p.boundary_mode < 0 || p.boundary_mode > 2) return set_err(h, GEON_ERR_ARG, "boundary_mode out of range");
+    if (p.topology < 0 || p.topology > 2) return set_err(h, GEON_ERR_ARG, "topology out of range");
+    if (!(p.theta >= 0)) return set_err(h, GEON_ERR_ARG, "theta must be >= 0");
+    if (!(p.softening > 0)) return set_err(h, GEON_ERR_ARG, "softening must be > 0");
+    if ((p.toggles & GEON_YUKAWA) && !(p.yukawa_mu > 0)) return set_err(h, GEON_ERR_ARG, "yukawa_mu must be > 0");
+    return GEON_OK;
+}
+
+static void derive_params(GeonHandle* h) {
+    const GeonParams& p = h->prm;
+    DevParams& P = h->P;
+    P = DevParams{};
+    P.toggles = p.toggles; P.flags = p.flags;
+    P.boundary = p.boundary_mode; P.topology = p.topology;
+    P.periodic = p.boundary_mode == GEON_BOUND_LOOP;
+    P.ghosts = P.periodic && !(p.flags & GEON_FLAG_NO_GHOSTS);
+    P.rel = (p.toggles & GEON_RELATIVITY) ? 1 : 0;
+    P.n_cap = h->n_cap;
+    P.Wd = p.domain_w; P.Hd = p.domain_h; P.offXd = p.off_x; P.offYd = p.off_y;
+    P.W = (float)p.domain_w; P.H = (float)p.domain_h;
+    P.W_lo = (float)(p.domain_w - (double)P.W); P.H_lo = (float)(p.domain_h - (double)P.H);
+    P.halfW = (float)(p.domain_w * 0.5); P.halfH = (float)(p.domain_h * 0.5);
+    P.rootX = p.off_x + p.domain_w / 2; P.rootY = p.off_y + p.domain_h / 2;     // integrator.js:727-730
+    P.rootW = p.domain_w * 2; P.rootH = p.domain_h * 2;
+    P.exact_grid = grid_exact(P.rootX, P.rootW) && grid_exact(P.rootY, P.rootH);
+    P.soft = (float)p.softening;
+    P.softSq = (float)(p.softening * p.softening);
+    P.thetaD = p.theta;
+    P.thetaSqD = p.theta * p.theta;
+    P.thetaSq = (float)P.thetaSqD;
+    P.yukOn = (p.toggles & GEON_YUKAWA) ? 1 : 0;
+    P.yukMu = (float)p.yukawa_mu;
+    if (P.yukOn) {
+        const double c = 6.0 / p.yukawa_mu;                                    // forces.js:82-83
+        P.yukCutSqD = c * c;
+        P.yukCutSq = (float)P.yukCutSqD;
+    }
+    P.extGx = (float)(p.ext_gravity * std::cos(p.ext_gravity_angle));         // integrator.js:553-560
+    P.extGy = (float)(p.ext_gravity * std::sin(p.ext_gravity_angle));
+    P.extEx = (float)(p.ext_electric * std::cos(p.ext_electric_angle));
+    P.extEy = (float)(p.ext_electric * std::sin(p.ext_electric_angle));
+    P.extBz = (float)p.ext_bz;
+    P.friction = (float)p.bounce_friction;
+}
+
+static void fill_state(DevArena& A, DevState& S, int cap) {
+    S.pos = A.alloc<float4>(cap); S.pos_lo = A.alloc<float2>(cap); S.vel = A.alloc<float4>(cap);
+    S.spin = A.alloc<float4>(cap); S.mom = A.alloc<float2>(cap); S.force = A.alloc<float4>(cap);
+    S.grad = A.alloc<float4>(cap); S.torque = A.alloc<float4>(cap); S.f1pn = A.alloc<float2>(cap);
+    S.f1pnOld = A.alloc<float2>(cap); S.brk = A.alloc<float>((size_t)12 * cap); S.ctime = A.alloc<double>(cap);
+    S.id = A.alloc<int>(cap); S.hist_cnt = A.alloc<int>(cap);
+    S.hist = nullptr; S.hist_angw = nullptr;
+}
+
+static int ensure_history(GeonHandle* h) {
+    if (h->hist_alloc || !h->P.rel) return GEON_OK;
+    const size_t cnt = (size_t)h->n_cap * HIST_LEN;
+    h->S.hist = h->hist_arena.alloc<float4>(cnt);
+    h->S.hist_angw = h->hist_arena.alloc<float>(cnt);
+    h->S2.hist = h->hist_arena.alloc<float4>(cnt);
+    h->S2.hist_angw = h->hist_arena.alloc<float>(cnt);
+    if (h->hist_arena.failed) { h->hist_arena.free_all(); return set_err(h, GEON_ERR_NOMEM, "history allocation failed"); }
+    h->hist_alloc = true;
+    return GEON_OK;
+}
+
+static int ensure_tree(GeonHandle* h) {
+    const bool per = h->P.ghosts != 0;
+    if (h->T.pt_ref && per == h->tree_periodic) return GEON_OK;
+    CK(cudaStreamSynchronize(h->st));
+    h->tree_arena.free_all();
+    h->tree_arena.failed = false;
+    TreeBufs& T = h->T;
+    T = TreeBufs{};
+    DevArena& A = h->tree_arena;
+    const int cap = h->n_cap;
+    const long long cp = (long long)cap * (per ? 1 + MAX_GHOSTS_PER_PARTICLE : 1);
+    if (cp > (1ll << 30)) return set_err(h, GEON_ERR_ARG, "tree point capacity too large");
+    T.cap_pts = (int)cp;
+    T.cap_int = T.cap_pts + 1024;
+    T.pt_ref = A.alloc<uint32_t>(T.cap_pts);
+    T.ghost_cnt = A.alloc<int>(cap); T.ghost_off = A.alloc<int>(cap);
+    T.key = A.alloc<uint64_t>(T.cap_pts); T.key_alt = A.alloc<uint64_t>(T.cap_pts);
+    T.idx = A.alloc<uint32_t>(T.cap_pts); T.idx_alt = A.alloc<uint32_t>(T.cap_pts);
+    T.sort_tmp = A.alloc<char>(radix_temp_bytes(T.cap_pts));
+    T.scan_tmp = A.alloc<int>(scan_temp_ints(T.cap_pts) + 16);
+    T.pt_pos = A.alloc<float4>(T.cap_pts); T.pt_lo = A.alloc<float2>(T.cap_pts);
+    T.pt_vel = A.alloc<float4>(T.cap_pts); T.pt_mom = A.alloc<float2>(T.cap_pts);
+    T.lcp_a = A.alloc<int>(T.cap_pts); T.int_cnt = A.alloc<int>(T.cap_pts); T.int_base = A.alloc<int>(T.cap_pts);
+    T.leaf_flag = A.alloc<int>(T.cap_pts); T.leaf_base = A.alloc<int>(T.cap_pts);
+    T.real_flag = A.alloc<int>(T.cap_pts); T.tgt_base = A.alloc<int>(T.cap_pts);
+    T.tgt = A.alloc<int>(cap);
+    T.int_a = A.alloc<float4>(T.cap_int); T.int_b = A.alloc<float4>(T.cap_int); T.int_c = A.alloc<float4>(T.cap_int);
+    T.int_child = A.alloc<int4>(T.cap_int); T.int_meta = A.alloc<int4>(T.cap_int); T.int_count = A.alloc<int>(T.cap_int);
+    T.leaf_a = A.alloc<float4>(T.cap_pts); T.leaf_b = A.alloc<float4>(T.cap_pts); T.leaf_c = A.alloc<float4>(T.cap_pts);
+    T.leaf_meta = A.alloc<int4>(T.cap_pts); T.leaf_of = A.alloc<int>(T.cap_pts);
+    if (A.failed) { A.free_all(); T = TreeBufs{}; return set_err(h, GEON_ERR_NOMEM, "tree allocation failed"); }
+    h->tree_periodic = per;
+    return GEON_OK;
+}
+
+// ---- small kernels local to the driver --------------------------------------------------------
+__global__ void set_n_kernel(FrameCtl* ctl, int n) { ctl->n = n; }
+
+__global__ void init_particles_kernel(DevParams P, DevState S, const float* __restrict__ rows, int cap, int first, int k,
+                                      double ctime, int id0) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < k; t += gridDim.x * blockDim.x) {
+        const float x = rows[t], y = rows[cap + t], wx = rows[2 * cap + t], wy = rows[3 * cap + t];
+        const float m = rows[4 * cap + t], q = rows[5 * cap + t], angw = rows[6 * cap + t];
+        const int i = first + t;
+        const float r = cbrtf(m);
+        float vx = wx, vy = wy, angVel = angw;
+        if (P.rel) {
+            const float invG = 1.f / sqrtf(1.f + wx * wx + wy * wy);
+            vx = wx * invG; vy = wy * invG;
+            angVel = angw / sqrtf(1.f + angw * angw * r * r);             // relativity.js:7-9
+        }
+        S.pos[i] = make_float4(x, y, m, q);
+        S.pos_lo[i] = make_float2(0.f, 0.f);
+        S.vel[i] = make_float4(wx, wy, vx, vy);
+        S.spin[i] = make_float4(angw, angVel, r, 1.f / m);
+        S.mom[i] = make_float2(0.f, 0.f);                                   // particle.js:53-54
+        S.force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        S.grad[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        S.torque[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        S.f1pn[i] = make_float2(0.f, 0.f);
+        S.f1pnOld[i] = make_float2(0.f, 0.f);
+        S.ctime[i] = ctime;
+        S.id[i] = id0 + t;
+        S.hist_cnt[i] = 0;
+        for (int rr = 0; rr < 12; rr++) S.brk[(size_t)rr * P.n_cap + i] = 0.f;
+    }
+}
+
+__global__ void bootstrap_angvel_kernel(DevParams P, DevState S, const FrameCtl* ctl) {   // integrator.js:751-753
+    const int n = ctl->n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 s = S.spin[i];
+        s.y = P.rel ? s.x / sqrtf(1.f + s.x * s.x * s.z * s.z) : s.x;
+        S.spin[i] = s;
+    }
+}
+
+template <class Tout>
+__global__ void pack_state_kernel(DevState S, int n, int rows, int cap, Tout* out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 p = S.pos[i];
+        const float2 pl = S.pos_lo[i];
+        const float4 v = S.vel[i];
+        const float4 s = S.spin[i];
+        double vals[GEON_ST_ROWS] = { (double)p.x + pl.x, (double)p.y + pl.y, v.x, v.y, p.z, p.w, s.x, v.z, v.w, s.y };
+        for (int r = 0; r < rows; r++) out[(size_t)r * cap + i] = (Tout)vals[r];
+    }
+}
+
+__global__ void pack_forces_kernel(DevState S, int n, int first, int rows, int cap, int n_cap, float* out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        for (int r = 0; r < rows; r++) {
+            const int row = first + r;
+            float v = 0.f;
+            const float4 f = S.force[i], g = S.grad[i], t = S.torque[i];
+            const float2 p1 = S.f1pn[i];
+            switch (row) {
+                case GEON_OUT_FX: v = f.x; break;
+                case GEON_OUT_FY: v = f.y; break;
+                case GEON_OUT_BZ: v = f.z; break;
+                case GEON_OUT_BGZ: v = f.w; break;
+                case GEON_OUT_DBZDX: v = g.x; break;
+                case GEON_OUT_DBZDY: v = g.y; break;
+                case GEON_OUT_DBGZDX: v = g.z; break;
+                case GEON_OUT_DBGZDY: v = g.w; break;
+                case GEON_OUT_TIDAL: v = t.x; break;
+                case GEON_OUT_FRAMEDRAG: v = t.y; break;
+                case GEON_OUT_F1PN_X: v = p1.x; break;
+                case GEON_OUT_F1PN_Y: v = p1.y; break;
+                case GEON_OUT_PE: v = t.w; break;
+                default: v = S.brk[(size_t)(row - GEON_OUT_GRAV_X) * n_cap + i]; break;
+            }
+            out[(size_t)r * cap + i] = v;
+        }
+    }
+}
+
+__global__ void history_upload_kernel(DevState S, int n, int count, const float* __restrict__ samples) {
+    const size_t plane = (size_t)n * count;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < plane; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = e / count, k = e % count;
+        S.hist[i * HIST_LEN + k] = make_float4(samples[e], samples[plane + e], samples[2 * plane + e], samples[3 * plane + e]);
+        S.hist_angw[i * HIST_LEN + k] = samples[4 * plane + e];
+        if (k == 0) S.hist_cnt[i] = count;
+    }
+}
+
+// FP32 FMA microbenchmark: 8 independent chains per thread.
+__global__ void fma_peak_kernel(float* out, int iters, float a, float b) {
+    float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+            x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+            x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+        }
+    }
+    const float s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == 123456.789f) out[0] = s;
+}
+
+static inline int grid_for(int n, int threads) {
+    int b = (n + threads - 1) / threads;
+    return std::max(1, std::min(b, 152 * 16));
+}
+
+static inline double bits_to_double(unsigned long long b) {
+    double d;
+    std::memcpy(&d, &b, sizeof(d));
+    return d;
+}
+
+static bool bh_on(const GeonHandle* h) { return (h->prm.toggles & GEON_BARNES_HUT) != 0; }
+
+static ForceCtx make_ctx(GeonHandle* h) {
+    ForceCtx C{};
+    C.simTime = h->simTime;
+    C.hist_t = h->hist_t;
+    C.hist_age = h->hist_age;
+    C.hist_segdt = h->hist_segdt;
+    C.hist_head = (int)(h->histTotal & HIST_MASK);
+    C.pe = (h->prm.flags & GEON_FLAG_PE) ? 1 : 0;
+    C.brk = (h->prm.flags & GEON_FLAG_BREAKDOWN) ? 1 : 0;
+    C.bounce = h->prm.boundary_mode == GEON_BOUND_BOUNCE;
+    return C;
+}
+
+static int read_ctl(GeonHandle* h) {
+    CK(cudaMemcpyAsync(h->ctl_h, h->ctl, sizeof(FrameCtl), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (h->ctl_h->err) {
+        const int e = h->ctl_h->err;
+        return set_err(h, GEON_ERR_OVERFLOW, std::string("device overflow flag ") + std::to_string(e) +
+                       ((e & ERR_NODE_OVERFLOW) ? " (node capacity)" : "") + ((e & ERR_STACK_OVERFLOW) ? " (walk stack)" : ""));
+    }
+    return GEON_OK;
+}
+
+static int build_tree(GeonHandle* h) {
+    int r = ensure_tree(h);
+    if (r) return r;
+    const int ps = prof_begin(h, PH_TREE);
+    tree_build(h->P, h->S, h->T, h->ctl, h->d_root, h->n_cap, h->st, h->lc);
+    prof_end(h, ps);
+    CKL();
+    return GEON_OK;
+}
+
+static int run_force_pass(GeonHandle* h, bool rebuild) {
+    const bool bh = bh_on(h);
+    if (bh && rebuild) { int r = build_tree(h); if (r) return r; }
+    if (h->P.rel) { launch_hist_tables(h->hist_t, h->simTime, h->hist_age, h->hist_segdt, h->st, h->lc); CKL(); }
+    const int ps = prof_begin(h, PH_FORCE);
+    force_pass(h->P, h->S, h->T, h->d_root, h->ctl, make_ctx(h), bh, h->n_cap, h->st, h->lc);
+    prof_end(h, ps);
+    CKL();
+    return GEON_OK;
+}
+
+static int compact(GeonHandle* h) {
+    const int n = h->n;
+    exclusive_scan(h->keep, h->dst, n, nullptr, nullptr, h->cscan_tmp, h->st, &h->lc);
+    launch_compact(h->S, h->S2, h->keep, h->dst, n, h->n_cap, h->hist_alloc, true, h->st, h->lc);
+    CKL();
+    std::swap(h->S, h->S2);
+    return GEON_OK;
+}
+
+// =============================================================================================
+extern "C" {
+
+const char* geon_version(void) { return GEON_VERSION_STRING; }
+
+const char* geon_last_error(GeonHandle* h) { return h ? h->err.c_str() : g_err.c_str(); }
+
+int geon_create(const GeonParams* params, int32_t max_particles, GeonHandle** out) {
+    if (!params || !out) return set_err(nullptr, GEON_ERR_ARG, "null argument");
+    if (max_particles <= 0 || max_particles > (int32_t)REF_INDEX_MASK) return set_err(nullptr, GEON_ERR_ARG, "max_particles out of range");
+    *out = nullptr;
+    GeonHandle* h = new GeonHandle();
+    h->prm = *params;
+    if (h->prm.max_substeps <= 0) h->prm.max_substeps = 32;
+    int r = validate_params(h, h->prm);
+    if (r) { g_err = h->err; delete h; return r; }
+    h->n_cap = max_particles;
+    derive_params(h);
+    if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
+        g_err = "cudaStreamCreate failed"; delete h; return GEON_ERR_CUDA;
+    }
+    DevArena& A = h->arena;
+    fill_state(A, h->S, h->n_cap);
+    fill_state(A, h->S2, h->n_cap);
+    h->ctl = A.alloc<FrameCtl>(1);
+    h->d_root = A.alloc<int>(1);
+    h->hist_t = A.alloc<double>(HIST_LEN);
+    h->hist_age = A.alloc<float>(HIST_LEN);
+    h->hist_segdt = A.alloc<float>(HIST_LEN);
+    h->keep = A.alloc<int>(h->n_cap);
+    h->dst = A.alloc<int>(h->n_cap);
+    h->cscan_tmp = A.alloc<int>(scan_temp_ints(h->n_cap) + 16);
+    h->staging = A.alloc<float>((size_t)GEON_ST_ROWS * h->n_cap);
+    h->staging_d = A.alloc<double>((size_t)GEON_ST_ROWS * h->n_cap);
+    h->stats_d = A.alloc<double>(16);
+    if (A.failed || cudaMallocHost(&h->ctl_h, sizeof(FrameCtl)) != cudaSuccess ||
+        cudaMallocHost(&h->stats_h, 16 * sizeof(double)) != cudaSuccess) {
+        A.free_all();
+        cudaStreamDestroy(h->st);
+        g_err = "device allocation failed";
+        delete h;
+        return GEON_ERR_NOMEM;
+    }
+    cudaMemsetAsync(h->ctl, 0, sizeof(FrameCtl), h->st);
+    cudaMemsetAsync(h->hist_t, 0, HIST_LEN * sizeof(double), h->st);
+    cudaMemsetAsync(h->S.hist_cnt, 0, h->n_cap * sizeof(int), h->st);
+    cudaMemsetAsync(h->S.brk, 0, (size_t)12 * h->n_cap * sizeof(float), h->st);
+    r = ensure_history(h);
+    if (!r) r = ensure_tree(h);
+    if (r) { g_err = h->err; geon_destroy(h); return r; }
+    if (cudaStreamSynchronize(h->st) != cudaSuccess) { g_err = "initialisation failed"; geon_destroy(h); return GEON_ERR_CUDA; }
+    *out = h;
+    return GEON_OK;
+}
+
+int geon_destroy(GeonHandle* h) {
+    if (!h) return GEON_ERR_ARG;
+    if (h->st) cudaStreamSynchronize(h->st);
+    h->tree_arena.free_all();
+    h->hist_arena.free_all();
+    h->arena.free_all();
+    prof_collect(h);
+    for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+    if (h->ctl_h) cudaFreeHost(h->ctl_h);
+    if (h->stats_h) cudaFreeHost(h->stats_h);
+    if (h->st) cudaStreamDestroy(h->st);
+    delete h;
+    return GEON_OK;
+}
+
+int geon_set_params(GeonHandle* h, const GeonParams* params) {
+    if (!h || !params) return GEON_ERR_ARG;
+    GeonParams p = *params;
+    if (p.max_substeps <= 0) p.max_substeps = 32;
+    int r = validate_params(h, p);
+    if (r) return r;
+    h->prm = p;
+    derive_params(h);
+    r = ensure_history(h);
+    if (r) return r;
+    return ensure_tree(h);
+}
+
+int geon_get_params(GeonHandle* h, GeonParams* out) {
+    if (!h || !out) return GEON_ERR_ARG;
+    *out = h->prm;
+    return GEON_OK;
+}
+
+int geon_add_particles(GeonHandle* h, int32_t n, const float* soa, double creation_time, int32_t* first_index) {
+    if (!h || (!soa && n > 0) || n < 0) return GEON_ERR_ARG;
+    if (n == 0) { if (first_index) *first_index = h->n; return GEON_OK; }
+    if ((long long)h->n + n > h->n_cap) return set_err(h, GEON_ERR_FULL, "particle capacity exhausted");
+    const int cap = h->n_cap;
+    for (int r = 0; r < GEON_ST_ROWS_IN; r++)
+        CK(cudaMemcpyAsync(h->staging + (size_t)r * cap, soa + (size_t)r * n, n * sizeof(float), cudaMemcpyHostToDevice, h->st));
+    init_particles_kernel<<<grid_for(n, 256), 256, 0, h->st>>>(h->P, h->S, h->staging, cap, h->n, n, creation_time, h->nextId);
+    CKL();
+    h->lc.add(1);
+    if (first_index) *first_index = h->n;
+    h->n += n;
+    h->nextId += n;
+    set_n_kernel<<<1, 1, 0, h->st>>>(h->ctl, h->n);
+    h->lc.add(1);
+    CK(cudaStreamSynchronize(h->st));
+    return GEON_OK;
+}
+
+int geon_remove_particle(GeonHandle* h, int32_t index) {
+    if (!h || index < 0 || index >= h->n) return GEON_ERR_ARG;
+    std::vector<int> keep(h->n, 1);
+    keep[index] = 0;
+    CK(cudaMemcpyAsync(h->keep, keep.data(), h->n * sizeof(int), cudaMemcpyHostToDevice, h->st));
+    int r = compact(h);
+    if (r) return r;
+    h->n -= 1;
+    set_n_kernel<<<1, 1, 0, h->st>>>(h->ctl, h->n);
+    h->lc.add(1);
+    CK(cudaStreamSynchronize(h->st));
+    return GEON_OK;
+}
+
+int geon_reset(GeonHandle* h) {
+    if (!h) return GEON_ERR_ARG;
+    h->n = 0;
+    h->simTime = 0;
+    h->forcesInit = false;
+    h->histStride = 0;
+    h->histTotal = 0;
+    h->lastSubsteps = 0;
+    CK(cudaMemsetAsync(h->ctl, 0, sizeof(FrameCtl), h->st));
+    CK(cudaMemsetAsync(h->hist_t, 0, HIST_LEN * sizeof(double), h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return GEON_OK;
+}
+
+int geon_upload_state(GeonHandle* h, int32_t n, const float* soa, double sim_time) {
+    int r = geon_reset(h);
+    if (r) return r;
+    h->simTime = sim_time;
+    // loaded particles are treated as always existing (save-load.js:231)
+    return geon_add_particles(h, n, soa, -INFINITY, nullptr);
+}
+
+int geon_particle_count(GeonHandle* h, int32_t* n) {
+    if (!h || !n) return GEON_ERR_ARG;
+    *n = h->n;
+    return GEON_OK;
+}
+
+int geon_download_state(GeonHandle* h, float* soa, int32_t rows, int32_t capacity, int32_t* n) {
+    if (!h || !soa || rows <= 0 || rows > GEON_ST_ROWS || capacity < 0) return GEON_ERR_ARG;
+    const int cnt = std::min(h->n, capacity);
+    if (cnt > 0) {
+        pack_state_kernel<float><<<grid_for(cnt, 256), 256, 0, h->st>>>(h->S, cnt, rows, h->n_cap, h->staging);
+        CKL();
+        h->lc.add(1);
+        for (int r = 0; r < rows; r++)
+            CK(cudaMemcpyAsync(soa + (size_t)r * capacity, h->staging + (size_t)r * h->n_cap, cnt * sizeof(float), cudaMemcpyDeviceToHost, h->st));
+    }
+    CK(cudaStreamSynchronize(h->st));
+    if (n) *n = h->n;
+    return GEON_OK;
+}
+
+int geon_download_state_f64(GeonHandle* h, double* soa, int32_t rows, int32_t capacity, int32_t* n) {
+    if (!h || !soa || rows <= 0 || rows > GEON_ST_ROWS || capacity < 0) return GEON_ERR_ARG;
+    const int cnt = std::min(h->n, capacity);
+    if (cnt > 0) {
+        pack_state_kernel<double><<<grid_for(cnt, 256), 256, 0, h->st>>>(h->S, cnt, rows, h->n_cap, h->staging_d);
+        CKL();
+        h->lc.add(1);
+        for (int r = 0; r < rows; r++)
+            CK(cudaMemcpyAsync(soa + (size_t)r * capacity, h->staging_d + (size_t)r * h->n_cap, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    }
+    CK(cudaStreamSynchronize(h->st));
+    if (n) *n = h->n;
+    return GEON_OK;
+}
+
+int geon_download_ids(GeonHandle* h, int32_t* ids, int32_t capacity, int32_t* n) {
+    if (!h || !ids || capacity < 0) return GEON_ERR_ARG;
+    const int cnt = std::min(h->n, capacity);
+    if (cnt > 0) CK(cudaMemcpyAsync(ids, h->S.id, cnt * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (n) *n = h->n;
+    return GEON_OK;
+}
+
+int geon_compute_forces(GeonHandle* h) {
+    if (!h) return GEON_ERR_ARG;
+    if (h->n == 0) return GEON_OK;
+    int r = run_force_pass(h, true);
+    if (r) return r;
+    return read_ctl(h);
+}
+
+int geon_compute_1pn(GeonHandle* h) {
+    if (!h) return GEON_ERR_ARG;
+    if (h->n == 0) return GEON_OK;
+    const bool bh = bh_on(h);
+    if (bh) { int r = build_tree(h); if (r) return r; }
+    launch_hist_tables(h->hist_t, h->simTime, h->hist_age, h->hist_segdt, h->st, h->lc);
+    onepn_pass(h->P, h->S, h->T, h->d_root, h->ctl, make_ctx(h), bh, h->n_cap, h->st, h->lc);
+    CKL();
+    return read_ctl(h);
+}
+
+int geon_download_forces(GeonHandle* h, int32_t first_row, int32_t rows, float* out, int32_t capacity) {
+    if (!h || !out || first_row < 0 || rows <= 0 || first_row + rows > GEON_OUT_ROWS || capacity < 0) return GEON_ERR_ARG;
+    const int cnt = std::min(h->n, capacity);
+    if (cnt > 0) {
+        // staging holds GEON_ST_ROWS rows of n_cap floats: pack in chunks of that many rows
+        for (int r0 = 0; r0 < rows; r0 += GEON_ST_ROWS) {
+            const int rr = std::min(GEON_ST_ROWS, rows - r0);
+            pack_forces_kernel<<<grid_for(cnt, 256), 256, 0, h->st>>>(h->S, cnt, first_row + r0, rr, h->n_cap, h->n_cap, h->staging);
+            CKL();
+            h->lc.add(1);
+            for (int r = 0; r < rr; r++)
+                CK(cudaMemcpyAsync(out + (size_t)(r0 + r) * capacity, h->staging + (size_t)r * h->n_cap, cnt * sizeof(float),
+                                   cudaMemcpyDeviceToHost, h->st));
+            CK(cudaStreamSynchronize(h->st));
+        }
+    }
+    CK(cudaStreamSynchronize(h->st));
+    return GEON_OK;
+}
+
+int geon_build_tree(GeonHandle* h, GeonTreeInfo* info) {
+    if (!h) return GEON_ERR_ARG;
+    int r = build_tree(h);
+    if (r) return r;
+    r = read_ctl(h);
+    if (r) return r;
+    if (info) {
+        const FrameCtl& c = *h->ctl_h;
+        info->n_points = c.nPts;
+        info->n_ghosts = c.nGhost;
+        info->n_dropped = c.nPts - c.nValid;
+        info->n_internal = c.nInternal;
+        info->n_leaves = c.nLeaves;
+        info->max_level = c.maxLevel;
+        info->n_bucket = c.nBucket;
+        info->reserved = 0;
+    }
+    return GEON_OK;
+}
+
+int geon_tree_leaves(GeonHandle* h, int32_t* leaf_of_point, int32_t n_points, double* leaf_bx, double* leaf_by,
+                     double* leaf_bw, int32_t* leaf_level, int32_t n_leaves) {
+    if (!h || !leaf_of_point || !leaf_bx || !leaf_by || !leaf_bw || !leaf_level) return GEON_ERR_ARG;
+    int r = read_ctl(h);
+    if (r) return r;
+    const FrameCtl c = *h->ctl_h;
+    if (n_points < c.nPts || n_leaves < c.nLeaves) return set_err(h, GEON_ERR_ARG, "output arrays too small");
+    DevArena tmp;
+    int* d_lop = tmp.alloc<int>(std::max(c.nPts, 1));
+    double* d_bx = tmp.alloc<double>(std::max(c.nLeaves, 1));
+    double* d_by = tmp.alloc<double>(std::max(c.nLeaves, 1));
+    double* d_bw = tmp.alloc<double>(std::max(c.nLeaves, 1));
+    int* d_lv = tmp.alloc<int>(std::max(c.nLeaves, 1));
+    if (tmp.failed) { tmp.free_all(); return set_err(h, GEON_ERR_NOMEM, "leaf dump allocation failed"); }
+    tree_leaf_dump(h->P, h->T, h->ctl, d_lop, d_bx, d_by, d_bw, d_lv, c.nPts, h->st, h->lc);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && c.nPts) e = cudaMemcpyAsync(leaf_of_point, d_lop, c.nPts * sizeof(int), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess && c.nLeaves) {
+        cudaMemcpyAsync(leaf_bx, d_bx, c.nLeaves * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+        cudaMemcpyAsync(leaf_by, d_by, c.nLeaves * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+        cudaMemcpyAsync(leaf_bw, d_bw, c.nLeaves * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+        e = cudaMemcpyAsync(leaf_level, d_lv, c.nLeaves * sizeof(int), cudaMemcpyDeviceToHost, h->st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    tmp.free_all();
+    return cuda_check(h, e, "leaf dump");
+}
+
+int geon_interaction_count(GeonHandle* h, int64_t* count) {
+    if (!h || !count) return GEON_ERR_ARG;
+    int r = read_ctl(h);
+    if (r) return r;
+    *count = (int64_t)h->ctl_h->interactions;
+    return GEON_OK;
+}
+
+int geon_update(GeonHandle* h, double dt, int32_t* substeps) {
+    if (!h) return GEON_ERR_ARG;
+    if (!(dt >= 0)) return set_err(h, GEON_ERR_ARG, "dt must be >= 0");
+    int r;
+    const GeonParams& p = h->prm;
+    const uint32_t tg = p.toggles;
+    const bool rel = (tg & GEON_RELATIVITY) != 0;
+    const bool hasGrav = tg & GEON_GRAVITY, hasMag = tg & GEON_MAGNETIC, hasGM = tg & GEON_GRAVITOMAG;
+    const bool has1PN = tg & GEON_ONE_PN;
+    const bool hasExtBz = p.ext_bz != 0;
+    const bool bh = bh_on(h);
+    const int maxSub = p.max_substeps;
+    const double EPS = 1e-12;
+    if (!h->forcesInit && h->n > 0) {                                      // integrator.js:750-782
+        bootstrap_angvel_kernel<<<grid_for(h->n, 256), 256, 0, h->st>>>(h->P, h->S, h->ctl);
+        CKL();
+        h->lc.add(1);
+        r = run_force_pass(h, true);
+        if (r) return r;
+        h->forcesInit = true;
+    }
+    // frame-start planner scan (integrator.js:813-836)
+    launch_frame_scan(h->P, h->S, h->ctl, h->n_cap, h->st, h->lc);
+    CKL();
+    r = read_ctl(h);
+    if (r) return r;
+    double curAccel = bits_to_double(h->ctl_h->maxAccelSqBits);
+    double curCyc = bits_to_double(h->ctl_h->maxCycBits);
+    double lastKick = 0.0;
+    PushFlags F{};
+    F.has1PN = has1PN;
+    F.needBoris = hasMag || hasGM || hasExtBz;
+    F.needSpinOrbit = (tg & GEON_SPIN_ORBIT) && (hasMag || hasGM);
+    F.needTorques = (hasGM && rel) || hasGrav;
+    double dtRemain = dt;
+    int totalSteps = 0;
+    while (dtRemain > EPS && totalSteps < maxSub) {                        // integrator.js:810
+        const double useAccel = totalSteps == 0 ? curAccel : lastKick;
+        double aMax = std::sqrt(useAccel);
+        if (aMax != aMax) aMax = 0;
+        double dtSafe = aMax > EPS ? std::sqrt(p.softening / aMax) : dtRemain;
+        if (curCyc > 0) {
+            const double dtCyc = 0.7853981633974483 / curCyc;
+            if (dtCyc < dtSafe) dtSafe = dtCyc;
+        }
+        const double need = std::ceil(dtRemain / dtSafe);
+        const double stepsNeeded = std::min(need, (double)(maxSub - totalSteps));
+        const double dtSub = dtRemain / stepsNeeded;
+        totalSteps++;
+        dtRemain -= dtSub;
+        lastKick = curAccel;
+        if (h->n > 0) {
+            const int ps = prof_begin(h, PH_PUSH);
+            launch_push(h->P, h->S, h->ctl, (float)dtSub, F, h->n_cap, h->st, h->lc);
+            prof_end(h, ps);
+            CKL();
+            if (h->prof) h->prof_acc.particle_substeps += h->n;
+        }
+        h->simTime += dtSub;
+        if (h->n == 0) continue;
+        bool haveTree = false;
+        if (has1PN) {                                                      // integrator.js:1297-1318
+            if (bh) { r = build_tree(h); if (r) return r; haveTree = true; }
+            launch_hist_tables(h->hist_t, h->simTime, h->hist_age, h->hist_segdt, h->st, h->lc);
+            const int ps = prof_begin(h, PH_ONEPN);
+            onepn_pass(h->P, h->S, h->T, h->d_root, h->ctl, make_ctx(h), bh, h->n_cap, h->st, h->lc);
+            prof_end(h, ps);
+            launch_vv_kick(h->P, h->S, h->ctl, (float)(dtSub * 0.5), h->n_cap, h->st, h->lc);
+            CKL();
+        }
+        r = run_force_pass(h, !haveTree);                                  // integrator.js:1336-1348, 1489-1493
+        if (r) return r;
+        r = read_ctl(h);
+        if (r) return r;
+        if (h->prof) h->prof_acc.interactions += (int64_t)h->ctl_h->interactions;
+        curAccel = bits_to_double(h->ctl_h->maxAccelSqBits);
+        curCyc = bits_to_double(h->ctl_h->maxCycBits);
+    }
+    h->lastSubsteps = totalSteps;
+    if (substeps) *substeps = totalSteps;
+    if (rel && h->n > 0 && ++h->histStride >= HIST_STRIDE) {               // integrator.js:1550-1565
+        h->histStride -= HIST_STRIDE;
+        r = ensure_history(h);
+        if (r) return r;
+        const int slot = (int)(h->histTotal & HIST_MASK);
+        launch_record_history(h->S, h->ctl, h->hist_t, slot, h->simTime, h->n_cap, h->st, h->lc);
+        CKL();
+        h->histTotal++;
+    }
+    if (h->n > 0) {                                                        // integrator.js:1798-1824
+        CK(cudaMemsetAsync(&h->ctl->nRemoved, 0, sizeof(int), h->st));
+        launch_boundary(h->P, h->S, h->ctl, h->keep, h->n_cap, h->st, h->lc);
+        CKL();
+        r = read_ctl(h);
+        if (r) return r;
+        const int removed = h->ctl_h->nRemoved;
+        if (removed > 0) {
+            r = compact(h);
+            if (r) return r;
+            h->n -= removed;
+            set_n_kernel<<<1, 1, 0, h->st>>>(h->ctl, h->n);
+            h->lc.add(1);
+            CK(cudaStreamSynchronize(h->st));
+        }
+    }
+    return GEON_OK;
+}
+
+int geon_synchronize(GeonHandle* h) {
+    if (!h) return GEON_ERR_ARG;
+    CK(cudaStreamSynchronize(h->st));
+    return GEON_OK;
+}
+
+int geon_stats(GeonHandle* h, GeonStats* out) {
+    if (!h || !out) return GEON_ERR_ARG;
+    launch_stats(h->P, h->S, h->ctl, h->stats_d, h->n_cap, h->st, h->lc);
+    CKL();
+    CK(cudaMemcpyAsync(h->stats_h, h->stats_d, 10 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    const double* s = h->stats_h;
+    out->linear_ke = s[0]; out->spin_ke = s[1]; out->px = s[2]; out->py = s[3];
+    out->total_mass = s[4];
+    out->com_x = s[4] > 0 ? s[5] / s[4] : 0; out->com_y = s[4] > 0 ? s[6] / s[4] : 0;
+    out->pe = s[7] * 0.5;
+    out->orbital_ang_mom = s[8]; out->spin_ang_mom = s[9];
+    out->sim_time = h->simTime;
+    out->alive_count = h->n;
+    out->last_substeps = h->lastSubsteps;
+    return GEON_OK;
+}
+
+int geon_upload_history(GeonHandle* h, int32_t n, int32_t count, const double* times, const float* samples) {
+    if (!h || n != h->n || count < 0 || count > HIST_LEN || (count > 0 && (!times || !samples)))
+        return set_err(h, GEON_ERR_ARG, "history upload: n must equal the particle count and count <= 256");
+    if (!h->P.rel) return set_err(h, GEON_ERR_ARG, "history needs the relativity toggle");
+    int r = ensure_history(h);
+    if (r) return r;
+    std::vector<double> t(HIST_LEN, 0.0);
+    for (int k = 0; k < count; k++) t[k] = times[k];
+    CK(cudaMemcpyAsync(h->hist_t, t.data(), HIST_LEN * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemsetAsync(h->S.hist_cnt, 0, h->n_cap * sizeof(int), h->st));
+    if (count > 0 && n > 0) {
+        const size_t elems = (size_t)5 * n * count;
+        float* d = nullptr;
+        CK(cudaMalloc(&d, elems * sizeof(float)));
+        cudaError_t e = cudaMemcpyAsync(d, samples, elems * sizeof(float), cudaMemcpyHostToDevice, h->st);
+        if (e == cudaSuccess) {
+            history_upload_kernel<<<grid_for(n * count, 256), 256, 0, h->st>>>(h->S, n, count, d);
+            e = cudaGetLastError();
+            h->lc.add(1);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+        cudaFree(d);
+        if (e != cudaSuccess) return cuda_check(h, e, "history upload");
+    }
+    h->histTotal = count;
+    CK(cudaStreamSynchronize(h->st));
+    return GEON_OK;
+}
+
+int geon_set_sim_time(GeonHandle* h, double sim_time) {
+    if (!h) return GEON_ERR_ARG;
+    h->simTime = sim_time;
+    return GEON_OK;
+}
+
+int geon_get_sim_time(GeonHandle* h, double* sim_time) {
+    if (!h || !sim_time) return GEON_ERR_ARG;
+    *sim_time = h->simTime;
+    return GEON_OK;
+}
+
+int geon_profile(GeonHandle* h, int32_t enable, GeonProfile* out) {
+    if (!h) return GEON_ERR_ARG;
+    prof_collect(h);
+    if (out) *out = h->prof_acc;
+    if (enable) { h->prof_acc = GeonProfile{}; h->prof = true; }
+    else h->prof = false;
+    return GEON_OK;
+}
+
+int geon_fp32_peak(GeonHandle* h, double* tflops) {
+    if (!h || !tflops) return GEON_ERR_ARG;
+    int dev = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int threads = 256, blocks = sms * 8, iters = 2048;
+    float* dummy = h->hist_age;
+    cudaEvent_t a = get_event(h), b = get_event(h);
+    fma_peak_kernel<<<blocks, threads, 0, h->st>>>(dummy, 64, 0.999999f, 1e-7f);   // warm-up
+    double best = 0.0;
+    for (int rep = 0; rep < 3; rep++) {
+        cudaEventRecord(a, h->st);
+        fma_peak_kernel<<<blocks, threads, 0, h->st>>>(dummy, iters, 0.999999f, 1e-7f);
+        cudaEventRecord(b, h->st);
+        CK(cudaEventSynchronize(b));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        const double flops = 2.0 * 8 * 16 * (double)iters * threads * blocks;
+        best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    }
+    h->ev_pool.push_back(a);
+    h->ev_pool.push_back(b);
+    h->lc.add(4);
+    *tflops = best;
+    return GEON_OK;
+}
+
+int geon_get_stream(GeonHandle* h, void** stream) {
+    if (!h || !stream) return GEON_ERR_ARG;
+    *stream = (void*)h->st;
+    return GEON_OK;
+}
+
+int geon_launch_count(GeonHandle* h, int64_t* count) {
+    if (!h || !count) return GEON_ERR_ARG;
+    *count = h->lc.n;
+    return GEON_OK;
+}
+
+}  // extern "C"

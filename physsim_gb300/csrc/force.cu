@@ -1,0 +1,1207 @@
+// force.cu — pairwise force accumulation: Barnes-Hut walk, O(N^2) pairwise
+// sum, and the 1PN-only passes used by the velocity-Verlet correction.
+//
+// Physics restated from the reference CPU path:
+//   pairForce          src/forces.js:163-442
+//   computeAllForces   src/forces.js:61-154 (moment caching :71-76, Yukawa
+//                      cutoff :82-83, pairwise loop :94-125)
+//   calculateForce     src/forces.js:622-694 (BH walk)
+//   _accum1PN / _compute1PNTreeWalk / compute1PN   src/forces.js:445-610
+//   getDelayedState    src/signal-delay.js:16-221
+//   external fields    src/integrator.js:563-593
+//   bounce walls       src/integrator.js:607-668
+//
+// Arithmetic is FP32.  Per-particle sums use partial sums flushed every 16
+// terms into compensated (hi, lo) accumulators.  Decisions that switch terms
+// on or off -- the opening test size^2 < theta^2 d^2 and the Yukawa cutoff
+// r^2 < (6/mu)^2 -- are re-evaluated in FP64 from the exact inputs when the
+// FP32 margin is within rounding, so the set of interactions matches the
+// FP64 reference.
+//
+// Walk: one warp per 32 particles taken in Morton order.  The warp shares a
+// stack of (node, lane mask) entries in shared memory; each lane applies its
+// own opening test and a ballot splits the mask into lanes that accept the
+// aggregate and lanes that descend, so every particle sees exactly the
+// interaction list of the reference's per-particle walk while node records
+// are fetched once per warp.
+#include "force.cuh"
+
+namespace geon {
+
+constexpr int WALK_THREADS = 128;
+constexpr int WALK_WARPS = WALK_THREADS / 32;
+constexpr int FLUSH_EVERY = 16;
+
+// ---- accumulators -----------------------------------------------------------
+enum { Q_FX = 0, Q_FY, Q_TID, Q_PE, Q_NBASE };
+enum { M_BZ = 0, M_BGZ, M_DBZX, M_DBZY, M_DBGZX, M_DBGZY, M_FD, M_F1X, M_F1Y, M_N };
+enum { K_GX = 0, K_GY, K_CX, K_CY, K_MX, K_MY, K_GMX, K_GMY, K_YX, K_YY, K_N };
+
+template <bool MAGGM, bool BRK>
+struct Acc {
+    static constexpr int QM = Q_NBASE;
+    static constexpr int QK = Q_NBASE + (MAGGM ? M_N : 0);
+    static constexpr int NQ = QK + (BRK ? K_N : 0);
+    float part[NQ], hi[NQ], lo[NQ];
+    int cnt;
+    __device__ __forceinline__ void init() {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) { part[q] = 0.f; hi[q] = 0.f; lo[q] = 0.f; }
+        cnt = 0;
+    }
+    __device__ __forceinline__ void flush() {
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+            df s = two_sum(hi[q], part[q]);
+            hi[q] = s.hi;
+            lo[q] = __fadd_rn(lo[q], s.lo);
+            part[q] = 0.f;
+        }
+    }
+    __device__ __forceinline__ void tick() {
+        if (++cnt >= FLUSH_EVERY) { flush(); cnt = 0; }
+    }
+    __device__ __forceinline__ float get(int q) const { return __fadd_rn(hi[q], lo[q]); }
+    __device__ __forceinline__ void add(int q, float v) { part[q] = __fadd_rn(part[q], v); }
+    __device__ __forceinline__ void addm(int q, float v) { if (MAGGM) add(QM + q, v); }
+    __device__ __forceinline__ void addk(int q, float v) { if (BRK) add(QK + q, v); }
+};
+
+// ---- target particle ---------------------------------------------------------------
+struct Tgt {
+    float x, y, xlo, ylo, vx, vy, m, q, angVel, mu, L, r, r2, ri5;
+    int idx;
+    __device__ __forceinline__ double xd() const { return (double)x + (double)xlo; }
+    __device__ __forceinline__ double yd() const { return (double)y + (double)ylo; }
+};
+
+__device__ __forceinline__ Tgt load_target(const DevState& S, int i) {
+    Tgt t;
+    const float4 p = S.pos[i], v = S.vel[i], s = S.spin[i];
+    const float2 lo = S.pos_lo[i];
+    t.x = p.x; t.y = p.y; t.xlo = lo.x; t.ylo = lo.y; t.m = p.z; t.q = p.w;
+    t.vx = v.z; t.vy = v.w;
+    t.angVel = s.y;
+    t.r = s.z;
+    t.r2 = s.z * s.z;                                   // bodyRadiusSq
+    t.mu = MAG_MOMENT_K * t.q * t.angVel * t.r2;        // forces.js:74
+    t.L = INERTIA_K * t.m * t.angVel * t.r2;            // forces.js:75
+    t.ri5 = t.r2 * t.r2 * sqrtf(t.r2);                  // forces.js:437-438
+    t.idx = i;
+    return t;
+}
+
+__device__ __forceinline__ bool on(const DevParams& P, uint32_t bit) { return (P.toggles & bit) != 0; }
+
+// ---- pairForce (forces.js:163-442) ----------------------------------------------------
+template <bool MAGGM, bool BRK>
+__device__ __forceinline__ void pair_force(const DevParams& P, const Tgt& t, float rx, float ry,
+                                           float svx, float svy, float sm, float sq, float sAngVel,
+                                           float sMu, float sL, bool delayed, bool yukIn, bool pe,
+                                           Acc<MAGGM, BRK>& A) {
+    const float rawRSq = __fmaf_rn(rx, rx, ry * ry);
+    const float rSq = rawRSq + P.softSq;
+    const float invR = rsqrtf(rSq);
+    const float invRSq = invR * invR;
+    const float invR3 = invR * invRSq;
+    const float invR5 = invR3 * invRSq;
+    float aberr = 1.f;
+    if (delayed) {                                                   // forces.js:182-187
+        const float nDotV = -(rx * svx + ry * svy) * invR;
+        const float denom = fmaxf(1.f - nDotV, 0.01f);
+        aberr = fminf(1.f / (denom * denom * denom), 100.f);
+    }
+    const float invR3a = invR3 * aberr;
+    const float invR5a = invR5 * aberr;
+    const bool grav = on(P, GEON_GRAVITY), coul = on(P, GEON_COULOMB);
+
+    if (grav) {                                                      // forces.js:205-220
+        const float k = t.m * sm;
+        const float fDir = k * invR3a;
+        A.add(Q_FX, rx * fDir); A.add(Q_FY, ry * fDir);
+        A.addk(K_GX, rx * fDir); A.addk(K_GY, ry * fDir);
+        if (pe) A.add(Q_PE, -k * invR);
+    }
+    if (coul) {                                                      // forces.js:225-240
+        const float k = -(t.q * sq);
+        const float fDir = k * invR3a;
+        A.add(Q_FX, rx * fDir); A.add(Q_FY, ry * fDir);
+        A.addk(K_CX, rx * fDir); A.addk(K_CY, ry * fDir);
+        if (pe) A.add(Q_PE, t.q * sq * invR);
+    }
+    if (MAGGM) {
+        const bool mag = on(P, GEON_MAGNETIC), gm = on(P, GEON_GRAVITOMAG), pn = on(P, GEON_ONE_PN);
+        const float crossSV = svx * ry - svy * rx;
+        if (pn && (gm || mag)) {                                     // forces.js:242-298
+            const float r = rSq * invR;
+            const float nx = rx * invR, ny = ry * invR;
+            const float v1DotV2 = t.vx * svx + t.vy * svy;
+            if (gm) {
+                const float v1Sq = t.vx * t.vx + t.vy * t.vy, v2Sq = svx * svx + svy * svy;
+                const float nDotV1 = nx * t.vx + ny * t.vy, nDotV2 = nx * svx + ny * svy;
+                const float radial = -v1Sq - 2.f * v2Sq + 1.5f * nDotV2 * nDotV2 + 5.f * t.m * invR + 4.f * sm * invR;
+                const float v1Coeff = 4.f * nDotV1 - 3.f * nDotV2, v2Coeff = 3.f * nDotV2;
+                const float base = t.m * sm * invR3;
+                const float fx = base * (rx * radial + (t.vx * v1Coeff + svx * v2Coeff) * r);
+                const float fy = base * (ry * radial + (t.vy * v1Coeff + svy * v2Coeff) * r);
+                A.add(Q_FX, fx); A.add(Q_FY, fy);
+                A.addm(M_F1X, fx); A.addm(M_F1Y, fy);
+                if (pe) A.add(Q_PE, -t.m * sm * invR * (1.5f * (v1Sq + v2Sq) - 3.5f * v1DotV2 - 0.5f * nDotV1 * nDotV2
+                                                        + t.m * invR + sm * invR));
+            }
+            if (mag) {
+                const float v2DotN = svx * nx + svy * ny, v1DotN = t.vx * nx + t.vy * ny;
+                const float coeff = 0.5f * t.q * sq * invRSq;
+                const float symX = coeff * (t.vx * v2DotN - 3.f * nx * v1DotN * v2DotN);
+                const float symY = coeff * (t.vy * v2DotN - 3.f * ny * v1DotN * v2DotN);
+                A.add(Q_FX, symX); A.add(Q_FY, symY);
+                A.addm(M_F1X, symX); A.addm(M_F1Y, symY);
+                if (pe) A.add(Q_PE, -0.5f * t.q * sq * invR * (v1DotV2 + v1DotN * v2DotN));
+            }
+        }
+        if (pn && gm && mag) {                                       // forces.js:300-316
+            const float crossCoeff = t.q * sq * (t.m + sm) - (t.q * t.q * sm + sq * sq * t.m);
+            const float fDir = crossCoeff * invRSq * invRSq;
+            A.add(Q_FX, rx * fDir); A.add(Q_FY, ry * fDir);
+            A.addm(M_F1X, rx * fDir); A.addm(M_F1Y, ry * fDir);
+            if (pe) A.add(Q_PE, 0.5f * crossCoeff * invRSq);
+        }
+        if (mag) {                                                   // forces.js:318-349
+            const float fDir = -3.f * (t.mu * sMu) * invR5a;
+            A.add(Q_FX, rx * fDir); A.add(Q_FY, ry * fDir);
+            A.addk(K_MX, rx * fDir); A.addk(K_MY, ry * fDir);
+            if (pe) A.add(Q_PE, (t.mu * sMu) * invR3);
+            const float BzMoving = sq * crossSV * invR3;
+            A.addm(M_BZ, BzMoving - sMu * invR3);
+            A.addm(M_DBZX, 3.f * BzMoving * rx * invRSq + sq * svy * invR3 - 3.f * sMu * rx * invR5);
+            A.addm(M_DBZY, 3.f * BzMoving * ry * invRSq - sq * svx * invR3 - 3.f * sMu * ry * invR5);
+        }
+        if (gm) {                                                    // forces.js:351-384
+            const float fDir = 3.f * (t.L * sL) * invR5a;
+            A.add(Q_FX, rx * fDir); A.add(Q_FY, ry * fDir);
+            A.addk(K_GMX, rx * fDir); A.addk(K_GMY, ry * fDir);
+            if (pe) A.add(Q_PE, -(t.L * sL) * invR3);
+            const float BgzMoving = -sm * crossSV * invR3;
+            A.addm(M_BGZ, BgzMoving - 2.f * sL * invR3);
+            A.addm(M_DBGZX, 3.f * BgzMoving * rx * invRSq - sm * svy * invR3 - 6.f * sL * rx * invR5);
+            A.addm(M_DBGZY, 3.f * BgzMoving * ry * invRSq + sm * svx * invR3 - 6.f * sL * ry * invR5);
+            A.addm(M_FD, 2.f * sL * (sAngVel - t.angVel) * invR3);
+        }
+    }
+    if (yukIn) {                                                     // forces.js:387-426
+        const float mu = P.yukMu;
+        const float r = rSq * invR;
+        const float expMuR = __expf(-mu * r);
+        const float g = YUKAWA_COUPLING * t.m * sm * expMuR;
+        const float fDir = g * (invRSq + mu * invR) * (invR * aberr);
+        A.add(Q_FX, rx * fDir); A.add(Q_FY, ry * fDir);
+        A.addk(K_YX, rx * fDir); A.addk(K_YY, ry * fDir);
+        if (pe) A.add(Q_PE, -g * invR);
+        if (MAGGM && on(P, GEON_ONE_PN)) {
+            const float nx = rx * invR, ny = ry * invR;
+            const float nDotV1 = nx * t.vx + ny * t.vy, nDotV2 = nx * svx + ny * svy;
+            const float v1DotV2 = t.vx * svx + t.vy * svy;
+            const float alpha = 1.f + mu * r;
+            const float beta = 0.5f * g * invRSq;
+            const float radial = -(alpha * v1DotV2 + (alpha * alpha + alpha + 1.f) * nDotV1 * nDotV2);
+            const float fx = beta * (radial * nx + alpha * (nDotV2 * t.vx + nDotV1 * svx));
+            const float fy = beta * (radial * ny + alpha * (nDotV2 * t.vy + nDotV1 * svy));
+            A.add(Q_FX, fx); A.add(Q_FY, fy);
+            A.addm(M_F1X, fx); A.addm(M_F1Y, fy);
+            if (pe) A.add(Q_PE, 0.5f * g * invR * (v1DotV2 + nDotV1 * nDotV2 * alpha));
+        }
+    }
+    if (grav) {                                                      // forces.js:428-441
+        const float crossRV = rx * (svy - t.vy) - ry * (svx - t.vx);
+        const float wOrbit = crossRV * invRSq;
+        const float dw = t.angVel - wOrbit;
+        float coupling = sm;
+        if (coul && t.m > EPS_F) coupling += t.q * sq / t.m;
+        const float invR6 = invRSq * invRSq * invRSq;
+        A.add(Q_TID, -TIDAL_STRENGTH * coupling * coupling * t.ri5 * invR6 * dw);
+    }
+    A.tick();
+}
+
+// ---- exact (FP64) displacement helpers for guard-band re-tests --------------------------
+__device__ __forceinline__ void exact_disp(const DevParams& P, double ox, double oy, double sx, double sy,
+                                           double& rx, double& ry) {
+    if (P.periodic) min_image_d(ox, oy, sx, sy, P.topology, P.Wd, P.Hd, rx, ry);
+    else { rx = sx - ox; ry = sy - oy; }
+}
+
+__device__ __forceinline__ bool yukawa_in(const DevParams& P, float rx, float ry, double sxd, double syd,
+                                          double oxd, double oyd) {
+    if (!P.yukOn) return false;
+    const float rr = __fmaf_rn(rx, rx, ry * ry);
+    const float cut = P.yukCutSq;
+    if (fabsf(rr - cut) > 1e-6f * cut) return rr < cut;
+    double dx, dy;
+    exact_disp(P, oxd, oyd, sxd, syd, dx, dy);
+    return dx * dx + dy * dy < P.yukCutSqD;
+}
+
+// Displacement from the target to the image (code) of a particle at
+// (x + xlo, y + ylo).  sxd/syd receive the image position in FP64.
+__device__ __forceinline__ void image_disp(const DevParams& P, const Tgt& t, float x, float y, float xlo, float ylo,
+                                           uint32_t code, float& rx, float& ry, double& sxd, double& syd) {
+    if (code == CODE_IDENTITY) {
+        sxd = (double)x + (double)xlo; syd = (double)y + (double)ylo;
+        displacement(P, t.x, t.y, x, xlo - t.xlo, y, ylo - t.ylo, rx, ry);
+        return;
+    }
+    image_pos_d((double)x + (double)xlo, (double)y + (double)ylo, code, P.Wd, P.Hd, sxd, syd);
+    if (!code_mx(code) && !code_my(code) && P.topology == GEON_TORUS) {
+        const int sx = code_sx(code), sy = code_sy(code);
+        df ix = sx ? two_sum(x, sx * P.W) : df{ x, 0.f };
+        df iy = sy ? two_sum(y, sy * P.H) : df{ y, 0.f };
+        ix.lo = __fadd_rn(ix.lo, sx * P.W_lo + (xlo - t.xlo));
+        iy.lo = __fadd_rn(iy.lo, sy * P.H_lo + (ylo - t.ylo));
+        displacement(P, t.x, t.y, ix.hi, ix.lo, iy.hi, iy.lo, rx, ry);
+    } else {
+        double dx, dy;
+        exact_disp(P, t.xd(), t.yd(), sxd, syd, dx, dy);
+        rx = (float)dx; ry = (float)dy;
+    }
+}
+
+// ---- signal delay (signal-delay.js:16-221) ----------------------------------------------
+struct Delayed { float x, y, vx, vy, angw; };
+
+__device__ bool delayed_state(const DevParams& P, const DevState& S, const ForceCtx& C, const float* s_age,
+                              const float* s_segdt, int j, float ox, float oy, Delayed& out) {
+    const int count = S.hist_cnt[j];
+    if (count < 2) return false;
+    const int start = (C.hist_head - count) & HIST_MASK;
+    const int newest = (C.hist_head - 1) & HIST_MASK;
+    const float timeSpan = s_age[start];
+    if (timeSpan < EPS_F) return false;
+    const float4* H = S.hist + (size_t)j * HIST_LEN;
+    const float* HA = S.hist_angw + (size_t)j * HIST_LEN;
+    float cdx, cdy;
+    {
+        const float4 hn = H[newest];
+        displacement(P, ox, oy, hn.x, 0.f, hn.y, 0.f, cdx, cdy);
+    }
+    const float distSq = cdx * cdx + cdy * cdy;
+    if (!(distSq > 4.f * timeSpan * timeSpan)) {
+        int lo = 0, hi = count - 2;
+        while (lo < hi) {                                            // :55-75
+            const int mid = (lo + hi) >> 1;
+            const int midIdx = (start + mid + 1) & HIST_MASK;
+            const float4 hm = H[midIdx];
+            float bx, by;
+            displacement(P, ox, oy, hm.x, 0.f, hm.y, 0.f, bx, by);
+            const float g = sqrtf(bx * bx + by * by) - s_age[midIdx];
+            if (g < 0.f) lo = mid + 1; else hi = mid;
+        }
+        const int center = lo;
+        for (int off = 0; off <= 1; off++) {                         // :80-159
+            for (int dir = (off == 0 ? 1 : -1); dir <= 1; dir += 2) {
+                const int k = center + off * dir;
+                if (k < 0 || k > count - 2) continue;
+                const int loIdx = (start + k) & HIST_MASK;
+                const int hiIdx = (loIdx + 1) & HIST_MASK;
+                const float segDt = s_segdt[loIdx];
+                if (segDt < EPS_F) continue;
+                const float4 hl = H[loIdx], hh = H[hiIdx];
+                float dx, dy, sgx, sgy;
+                displacement(P, ox, oy, hl.x, 0.f, hl.y, 0.f, dx, dy);
+                if (P.periodic) displacement(P, hl.x, hl.y, hh.x, 0.f, hh.y, 0.f, sgx, sgy);
+                else { sgx = hh.x - hl.x; sgy = hh.y - hl.y; }
+                const float vx = sgx / segDt, vy = sgy / segDt;
+                const float rSq = dx * dx + dy * dy, vSq = vx * vx + vy * vy, dDotV = dx * vx + dy * vy;
+                const float T = s_age[loIdx];
+                const float a = vSq - 1.f, h = dDotV + T, c = rSq - T * T;
+                const float disc = h * h - a * c;
+                if (!(disc >= 0.f)) continue;
+                const float sqrtDisc = sqrtf(disc);
+                float s;
+                if (fabsf(a) < EPS_F) {
+                    if (fabsf(h) < EPS_F) continue;
+                    s = -c / (2.f * h);
+                } else {
+                    const float s1 = (-h + sqrtDisc) / a, s2 = (-h - sqrtDisc) / a;
+                    const bool ok1 = s1 >= -EPS_F && s1 <= segDt + EPS_F;
+                    const bool ok2 = s2 >= -EPS_F && s2 <= segDt + EPS_F;
+                    if (ok1 && ok2) s = fmaxf(s1, s2);
+                    else if (ok1) s = s1;
+                    else if (ok2) s = s2;
+                    else continue;
+                }
+                if (s < 0.f) s = 0.f; else if (s > segDt) s = segDt;
+                const float frac = s / segDt;
+                out.x = hl.x + frac * sgx;
+                out.y = hl.y + frac * sgy;
+                out.vx = hl.z + frac * (hh.z - hl.z);
+                out.vy = hl.w + frac * (hh.w - hl.w);
+                const float al = HA[loIdx];
+                out.angw = al + frac * (HA[hiIdx] - al);
+                return true;
+            }
+        }
+    }
+    {                                                                // :166-220
+        const float4 hs = H[start];
+        float dx, dy;
+        displacement(P, ox, oy, hs.x, 0.f, hs.y, 0.f, dx, dy);
+        const float vx = hs.z, vy = hs.w;
+        const float rSq = dx * dx + dy * dy, vSq = vx * vx + vy * vy, dDotV = dx * vx + dy * vy;
+        const float T = timeSpan;
+        const float a = vSq - 1.f, h = dDotV + T, c = rSq - T * T;
+        const float disc = h * h - a * c;
+        if (!(disc >= 0.f)) return false;
+        const float sqrtDisc = sqrtf(disc);
+        float s;
+        if (fabsf(a) < EPS_F) {
+            if (fabsf(h) < EPS_F) return false;
+            s = -c / (2.f * h);
+        } else {
+            const float s1 = (-h + sqrtDisc) / a, s2 = (-h - sqrtDisc) / a;
+            const bool ok1 = s1 <= EPS_F, ok2 = s2 <= EPS_F;
+            if (ok1 && ok2) s = fmaxf(s1, s2);
+            else if (ok1) s = s1;
+            else if (ok2) s = s2;
+            else return false;
+        }
+        if (s > 0.f) s = 0.f;
+        if (C.hist_t[start] + (double)s < S.ctime[j]) return false;
+        out.x = hs.x + vx * s;
+        out.y = hs.y + vy * s;
+        out.vx = vx; out.vy = vy;
+        out.angw = HA[start];
+        return true;
+    }
+}
+
+// Displacement to a delayed source; ghosts add their current image offset
+// (forces.js:656-661).
+__device__ __forceinline__ void delayed_disp(const DevParams& P, const Tgt& t, const Delayed& d,
+                                             float xj, float yj, uint32_t code, float& rx, float& ry,
+                                             double& sxd, double& syd) {
+    if (code == CODE_IDENTITY) {
+        sxd = d.x; syd = d.y;
+        displacement(P, t.x, t.y, d.x, -t.xlo, d.y, -t.ylo, rx, ry);
+        return;
+    }
+    double gx, gy;
+    image_pos_d((double)xj, (double)yj, code, P.Wd, P.Hd, gx, gy);
+    sxd = (double)d.x + (gx - (double)xj);
+    syd = (double)d.y + (gy - (double)yj);
+    if (!code_mx(code) && !code_my(code) && P.topology == GEON_TORUS) {
+        const int sx = code_sx(code), sy = code_sy(code);
+        df ix = sx ? two_sum(d.x, sx * P.W) : df{ d.x, 0.f };
+        df iy = sy ? two_sum(d.y, sy * P.H) : df{ d.y, 0.f };
+        ix.lo = __fadd_rn(ix.lo, sx * P.W_lo - t.xlo);
+        iy.lo = __fadd_rn(iy.lo, sy * P.H_lo - t.ylo);
+        displacement(P, t.x, t.y, ix.hi, ix.lo, iy.hi, iy.lo, rx, ry);
+    } else {
+        double dx, dy;
+        exact_disp(P, t.xd(), t.yd(), sxd, syd, dx, dy);
+        rx = (float)dx; ry = (float)dy;
+    }
+}
+
+// ---- epilogue: outputs, external fields, walls, planner reductions -------------------------
+template <bool MAGGM, bool BRK>
+__device__ __forceinline__ void finalize_target(const DevParams& P, const DevState& S, const ForceCtx& C,
+                                                FrameCtl* ctl, const Tgt& t, bool valid, Acc<MAGGM, BRK>& A,
+                                                unsigned long long inter) {
+    A.flush();
+    double aSq = 0.0, wc = 0.0;
+    if (valid) {
+        float fx = A.get(Q_FX), fy = A.get(Q_FY);
+        float Bz = MAGGM ? A.get(A.QM + M_BZ) : 0.f, Bgz = MAGGM ? A.get(A.QM + M_BGZ) : 0.f;
+        float ex = 0.f, ey = 0.f, contact = 0.f;
+        if (P.extGx != 0.f || P.extGy != 0.f) { ex += t.m * P.extGx; ey += t.m * P.extGy; }   // integrator.js:575-581
+        if (P.extEx != 0.f || P.extEy != 0.f) { ex += t.q * P.extEx; ey += t.q * P.extEy; }
+        if (P.extBz != 0.f) Bz += P.extBz;
+        if (C.bounce) {                                              // integrator.js:607-668
+            const float r = t.r, fr = P.friction;
+            const float left = (float)P.offXd, top = (float)P.offYd;
+            const float right = (float)(P.offXd + P.Wd), bottom = (float)(P.offYd + P.Hd);
+            auto clamp1 = [](float v) { return fminf(1.f, fmaxf(-1.f, v)); };
+            float delta = r - (t.x - left);
+            if (delta > 0.f) {
+                const float Fn = delta * sqrtf(delta);
+                ex += Fn;
+                if (fr > 0.f) { const float Ft = -fr * Fn * clamp1((t.vy + t.angVel * r) * 10.f); fy += Ft; contact += r * Ft; }
+            }
+            delta = r - (right - t.x);
+            if (delta > 0.f) {
+                const float Fn = delta * sqrtf(delta);
+                ex -= Fn;
+                if (fr > 0.f) { const float Ft = -fr * Fn * clamp1((-t.vy - t.angVel * r) * 10.f); fy -= Ft; contact -= r * Ft; }
+            }
+            delta = r - (t.y - top);
+            if (delta > 0.f) {
+                const float Fn = delta * sqrtf(delta);
+                ey += Fn;
+                if (fr > 0.f) { const float Ft = -fr * Fn * clamp1((-t.vx + t.angVel * r) * 10.f); fx -= Ft; contact += r * Ft; }
+            }
+            delta = r - (bottom - t.y);
+            if (delta > 0.f) {
+                const float Fn = delta * sqrtf(delta);
+                ey -= Fn;
+                if (fr > 0.f) { const float Ft = -fr * Fn * clamp1((t.vx - t.angVel * r) * 10.f); fx += Ft; contact -= r * Ft; }
+            }
+        }
+        fx += ex; fy += ey;
+        const int i = t.idx;
+        S.force[i] = make_float4(fx, fy, Bz, Bgz);
+        if (MAGGM) {
+            S.grad[i] = make_float4(A.get(A.QM + M_DBZX), A.get(A.QM + M_DBZY), A.get(A.QM + M_DBGZX), A.get(A.QM + M_DBGZY));
+            S.f1pn[i] = make_float2(A.get(A.QM + M_F1X), A.get(A.QM + M_F1Y));
+        } else {
+            S.grad[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            S.f1pn[i] = make_float2(0.f, 0.f);
+        }
+        S.torque[i] = make_float4(A.get(Q_TID), MAGGM ? A.get(A.QM + M_FD) : 0.f, contact, A.get(Q_PE));
+        S.mom[i] = make_float2(t.mu, t.L);
+        if (BRK) {
+            const int cap = P.n_cap;
+            float* b = S.brk;
+#pragma unroll
+            for (int q = 0; q < K_N; q++) b[(size_t)q * cap + i] = A.get(A.QK + q);
+            b[(size_t)K_N * cap + i] = ex;
+            b[(size_t)(K_N + 1) * cap + i] = ey;
+        } else if (S.brk) {
+            const int cap = P.n_cap;
+            S.brk[(size_t)K_N * cap + i] = ex;
+            S.brk[(size_t)(K_N + 1) * cap + i] = ey;
+        }
+        // planner reductions (integrator.js:816-836)
+        const double im = (double)S.spin[i].w;
+        aSq = ((double)fx * fx + (double)fy * fy) * im * im;
+        if (on(P, GEON_MAGNETIC) || P.extBz != 0.f) {
+            const double absBz = fabs((double)Bz);
+            if (absBz > 0) wc = fmax(wc, fabs((double)t.q) * absBz * im);
+        }
+        if (on(P, GEON_GRAVITOMAG)) {
+            const double absBgz = fabs((double)Bgz);
+            if (absBgz > 0) wc = fmax(wc, 4.0 * absBgz);
+        }
+        if (!(aSq == aSq)) aSq = 0.0;
+        if (!(wc == wc)) wc = 0.0;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        aSq = fmax(aSq, __shfl_xor_sync(0xffffffffu, aSq, o));
+        wc = fmax(wc, __shfl_xor_sync(0xffffffffu, wc, o));
+        inter += __shfl_xor_sync(0xffffffffu, inter, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomic_max_pos_double(&ctl->maxAccelSqBits, aSq);
+        atomic_max_pos_double(&ctl->maxCycBits, wc);
+        if (inter) atomicAdd(&ctl->interactions, inter);
+    }
+}
+
+__device__ __forceinline__ void load_hist_tables(const ForceCtx& C, float* s_age, float* s_segdt) {
+    for (int k = threadIdx.x; k < HIST_LEN; k += blockDim.x) {
+        s_age[k] = C.hist_age[k];
+        s_segdt[k] = C.hist_segdt[k];
+    }
+    __syncthreads();
+}
+
+// ---- Barnes-Hut walk (forces.js:622-694) -----------------------------------------------------
+template <bool MAGGM, bool REL, bool BRK>
+__global__ void __launch_bounds__(WALK_THREADS)
+walk_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
+    __shared__ int s_node[WALK_WARPS][WALK_STACK];
+    __shared__ unsigned s_mask[WALK_WARPS][WALK_STACK];
+    __shared__ float s_age[REL ? HIST_LEN : 1], s_segdt[REL ? HIST_LEN : 1];
+    if (REL) load_hist_tables(C, s_age, s_segdt);
+    const int n = ctl->n;
+    const int warp = threadIdx.x >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    const int k = (blockIdx.x * WALK_WARPS + warp) * 32 + (int)lane;
+    const bool valid = k < n;
+    const unsigned active = __ballot_sync(0xffffffffu, valid);
+    if (active == 0) return;
+    Tgt t;
+    if (valid) t = load_target(S, T.tgt[k]);
+    else { t = Tgt{}; t.idx = -1; }
+    Acc<MAGGM, BRK> A;
+    A.init();
+    unsigned long long inter = 0;
+    const bool pe = C.pe != 0;
+    const int root = *d_root;
+    const bool treeOk = (ctl->err & (ERR_NODE_OVERFLOW | ERR_BAD_INDEX)) == 0;
+    const int nIntW = ctl->nInternal, nLeafW = ctl->nLeaves, nValidW = ctl->nValid;
+    int top = 0;
+    if (root != ROOT_NONE && treeOk) {
+        if (lane == 0) { s_node[warp][0] = root; s_mask[warp][0] = active; }
+        top = 1;
+    }
+    __syncwarp();
+    while (top > 0) {
+        top--;
+        const int node = s_node[warp][top];
+        const unsigned mask = s_mask[warp][top];
+        __syncwarp();
+        const bool in = (mask >> lane) & 1u;
+        if (node & LEAF_REF) {
+            const int li = node & ~LEAF_REF;
+            if (li >= nLeafW) { if (lane == 0) atomicOr(&ctl->err, ERR_BAD_INDEX); continue; }
+            const float lmass = T.leaf_a[li].z;
+            if (lmass < EPS_F) continue;                             // forces.js:630
+            const int4 lm = T.leaf_meta[li];
+            if (lm.x < 0 || lm.x + lm.y > nValidW) { if (lane == 0) atomicOr(&ctl->err, ERR_BAD_INDEX); continue; }
+            for (int q = lm.x; q < lm.x + lm.y; q++) {               // forces.js:643-679
+                const float4 pp = T.pt_pos[q];
+                const float4 pv = T.pt_vel[q];
+                const uint32_t ref = __float_as_uint(pv.w);
+                const int j = (int)ref_index(ref);
+                const uint32_t code = ref_code(ref);
+                if (!in || j == t.idx) continue;
+                float rx, ry; double sxd, syd;
+                float svx, svy, sAng, sMu, sL;
+                bool dl = false;
+                if (REL) {
+                    Delayed d;
+                    if (!delayed_state(P, S, C, s_age, s_segdt, j, t.x, t.y, d)) continue;
+                    delayed_disp(P, t, d, pp.x, pp.y, code, rx, ry, sxd, syd);
+                    svx = d.vx; svy = d.vy;
+                    const float rj = S.spin[j].z, rj2 = rj * rj;
+                    sAng = d.angw * rsqrtf(1.f + d.angw * d.angw * rj2);
+                    sMu = MAG_MOMENT_K * pp.w * sAng * rj2;
+                    sL = INERTIA_K * pp.z * sAng * rj2;
+                    dl = true;
+                } else {
+                    const float2 pl = T.pt_lo[q];
+                    image_disp(P, t, pp.x, pp.y, pl.x, pl.y, code, rx, ry, sxd, syd);
+                    const float2 pm = T.pt_mom[q];
+                    svx = pv.x; svy = pv.y; sAng = pv.z; sMu = pm.x; sL = pm.y;
+                }
+                const bool yk = yukawa_in(P, rx, ry, sxd, syd, t.xd(), t.yd());
+                pair_force<MAGGM, BRK>(P, t, rx, ry, svx, svy, pp.z, pp.w, sAng, sMu, sL, dl, yk, pe, A);
+                inter++;
+            }
+        } else {
+            if (node < 0 || node >= nIntW) { if (lane == 0) atomicOr(&ctl->err, ERR_BAD_INDEX); continue; }
+            const float4 a = T.int_a[node];
+            if (a.z < EPS_F) continue;
+            const float4 c = T.int_c[node];
+            bool accept = false;
+            float rx = 0.f, ry = 0.f;
+            if (in) {
+                displacement(P, t.x, t.y, a.x, c.x - t.xlo, a.y, c.y - t.ylo, rx, ry);
+                const float dSq = __fmaf_rn(rx, rx, ry * ry);
+                const float rhs = P.thetaSq * dSq;
+                accept = c.z < rhs;                                  // forces.js:680
+                if (fabsf(rhs - c.z) <= 1e-6f * c.z) {
+                    double dx, dy;
+                    exact_disp(P, t.xd(), t.yd(), (double)a.x + (double)c.x, (double)a.y + (double)c.y, dx, dy);
+                    const double size = 2.0 * ldexp(P.rootW, -(int)c.w);
+                    accept = size * size < P.thetaSqD * (dx * dx + dy * dy);
+                }
+            }
+            const unsigned acc = __ballot_sync(0xffffffffu, accept);
+            const unsigned open = mask & ~acc;
+            if (accept) {                                            // forces.js:682-685
+                const float4 b = T.int_b[node];
+                const bool yk = yukawa_in(P, rx, ry, (double)a.x + (double)c.x, (double)a.y + (double)c.y, t.xd(), t.yd());
+                pair_force<MAGGM, BRK>(P, t, rx, ry, b.x, b.y, a.z, a.w, 0.f, b.z, b.w, false, yk, pe, A);
+                inter++;
+            }
+            if (open) {                                              // forces.js:686-692
+                const int4 ch = T.int_child[node];
+                const int np = (ch.x >= 0) + (ch.y >= 0) + (ch.z >= 0) + (ch.w >= 0);
+                if (top + np > WALK_STACK) {
+                    if (lane == 0) atomicOr(&ctl->err, ERR_STACK_OVERFLOW);
+                } else {
+                    if (lane == 0) {
+                        int tp = top;
+                        if (ch.x >= 0) { s_node[warp][tp] = ch.x; s_mask[warp][tp++] = open; }
+                        if (ch.y >= 0) { s_node[warp][tp] = ch.y; s_mask[warp][tp++] = open; }
+                        if (ch.z >= 0) { s_node[warp][tp] = ch.z; s_mask[warp][tp++] = open; }
+                        if (ch.w >= 0) { s_node[warp][tp] = ch.w; s_mask[warp][tp++] = open; }
+                    }
+                    top += np;
+                }
+                __syncwarp();
+            }
+        }
+    }
+    finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter);
+}
+
+// ---- batched Barnes-Hut walk ----------------------------------------------------------------
+// Same interaction lists as walk_kernel, restructured for throughput:
+//  * up to 32 stack entries are popped per iteration, one per lane, so the
+//    node records are fetched with one wide load instead of 32 dependent ones;
+//  * every lane's opening test against each of those nodes runs from
+//    shuffled registers, and one ballot per node splits its lane mask;
+//  * accepted aggregates and the points of reached leaves are staged, with
+//    their lane masks, in a per-warp source list in shared memory, which is
+//    evaluated in a tight loop once it fills (all reads are broadcasts).
+constexpr int WB_THREADS = 128;
+constexpr int WB_WARPS = WB_THREADS / 32;
+constexpr int WB_STACK = 512;
+constexpr int WB_SRC = 160;
+constexpr uint32_t AGG_REF = 0xffffffffu;
+
+struct WalkSmem {
+    int stk_node[WB_STACK];
+    unsigned stk_mask[WB_STACK];
+    float4 sA[WB_SRC];       // x_hi, y_hi, mass, charge
+    float4 sB[WB_SRC];       // x_lo, y_lo, vx, vy
+    float4 sC[WB_SRC];       // angVel, mu, L, ref bits (AGG_REF for aggregates)
+    unsigned sM[WB_SRC];     // lane mask
+};
+
+__device__ __forceinline__ int warp_incl_scan_i(int v) {
+    const unsigned lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= (unsigned)o) v += t;
+    }
+    return v;
+}
+
+// Image position of sorted point q as a compensated pair (ghost shifts and mirrors applied).
+__device__ __forceinline__ void point_image(const DevParams& P, float x, float y, float xlo, float ylo, uint32_t code,
+                                            float& ix, float& ixlo, float& iy, float& iylo) {
+    if (code == CODE_IDENTITY) { ix = x; ixlo = xlo; iy = y; iylo = ylo; return; }
+    df a = code_mx(code) ? df_add(df{ P.W, P.W_lo }, df{ -x, -xlo }) : df{ x, xlo };
+    df b = code_my(code) ? df_add(df{ P.H, P.H_lo }, df{ -y, -ylo }) : df{ y, ylo };
+    const int sx = code_sx(code), sy = code_sy(code);
+    if (sx) a = df_add(a, df{ sx * P.W, sx * P.W_lo });
+    if (sy) b = df_add(b, df{ sy * P.H, sy * P.H_lo });
+    ix = a.hi; ixlo = a.lo; iy = b.hi; iylo = b.lo;
+}
+
+__device__ __forceinline__ void stage_point(const DevParams& P, const TreeBufs& T, WalkSmem& W, int e, int q, unsigned mask) {
+    const float4 pp = T.pt_pos[q];
+    const float2 pl = T.pt_lo[q];
+    const float4 pv = T.pt_vel[q];
+    const float2 pm = T.pt_mom[q];
+    const uint32_t ref = __float_as_uint(pv.w);
+    float ix, ixlo, iy, iylo;
+    point_image(P, pp.x, pp.y, pl.x, pl.y, ref_code(ref), ix, ixlo, iy, iylo);
+    W.sA[e] = make_float4(ix, iy, pp.z, pp.w);
+    W.sB[e] = make_float4(ixlo, iylo, pv.x, pv.y);
+    W.sC[e] = make_float4(pv.z, pm.x, pm.y, pv.w);
+    W.sM[e] = mask;
+}
+
+template <bool MAGGM, bool REL, bool BRK>
+__device__ __forceinline__ void eval_sources(const DevParams& P, const DevState& S, const ForceCtx& C,
+                                             const float* s_age, const float* s_segdt, const WalkSmem& W, int cnt,
+                                             const Tgt& t, Acc<MAGGM, BRK>& A, unsigned long long& inter, bool pe) {
+    const unsigned lane = threadIdx.x & 31;
+    for (int e = 0; e < cnt; e++) {
+        if (!((W.sM[e] >> lane) & 1u)) continue;
+        const float4 a = W.sA[e];
+        const float4 b = W.sB[e];
+        const float4 c = W.sC[e];
+        const uint32_t ref = __float_as_uint(c.w);
+        float rx, ry, svx, svy, sAng, sMu, sL;
+        double sxd, syd;
+        bool dl = false;
+        if (ref == AGG_REF) {
+            displacement(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
+            sxd = (double)a.x + (double)b.x; syd = (double)a.y + (double)b.y;
+            svx = b.z; svy = b.w; sAng = 0.f; sMu = c.y; sL = c.z;
+        } else {
+            const int j = (int)ref_index(ref);
+            if (j == t.idx) continue;                                 // self and own ghosts (forces.js:648-649)
+            if (REL) {
+                Delayed d;
+                if (!delayed_state(P, S, C, s_age, s_segdt, j, t.x, t.y, d)) continue;
+                const uint32_t code = ref_code(ref);
+                float xj = 0.f, yj = 0.f;
+                if (code != CODE_IDENTITY && (code_mx(code) || code_my(code) || P.topology != GEON_TORUS)) {
+                    const float4 pj = S.pos[j];
+                    xj = pj.x; yj = pj.y;
+                }
+                delayed_disp(P, t, d, xj, yj, code, rx, ry, sxd, syd);
+                svx = d.vx; svy = d.vy;
+                const float rj = S.spin[j].z, rj2 = rj * rj;
+                sAng = d.angw * rsqrtf(1.f + d.angw * d.angw * rj2);
+                sMu = MAG_MOMENT_K * a.w * sAng * rj2;
+                sL = INERTIA_K * a.z * sAng * rj2;
+                dl = true;
+            } else {
+                displacement(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
+                sxd = (double)a.x + (double)b.x; syd = (double)a.y + (double)b.y;
+                svx = b.z; svy = b.w; sAng = c.x; sMu = c.y; sL = c.z;
+            }
+        }
+        const bool yk = yukawa_in(P, rx, ry, sxd, syd, t.xd(), t.yd());
+        pair_force<MAGGM, BRK>(P, t, rx, ry, svx, svy, a.z, a.w, sAng, sMu, sL, dl, yk, pe, A);
+        inter++;
+    }
+}
+
+template <bool MAGGM, bool REL, bool BRK>
+__global__ void __launch_bounds__(WB_THREADS)
+walkb_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
+    extern __shared__ __align__(16) unsigned char wb_smem[];
+    WalkSmem* Wall = reinterpret_cast<WalkSmem*>(wb_smem);
+    float* s_age = reinterpret_cast<float*>(Wall + WB_WARPS);
+    float* s_segdt = s_age + HIST_LEN;
+    if (REL) load_hist_tables(C, s_age, s_segdt);
+    const int n = ctl->n;
+    const int warp = threadIdx.x >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    WalkSmem& W = Wall[warp];
+    const int k0 = (blockIdx.x * WB_WARPS + warp) * 32 + (int)lane;
+    const bool valid = k0 < n;
+    const unsigned active = __ballot_sync(0xffffffffu, valid);
+    if (active == 0) return;
+    Tgt t;
+    if (valid) t = load_target(S, T.tgt[k0]);
+    else { t = Tgt{}; t.idx = -1; }
+    Acc<MAGGM, BRK> A;
+    A.init();
+    unsigned long long inter = 0;
+    const bool pe = C.pe != 0;
+    const int root = *d_root;
+    const bool treeOk = (ctl->err & (ERR_NODE_OVERFLOW | ERR_BAD_INDEX)) == 0;
+    const int nIntW = ctl->nInternal, nLeafW = ctl->nLeaves, nValidW = ctl->nValid;
+    const unsigned lt = lanemask_lt();
+    int top = 0, cnt = 0;
+    if (root != ROOT_NONE && treeOk) {
+        if (lane == 0) { W.stk_node[0] = root; W.stk_mask[0] = active; }
+        top = 1;
+    }
+    __syncwarp();
+    while (top > 0) {
+        // popping k entries and pushing up to 4 children each must fit the stack
+        const int k = min(min(32, top), (WB_STACK - top) / 3);
+        if (k <= 0) { if (lane == 0) atomicOr(&ctl->err, ERR_STACK_OVERFLOW); break; }
+        int node = -1;
+        unsigned mask = 0;
+        if ((int)lane < k) { node = W.stk_node[top - k + lane]; mask = W.stk_mask[top - k + lane]; }
+        __syncwarp();
+        top -= k;
+        // fetch the popped node records, one per lane
+        bool isLeaf = false, skip = true;
+        float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nc = make_float4(0.f, 0.f, 0.f, 0.f);
+        int4 lm = make_int4(0, 0, 0, 0);
+        if (node >= 0) {
+            if (node & LEAF_REF) {
+                const int li = node & ~LEAF_REF;
+                if (li < nLeafW) {
+                    isLeaf = true;
+                    lm = T.leaf_meta[li];
+                    na.z = T.leaf_a[li].z;
+                    skip = na.z < EPS_F || lm.x < 0 || lm.x + lm.y > nValidW;
+                } else atomicOr(&ctl->err, ERR_BAD_INDEX);
+            } else if (node < nIntW) {
+                na = T.int_a[node];
+                nc = T.int_c[node];
+                skip = na.z < EPS_F;                                  // forces.js:630
+            } else atomicOr(&ctl->err, ERR_BAD_INDEX);
+        }
+        // per-lane opening tests against each popped internal node (forces.js:680)
+        unsigned myAcc = 0, myOpen = 0;
+        const unsigned testMask = __ballot_sync(0xffffffffu, !skip && !isLeaf);
+        for (unsigned tm = testMask; tm; tm &= tm - 1) {
+            const int jj = __ffs(tm) - 1;
+            const float cx = __shfl_sync(0xffffffffu, na.x, jj), cy = __shfl_sync(0xffffffffu, na.y, jj);
+            const float clx = __shfl_sync(0xffffffffu, nc.x, jj), cly = __shfl_sync(0xffffffffu, nc.y, jj);
+            const float s2 = __shfl_sync(0xffffffffu, nc.z, jj), lvl = __shfl_sync(0xffffffffu, nc.w, jj);
+            const unsigned msk = __shfl_sync(0xffffffffu, mask, jj);
+            bool accept = false;
+            if ((msk >> lane) & 1u) {
+                float rx, ry;
+                displacement(P, t.x, t.y, cx, clx - t.xlo, cy, cly - t.ylo, rx, ry);
+                const float rhs = P.thetaSq * __fmaf_rn(rx, rx, ry * ry);
+                accept = s2 < rhs;
+                if (fabsf(rhs - s2) <= 1e-6f * s2) {
+                    double dx, dy;
+                    exact_disp(P, t.xd(), t.yd(), (double)cx + (double)clx, (double)cy + (double)cly, dx, dy);
+                    const double size = 2.0 * ldexp(P.rootW, -(int)lvl);
+                    accept = size * size < P.thetaSqD * (dx * dx + dy * dy);
+                }
+            }
+            const unsigned acc = __ballot_sync(0xffffffffu, accept);
+            if ((int)lane == jj) { myAcc = acc; myOpen = msk & ~acc; }
+        }
+        const unsigned leafMask = (isLeaf && !skip) ? mask : 0u;
+        const bool bucket = leafMask && lm.y > LEAF_CAP;
+        const int myPts = (leafMask && !bucket) ? lm.y : 0;
+        const unsigned aggBal = __ballot_sync(0xffffffffu, myAcc != 0);
+        const int ptsIncl = warp_incl_scan_i(myPts);
+        const int ptsTot = __shfl_sync(0xffffffffu, ptsIncl, 31);
+        if (cnt + __popc(aggBal) + ptsTot > WB_SRC) {
+            __syncwarp();
+            eval_sources<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, cnt, t, A, inter, pe);
+            __syncwarp();
+            cnt = 0;
+        }
+        if (myAcc) {                                                  // forces.js:682-685
+            const int e = cnt + __popc(aggBal & lt);
+            const float4 nb = T.int_b[node];
+            W.sA[e] = na;
+            W.sB[e] = make_float4(nc.x, nc.y, nb.x, nb.y);
+            W.sC[e] = make_float4(0.f, nb.z, nb.w, __uint_as_float(AGG_REF));
+            W.sM[e] = myAcc;
+        }
+        cnt += __popc(aggBal);
+        {                                                             // forces.js:643-679
+            const int base = cnt + ptsIncl - myPts;
+            for (int q = 0; q < myPts; q++) stage_point(P, T, W, base + q, lm.x + q, leafMask);
+            cnt += ptsTot;
+        }
+        for (unsigned bk = __ballot_sync(0xffffffffu, bucket); bk; bk &= bk - 1) {   // leaves deeper than the key
+            const int jj = __ffs(bk) - 1;
+            const int bstart = __shfl_sync(0xffffffffu, lm.x, jj), bcount = __shfl_sync(0xffffffffu, lm.y, jj);
+            const unsigned bmask = __shfl_sync(0xffffffffu, leafMask, jj);
+            for (int b0 = 0; b0 < bcount; b0 += 32) {
+                const int chunk = min(32, bcount - b0);
+                if (cnt + chunk > WB_SRC) {
+                    __syncwarp();
+                    eval_sources<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, cnt, t, A, inter, pe);
+                    __syncwarp();
+                    cnt = 0;
+                }
+                if ((int)lane < chunk) stage_point(P, T, W, cnt + lane, bstart + b0 + lane, bmask);
+                cnt += chunk;
+            }
+        }
+        // push children of the nodes some lanes must open (forces.js:686-692)
+        int4 ch = make_int4(-1, -1, -1, -1);
+        int myCh = 0;
+        if (myOpen) {
+            ch = T.int_child[node];
+            myCh = (ch.x >= 0) + (ch.y >= 0) + (ch.z >= 0) + (ch.w >= 0);
+        }
+        const int chIncl = warp_incl_scan_i(myCh);
+        const int chTot = __shfl_sync(0xffffffffu, chIncl, 31);
+        if (myCh) {
+            int pos = top + chIncl - myCh;
+            if (ch.x >= 0) { W.stk_node[pos] = ch.x; W.stk_mask[pos++] = myOpen; }
+            if (ch.y >= 0) { W.stk_node[pos] = ch.y; W.stk_mask[pos++] = myOpen; }
+            if (ch.z >= 0) { W.stk_node[pos] = ch.z; W.stk_mask[pos++] = myOpen; }
+            if (ch.w >= 0) { W.stk_node[pos] = ch.w; W.stk_mask[pos++] = myOpen; }
+        }
+        top += chTot;
+        __syncwarp();
+    }
+    __syncwarp();
+    eval_sources<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, cnt, t, A, inter, pe);
+    finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter);
+}
+
+constexpr size_t WB_SMEM = sizeof(WalkSmem) * WB_WARPS + 2 * HIST_LEN * sizeof(float);
+
+// ---- pairwise O(N^2) sum (forces.js:94-125) -------------------------------------------------
+constexpr int DIRECT_THREADS = 256;
+
+template <bool MAGGM, bool REL, bool BRK>
+__global__ void __launch_bounds__(DIRECT_THREADS)
+direct_kernel(DevParams P, DevState S, FrameCtl* ctl, ForceCtx C) {
+    __shared__ float4 s_pos[DIRECT_THREADS];
+    __shared__ float4 s_vel[DIRECT_THREADS];   // vx, vy, angVel, radius^2
+    __shared__ float2 s_lo[DIRECT_THREADS];
+    __shared__ float s_age[REL ? HIST_LEN : 1], s_segdt[REL ? HIST_LEN : 1];
+    if (REL) load_hist_tables(C, s_age, s_segdt);
+    const int n = ctl->n;
+    const int i = blockIdx.x * DIRECT_THREADS + threadIdx.x;
+    const bool valid = i < n;
+    Tgt t;
+    if (valid) t = load_target(S, i);
+    else { t = Tgt{}; t.idx = -1; }
+    Acc<MAGGM, BRK> A;
+    A.init();
+    unsigned long long inter = 0;
+    const bool pe = C.pe != 0;
+    for (int base = 0; base < n; base += DIRECT_THREADS) {
+        const int j = base + threadIdx.x;
+        __syncthreads();
+        if (j < n) {
+            const float4 sv = S.vel[j], ss = S.spin[j];
+            s_pos[threadIdx.x] = S.pos[j];
+            s_lo[threadIdx.x] = S.pos_lo[j];
+            s_vel[threadIdx.x] = make_float4(sv.z, sv.w, ss.y, ss.z * ss.z);
+        }
+        __syncthreads();
+        const int cnt = min(DIRECT_THREADS, n - base);
+        if (!valid) continue;
+        for (int jj = 0; jj < cnt; jj++) {
+            const int jg = base + jj;
+            if (jg == i) continue;
+            const float4 sp = s_pos[jj];
+            const float4 sv = s_vel[jj];
+            float rx, ry; double sxd, syd;
+            float svx, svy, sAng;
+            bool dl = false;
+            if (REL) {
+                Delayed d;
+                if (!delayed_state(P, S, C, s_age, s_segdt, jg, t.x, t.y, d)) continue;
+                sxd = d.x; syd = d.y;
+                displacement(P, t.x, t.y, d.x, -t.xlo, d.y, -t.ylo, rx, ry);
+                svx = d.vx; svy = d.vy;
+                sAng = d.angw * rsqrtf(1.f + d.angw * d.angw * sv.w);
+                dl = true;
+            } else {
+                const float2 sl = s_lo[jj];
+                sxd = (double)sp.x + (double)sl.x; syd = (double)sp.y + (double)sl.y;
+                displacement(P, t.x, t.y, sp.x, sl.x - t.xlo, sp.y, sl.y - t.ylo, rx, ry);
+                svx = sv.x; svy = sv.y; sAng = sv.z;
+            }
+            const float sMu = MAG_MOMENT_K * sp.w * sAng * sv.w;
+            const float sL = INERTIA_K * sp.z * sAng * sv.w;
+            const bool yk = yukawa_in(P, rx, ry, sxd, syd, t.xd(), t.yd());
+            pair_force<MAGGM, BRK>(P, t, rx, ry, svx, svy, sp.z, sp.w, sAng, sMu, sL, dl, yk, pe, A);
+            inter++;
+        }
+    }
+    finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter);
+}
+
+// ---- 1PN-only passes (forces.js:445-610) ----------------------------------------------------
+__device__ __forceinline__ void accum_1pn(const DevParams& P, const Tgt& t, float rx, float ry, float svx, float svy,
+                                          float sm, float sq, float& ox, float& oy) {
+    const float rSq = __fmaf_rn(rx, rx, ry * ry) + P.softSq;
+    const float invR = rsqrtf(rSq);
+    const float invRSq = invR * invR;
+    const float r = rSq * invR;
+    const float nx = rx * invR, ny = ry * invR;
+    const bool gm = on(P, GEON_GRAVITOMAG), mag = on(P, GEON_MAGNETIC);
+    if (gm) {
+        const float v1Sq = t.vx * t.vx + t.vy * t.vy, v2Sq = svx * svx + svy * svy;
+        const float nDotV1 = nx * t.vx + ny * t.vy, nDotV2 = nx * svx + ny * svy;
+        const float radial = -v1Sq - 2.f * v2Sq + 1.5f * nDotV2 * nDotV2 + 5.f * t.m * invR + 4.f * sm * invR;
+        const float v1Coeff = 4.f * nDotV1 - 3.f * nDotV2, v2Coeff = 3.f * nDotV2;
+        const float base = t.m * sm * invRSq * invR;
+        ox += base * (rx * radial + (t.vx * v1Coeff + svx * v2Coeff) * r);
+        oy += base * (ry * radial + (t.vy * v1Coeff + svy * v2Coeff) * r);
+    }
+    if (mag) {
+        const float v2DotN = svx * nx + svy * ny, v1DotN = t.vx * nx + t.vy * ny;
+        const float coeff = 0.5f * t.q * sq * invRSq;
+        ox += coeff * (t.vx * v2DotN - 3.f * nx * v1DotN * v2DotN);
+        oy += coeff * (t.vy * v2DotN - 3.f * ny * v1DotN * v2DotN);
+    }
+    if (gm && mag) {
+        const float crossCoeff = t.q * sq * (t.m + sm) - (t.q * t.q * sm + sq * sq * t.m);
+        const float fDir = crossCoeff * invRSq * invRSq;
+        ox += rx * fDir; oy += ry * fDir;
+    }
+    if (on(P, GEON_YUKAWA)) {                                        // no cutoff in the 1PN pass
+        const float mu = P.yukMu;
+        const float expMuR = __expf(-mu * r);
+        const float nDotV1 = nx * t.vx + ny * t.vy, nDotV2 = nx * svx + ny * svy;
+        const float v1DotV2 = t.vx * svx + t.vy * svy;
+        const float alpha = 1.f + mu * r;
+        const float beta = 0.5f * YUKAWA_COUPLING * t.m * sm * expMuR * invRSq;
+        const float radial = -(alpha * v1DotV2 + (alpha * alpha + alpha + 1.f) * nDotV1 * nDotV2);
+        ox += beta * (radial * nx + alpha * (nDotV2 * t.vx + nDotV1 * svx));
+        oy += beta * (radial * ny + alpha * (nDotV2 * t.vy + nDotV1 * svy));
+    }
+}
+
+struct Acc2 {
+    float px, py; CAcc x, y; int cnt;
+    __device__ __forceinline__ void init() { px = py = 0.f; x.init(); y.init(); cnt = 0; }
+    __device__ __forceinline__ void flush() { x.add(px); y.add(py); px = py = 0.f; }
+    __device__ __forceinline__ void tick() { if (++cnt >= FLUSH_EVERY) { flush(); cnt = 0; } }
+};
+
+__global__ void __launch_bounds__(WALK_THREADS)
+walk1pn_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
+    __shared__ int s_node[WALK_WARPS][WALK_STACK];
+    __shared__ unsigned s_mask[WALK_WARPS][WALK_STACK];
+    __shared__ float s_age[HIST_LEN], s_segdt[HIST_LEN];
+    load_hist_tables(C, s_age, s_segdt);
+    const int n = ctl->n;
+    const int warp = threadIdx.x >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    const int k = (blockIdx.x * WALK_WARPS + warp) * 32 + (int)lane;
+    const bool valid = k < n;
+    const unsigned active = __ballot_sync(0xffffffffu, valid);
+    if (active == 0) return;
+    Tgt t;
+    if (valid) t = load_target(S, T.tgt[k]);
+    else { t = Tgt{}; t.idx = -1; }
+    Acc2 A; A.init();
+    const int root = *d_root;
+    const bool treeOk = (ctl->err & (ERR_NODE_OVERFLOW | ERR_BAD_INDEX)) == 0;
+    const int nIntW = ctl->nInternal, nLeafW = ctl->nLeaves, nValidW = ctl->nValid;
+    int top = 0;
+    if (root != ROOT_NONE && treeOk) {
+        if (lane == 0) { s_node[warp][0] = root; s_mask[warp][0] = active; }
+        top = 1;
+    }
+    __syncwarp();
+    while (top > 0) {
+        top--;
+        const int node = s_node[warp][top];
+        const unsigned mask = s_mask[warp][top];
+        __syncwarp();
+        const bool in = (mask >> lane) & 1u;
+        if (node & LEAF_REF) {
+            const int li = node & ~LEAF_REF;
+            if (li >= nLeafW) { if (lane == 0) atomicOr(&ctl->err, ERR_BAD_INDEX); continue; }
+            if (T.leaf_a[li].z < EPS_F) continue;
+            const int4 lm = T.leaf_meta[li];
+            if (lm.x < 0 || lm.x + lm.y > nValidW) { if (lane == 0) atomicOr(&ctl->err, ERR_BAD_INDEX); continue; }
+            for (int q = lm.x; q < lm.x + lm.y; q++) {               // forces.js:534-554
+                const float4 pp = T.pt_pos[q];
+                const float4 pv = T.pt_vel[q];
+                const uint32_t ref = __float_as_uint(pv.w);
+                const int j = (int)ref_index(ref);
+                const uint32_t code = ref_code(ref);
+                if (!in || j == t.idx) continue;
+                float rx, ry, svx, svy;
+                double sxd, syd;
+                if (code == CODE_IDENTITY) {
+                    Delayed d;
+                    if (!delayed_state(P, S, C, s_age, s_segdt, j, t.x, t.y, d)) continue;
+                    displacement(P, t.x, t.y, d.x, -t.xlo, d.y, -t.ylo, rx, ry);
+                    svx = d.vx; svy = d.vy;
+                } else {
+                    const float2 pl = T.pt_lo[q];
+                    image_disp(P, t, pp.x, pp.y, pl.x, pl.y, code, rx, ry, sxd, syd);
+                    svx = pv.x; svy = pv.y;
+                }
+                accum_1pn(P, t, rx, ry, svx, svy, pp.z, pp.w, A.px, A.py);
+                A.tick();
+            }
+        } else {
+            if (node < 0 || node >= nIntW) { if (lane == 0) atomicOr(&ctl->err, ERR_BAD_INDEX); continue; }
+            const float4 a = T.int_a[node];
+            if (a.z < EPS_F) continue;
+            const float4 c = T.int_c[node];
+            bool accept = false;
+            float rx = 0.f, ry = 0.f;
+            if (in) {
+                displacement(P, t.x, t.y, a.x, c.x - t.xlo, a.y, c.y - t.ylo, rx, ry);
+                const float dSq = __fmaf_rn(rx, rx, ry * ry);
+                const float rhs = P.thetaSq * dSq;
+                accept = c.z < rhs;
+                if (fabsf(rhs - c.z) <= 1e-6f * c.z) {
+                    double dx, dy;
+                    exact_disp(P, t.xd(), t.yd(), (double)a.x + (double)c.x, (double)a.y + (double)c.y, dx, dy);
+                    const double size = 2.0 * ldexp(P.rootW, -(int)c.w);
+                    accept = size * size < P.thetaSqD * (dx * dx + dy * dy);
+                }
+            }
+            const unsigned acc = __ballot_sync(0xffffffffu, accept);
+            const unsigned open = mask & ~acc;
+            if (accept) {
+                const float4 b = T.int_b[node];
+                accum_1pn(P, t, rx, ry, b.x, b.y, a.z, a.w, A.px, A.py);
+                A.tick();
+            }
+            if (open) {
+                const int4 ch = T.int_child[node];
+                const int np = (ch.x >= 0) + (ch.y >= 0) + (ch.z >= 0) + (ch.w >= 0);
+                if (top + np > WALK_STACK) {
+                    if (lane == 0) atomicOr(&ctl->err, ERR_STACK_OVERFLOW);
+                } else {
+                    if (lane == 0) {
+                        int tp = top;
+                        if (ch.x >= 0) { s_node[warp][tp] = ch.x; s_mask[warp][tp++] = open; }
+                        if (ch.y >= 0) { s_node[warp][tp] = ch.y; s_mask[warp][tp++] = open; }
+                        if (ch.z >= 0) { s_node[warp][tp] = ch.z; s_mask[warp][tp++] = open; }
+                        if (ch.w >= 0) { s_node[warp][tp] = ch.w; s_mask[warp][tp++] = open; }
+                    }
+                    top += np;
+                }
+                __syncwarp();
+            }
+        }
+    }
+    A.flush();
+    if (valid) S.f1pn[t.idx] = make_float2(A.x.value(), A.y.value());
+}
+
+__global__ void __launch_bounds__(DIRECT_THREADS)
+direct1pn_kernel(DevParams P, DevState S, FrameCtl* ctl, ForceCtx C) {
+    __shared__ float4 s_pos[DIRECT_THREADS];
+    __shared__ float s_age[HIST_LEN], s_segdt[HIST_LEN];
+    load_hist_tables(C, s_age, s_segdt);
+    const int n = ctl->n;
+    const int i = blockIdx.x * DIRECT_THREADS + threadIdx.x;
+    const bool valid = i < n;
+    Tgt t;
+    if (valid) t = load_target(S, i);
+    else { t = Tgt{}; t.idx = -1; }
+    Acc2 A; A.init();
+    for (int base = 0; base < n; base += DIRECT_THREADS) {
+        const int j = base + threadIdx.x;
+        __syncthreads();
+        if (j < n) s_pos[threadIdx.x] = S.pos[j];
+        __syncthreads();
+        if (!valid) continue;
+        const int cnt = min(DIRECT_THREADS, n - base);
+        for (int jj = 0; jj < cnt; jj++) {                           // forces.js:592-608
+            const int jg = base + jj;
+            if (jg == i) continue;
+            Delayed d;
+            if (!delayed_state(P, S, C, s_age, s_segdt, jg, t.x, t.y, d)) continue;
+            float rx, ry;
+            displacement(P, t.x, t.y, d.x, -t.xlo, d.y, -t.ylo, rx, ry);
+            const float4 sp = s_pos[jj];
+            accum_1pn(P, t, rx, ry, d.vx, d.vy, sp.z, sp.w, A.px, A.py);
+            A.tick();
+        }
+    }
+    A.flush();
+    if (valid) S.f1pn[i] = make_float2(A.x.value(), A.y.value());
+}
+
+// ---- dispatch ---------------------------------------------------------------------------------
+__global__ void clear_reductions_kernel(FrameCtl* ctl) {
+    ctl->maxAccelSqBits = 0ull;
+    ctl->maxCycBits = 0ull;
+    ctl->interactions = 0ull;
+}
+
+template <bool MAGGM, bool REL, bool BRK>
+static void launch_force(bool bh, const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root,
+                         FrameCtl* ctl, const ForceCtx& C, int n_cap, cudaStream_t st) {
+    if (bh && (P.flags & GEON_FLAG_SIMPLE_WALK)) {
+        const int blocks = std::max(1, (n_cap + WALK_THREADS - 1) / WALK_THREADS);
+        walk_kernel<MAGGM, REL, BRK><<<blocks, WALK_THREADS, 0, st>>>(P, S, T, d_root, ctl, C);
+    } else if (bh) {
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(walkb_kernel<MAGGM, REL, BRK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WB_SMEM);
+            attr = true;
+        }
+        const int blocks = std::max(1, (n_cap + WB_THREADS - 1) / WB_THREADS);
+        walkb_kernel<MAGGM, REL, BRK><<<blocks, WB_THREADS, WB_SMEM, st>>>(P, S, T, d_root, ctl, C);
+    } else {
+        const int blocks = std::max(1, (n_cap + DIRECT_THREADS - 1) / DIRECT_THREADS);
+        direct_kernel<MAGGM, REL, BRK><<<blocks, DIRECT_THREADS, 0, st>>>(P, S, ctl, C);
+    }
+}
+
+void force_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
+                const ForceCtx& C, bool bh, int n_cap, cudaStream_t st, LaunchCounter& lc) {
+    clear_reductions_kernel<<<1, 1, 0, st>>>(ctl);
+    const bool maggm = (P.toggles & (GEON_MAGNETIC | GEON_GRAVITOMAG | GEON_ONE_PN)) != 0;
+    const bool rel = P.rel != 0;
+    const bool brk = C.brk != 0;
+    if (maggm) {
+        if (rel) { if (brk) launch_force<true, true, true>(bh, P, S, T, d_root, ctl, C, n_cap, st); else launch_force<true, true, false>(bh, P, S, T, d_root, ctl, C, n_cap, st); }
+        else     { if (brk) launch_force<true, false, true>(bh, P, S, T, d_root, ctl, C, n_cap, st); else launch_force<true, false, false>(bh, P, S, T, d_root, ctl, C, n_cap, st); }
+    } else {
+        if (rel) { if (brk) launch_force<false, true, true>(bh, P, S, T, d_root, ctl, C, n_cap, st); else launch_force<false, true, false>(bh, P, S, T, d_root, ctl, C, n_cap, st); }
+        else     { if (brk) launch_force<false, false, true>(bh, P, S, T, d_root, ctl, C, n_cap, st); else launch_force<false, false, false>(bh, P, S, T, d_root, ctl, C, n_cap, st); }
+    }
+    lc.add(2);
+}
+
+void onepn_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
+                const ForceCtx& C, bool bh, int n_cap, cudaStream_t st, LaunchCounter& lc) {
+    if (bh) {
+        const int blocks = std::max(1, (n_cap + WALK_THREADS - 1) / WALK_THREADS);
+        walk1pn_kernel<<<blocks, WALK_THREADS, 0, st>>>(P, S, T, d_root, ctl, C);
+    } else {
+        const int blocks = std::max(1, (n_cap + DIRECT_THREADS - 1) / DIRECT_THREADS);
+        direct1pn_kernel<<<blocks, DIRECT_THREADS, 0, st>>>(P, S, ctl, C);
+    }
+    lc.add(1);
+}
+
+}  // namespace geon

@@ -1,0 +1,32 @@
+// force.cuh — declarations shared by the force kernels (force.cu) and the
+// frame driver (capi.cu).
+#pragma once
+
+#include "state.cuh"
+
+namespace geon {
+
+// Per-pass context for the force kernels.
+struct ForceCtx {
+    double simTime;
+    const double* hist_t;     // [256] sample times (ring, shared by all particles)
+    const float* hist_age;    // [256] simTime - t[slot]
+    const float* hist_segdt;  // [256] t[slot+1] - t[slot]
+    int hist_head;            // next ring slot to be written
+    int pe;                   // accumulate potential energy
+    int brk;                  // keep per-type vectors
+    int bounce;               // boundary == BOUNCE (wall forces)
+};
+
+// Force pass: resetForces + computeAllForces (+ external fields, bounce
+// walls) for every particle, with the max-acceleration / cyclotron
+// reductions for the substep planner.  `bh` selects the tree walk (tree must
+// be built) or the pairwise sum.
+void force_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
+                const ForceCtx& C, bool bh, int n_cap, cudaStream_t st, LaunchCounter& lc);
+
+// 1PN-only pass (forces.js:578-610): writes S.f1pn.
+void onepn_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
+                const ForceCtx& C, bool bh, int n_cap, cudaStream_t st, LaunchCounter& lc);
+
+}  // namespace geon

@@ -1,0 +1,178 @@
+"""Pythonic handle over the C ABI: one GPU-resident particle system."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+
+class GeonSystem:
+    """Owns one ``GeonHandle``.  Arrays in and out are host NumPy arrays."""
+
+    def __init__(self, params: N.GeonParams, capacity: int):
+        self.lib = N.load()
+        self._h = C.c_void_p()
+        rc = self.lib.geon_create(C.byref(params), int(capacity), C.byref(self._h))
+        if rc < 0:
+            raise N.GeonError(rc, self.lib.geon_last_error(None).decode())
+        self.capacity = int(capacity)
+
+    # -- lifetime -----------------------------------------------------------
+    def close(self):
+        if self._h:
+            self.lib.geon_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc):
+        return N.check(self.lib, self._h, rc)
+
+    # -- parameters -----------------------------------------------------------
+    def set_params(self, params: N.GeonParams):
+        self._ck(self.lib.geon_set_params(self._h, C.byref(params)))
+
+    def params(self) -> N.GeonParams:
+        p = N.GeonParams()
+        self._ck(self.lib.geon_get_params(self._h, C.byref(p)))
+        return p
+
+    # -- state ------------------------------------------------------------------
+    @staticmethod
+    def _rows(x, y, wx, wy, mass, charge, angw) -> np.ndarray:
+        cols = [np.asarray(a, dtype=np.float32).ravel() for a in (x, y, wx, wy, mass, charge, angw)]
+        n = cols[0].size
+        if any(c.size != n for c in cols):
+            raise ValueError("state arrays must have equal length")
+        return np.ascontiguousarray(np.stack(cols)), n
+
+    def add(self, x, y, wx, wy, mass, charge, angw, creation_time: float = float("-inf")) -> int:
+        rows, n = self._rows(x, y, wx, wy, mass, charge, angw)
+        first = C.c_int32()
+        self._ck(self.lib.geon_add_particles(self._h, n, N.fptr(rows), creation_time, C.byref(first)))
+        return first.value
+
+    def upload(self, x, y, wx, wy, mass, charge, angw, sim_time: float = 0.0):
+        rows, n = self._rows(x, y, wx, wy, mass, charge, angw)
+        self._ck(self.lib.geon_upload_state(self._h, n, N.fptr(rows), sim_time))
+
+    def count(self) -> int:
+        n = C.c_int32()
+        self._ck(self.lib.geon_particle_count(self._h, C.byref(n)))
+        return n.value
+
+    def state(self, f64: bool = False) -> dict:
+        n = self.count()
+        cap = max(n, 1)
+        if f64:
+            out = np.zeros((N.ST_ROWS, cap), dtype=np.float64)
+            self._ck(self.lib.geon_download_state_f64(self._h, N.dptr(out), N.ST_ROWS, cap, None))
+        else:
+            out = np.zeros((N.ST_ROWS, cap), dtype=np.float32)
+            self._ck(self.lib.geon_download_state(self._h, N.fptr(out), N.ST_ROWS, cap, None))
+        return {k: out[r, :n].copy() for r, k in enumerate(N.ST_NAMES)}
+
+    def ids(self) -> np.ndarray:
+        n = self.count()
+        out = np.zeros(max(n, 1), dtype=np.int32)
+        self._ck(self.lib.geon_download_ids(self._h, N.iptr(out), out.size, None))
+        return out[:n]
+
+    def remove(self, index: int):
+        self._ck(self.lib.geon_remove_particle(self._h, int(index)))
+
+    def reset(self):
+        self._ck(self.lib.geon_reset(self._h))
+
+    # -- stepping ------------------------------------------------------------
+    def update(self, dt: float) -> int:
+        s = C.c_int32()
+        self._ck(self.lib.geon_update(self._h, float(dt), C.byref(s)))
+        return s.value
+
+    def synchronize(self):
+        self._ck(self.lib.geon_synchronize(self._h))
+
+    def compute_forces(self):
+        self._ck(self.lib.geon_compute_forces(self._h))
+
+    def compute_1pn(self):
+        self._ck(self.lib.geon_compute_1pn(self._h))
+
+    def forces(self) -> dict:
+        n = self.count()
+        cap = max(n, 1)
+        out = np.zeros((N.OUT_ROWS, cap), dtype=np.float32)
+        self._ck(self.lib.geon_download_forces(self._h, 0, N.OUT_ROWS, N.fptr(out), cap))
+        return {k: out[r, :n].copy() for r, k in enumerate(N.OUT_NAMES)}
+
+    # -- tree --------------------------------------------------------------
+    def build_tree(self) -> dict:
+        info = N.GeonTreeInfo()
+        self._ck(self.lib.geon_build_tree(self._h, C.byref(info)))
+        return info.as_dict()
+
+    def leaves(self, info: dict | None = None):
+        info = info or self.build_tree()
+        npts, nl = max(info["n_points"], 1), max(info["n_leaves"], 1)
+        lop = np.zeros(npts, dtype=np.int32)
+        bx = np.zeros(nl); by = np.zeros(nl); bw = np.zeros(nl)
+        lv = np.zeros(nl, dtype=np.int32)
+        self._ck(self.lib.geon_tree_leaves(self._h, N.iptr(lop), npts, N.dptr(bx), N.dptr(by), N.dptr(bw),
+                                           N.iptr(lv), nl))
+        n = info["n_leaves"]
+        return lop[:info["n_points"]], bx[:n], by[:n], bw[:n], lv[:n]
+
+    def interactions(self) -> int:
+        c = C.c_int64()
+        self._ck(self.lib.geon_interaction_count(self._h, C.byref(c)))
+        return c.value
+
+    # -- diagnostics ---------------------------------------------------------------
+    def stats(self) -> dict:
+        s = N.GeonStats()
+        self._ck(self.lib.geon_stats(self._h, C.byref(s)))
+        return s.as_dict()
+
+    def upload_history(self, times, x, y, vx, vy, angw):
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        planes = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, vx, vy, angw)]
+        n, count = planes[0].shape
+        samples = np.ascontiguousarray(np.stack(planes))
+        self._ck(self.lib.geon_upload_history(self._h, n, count, N.dptr(times), N.fptr(samples)))
+
+    def set_sim_time(self, t: float):
+        self._ck(self.lib.geon_set_sim_time(self._h, float(t)))
+
+    def sim_time(self) -> float:
+        t = C.c_double()
+        self._ck(self.lib.geon_get_sim_time(self._h, C.byref(t)))
+        return t.value
+
+    def profile(self, enable: bool) -> dict:
+        """Starts (True) or stops (False) per-phase CUDA-event timing; returns totals so far."""
+        out = N.GeonProfile()
+        self._ck(self.lib.geon_profile(self._h, 1 if enable else 0, C.byref(out)))
+        return out.as_dict()
+
+    def stream_ptr(self) -> int:
+        p = C.c_void_p()
+        self._ck(self.lib.geon_get_stream(self._h, C.byref(p)))
+        return p.value or 0
+
+    def launch_count(self) -> int:
+        c = C.c_int64()
+        self._ck(self.lib.geon_launch_count(self._h, C.byref(c)))
+        return c.value

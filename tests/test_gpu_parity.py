@@ -1,0 +1,248 @@
+"""Parity of the CUDA path (through the C ABI) against the FP64 oracle.
+
+Tolerances (FP32 on the GPU vs FP64 oracle):
+  * tree membership: bit-exact (every tree point in a leaf with the same
+    centre, half-size and level, and the same grouping);
+  * forces and fields: norm-wise relative error ||gpu - ref|| / ||ref|| <= 1e-5
+    per quantity (FORCE_TOL), and per particle <= 1e-3 relative to
+    max(|ref|, 1e-3 rms) (the FP32 resolution of a single term);
+  * one frame of trajectories: positions 1e-5 norm-wise, velocities 1e-5.
+"""
+import numpy as np
+import pytest
+
+from physsim_gb300 import _native as N
+from physsim_gb300 import workloads as W
+from tests.parity import load_both, compare_trees, vec_err, rel_err, STATE_KEYS
+
+pytestmark = pytest.mark.gpu
+
+FORCE_TOL = 1e-5
+POINT_TOL = 1e-3
+TRAJ_TOL = 1e-5
+
+
+def check_tree(wl, **kw):
+    g, o = load_both(wl, **kw)
+    res = compare_trees(g, o)
+    g.close()
+    assert res["gpu_points"] == res["oracle_points"], res
+    assert res["mismatch"] == 0 and res["groups_equal"], res
+    return res
+
+
+def check_forces(wl, keys, history=None, tol=FORCE_TOL):
+    g, o = load_both(wl, history=history)
+    g.compute_forces()
+    o.compute_forces()
+    fg, fo = g.forces(), o.forces()
+    if wl.params.toggles & N.BARNES_HUT:
+        assert g.interactions() == o.interactions()
+    out = {}
+    e = vec_err(fg["fx"], fg["fy"], fo["fx"], fo["fy"])
+    out["force"] = e
+    assert e["norm"] <= tol, ("force", e)
+    assert e["max"] <= POINT_TOL, ("force", e)
+    for k in keys:
+        if not np.any(fo[k]):
+            assert not np.any(fg[k]), (k, "oracle zero, gpu nonzero")
+            continue
+        r = rel_err(fg[k], fo[k])
+        out[k] = r
+        assert r["norm"] <= tol, (k, r)
+    g.close()
+    return out
+
+
+# ---- tree membership -------------------------------------------------------------------
+@pytest.mark.parametrize("n", [1, 4, 5, 64, 2048])
+def test_tree_small_disk(gpu_lib, oracle_mod, n):
+    check_tree(W.small_disk(n, relativity=False, softening=8.0))
+
+
+def test_tree_torus_with_ghosts(gpu_lib, oracle_mod):
+    res = check_tree(W.clusters_torus(4096))
+    assert res["gpu_points"] > 4096
+
+
+def test_tree_plummer_65536(gpu_lib, oracle_mod):
+    check_tree(W.plummer_disk(65536))
+
+
+def test_tree_edge_points(gpu_lib, oracle_mod):
+    """Points on node boundaries (ties go NW), on the root box edge, and outside it."""
+    p = N.make_params(domain_w=100, domain_h=100)
+    xs = np.array([50, 50, 25, 75, 50, -150, 250, 260, 12.5, 12.5, 12.5, 12.5, 12.5, 37.5], float)
+    ys = np.array([50, 25, 50, 50, 75, 10, 10, 10, 12.5, 12.5, 25, 37.5, 12.5, 12.5], float)
+    z = np.zeros(xs.size)
+    wl = W.Workload("edges", p, {"x": xs, "y": ys, "wx": z, "wy": z, "mass": np.ones(xs.size), "charge": z,
+                                 "angw": z}, 1 / 60, 1)
+    check_tree(wl)
+
+
+def test_tree_coincident_points_bucket(gpu_lib, oracle_mod):
+    """Five coincident points: the reference never terminates there; the GPU
+    tree stops at level 31 with one bucket leaf and reports it."""
+    from physsim_gb300.system import GeonSystem
+    p = N.make_params(domain_w=100, domain_h=100)
+    xs = np.array([10, 10, 10, 10, 10, 70.0])
+    ys = np.array([20, 20, 20, 20, 20, 70.0])
+    z = np.zeros(6)
+    g = GeonSystem(p, 8)
+    g.upload(xs, ys, z, z, np.ones(6), z, z)
+    info = g.build_tree()
+    assert info["n_bucket"] == 1 and info["max_level"] == 31
+    lop, bx, by, bw, lv = g.leaves(info)
+    assert len(set(lop[:5])) == 1
+    g.close()
+
+
+# ---- forces ---------------------------------------------------------------------------
+GC_KEYS = ("tidal", "pe", "grav_x", "coul_x")
+FULL_KEYS = ("Bz", "Bgz", "dBzdx", "dBzdy", "dBgzdx", "dBgzdy", "tidal", "frameDrag", "f1pn_x", "f1pn_y", "pe")
+
+
+def _with(wl, flags=0, toggles_add=0, toggles_del=0):
+    p = wl.params
+    p.flags |= flags
+    p.toggles = (p.toggles | toggles_add) & ~toggles_del
+    return wl
+
+
+def test_forces_small_disk_bh(gpu_lib, oracle_mod):
+    check_forces(_with(W.small_disk(2048, relativity=False, softening=8.0), N.FLAG_PE | N.FLAG_BREAKDOWN), GC_KEYS)
+
+
+def test_forces_small_disk_direct(gpu_lib, oracle_mod):
+    wl = W.small_disk(2048, relativity=False, softening=8.0, barnes_hut=False)
+    check_forces(_with(wl, N.FLAG_PE | N.FLAG_BREAKDOWN), GC_KEYS)
+
+
+def test_forces_small_disk_softening_01_cold_history(gpu_lib, oracle_mod):
+    """Config as stated (relativity on, softening 0.1): with no history the
+    leaf sources are skipped (forces.js:653) and only aggregates act."""
+    check_forces(_with(W.small_disk(2048), N.FLAG_PE), ("tidal", "pe"))
+
+
+def test_forces_small_disk_warm_history(gpu_lib, oracle_mod):
+    wl = _with(W.small_disk(2048, softening=0.1), N.FLAG_PE)
+    hist = W.straight_line_history(wl.state, 128, 200.0, 64 / 60)
+    check_forces(wl, ("tidal", "pe"), history=hist)
+
+
+def test_forces_plummer_gcy(gpu_lib, oracle_mod):
+    check_forces(_with(W.plummer_disk(65536), N.FLAG_PE | N.FLAG_BREAKDOWN), ("tidal", "pe", "yuk_x", "yuk_y"))
+
+
+@pytest.mark.parametrize("bh", [True, False])
+def test_forces_full_set_torus(gpu_lib, oracle_mod, bh):
+    wl = _with(W.clusters_torus(4096, barnes_hut=bh), N.FLAG_PE | N.FLAG_BREAKDOWN)
+    hist = W.straight_line_history(wl.state, 96, 120.0, 64 / 60)
+    check_forces(wl, FULL_KEYS, history=hist)
+
+
+def test_forces_full_set_torus_no_relativity(gpu_lib, oracle_mod):
+    wl = _with(W.clusters_torus(4096, relativity=False), N.FLAG_PE | N.FLAG_BREAKDOWN)
+    check_forces(wl, FULL_KEYS)
+
+
+@pytest.mark.parametrize("bh", [True, False])
+def test_onepn_pass(gpu_lib, oracle_mod, bh):
+    wl = W.clusters_torus(2048, barnes_hut=bh)
+    hist = W.straight_line_history(wl.state, 96, 120.0, 64 / 60)
+    g, o = load_both(wl, history=hist)
+    g.compute_1pn()
+    o.compute_1pn()
+    fg, fo = g.forces(), o.forces()
+    e = vec_err(fg["f1pn_x"], fg["f1pn_y"], fo["f1pn_x"], fo["f1pn_y"])
+    assert e["norm"] <= FORCE_TOL, e
+    g.close()
+
+
+def test_external_fields_and_bounce_walls(gpu_lib, oracle_mod):
+    wl = W.small_disk(512, relativity=False, softening=8.0)
+    p = wl.params
+    p.boundary_mode = N.BOUND_BOUNCE
+    p.ext_gravity, p.ext_electric, p.ext_bz = 0.3, 0.2, 0.05
+    p.toggles |= N.MAGNETIC
+    p.flags |= N.FLAG_BREAKDOWN
+    wl.state["x"][:8] = np.linspace(0.1, 0.8, 8)
+    check_forces(wl, ("ext_x", "ext_y", "Bz"))
+
+
+# ---- frames -----------------------------------------------------------------------------
+def run_frames(wl, frames, history=None):
+    g, o = load_both(wl, history=history)
+    for _ in range(frames):
+        a = g.update(wl.dt)
+        b = o.update(wl.dt)
+        assert a == b, ("substeps", a, b)
+    assert g.count() == o.count()
+    assert np.array_equal(g.ids(), o.ids())
+    sg, so = g.state(f64=True), o.state()
+    errs = {k: rel_err(sg[k], so[k]) for k in ("x", "y", "wx", "wy", "angw")}
+    st = (g.stats(), o.stats())
+    g.close()
+    return errs, st
+
+
+def test_frame_small_disk(gpu_lib, oracle_mod):
+    errs, _ = run_frames(W.small_disk(2048, relativity=False, softening=8.0), 1)
+    for k, e in errs.items():
+        assert e["norm"] <= TRAJ_TOL, (k, e)
+
+
+def test_frames_small_disk_config(gpu_lib, oracle_mod):
+    """The stated small config: relativity on, softening 0.1, 10 frames."""
+    errs, _ = run_frames(W.small_disk(2048), 10)
+    for k in ("x", "y"):
+        assert errs[k]["norm"] <= TRAJ_TOL, (k, errs[k])
+    for k in ("wx", "wy", "angw"):
+        assert errs[k]["norm"] <= 1e-4, (k, errs[k])
+
+
+def test_frame_full_set_torus(gpu_lib, oracle_mod):
+    wl = W.clusters_torus(2048)
+    hist = W.straight_line_history(wl.state, 96, 120.0, 64 / 60)
+    errs, _ = run_frames(wl, 1, history=hist)
+    for k, e in errs.items():
+        assert e["norm"] <= TRAJ_TOL, (k, e)
+
+
+def test_despawn_compaction_matches(gpu_lib, oracle_mod):
+    wl = W.small_disk(256, relativity=False, softening=8.0)
+    wl.state["x"][[3, 100, 200]] = [170.0, -70.0, 180.0]
+    errs, (sg, so) = run_frames(wl, 2)
+    assert sg["alive_count"] == so["alive_count"] == 253
+
+
+def test_stats_fp64(gpu_lib, oracle_mod):
+    wl = W.small_disk(2048, relativity=True, softening=8.0)
+    wl.params.flags |= N.FLAG_PE
+    g, o = load_both(wl)
+    g.compute_forces()
+    o.compute_forces()
+    sg, so = g.stats(), o.stats()
+    for k in ("linear_ke", "spin_ke", "px", "py", "orbital_ang_mom", "spin_ang_mom", "com_x", "com_y", "total_mass"):
+        assert np.isclose(sg[k], so[k], rtol=1e-6, atol=1e-9 * max(1.0, abs(so[k]))), (k, sg[k], so[k])
+    assert np.isclose(sg["pe"], o.pe(), rtol=1e-5)
+    g.close()
+
+
+# ---- errors --------------------------------------------------------------------------------
+def test_capacity_full_is_reported(gpu_lib):
+    from physsim_gb300.system import GeonSystem
+    g = GeonSystem(N.make_params(), 4)
+    z = np.zeros(5)
+    with pytest.raises(N.GeonError) as ei:
+        g.add(z, z, z, z, np.ones(5), z, z)
+    assert ei.value.code == N.GEON_ERR_FULL
+    g.close()
+
+
+def test_empty_system_update(gpu_lib):
+    from physsim_gb300.system import GeonSystem
+    g = GeonSystem(N.make_params(toggles=N.GRAVITY | N.BARNES_HUT), 16)
+    assert g.update(1 / 60) == 1
+    assert abs(g.sim_time() - 1 / 60) < 1e-15
+    g.close()

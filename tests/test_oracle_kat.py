@@ -1,0 +1,230 @@
+"""Known-answer tests of the FP64 oracle (CPU only).
+
+The reference ships no tests or golden vectors, so the oracle is anchored by
+answers derived from first principles for the formulas it restates
+(src/forces.js, src/signal-delay.js, src/topology.js, src/quadtree.js,
+src/integrator.js), and by structural invariants of the reference tree.
+"""
+import numpy as np
+import pytest
+
+from physsim_gb300 import _native as N
+from physsim_gb300 import workloads as W
+
+
+def sim(params, x, y, wx=None, wy=None, m=None, q=None, angw=None, threads=1):
+    from oracle.oracle import OracleSim
+    n = len(x)
+    z = np.zeros(n)
+    o = OracleSim(params, threads=threads)
+    o.add(np.asarray(x, float), np.asarray(y, float), z if wx is None else wx, z if wy is None else wy,
+          np.ones(n) if m is None else m, z if q is None else q, z if angw is None else angw)
+    return o
+
+
+def test_gravity_two_body_softened(oracle_mod):
+    eps = 1.5
+    o = sim(N.make_params(toggles=N.GRAVITY, softening=eps), [10, 13], [20, 24], m=[2.0, 3.0])
+    o.compute_forces()
+    f = o.forces()
+    r2 = 25 + eps * eps
+    expect = 2 * 3 / r2 ** 1.5 * np.array([3.0, 4.0])
+    assert np.allclose([f["fx"][0], f["fy"][0]], expect, rtol=1e-14)
+    assert np.allclose([f["fx"][1], f["fy"][1]], -expect, rtol=1e-14)
+    assert np.isclose(o.pe(), -6 / np.sqrt(r2), rtol=1e-14)
+
+
+def test_coulomb_like_charges_repel(oracle_mod):
+    o = sim(N.make_params(toggles=N.COULOMB, softening=1.0), [0, 2], [0, 0], q=[0.5, 0.3])
+    o.compute_forces()
+    f = o.forces()
+    assert f["fx"][0] < 0 and f["fx"][1] > 0
+    assert np.isclose(f["fx"][0], -0.15 * 2 / 5 ** 1.5, rtol=1e-14)
+
+
+def test_yukawa_force_and_cutoff(oracle_mod):
+    mu, eps = 0.15, 1.0
+    for d, inside in ((10.0, True), (6 / mu + 0.5, False)):
+        o = sim(N.make_params(toggles=N.YUKAWA, softening=eps, yukawa_mu=mu), [0, d], [0, 0], m=[2.0, 1.5])
+        o.compute_forces()
+        f = o.forces()
+        r = np.sqrt(d * d + eps * eps)
+        expect = 14 * 3 * np.exp(-mu * r) * (1 / r ** 2 + mu / r) / r * d if inside else 0.0
+        assert np.isclose(f["fx"][0], expect, rtol=1e-13, atol=0.0)
+
+
+def test_aligned_magnetic_dipoles_repel(oracle_mod):
+    p = N.make_params(toggles=N.MAGNETIC, softening=1.0)
+    o = sim(p, [0, 3], [0, 0], m=[1.0, 1.0], q=[1.0, 1.0], angw=[0.5, 0.5])
+    o.set_forces_init(False)
+    o.update(1e-9)            # bootstrap caches angVel and moments, then one tiny substep
+    o.compute_forces()
+    f = o.forces()
+    assert f["mag_x"][0] < 0 < f["mag_x"][1]
+
+
+def test_min_image_torus_antisymmetric_and_bounded(oracle_mod):
+    rng = np.random.default_rng(0)
+    W_, H_ = 400.0, 300.0
+    for _ in range(200):
+        a = rng.random(2) * [W_, H_]
+        b = rng.random(2) * [W_, H_]
+        d1 = oracle_mod.min_image(a[0], a[1], b[0], b[1], N.TORUS, W_, H_)
+        d2 = oracle_mod.min_image(b[0], b[1], a[0], a[1], N.TORUS, W_, H_)
+        assert np.allclose(d1, -d2, atol=1e-12)
+        assert abs(d1[0]) <= W_ / 2 + 1e-12 and abs(d1[1]) <= H_ / 2 + 1e-12
+
+
+def test_min_image_klein_rp2_not_longer_than_direct(oracle_mod):
+    rng = np.random.default_rng(1)
+    for topo in (N.KLEIN, N.RP2):
+        for _ in range(100):
+            a = rng.random(2) * 100
+            b = rng.random(2) * 100
+            d = oracle_mod.min_image(a[0], a[1], b[0], b[1], topo, 100.0, 100.0)
+            assert np.hypot(*d) <= np.hypot(*(b - a)) + 1e-12
+
+
+def test_boris_rotation_preserves_speed(oracle_mod):
+    """Pure uniform Bz: the Boris rotation keeps |w| exactly (integrator.js:900-915)."""
+    p = N.make_params(toggles=N.MAGNETIC | N.RELATIVITY, ext_bz=2.0, boundary_mode=N.BOUND_LOOP,
+                      domain_w=1000, domain_h=1000, softening=8.0)
+    o = sim(p, [500.0], [500.0], wx=[0.3], wy=[0.1], m=[1.0], q=[1.0])
+    w0 = np.hypot(0.3, 0.1)
+    for _ in range(50):
+        o.update(1 / 60)
+    s = o.state()
+    assert np.isclose(np.hypot(s["wx"][0], s["wy"][0]), w0, rtol=1e-12)
+    assert o.last_substeps() >= 1
+
+
+def test_light_cone_solution_on_straight_history(oracle_mod):
+    """signal-delay.js: the returned point satisfies |x(t_r) - x_obs| = now - t_r."""
+    p = N.make_params(toggles=N.GRAVITY | N.RELATIVITY, domain_w=1000, domain_h=1000)
+    v = np.array([0.4, -0.2])
+    g = 1 / np.sqrt(1 - v @ v)
+    o = sim(p, [500.0, 530.0], [500.0, 520.0], wx=[v[0] * g, 0], wy=[v[1] * g, 0])
+    times = 100.0 - np.arange(64)[::-1] * 1.0
+    X = np.stack([500.0 + v[0] * (times - 100.0), np.full(64, 530.0)])
+    Y = np.stack([500.0 + v[1] * (times - 100.0), np.full(64, 520.0)])
+    VX = np.stack([np.full(64, v[0]), np.zeros(64)])
+    VY = np.stack([np.full(64, v[1]), np.zeros(64)])
+    o.upload_history(times, X, Y, VX, VY, np.zeros((2, 64)))
+    o.set_sim_time(100.0)
+    r = o.delayed_state(0, 530.0, 520.0)
+    assert r is not None
+    t_r = 100.0 + (r[0] - 500.0) / v[0]
+    assert np.isclose(np.hypot(r[0] - 530.0, r[1] - 520.0), 100.0 - t_r, rtol=1e-12)
+    assert np.isclose(r[1], 500.0 + v[1] * (t_r - 100.0), rtol=1e-12)
+    assert np.allclose(r[2:4], v, rtol=1e-12)
+
+
+def test_signal_delay_needs_two_samples(oracle_mod):
+    p = N.make_params(toggles=N.GRAVITY | N.RELATIVITY | N.BARNES_HUT)
+    o = sim(p, [10, 12], [10, 10], m=[1.0, 1.0])
+    o.compute_forces()
+    # cold history: leaf sources are skipped (forces.js:653)
+    assert o.forces()["fx"][0] == 0.0
+
+
+def _tree_leaves_by_point(o):
+    npts, _ = o.build_tree()
+    lop, bx, by, bw, lv = o.leaves(npts)
+    return [None if l < 0 else (bx[l], by[l], bw[l], lv[l]) for l in lop]
+
+
+def test_tree_capacity_and_order_independence(oracle_mod):
+    wl = W.small_disk(3000, relativity=False, softening=8.0)
+    s = wl.state
+    keys = ("x", "y", "wx", "wy", "mass", "charge", "angw")
+    o = sim(wl.params, *[s[k] for k in keys[:2]])
+    sig = _tree_leaves_by_point(o)
+    counts = {}
+    for t in sig:
+        counts[t] = counts.get(t, 0) + 1
+    assert max(counts.values()) <= 4
+    perm = np.random.default_rng(7).permutation(wl.n)
+    o2 = sim(wl.params, s["x"][perm], s["y"][perm])
+    sig2 = _tree_leaves_by_point(o2)
+    assert [sig[i] for i in perm] == sig2
+
+
+def test_tree_divided_iff_more_than_four(oracle_mod):
+    wl = W.small_disk(1500, relativity=False)
+    o = sim(wl.params, wl.state["x"], wl.state["y"], m=wl.state["mass"])
+    npts, _ = o.build_tree()
+    nodes = o.tree_nodes()
+    lop, *_ = o.leaves(npts)
+    # a divided node's children hold all its points; leaves hold <= 4
+    assert np.all(nodes["count"][nodes["divided"] == 0] <= 4)
+    assert np.isclose(nodes["mass"][0], wl.state["mass"].sum(), rtol=1e-12)
+
+
+def test_points_outside_root_box_are_dropped(oracle_mod):
+    p = N.make_params(domain_w=100, domain_h=100)
+    # root box is centre (50, 50), half-size 200: [-150, 250]^2
+    o = sim(p, [10.0, 260.0, -150.0, 250.0], [10.0, 10.0, 10.0, 10.0])
+    npts, _ = o.build_tree()
+    lop, *_ = o.leaves(npts)
+    assert list(lop >= 0) == [True, False, True, True]
+
+
+def test_tie_goes_north_west(oracle_mod):
+    """quadtree.js:175-179: px <= cx -> west, py <= cy -> north."""
+    p = N.make_params(domain_w=100, domain_h=100)
+    xs = [50.0, 50.0, 10, 20, 30]
+    ys = [50.0, 60.0, 70, 80, 90]
+    o = sim(p, xs, ys)
+    npts, _ = o.build_tree()
+    lop, bx, by, bw, lv = o.leaves(npts)
+    assert bx[lop[0]] < 50 and by[lop[0]] < 50      # (50, 50) on both ties -> NW child
+    assert bx[lop[1]] < 50 and by[lop[1]] > 50      # x tie -> west, y > cy -> south
+
+
+def test_despawn_removes_far_particles(oracle_mod):
+    p = N.make_params(toggles=N.GRAVITY, domain_w=100, domain_h=100)
+    o = sim(p, [50.0, 170.0], [50.0, 50.0])
+    o.update(1 / 60)
+    assert o.count() == 1
+    assert list(o.ids()) == [0]
+
+
+def test_torus_wrap_keeps_particle_in_box(oracle_mod):
+    p = N.make_params(toggles=N.GRAVITY, domain_w=100, domain_h=100, boundary_mode=N.BOUND_LOOP)
+    o = sim(p, [99.99], [0.001], wx=[1.0], wy=[-1.0])
+    o.update(1 / 60)
+    s = o.state()
+    assert 0 <= s["x"][0] <= 100 and 0 <= s["y"][0] <= 100
+
+
+def test_kepler_energy_drift_small(oracle_mod):
+    p = N.make_params(toggles=N.GRAVITY, domain_w=1000, domain_h=1000, softening=0.01, flags=N.FLAG_PE)
+    m1, m2, a = 100.0, 1.0, 20.0
+    v = np.sqrt(m1 / a)
+    g = 1.0
+    o = sim(p, [500.0, 520.0], [500.0, 500.0], wx=[0.0, 0.0], wy=[-v * m2 / m1, v], m=[m1, m2])
+    o.compute_forces()
+    s0 = o.stats()
+    e0 = s0["linear_ke"] + o.pe()
+    for _ in range(120):
+        o.update(1 / 30)
+    e1 = o.stats()["linear_ke"] + o.pe()
+    assert abs(e1 - e0) / abs(e0) < 1e-3
+
+
+def test_periodic_bh_counts_each_image(oracle_mod):
+    """Reference quirk: with ghosts in the tree and min-image in pairForce,
+    a source is counted once per copy of it the walk reaches
+    (integrator.js:248-257, forces.js:165-167)."""
+    p = N.make_params(toggles=N.GRAVITY | N.BARNES_HUT, boundary_mode=N.BOUND_LOOP, domain_w=100, domain_h=100,
+                      softening=1.0)
+    o = sim(p, [40.0, 60.0], [50.0, 50.0], m=[1.0, 1.0])
+    o.compute_forces()
+    f_bh = o.forces()["fx"][0]
+    pd = N.make_params(toggles=N.GRAVITY, boundary_mode=N.BOUND_LOOP, domain_w=100, domain_h=100, softening=1.0)
+    od = sim(pd, [40.0, 60.0], [50.0, 50.0], m=[1.0, 1.0])
+    od.compute_forces()
+    f_direct = od.forces()["fx"][0]
+    ghosts = o.ghost_origins()
+    copies_of_1 = 1 + int(np.sum(ghosts == 1))
+    assert np.isclose(f_bh, copies_of_1 * f_direct, rtol=1e-12)
