@@ -224,52 +224,75 @@ __device__ __forceinline__ void pair_force(const DevParams& P, const Tgt& t, flo
 }
 
 // ---- exact (FP64) displacement helpers for guard-band re-tests --------------------------
+// Every FP64 operation sits behind a guard that is taken only when an FP32
+// margin is within rounding: FP64 runs at a small fraction of the FP32 rate.
 __device__ __forceinline__ void exact_disp(const DevParams& P, double ox, double oy, double sx, double sy,
                                            double& rx, double& ry) {
     if (P.periodic) min_image_d(ox, oy, sx, sy, P.topology, P.Wd, P.Hd, rx, ry);
     else { rx = sx - ox; ry = sy - oy; }
 }
 
-__device__ __forceinline__ bool yukawa_in(const DevParams& P, float rx, float ry, double sxd, double syd,
-                                          double oxd, double oyd) {
+// A source position as unevaluated (hi, lo) pairs, converted to FP64 only in guard paths.
+struct SPos { float x, xlo, y, ylo; };
+
+__device__ __forceinline__ bool yukawa_in(const DevParams& P, float rx, float ry, const SPos& sp, const Tgt& t) {
     if (!P.yukOn) return false;
     const float rr = __fmaf_rn(rx, rx, ry * ry);
     const float cut = P.yukCutSq;
     if (fabsf(rr - cut) > 1e-6f * cut) return rr < cut;
     double dx, dy;
-    exact_disp(P, oxd, oyd, sxd, syd, dx, dy);
+    exact_disp(P, t.xd(), t.yd(), (double)sp.x + (double)sp.xlo, (double)sp.y + (double)sp.ylo, dx, dy);
     return dx * dx + dy * dy < P.yukCutSqD;
 }
 
-// Displacement from the target to the image (code) of a particle at
-// (x + xlo, y + ylo).  sxd/syd receive the image position in FP64.
+// Image position of a particle under a point code as compensated pairs
+// (ghost shifts and mirrors, integrator.js:176-244).
+__device__ __forceinline__ void point_image(const DevParams& P, float x, float y, float xlo, float ylo, uint32_t code,
+                                            float& ix, float& ixlo, float& iy, float& iylo) {
+    if (code == CODE_IDENTITY) { ix = x; ixlo = xlo; iy = y; iylo = ylo; return; }
+    df a = code_mx(code) ? df_add(df{ P.W, P.W_lo }, df{ -x, -xlo }) : df{ x, xlo };
+    df b = code_my(code) ? df_add(df{ P.H, P.H_lo }, df{ -y, -ylo }) : df{ y, ylo };
+    const int sx = code_sx(code), sy = code_sy(code);
+    if (sx) a = df_add(a, df{ sx * P.W, sx * P.W_lo });
+    if (sy) b = df_add(b, df{ sy * P.H, sy * P.H_lo });
+    ix = a.hi; ixlo = a.lo; iy = b.hi; iylo = b.lo;
+}
+
+// Displacement from the target to the image (code) of a particle at (x + xlo, y + ylo).
 __device__ __forceinline__ void image_disp(const DevParams& P, const Tgt& t, float x, float y, float xlo, float ylo,
-                                           uint32_t code, float& rx, float& ry, double& sxd, double& syd) {
-    if (code == CODE_IDENTITY) {
-        sxd = (double)x + (double)xlo; syd = (double)y + (double)ylo;
-        displacement(P, t.x, t.y, x, xlo - t.xlo, y, ylo - t.ylo, rx, ry);
-        return;
-    }
-    image_pos_d((double)x + (double)xlo, (double)y + (double)ylo, code, P.Wd, P.Hd, sxd, syd);
-    if (!code_mx(code) && !code_my(code) && P.topology == GEON_TORUS) {
-        const int sx = code_sx(code), sy = code_sy(code);
-        df ix = sx ? two_sum(x, sx * P.W) : df{ x, 0.f };
-        df iy = sy ? two_sum(y, sy * P.H) : df{ y, 0.f };
-        ix.lo = __fadd_rn(ix.lo, sx * P.W_lo + (xlo - t.xlo));
-        iy.lo = __fadd_rn(iy.lo, sy * P.H_lo + (ylo - t.ylo));
-        displacement(P, t.x, t.y, ix.hi, ix.lo, iy.hi, iy.lo, rx, ry);
+                                           uint32_t code, float& rx, float& ry, SPos& sp) {
+    point_image(P, x, y, xlo, ylo, code, sp.x, sp.xlo, sp.y, sp.ylo);
+    displacement(P, t.x, t.y, sp.x, sp.xlo - t.xlo, sp.y, sp.ylo - t.ylo, rx, ry);
+}
+
+// ---- signal delay (signal-delay.js:16-221) ----------------------------------------------
+// Returns the retarded source state.  The position comes back as the
+// displacement (rx, ry) from the target, formed as (sample - target) + frac *
+// segment so that FP32 rounding is relative to the separation, not to the
+// absolute coordinate; (x, y) is the absolute position for guard paths.
+struct Delayed { float rx, ry, x, y, vx, vy, angw; };
+
+// Displacement from target t to the point base + step (base a history sample).
+__device__ __forceinline__ void retarded_disp(const DevParams& P, const Tgt& t, float bx, float by, float stx, float sty,
+                                              float& rx, float& ry) {
+    if (!P.periodic) {
+        rx = __fsub_rn(__fadd_rn(__fsub_rn(bx, t.x), stx), t.xlo);
+        ry = __fsub_rn(__fadd_rn(__fsub_rn(by, t.y), sty), t.ylo);
+    } else if (P.topology == GEON_TORUS) {
+        const float dx0 = wrap_axis_comp(bx, t.x, -t.xlo, P.W, P.W_lo, P.halfW);
+        const float dy0 = wrap_axis_comp(by, t.y, -t.ylo, P.H, P.H_lo, P.halfH);
+        rx = torus_wrap_f(dx0 + stx, P.W, P.halfW);
+        ry = torus_wrap_f(dy0 + sty, P.H, P.halfH);
     } else {
         double dx, dy;
-        exact_disp(P, t.xd(), t.yd(), sxd, syd, dx, dy);
+        min_image_d(t.xd(), t.yd(), (double)bx + (double)stx, (double)by + (double)sty, P.topology, P.Wd, P.Hd, dx, dy);
         rx = (float)dx; ry = (float)dy;
     }
 }
 
-// ---- signal delay (signal-delay.js:16-221) ----------------------------------------------
-struct Delayed { float x, y, vx, vy, angw; };
-
 __device__ bool delayed_state(const DevParams& P, const DevState& S, const ForceCtx& C, const float* s_age,
-                              const float* s_segdt, int j, float ox, float oy, Delayed& out) {
+                              const float* s_segdt, int j, const Tgt& t, Delayed& out) {
+    const float ox = t.x, oy = t.y;
     const int count = S.hist_cnt[j];
     if (count < 2) return false;
     const int start = (C.hist_head - count) & HIST_MASK;
@@ -331,6 +354,7 @@ __device__ bool delayed_state(const DevParams& P, const DevState& S, const Force
                 }
                 if (s < 0.f) s = 0.f; else if (s > segDt) s = segDt;
                 const float frac = s / segDt;
+                retarded_disp(P, t, hl.x, hl.y, frac * sgx, frac * sgy, out.rx, out.ry);
                 out.x = hl.x + frac * sgx;
                 out.y = hl.y + frac * sgy;
                 out.vx = hl.z + frac * (hh.z - hl.z);
@@ -365,7 +389,8 @@ __device__ bool delayed_state(const DevParams& P, const DevState& S, const Force
             else return false;
         }
         if (s > 0.f) s = 0.f;
-        if (C.hist_t[start] + (double)s < S.ctime[j]) return false;
+        if (C.hist_t[start] + (double)s < S.ctime[j]) return false;   // particle did not exist yet
+        retarded_disp(P, t, hs.x, hs.y, vx * s, vy * s, out.rx, out.ry);
         out.x = hs.x + vx * s;
         out.y = hs.y + vy * s;
         out.vx = vx; out.vy = vy;
@@ -374,32 +399,24 @@ __device__ bool delayed_state(const DevParams& P, const DevState& S, const Force
     }
 }
 
-// Displacement to a delayed source; ghosts add their current image offset
-// (forces.js:656-661).
+// Displacement to a delayed source.  Ghosts add their current image offset
+// (forces.js:656-661); on the torus that offset is a whole period and the
+// minimum image removes it, on Klein / RP^2 it is formed in FP64.
 __device__ __forceinline__ void delayed_disp(const DevParams& P, const Tgt& t, const Delayed& d,
-                                             float xj, float yj, uint32_t code, float& rx, float& ry,
-                                             double& sxd, double& syd) {
-    if (code == CODE_IDENTITY) {
-        sxd = d.x; syd = d.y;
-        displacement(P, t.x, t.y, d.x, -t.xlo, d.y, -t.ylo, rx, ry);
+                                             float xj, float yj, uint32_t code, float& rx, float& ry, SPos& sp) {
+    sp = SPos{ d.x, 0.f, d.y, 0.f };
+    if (code == CODE_IDENTITY || (!code_mx(code) && !code_my(code) && P.topology == GEON_TORUS)) {
+        rx = d.rx; ry = d.ry;
         return;
     }
     double gx, gy;
     image_pos_d((double)xj, (double)yj, code, P.Wd, P.Hd, gx, gy);
-    sxd = (double)d.x + (gx - (double)xj);
-    syd = (double)d.y + (gy - (double)yj);
-    if (!code_mx(code) && !code_my(code) && P.topology == GEON_TORUS) {
-        const int sx = code_sx(code), sy = code_sy(code);
-        df ix = sx ? two_sum(d.x, sx * P.W) : df{ d.x, 0.f };
-        df iy = sy ? two_sum(d.y, sy * P.H) : df{ d.y, 0.f };
-        ix.lo = __fadd_rn(ix.lo, sx * P.W_lo - t.xlo);
-        iy.lo = __fadd_rn(iy.lo, sy * P.H_lo - t.ylo);
-        displacement(P, t.x, t.y, ix.hi, ix.lo, iy.hi, iy.lo, rx, ry);
-    } else {
-        double dx, dy;
-        exact_disp(P, t.xd(), t.yd(), sxd, syd, dx, dy);
-        rx = (float)dx; ry = (float)dy;
-    }
+    const double sxd = (double)d.x + (gx - (double)xj);
+    const double syd = (double)d.y + (gy - (double)yj);
+    double dx, dy;
+    exact_disp(P, t.xd(), t.yd(), sxd, syd, dx, dy);
+    rx = (float)dx; ry = (float)dy;
+    sp = SPos{ (float)sxd, (float)(sxd - (double)(float)sxd), (float)syd, (float)(syd - (double)(float)syd) };
 }
 
 // ---- epilogue: outputs, external fields, walls, planner reductions -------------------------
@@ -556,13 +573,14 @@ walk_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root,
                 const int j = (int)ref_index(ref);
                 const uint32_t code = ref_code(ref);
                 if (!in || j == t.idx) continue;
-                float rx, ry; double sxd, syd;
+                float rx, ry;
+                SPos sp;
                 float svx, svy, sAng, sMu, sL;
                 bool dl = false;
                 if (REL) {
                     Delayed d;
-                    if (!delayed_state(P, S, C, s_age, s_segdt, j, t.x, t.y, d)) continue;
-                    delayed_disp(P, t, d, pp.x, pp.y, code, rx, ry, sxd, syd);
+                    if (!delayed_state(P, S, C, s_age, s_segdt, j, t, d)) continue;
+                    delayed_disp(P, t, d, pp.x, pp.y, code, rx, ry, sp);
                     svx = d.vx; svy = d.vy;
                     const float rj = S.spin[j].z, rj2 = rj * rj;
                     sAng = d.angw * rsqrtf(1.f + d.angw * d.angw * rj2);
@@ -571,11 +589,11 @@ walk_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root,
                     dl = true;
                 } else {
                     const float2 pl = T.pt_lo[q];
-                    image_disp(P, t, pp.x, pp.y, pl.x, pl.y, code, rx, ry, sxd, syd);
+                    image_disp(P, t, pp.x, pp.y, pl.x, pl.y, code, rx, ry, sp);
                     const float2 pm = T.pt_mom[q];
                     svx = pv.x; svy = pv.y; sAng = pv.z; sMu = pm.x; sL = pm.y;
                 }
-                const bool yk = yukawa_in(P, rx, ry, sxd, syd, t.xd(), t.yd());
+                const bool yk = yukawa_in(P, rx, ry, sp, t);
                 pair_force<MAGGM, BRK>(P, t, rx, ry, svx, svy, pp.z, pp.w, sAng, sMu, sL, dl, yk, pe, A);
                 inter++;
             }
@@ -602,7 +620,7 @@ walk_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root,
             const unsigned open = mask & ~acc;
             if (accept) {                                            // forces.js:682-685
                 const float4 b = T.int_b[node];
-                const bool yk = yukawa_in(P, rx, ry, (double)a.x + (double)c.x, (double)a.y + (double)c.y, t.xd(), t.yd());
+                const bool yk = yukawa_in(P, rx, ry, SPos{ a.x, c.x, a.y, c.y }, t);
                 pair_force<MAGGM, BRK>(P, t, rx, ry, b.x, b.y, a.z, a.w, 0.f, b.z, b.w, false, yk, pe, A);
                 inter++;
             }
@@ -662,18 +680,6 @@ __device__ __forceinline__ int warp_incl_scan_i(int v) {
     return v;
 }
 
-// Image position of sorted point q as a compensated pair (ghost shifts and mirrors applied).
-__device__ __forceinline__ void point_image(const DevParams& P, float x, float y, float xlo, float ylo, uint32_t code,
-                                            float& ix, float& ixlo, float& iy, float& iylo) {
-    if (code == CODE_IDENTITY) { ix = x; ixlo = xlo; iy = y; iylo = ylo; return; }
-    df a = code_mx(code) ? df_add(df{ P.W, P.W_lo }, df{ -x, -xlo }) : df{ x, xlo };
-    df b = code_my(code) ? df_add(df{ P.H, P.H_lo }, df{ -y, -ylo }) : df{ y, ylo };
-    const int sx = code_sx(code), sy = code_sy(code);
-    if (sx) a = df_add(a, df{ sx * P.W, sx * P.W_lo });
-    if (sy) b = df_add(b, df{ sy * P.H, sy * P.H_lo });
-    ix = a.hi; ixlo = a.lo; iy = b.hi; iylo = b.lo;
-}
-
 __device__ __forceinline__ void stage_point(const DevParams& P, const TreeBufs& T, WalkSmem& W, int e, int q, unsigned mask) {
     const float4 pp = T.pt_pos[q];
     const float2 pl = T.pt_lo[q];
@@ -700,25 +706,24 @@ __device__ __forceinline__ void eval_sources(const DevParams& P, const DevState&
         const float4 c = W.sC[e];
         const uint32_t ref = __float_as_uint(c.w);
         float rx, ry, svx, svy, sAng, sMu, sL;
-        double sxd, syd;
+        SPos sp{ a.x, b.x, a.y, b.y };
         bool dl = false;
         if (ref == AGG_REF) {
             displacement(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
-            sxd = (double)a.x + (double)b.x; syd = (double)a.y + (double)b.y;
             svx = b.z; svy = b.w; sAng = 0.f; sMu = c.y; sL = c.z;
         } else {
             const int j = (int)ref_index(ref);
             if (j == t.idx) continue;                                 // self and own ghosts (forces.js:648-649)
             if (REL) {
                 Delayed d;
-                if (!delayed_state(P, S, C, s_age, s_segdt, j, t.x, t.y, d)) continue;
+                if (!delayed_state(P, S, C, s_age, s_segdt, j, t, d)) continue;
                 const uint32_t code = ref_code(ref);
                 float xj = 0.f, yj = 0.f;
                 if (code != CODE_IDENTITY && (code_mx(code) || code_my(code) || P.topology != GEON_TORUS)) {
                     const float4 pj = S.pos[j];
                     xj = pj.x; yj = pj.y;
                 }
-                delayed_disp(P, t, d, xj, yj, code, rx, ry, sxd, syd);
+                delayed_disp(P, t, d, xj, yj, code, rx, ry, sp);
                 svx = d.vx; svy = d.vy;
                 const float rj = S.spin[j].z, rj2 = rj * rj;
                 sAng = d.angw * rsqrtf(1.f + d.angw * d.angw * rj2);
@@ -727,11 +732,10 @@ __device__ __forceinline__ void eval_sources(const DevParams& P, const DevState&
                 dl = true;
             } else {
                 displacement(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
-                sxd = (double)a.x + (double)b.x; syd = (double)a.y + (double)b.y;
                 svx = b.z; svy = b.w; sAng = c.x; sMu = c.y; sL = c.z;
             }
         }
-        const bool yk = yukawa_in(P, rx, ry, sxd, syd, t.xd(), t.yd());
+        const bool yk = yukawa_in(P, rx, ry, sp, t);
         pair_force<MAGGM, BRK>(P, t, rx, ry, svx, svy, a.z, a.w, sAng, sMu, sL, dl, yk, pe, A);
         inter++;
     }
@@ -929,26 +933,27 @@ direct_kernel(DevParams P, DevState S, FrameCtl* ctl, ForceCtx C) {
             if (jg == i) continue;
             const float4 sp = s_pos[jj];
             const float4 sv = s_vel[jj];
-            float rx, ry; double sxd, syd;
+            float rx, ry;
+            SPos spos;
             float svx, svy, sAng;
             bool dl = false;
             if (REL) {
                 Delayed d;
-                if (!delayed_state(P, S, C, s_age, s_segdt, jg, t.x, t.y, d)) continue;
-                sxd = d.x; syd = d.y;
-                displacement(P, t.x, t.y, d.x, -t.xlo, d.y, -t.ylo, rx, ry);
+                if (!delayed_state(P, S, C, s_age, s_segdt, jg, t, d)) continue;
+                spos = SPos{ d.x, 0.f, d.y, 0.f };
+                rx = d.rx; ry = d.ry;
                 svx = d.vx; svy = d.vy;
                 sAng = d.angw * rsqrtf(1.f + d.angw * d.angw * sv.w);
                 dl = true;
             } else {
                 const float2 sl = s_lo[jj];
-                sxd = (double)sp.x + (double)sl.x; syd = (double)sp.y + (double)sl.y;
+                spos = SPos{ sp.x, sl.x, sp.y, sl.y };
                 displacement(P, t.x, t.y, sp.x, sl.x - t.xlo, sp.y, sl.y - t.ylo, rx, ry);
                 svx = sv.x; svy = sv.y; sAng = sv.z;
             }
             const float sMu = MAG_MOMENT_K * sp.w * sAng * sv.w;
             const float sL = INERTIA_K * sp.z * sAng * sv.w;
-            const bool yk = yukawa_in(P, rx, ry, sxd, syd, t.xd(), t.yd());
+            const bool yk = yukawa_in(P, rx, ry, spos, t);
             pair_force<MAGGM, BRK>(P, t, rx, ry, svx, svy, sp.z, sp.w, sAng, sMu, sL, dl, yk, pe, A);
             inter++;
         }
@@ -1051,15 +1056,15 @@ walk1pn_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_ro
                 const uint32_t code = ref_code(ref);
                 if (!in || j == t.idx) continue;
                 float rx, ry, svx, svy;
-                double sxd, syd;
                 if (code == CODE_IDENTITY) {
                     Delayed d;
-                    if (!delayed_state(P, S, C, s_age, s_segdt, j, t.x, t.y, d)) continue;
-                    displacement(P, t.x, t.y, d.x, -t.xlo, d.y, -t.ylo, rx, ry);
+                    if (!delayed_state(P, S, C, s_age, s_segdt, j, t, d)) continue;
+                    rx = d.rx; ry = d.ry;
                     svx = d.vx; svy = d.vy;
                 } else {
                     const float2 pl = T.pt_lo[q];
-                    image_disp(P, t, pp.x, pp.y, pl.x, pl.y, code, rx, ry, sxd, syd);
+                    SPos sp;
+                    image_disp(P, t, pp.x, pp.y, pl.x, pl.y, code, rx, ry, sp);
                     svx = pv.x; svy = pv.y;
                 }
                 accum_1pn(P, t, rx, ry, svx, svy, pp.z, pp.w, A.px, A.py);
@@ -1137,9 +1142,8 @@ direct1pn_kernel(DevParams P, DevState S, FrameCtl* ctl, ForceCtx C) {
             const int jg = base + jj;
             if (jg == i) continue;
             Delayed d;
-            if (!delayed_state(P, S, C, s_age, s_segdt, jg, t.x, t.y, d)) continue;
-            float rx, ry;
-            displacement(P, t.x, t.y, d.x, -t.xlo, d.y, -t.ylo, rx, ry);
+            if (!delayed_state(P, S, C, s_age, s_segdt, jg, t, d)) continue;
+            const float rx = d.rx, ry = d.ry;
             const float4 sp = s_pos[jj];
             accum_1pn(P, t, rx, ry, d.vx, d.vy, sp.z, sp.w, A.px, A.py);
             A.tick();

@@ -1,0 +1,261 @@
+"""GeonGPUPhysics — the reference's GPUPhysics backend surface over libgeon_cuda.so.
+
+Method names, argument meaning and return conventions follow
+src/gpu/gpu-physics.js (constructor :155, addParticle :1857, removeParticle
+:1936, setToggles :1969, update :3345, serialize :3749, deserialize :3886,
+reset :3973, requestStats/readStats :4146/:4234, getParticleCount :4287,
+destroy :4291) so a host that drives GPUPhysics can drive this class.
+
+Differences, all toward the CPU path (src/integrator.js), which is the
+authoritative semantics:
+  * addParticle takes coordinate velocity (vx, vy) and stores proper
+    velocity w = gamma v with |v| clamped below 0.999 (relativity.js:15-25,
+    as main.js:504-539 does for the CPU backend); GPUPhysics stores the
+    numbers it is given as w directly.
+  * removeParticle removes the slot at once and later slots shift down (the
+    CPU path's array compaction); ids from getParticleIds() stay stable.
+  * Scalar fields, bosons, collisions, heatmap, trails and rendering are not
+    part of this library; their GPUPhysics methods are inert stubs.
+"""
+from __future__ import annotations
+
+import math
+from typing import Any
+
+import numpy as np
+
+from . import _native as N
+from .system import GeonSystem
+
+GPU_MAX_PARTICLES = 512          # src/config.js:128 (the reference's buffer cap)
+MAX_SPEED_RATIO = 0.999          # src/config.js:32
+BOSON_CHARGE = 0.1               # src/config.js:75
+BOUND_NAMES = ["despawn", "bounce", "loop"]
+TOPO_NAMES = ["torus", "klein", "rp2"]
+
+
+def set_velocity(vx: float, vy: float):
+    """relativity.js:15-25: clamp |v| < 0.999, return (v, w = gamma v)."""
+    speed_sq = vx * vx + vy * vy
+    if speed_sq >= 1:
+        s = MAX_SPEED_RATIO / math.sqrt(speed_sq)
+        vx *= s
+        vy *= s
+    gamma = 1 / math.sqrt(max(1 - MAX_SPEED_RATIO * MAX_SPEED_RATIO, 1 - vx * vx - vy * vy))
+    return (vx, vy), (vx * gamma, vy * gamma)
+
+
+def quantise_charge(q: float) -> float:
+    """main.js:511 / gpu-physics.js:1873: charge is a multiple of 0.1."""
+    return round(q / BOSON_CHARGE) * BOSON_CHARGE
+
+
+def _get(obj: Any, name: str, default=None):
+    if isinstance(obj, dict):
+        return obj.get(name, default)
+    return getattr(obj, name, default)
+
+
+class GeonGPUPhysics:
+    """Drop-in for GPUPhysics; `device` is accepted for signature parity (the CUDA device is the current one)."""
+
+    def __init__(self, device=None, domainW: float = 100.0, domainH: float = 100.0,
+                 maxParticles: int = GPU_MAX_PARTICLES):
+        self.device = device
+        self.domainW = float(domainW)
+        self.domainH = float(domainH)
+        self.maxParticles = int(maxParticles)
+        self.boundaryMode = 0       # despawn
+        self.topologyMode = 0       # torus
+        self._collisionMode = 0
+        self.offX = 0.0
+        self.offY = 0.0
+        self._toggles = N.GRAVITY | N.COULOMB | N.MAGNETIC | N.GRAVITOMAG | N.ONE_PN | N.RELATIVITY | N.SPIN_ORBIT
+        self._flags = N.FLAG_PE | N.FLAG_BREAKDOWN
+        self._yukawaMu = 0.15
+        self._theta = 0.5
+        self._softening = 8.0
+        self._ext = dict(ext_gravity=0.0, ext_gravity_angle=math.pi * 0.5, ext_electric=0.0,
+                         ext_electric_angle=0.0, ext_bz=0.0)
+        self._bounceFriction = 0.4
+        self._sys: GeonSystem | None = None
+        self._stats = None
+        self._selected = -1
+        self._ready = False
+
+    # -- lifecycle --------------------------------------------------------------
+    def init(self):
+        """GPUPhysics.init(): allocates the device buffers."""
+        self._sys = GeonSystem(self._params(), self.maxParticles)
+        self._ready = True
+        return self
+
+    def destroy(self):
+        if self._sys:
+            self._sys.close()
+        self._sys = None
+        self._ready = False
+
+    def _params(self) -> N.GeonParams:
+        return N.make_params(toggles=self._toggles, flags=self._flags, boundary_mode=self.boundaryMode,
+                             topology=self.topologyMode, domain_w=self.domainW, domain_h=self.domainH,
+                             off_x=self.offX, off_y=self.offY, theta=self._theta, softening=self._softening,
+                             yukawa_mu=self._yukawaMu, bounce_friction=self._bounceFriction, **self._ext)
+
+    def _sync(self):
+        if self._sys:
+            self._sys.set_params(self._params())
+
+    # -- toggles (gpu-physics.js:1969-2000) -----------------------------------------
+    def setToggles(self, physics):
+        bits = [("gravityEnabled", N.GRAVITY), ("coulombEnabled", N.COULOMB), ("magneticEnabled", N.MAGNETIC),
+                ("gravitomagEnabled", N.GRAVITOMAG), ("onePNEnabled", N.ONE_PN),
+                ("relativityEnabled", N.RELATIVITY), ("spinOrbitEnabled", N.SPIN_ORBIT),
+                ("radiationEnabled", N.RADIATION), ("blackHoleEnabled", N.BLACK_HOLE),
+                ("yukawaEnabled", N.YUKAWA), ("higgsEnabled", N.HIGGS), ("axionEnabled", N.AXION),
+                ("barnesHutEnabled", N.BARNES_HUT)]
+        t = 0
+        for name, bit in bits:
+            if _get(physics, name, False):
+                t |= bit
+        self._toggles = t
+        self._yukawaMu = float(_get(physics, "yukawaMu", self._yukawaMu))
+        self._bounceFriction = float(_get(physics, "bounceFriction", self._bounceFriction))
+        for key, name in (("ext_gravity", "extGravity"), ("ext_gravity_angle", "extGravityAngle"),
+                          ("ext_electric", "extElectric"), ("ext_electric_angle", "extElectricAngle"),
+                          ("ext_bz", "extBz")):
+            v = _get(physics, name, None)
+            if v is not None:
+                self._ext[key] = float(v)
+        cm = _get(physics, "collisionMode", None)
+        if cm is not None:
+            self._collisionMode = cm
+        self._sync()
+
+    def setBoundary(self, boundaryMode: int, topologyMode: int = 0):
+        self.boundaryMode = int(boundaryMode)
+        self.topologyMode = int(topologyMode)
+        self._sync()
+
+    def setDomain(self, domainW: float, domainH: float, offX: float = 0.0, offY: float = 0.0):
+        self.domainW, self.domainH, self.offX, self.offY = float(domainW), float(domainH), float(offX), float(offY)
+        self._sync()
+
+    def setMethod(self, theta: float = 0.5, softening: float = 8.0):
+        """theta and softening are run-time parameters here (constants in config.js:44,57)."""
+        self._theta, self._softening = float(theta), float(softening)
+        self._sync()
+
+    # -- particles -----------------------------------------------------------------------
+    @property
+    def aliveCount(self) -> int:
+        return self._sys.count() if self._sys else 0
+
+    @property
+    def simTime(self) -> float:
+        return self._sys.sim_time() if self._sys else 0.0
+
+    def getParticleCount(self) -> int:
+        return self.aliveCount
+
+    def addParticle(self, p) -> int:
+        """{x, y, vx, vy, mass, charge, angw, antimatter} -> slot index, or -1 when full."""
+        if self.aliveCount >= self.maxParticles:
+            return -1
+        m = float(_get(p, "mass", 1.0))
+        (_, _), (wx, wy) = set_velocity(float(_get(p, "vx", 0.0)), float(_get(p, "vy", 0.0)))
+        q = quantise_charge(float(_get(p, "charge", 0.0)))
+        try:
+            return self._sys.add([_get(p, "x")], [_get(p, "y")], [wx], [wy], [m], [q],
+                                 [float(_get(p, "angw", 0.0))], creation_time=self.simTime)
+        except N.GeonError as e:
+            if e.code == N.GEON_ERR_FULL:
+                return -1
+            raise
+
+    def removeParticle(self, idx: int, deathMass: float = 0.0, deathAngVel: float = 0.0):
+        if 0 <= idx < self.aliveCount:
+            self._sys.remove(idx)
+
+    def patchMass(self, idx: int, newMass: float, newBaseMass: float):
+        """Roche-lobe transfer belongs to disintegration, which is not part of this library."""
+
+    def getParticleIds(self) -> np.ndarray:
+        return self._sys.ids()
+
+    # -- stepping ---------------------------------------------------------------------------
+    def update(self, dt: float):
+        """GPUPhysics.update(dt): one frame (gpu-physics.js:3345); returns the substeps taken."""
+        if not self._ready or dt <= 0:
+            return 0
+        return self._sys.update(dt)
+
+    # -- save / load (gpu-physics.js:3749-3972; save format save-load.js:89-120) --------------
+    def serialize(self, sim=None) -> dict:
+        st = self._sys.state()
+        parts = [{"x": float(st["x"][i]), "y": float(st["y"][i]), "wx": float(st["wx"][i]),
+                  "wy": float(st["wy"][i]), "mass": float(st["mass"][i]), "baseMass": float(st["mass"][i]),
+                  "charge": float(st["charge"][i]), "angw": float(st["angw"][i]), "antimatter": False}
+                 for i in range(st["x"].size)]
+        return {"version": 1, "particles": parts, "toggles": {},
+                "settings": {"boundary": BOUND_NAMES[self.boundaryMode], "topology": TOPO_NAMES[self.topologyMode]},
+                "yukawaMu": self._yukawaMu, "simTime": self.simTime}
+
+    def deserialize(self, state: dict, sim=None) -> bool:
+        if not state or state.get("version") != 1:
+            return False
+        parts = state.get("particles", [])[: self.maxParticles]
+        cols = {k: np.array([float(p.get(k, 0.0) or 0.0) for p in parts]) for k in ("x", "y", "wx", "wy", "charge", "angw")}
+        cols["mass"] = np.array([float(p.get("mass") or 1.0) for p in parts])
+        if "yukawaMu" in state:
+            self._yukawaMu = float(state["yukawaMu"])
+            self._sync()
+        self._sys.upload(cols["x"], cols["y"], cols["wx"], cols["wy"], cols["mass"], cols["charge"], cols["angw"],
+                         sim_time=float(state.get("simTime", 0.0)))
+        return True
+
+    def reset(self):
+        self._sys.reset()
+        self._stats = None
+
+    # -- stats (gpu-physics.js:4146-4283) ----------------------------------------------------
+    def requestStats(self, selectedGpuIdx: int = -1):
+        self._selected = int(selectedGpuIdx)
+        self._stats = self._sys.stats()
+
+    def readStats(self):
+        if self._stats is None:
+            return None
+        s = self._stats
+        self._stats = None
+        res = {"linearKE": s["linear_ke"], "spinKE": s["spin_ke"], "px": s["px"], "py": s["py"],
+               "orbitalAngMom": s["orbital_ang_mom"], "spinAngMom": s["spin_ang_mom"], "comX": s["com_x"],
+               "comY": s["com_y"], "totalMass": s["total_mass"], "aliveCount": s["alive_count"], "pe": s["pe"],
+               "selected": None}
+        i = self._selected
+        if 0 <= i < s["alive_count"]:
+            st = self._sys.state()
+            f = self._sys.forces()
+            res["selected"] = {
+                "posX": st["x"][i], "posY": st["y"][i], "velWX": st["wx"][i], "velWY": st["wy"][i],
+                "mass": st["mass"][i], "charge": st["charge"][i], "angW": st["angw"][i],
+                "velX": st["vx"][i], "velY": st["vy"][i], "angVel": st["angVel"][i],
+                "forceGravity": {"x": f["grav_x"][i], "y": f["grav_y"][i]},
+                "forceCoulomb": {"x": f["coul_x"][i], "y": f["coul_y"][i]},
+                "forceMagnetic": {"x": f["mag_x"][i], "y": f["mag_y"][i]},
+                "forceGravitomag": {"x": f["gm_x"][i], "y": f["gm_y"][i]},
+                "force1PN": {"x": f["f1pn_x"][i], "y": f["f1pn_y"][i]},
+                "forceYukawa": {"x": f["yuk_x"][i], "y": f["yuk_y"][i]},
+                "forceExternal": {"x": f["ext_x"][i], "y": f["ext_y"][i]},
+            }
+        return res
+
+    # -- inert stubs for the out-of-scope parts of GPUPhysics --------------------------------
+    def _stub(self, *a, **k):
+        return None
+
+    setHeatmapEnabled = setTrailsEnabled = dispatchHeatmap = resetFields = _stub
+    hitTest = _stub
+
+    def getFieldData(self, *a, **k):
+        return np.zeros(0, dtype=np.float32)
