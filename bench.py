@@ -46,11 +46,15 @@ STATE_KEYS = ("x", "y", "wx", "wy", "mass", "charge", "angw")
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--n", type=int, default=1 << 20)
-    ap.add_argument("--theta", type=float, default=0.5)
+    ap.add_argument("--theta", type=float, default=None,
+                    help="fixed opening angle; default: the largest theta whose RMS relative force error "
+                         "vs the pairwise sum is <= --target-error")
+    ap.add_argument("--target-error", type=float, default=1e-3)
+    ap.add_argument("--error-sample", type=int, default=16384)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=8192, help="targets per CPU sample step")
     return ap.parse_args()
@@ -113,7 +117,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
@@ -180,7 +184,7 @@ def run_reference(args, ws, rank):
         return
     from oracle import oracle
     threads = oracle.max_threads()
-    wl = W.plummer_disk(args.n, theta=args.theta)
+    wl = W.plummer_disk(args.n, theta=args.theta or 0.1)
     vals = []
     t0 = time.perf_counter()
     for s in range(args.warmup + args.steps):
@@ -193,7 +197,7 @@ def run_reference(args, ws, rank):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wl.n / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": wl.name, "n": wl.n, "theta": args.theta, "forces": "gravity+coulomb+yukawa",
+        "config": {"workload": wl.name, "n": wl.n, "theta": wl.params.theta, "forces": "gravity+coulomb+yukawa",
                    "dt": wl.dt, "leaf_capacity": 4},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"per step: full tree build of N={wl.n} plus the force walk of "
@@ -205,6 +209,46 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def force_error(g, idx, ref_fx, ref_fy) -> float:
+    """RMS over the sample of |F_bh - F_direct| / |F_direct| at the current state."""
+    g.compute_forces()
+    f = g.forces()
+    ex = f["fx"][idx].astype(np.float64) - ref_fx
+    ey = f["fy"][idx].astype(np.float64) - ref_fy
+    mag = np.hypot(ref_fx, ref_fy)
+    return float(np.sqrt(np.mean((np.hypot(ex, ey) / np.maximum(mag, 1e-30)) ** 2)))
+
+
+def calibrate_theta(g, n, target, sample, seed=11):
+    """Largest theta (to 2 %) with RMS relative force error <= target, by
+    bisection in log theta; errors grow monotonically with theta here."""
+    idx = np.sort(np.random.default_rng(seed).choice(n, size=min(sample, n), replace=False)).astype(np.int32)
+    fx, fy = g.direct_forces(idx)
+    fx = fx.astype(np.float64); fy = fy.astype(np.float64)
+    p = g.params()
+    lo, hi = 0.02, 1.0
+    errs = {}
+
+    def err_at(th):
+        p.theta = th
+        g.set_params(p)
+        e = force_error(g, idx, fx, fy)
+        errs[round(th, 5)] = e
+        return e
+
+    if err_at(hi) <= target:
+        lo = hi
+    else:
+        while hi / lo > 1.02:
+            mid = np.sqrt(lo * hi)
+            if err_at(mid) <= target:
+                lo = mid
+            else:
+                hi = mid
+    e = err_at(lo)
+    return lo, e, errs, len(idx)
+
+
 def run_native(args, ws, rank, local):
     import torch
     from physsim_gb300 import build, workloads as W
@@ -212,11 +256,23 @@ def run_native(args, ws, rank, local):
 
     build()
     torch.cuda.set_device(local)
-    wl = W.plummer_disk(args.n, theta=args.theta)
+    wl = W.plummer_disk(args.n, theta=args.theta or 0.5)
     n = wl.n
     g = GeonSystem(wl.params, n)
     stream = torch.cuda.ExternalStream(g.stream_ptr())
     host = {k: np.ascontiguousarray(wl.state[k], dtype=np.float32) for k in STATE_KEYS}
+    g.upload(*[host[k] for k in STATE_KEYS])
+    if args.theta is None:
+        theta, err, sweep, nsample = calibrate_theta(g, n, args.target_error, args.error_sample)
+    else:
+        idx = np.sort(np.random.default_rng(11).choice(n, size=min(args.error_sample, n), replace=False)).astype(np.int32)
+        fx, fy = g.direct_forces(idx)
+        theta, sweep, nsample = args.theta, {}, len(idx)
+        err = force_error(g, idx, fx.astype(np.float64), fy.astype(np.float64))
+    p = g.params()
+    p.theta = theta
+    g.set_params(p)
+    wl.params.theta = theta
     g.upload(*[host[k] for k in STATE_KEYS])
 
     # ---- device-resident timing ----
@@ -297,7 +353,7 @@ def run_native(args, ws, rank, local):
     if not args.no_cpu_baseline:
         from oracle import oracle
         threads = oracle.max_threads()
-        v, info = cpu_sample(wl, threads, args.cpu_sample)
+        v, info = cpu_sample(wl, threads, args.cpu_sample // 4 if theta < 0.2 else args.cpu_sample)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"one substep: full tree build of N={n} ({info['tree_s']:.2f} s) plus the force walk of "
                          f"{info['targets']} random targets ({info['walk_s']:.2f} s), extrapolated to N targets; "
@@ -306,8 +362,11 @@ def run_native(args, ws, rank, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": wl.name, "n": n, "theta": args.theta, "forces": "gravity+coulomb+yukawa+tidal",
-                   "method": "plain Barnes-Hut (learned correction not in this line)", "dt": wl.dt,
+        "config": {"workload": wl.name, "n": n, "theta": theta, "forces": "gravity+coulomb+yukawa+tidal",
+                   "method": "plain Barnes-Hut at the theta reaching the target error",
+                   "target_rms_rel_force_error": args.target_error, "rms_rel_force_error": err,
+                   "error_sample": f"{nsample} random particles vs the pairwise sum (geon_direct_forces)",
+                   "theta_search": {str(k): v for k, v in sorted(sweep.items())}, "dt": wl.dt,
                    "substeps_per_step": substeps / args.steps, "leaf_capacity": 4,
                    "l2": "working set ~0.5 GB > 129 MB L2 (no flush needed)",
                    "parallelism": "replicas" if ws > 1 else "single"},

@@ -232,6 +232,13 @@ int geon_compute_forces(GeonHandle* h);
  * the GEON_OUT_F1PN_* rows. */
 int geon_compute_1pn(GeonHandle* h);
 
+/* Pairwise forces on a subset of particles: the O(N^2) sum of
+ * computeAllForces' pairwise branch (src/forces.js:94-125) for the k listed
+ * particle indices, against all particles, written to fx[k], fy[k] (host
+ * arrays).  The particle state and stored forces are not changed.  This is the
+ * exact reference for measuring the Barnes-Hut force error on a subsample. */
+int geon_direct_forces(GeonHandle* h, const int32_t* idx, int32_t k, float* fx, float* fy);
+
 /* Copies `rows` rows (GEON_OUT_*) of per-particle force data, each `capacity`
  * floats, starting at row `first_row`. */
 int geon_download_forces(GeonHandle* h, int32_t first_row, int32_t rows,

@@ -146,6 +146,7 @@ SIGNATURES = {
     "geon_synchronize": [_handle_t],
     "geon_compute_forces": [_handle_t],
     "geon_compute_1pn": [_handle_t],
+    "geon_direct_forces": [_handle_t, _P(C.c_int32), C.c_int32, _P(C.c_float), _P(C.c_float)],
     "geon_download_forces": [_handle_t, C.c_int32, C.c_int32, _P(C.c_float), C.c_int32],
     "geon_build_tree": [_handle_t, _P(GeonTreeInfo)],
     "geon_tree_leaves": [_handle_t, _P(C.c_int32), C.c_int32, _P(C.c_double), _P(C.c_double), _P(C.c_double),

@@ -241,8 +241,7 @@ static int ensure_tree(GeonHandle* h) {
     T.idx = A.alloc<uint32_t>(T.cap_pts); T.idx_alt = A.alloc<uint32_t>(T.cap_pts);
     T.sort_tmp = A.alloc<char>(radix_temp_bytes(T.cap_pts));
     T.scan_tmp = A.alloc<int>(scan_temp_ints(T.cap_pts) + 16);
-    T.pt_pos = A.alloc<float4>(T.cap_pts); T.pt_lo = A.alloc<float2>(T.cap_pts);
-    T.pt_vel = A.alloc<float4>(T.cap_pts); T.pt_mom = A.alloc<float2>(T.cap_pts);
+    T.ps_a = A.alloc<float4>(T.cap_pts); T.ps_b = A.alloc<float4>(T.cap_pts); T.ps_c = A.alloc<float4>(T.cap_pts);
     T.lcp_a = A.alloc<int>(T.cap_pts); T.int_cnt = A.alloc<int>(T.cap_pts); T.int_base = A.alloc<int>(T.cap_pts);
     T.leaf_flag = A.alloc<int>(T.cap_pts); T.leaf_base = A.alloc<int>(T.cap_pts);
     T.real_flag = A.alloc<int>(T.cap_pts); T.tgt_base = A.alloc<int>(T.cap_pts);
@@ -635,6 +634,29 @@ int geon_compute_1pn(GeonHandle* h) {
     onepn_pass(h->P, h->S, h->T, h->d_root, h->ctl, make_ctx(h), bh, h->n_cap, h->st, h->lc);
     CKL();
     return read_ctl(h);
+}
+
+int geon_direct_forces(GeonHandle* h, const int32_t* idx, int32_t k, float* fx, float* fy) {
+    if (!h || k < 0 || (k > 0 && (!idx || !fx || !fy))) return GEON_ERR_ARG;
+    if (k == 0 || h->n == 0) return GEON_OK;
+    for (int i = 0; i < k; i++)
+        if (idx[i] < 0 || idx[i] >= h->n) return set_err(h, GEON_ERR_ARG, "index out of range");
+    DevArena tmp;
+    int* d_idx = tmp.alloc<int>(k);
+    float* d_fx = tmp.alloc<float>(k);
+    float* d_fy = tmp.alloc<float>(k);
+    if (tmp.failed) { tmp.free_all(); return set_err(h, GEON_ERR_NOMEM, "direct-forces allocation failed"); }
+    cudaError_t e = cudaMemcpyAsync(d_idx, idx, k * sizeof(int), cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess && h->P.rel) { launch_hist_tables(h->hist_t, h->simTime, h->hist_age, h->hist_segdt, h->st, h->lc); e = cudaGetLastError(); }
+    if (e == cudaSuccess) {
+        direct_subset(h->P, h->S, h->ctl, make_ctx(h), d_idx, k, d_fx, d_fy, h->st, h->lc);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fx, d_fx, k * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fy, d_fy, k * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    tmp.free_all();
+    return cuda_check(h, e, "direct forces");
 }
 
 int geon_download_forces(GeonHandle* h, int32_t first_row, int32_t rows, float* out, int32_t capacity) {

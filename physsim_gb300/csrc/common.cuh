@@ -236,6 +236,19 @@ __host__ __device__ inline void image_pos_d(double x, double y, uint32_t code, d
     gy = sy == 0 ? by : (sy > 0 ? by + H : by - H);
 }
 
+// Image position of particle (x + xlo, y + ylo) under a point code, as
+// compensated pairs (ghost shifts and mirrors, integrator.js:176-244).
+__device__ __forceinline__ void point_image(const DevParams& P, float x, float y, float xlo, float ylo, uint32_t code,
+                                            float& ix, float& ixlo, float& iy, float& iylo) {
+    if (code == CODE_IDENTITY) { ix = x; ixlo = xlo; iy = y; iylo = ylo; return; }
+    df a = code_mx(code) ? df_add(df{ P.W, P.W_lo }, df{ -x, -xlo }) : df{ x, xlo };
+    df b = code_my(code) ? df_add(df{ P.H, P.H_lo }, df{ -y, -ylo }) : df{ y, ylo };
+    const int sx = code_sx(code), sy = code_sy(code);
+    if (sx) a = df_add(a, df{ sx * P.W, sx * P.W_lo });
+    if (sy) b = df_add(b, df{ sy * P.H, sy * P.H_lo });
+    ix = a.hi; ixlo = a.lo; iy = b.hi; iylo = b.lo;
+}
+
 // Warp helpers
 __device__ __forceinline__ unsigned lane_id() { unsigned r; asm volatile("mov.u32 %0, %%laneid;" : "=r"(r)); return r; }
 __device__ __forceinline__ unsigned lanemask_lt() { unsigned r; asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(r)); return r; }

@@ -69,7 +69,9 @@ struct Acc {
 
 // ---- target particle ---------------------------------------------------------------
 struct Tgt {
-    float x, y, xlo, ylo, vx, vy, m, q, angVel, mu, L, r, r2, ri5;
+    float x, y, xlo, ylo, vx, vy, m, q, angVel, mu, L, r, r2;
+    float qm;       // q/m for the Coulomb share of the tidal coupling (forces.js:436), 0 when unused
+    float tk;       // -TIDAL_STRENGTH * bodyRadius^5 (forces.js:437-440)
     int idx;
     __device__ __forceinline__ double xd() const { return (double)x + (double)xlo; }
     __device__ __forceinline__ double yd() const { return (double)y + (double)ylo; }
@@ -86,9 +88,14 @@ __device__ __forceinline__ Tgt load_target(const DevState& S, int i) {
     t.r2 = s.z * s.z;                                   // bodyRadiusSq
     t.mu = MAG_MOMENT_K * t.q * t.angVel * t.r2;        // forces.js:74
     t.L = INERTIA_K * t.m * t.angVel * t.r2;            // forces.js:75
-    t.ri5 = t.r2 * t.r2 * sqrtf(t.r2);                  // forces.js:437-438
+    t.tk = -TIDAL_STRENGTH * (t.r2 * t.r2 * sqrtf(t.r2));
+    t.qm = 0.f;
     t.idx = i;
     return t;
+}
+
+__device__ __forceinline__ void target_coupling(const DevParams& P, Tgt& t) {
+    t.qm = ((P.toggles & GEON_COULOMB) && t.m > EPS_F) ? t.q / t.m : 0.f;
 }
 
 __device__ __forceinline__ bool on(const DevParams& P, uint32_t bit) { return (P.toggles & bit) != 0; }
@@ -114,18 +121,19 @@ __device__ __forceinline__ void pair_force(const DevParams& P, const Tgt& t, flo
     const float invR3a = invR3 * aberr;
     const float invR5a = invR5 * aberr;
     const bool grav = on(P, GEON_GRAVITY), coul = on(P, GEON_COULOMB);
+    float fr = 0.f;                                                  // sum of the radial (r-parallel) terms
 
     if (grav) {                                                      // forces.js:205-220
         const float k = t.m * sm;
         const float fDir = k * invR3a;
-        A.add(Q_FX, rx * fDir); A.add(Q_FY, ry * fDir);
+        fr += fDir;
         A.addk(K_GX, rx * fDir); A.addk(K_GY, ry * fDir);
         if (pe) A.add(Q_PE, -k * invR);
     }
     if (coul) {                                                      // forces.js:225-240
         const float k = -(t.q * sq);
         const float fDir = k * invR3a;
-        A.add(Q_FX, rx * fDir); A.add(Q_FY, ry * fDir);
+        fr += fDir;
         A.addk(K_CX, rx * fDir); A.addk(K_CY, ry * fDir);
         if (pe) A.add(Q_PE, t.q * sq * invR);
     }
@@ -162,13 +170,13 @@ __device__ __forceinline__ void pair_force(const DevParams& P, const Tgt& t, flo
         if (pn && gm && mag) {                                       // forces.js:300-316
             const float crossCoeff = t.q * sq * (t.m + sm) - (t.q * t.q * sm + sq * sq * t.m);
             const float fDir = crossCoeff * invRSq * invRSq;
-            A.add(Q_FX, rx * fDir); A.add(Q_FY, ry * fDir);
+            fr += fDir;
             A.addm(M_F1X, rx * fDir); A.addm(M_F1Y, ry * fDir);
             if (pe) A.add(Q_PE, 0.5f * crossCoeff * invRSq);
         }
         if (mag) {                                                   // forces.js:318-349
             const float fDir = -3.f * (t.mu * sMu) * invR5a;
-            A.add(Q_FX, rx * fDir); A.add(Q_FY, ry * fDir);
+            fr += fDir;
             A.addk(K_MX, rx * fDir); A.addk(K_MY, ry * fDir);
             if (pe) A.add(Q_PE, (t.mu * sMu) * invR3);
             const float BzMoving = sq * crossSV * invR3;
@@ -178,7 +186,7 @@ __device__ __forceinline__ void pair_force(const DevParams& P, const Tgt& t, flo
         }
         if (gm) {                                                    // forces.js:351-384
             const float fDir = 3.f * (t.L * sL) * invR5a;
-            A.add(Q_FX, rx * fDir); A.add(Q_FY, ry * fDir);
+            fr += fDir;
             A.addk(K_GMX, rx * fDir); A.addk(K_GMY, ry * fDir);
             if (pe) A.add(Q_PE, -(t.L * sL) * invR3);
             const float BgzMoving = -sm * crossSV * invR3;
@@ -194,7 +202,7 @@ __device__ __forceinline__ void pair_force(const DevParams& P, const Tgt& t, flo
         const float expMuR = __expf(-mu * r);
         const float g = YUKAWA_COUPLING * t.m * sm * expMuR;
         const float fDir = g * (invRSq + mu * invR) * (invR * aberr);
-        A.add(Q_FX, rx * fDir); A.add(Q_FY, ry * fDir);
+        fr += fDir;
         A.addk(K_YX, rx * fDir); A.addk(K_YY, ry * fDir);
         if (pe) A.add(Q_PE, -g * invR);
         if (MAGGM && on(P, GEON_ONE_PN)) {
@@ -211,16 +219,15 @@ __device__ __forceinline__ void pair_force(const DevParams& P, const Tgt& t, flo
             if (pe) A.add(Q_PE, 0.5f * g * invR * (v1DotV2 + nDotV1 * nDotV2 * alpha));
         }
     }
+    A.add(Q_FX, rx * fr);
+    A.add(Q_FY, ry * fr);
     if (grav) {                                                      // forces.js:428-441
         const float crossRV = rx * (svy - t.vy) - ry * (svx - t.vx);
-        const float wOrbit = crossRV * invRSq;
-        const float dw = t.angVel - wOrbit;
-        float coupling = sm;
-        if (coul && t.m > EPS_F) coupling += t.q * sq / t.m;
+        const float dw = __fmaf_rn(-crossRV, invRSq, t.angVel);
+        const float coupling = __fmaf_rn(t.qm, sq, sm);
         const float invR6 = invRSq * invRSq * invRSq;
-        A.add(Q_TID, -TIDAL_STRENGTH * coupling * coupling * t.ri5 * invR6 * dw);
+        A.add(Q_TID, t.tk * (coupling * coupling) * invR6 * dw);
     }
-    A.tick();
 }
 
 // ---- exact (FP64) displacement helpers for guard-band re-tests --------------------------
@@ -243,26 +250,6 @@ __device__ __forceinline__ bool yukawa_in(const DevParams& P, float rx, float ry
     double dx, dy;
     exact_disp(P, t.xd(), t.yd(), (double)sp.x + (double)sp.xlo, (double)sp.y + (double)sp.ylo, dx, dy);
     return dx * dx + dy * dy < P.yukCutSqD;
-}
-
-// Image position of a particle under a point code as compensated pairs
-// (ghost shifts and mirrors, integrator.js:176-244).
-__device__ __forceinline__ void point_image(const DevParams& P, float x, float y, float xlo, float ylo, uint32_t code,
-                                            float& ix, float& ixlo, float& iy, float& iylo) {
-    if (code == CODE_IDENTITY) { ix = x; ixlo = xlo; iy = y; iylo = ylo; return; }
-    df a = code_mx(code) ? df_add(df{ P.W, P.W_lo }, df{ -x, -xlo }) : df{ x, xlo };
-    df b = code_my(code) ? df_add(df{ P.H, P.H_lo }, df{ -y, -ylo }) : df{ y, ylo };
-    const int sx = code_sx(code), sy = code_sy(code);
-    if (sx) a = df_add(a, df{ sx * P.W, sx * P.W_lo });
-    if (sy) b = df_add(b, df{ sy * P.H, sy * P.H_lo });
-    ix = a.hi; ixlo = a.lo; iy = b.hi; iylo = b.lo;
-}
-
-// Displacement from the target to the image (code) of a particle at (x + xlo, y + ylo).
-__device__ __forceinline__ void image_disp(const DevParams& P, const Tgt& t, float x, float y, float xlo, float ylo,
-                                           uint32_t code, float& rx, float& ry, SPos& sp) {
-    point_image(P, x, y, xlo, ylo, code, sp.x, sp.xlo, sp.y, sp.ylo);
-    displacement(P, t.x, t.y, sp.x, sp.xlo - t.xlo, sp.y, sp.ylo - t.ylo, rx, ry);
 }
 
 // ---- signal delay (signal-delay.js:16-221) ----------------------------------------------
@@ -423,7 +410,8 @@ __device__ __forceinline__ void delayed_disp(const DevParams& P, const Tgt& t, c
 template <bool MAGGM, bool BRK>
 __device__ __forceinline__ void finalize_target(const DevParams& P, const DevState& S, const ForceCtx& C,
                                                 FrameCtl* ctl, const Tgt& t, bool valid, Acc<MAGGM, BRK>& A,
-                                                unsigned long long inter) {
+                                                unsigned inter32) {
+    unsigned long long inter = inter32;
     A.flush();
     double aSq = 0.0, wc = 0.0;
     if (valid) {
@@ -538,11 +526,11 @@ walk_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root,
     const unsigned active = __ballot_sync(0xffffffffu, valid);
     if (active == 0) return;
     Tgt t;
-    if (valid) t = load_target(S, T.tgt[k]);
+    if (valid) { t = load_target(S, T.tgt[k]); target_coupling(P, t); }
     else { t = Tgt{}; t.idx = -1; }
     Acc<MAGGM, BRK> A;
     A.init();
-    unsigned long long inter = 0;
+    unsigned inter = 0;
     const bool pe = C.pe != 0;
     const int root = *d_root;
     const bool treeOk = (ctl->err & (ERR_NODE_OVERFLOW | ERR_BAD_INDEX)) == 0;
@@ -567,34 +555,39 @@ walk_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root,
             const int4 lm = T.leaf_meta[li];
             if (lm.x < 0 || lm.x + lm.y > nValidW) { if (lane == 0) atomicOr(&ctl->err, ERR_BAD_INDEX); continue; }
             for (int q = lm.x; q < lm.x + lm.y; q++) {               // forces.js:643-679
-                const float4 pp = T.pt_pos[q];
-                const float4 pv = T.pt_vel[q];
-                const uint32_t ref = __float_as_uint(pv.w);
+                const float4 pa = T.ps_a[q];
+                const float4 pb = T.ps_b[q];
+                const float4 pc = T.ps_c[q];
+                const uint32_t ref = __float_as_uint(pc.w);
                 const int j = (int)ref_index(ref);
                 const uint32_t code = ref_code(ref);
                 if (!in || j == t.idx) continue;
                 float rx, ry;
-                SPos sp;
+                SPos sp{ pa.x, pb.x, pa.y, pb.y };
                 float svx, svy, sAng, sMu, sL;
                 bool dl = false;
                 if (REL) {
                     Delayed d;
                     if (!delayed_state(P, S, C, s_age, s_segdt, j, t, d)) continue;
-                    delayed_disp(P, t, d, pp.x, pp.y, code, rx, ry, sp);
+                    float xj = 0.f, yj = 0.f;
+                    if (code != CODE_IDENTITY && (code_mx(code) || code_my(code) || P.topology != GEON_TORUS)) {
+                        const float4 pj = S.pos[j];
+                        xj = pj.x; yj = pj.y;
+                    }
+                    delayed_disp(P, t, d, xj, yj, code, rx, ry, sp);
                     svx = d.vx; svy = d.vy;
                     const float rj = S.spin[j].z, rj2 = rj * rj;
                     sAng = d.angw * rsqrtf(1.f + d.angw * d.angw * rj2);
-                    sMu = MAG_MOMENT_K * pp.w * sAng * rj2;
-                    sL = INERTIA_K * pp.z * sAng * rj2;
+                    sMu = MAG_MOMENT_K * pa.w * sAng * rj2;
+                    sL = INERTIA_K * pa.z * sAng * rj2;
                     dl = true;
                 } else {
-                    const float2 pl = T.pt_lo[q];
-                    image_disp(P, t, pp.x, pp.y, pl.x, pl.y, code, rx, ry, sp);
-                    const float2 pm = T.pt_mom[q];
-                    svx = pv.x; svy = pv.y; sAng = pv.z; sMu = pm.x; sL = pm.y;
+                    displacement(P, t.x, t.y, pa.x, pb.x - t.xlo, pa.y, pb.y - t.ylo, rx, ry);
+                    svx = pb.z; svy = pb.w; sAng = pc.x; sMu = pc.y; sL = pc.z;
                 }
                 const bool yk = yukawa_in(P, rx, ry, sp, t);
-                pair_force<MAGGM, BRK>(P, t, rx, ry, svx, svy, pp.z, pp.w, sAng, sMu, sL, dl, yk, pe, A);
+                pair_force<MAGGM, BRK>(P, t, rx, ry, svx, svy, pa.z, pa.w, sAng, sMu, sL, dl, yk, pe, A);
+                A.tick();
                 inter++;
             }
         } else {
@@ -622,6 +615,7 @@ walk_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root,
                 const float4 b = T.int_b[node];
                 const bool yk = yukawa_in(P, rx, ry, SPos{ a.x, c.x, a.y, c.y }, t);
                 pair_force<MAGGM, BRK>(P, t, rx, ry, b.x, b.y, a.z, a.w, 0.f, b.z, b.w, false, yk, pe, A);
+                A.tick();
                 inter++;
             }
             if (open) {                                              // forces.js:686-692
@@ -648,26 +642,35 @@ walk_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root,
 
 // ---- batched Barnes-Hut walk ----------------------------------------------------------------
 // Same interaction lists as walk_kernel, restructured for throughput:
-//  * up to 32 stack entries are popped per iteration, one per lane, so the
-//    node records are fetched with one wide load instead of 32 dependent ones;
-//  * every lane's opening test against each of those nodes runs from
-//    shuffled registers, and one ballot per node splits its lane mask;
-//  * accepted aggregates and the points of reached leaves are staged, with
-//    their lane masks, in a per-warp source list in shared memory, which is
-//    evaluated in a tight loop once it fills (all reads are broadcasts).
-constexpr int WB_THREADS = 128;
-constexpr int WB_WARPS = WB_THREADS / 32;
-constexpr int WB_STACK = 512;
-constexpr int WB_SRC = 160;
+//  * each iteration pops up to WC_POP stack entries, one per lane, so the node
+//    records arrive with one wide load;
+//  * a lane first tests its node against the bounding box of the warp's 32
+//    particles: if every particle accepts the node, or every particle opens
+//    it, no per-particle test is needed; only the remaining ("mixed") nodes
+//    get the per-lane test, from shuffled registers, with a ballot;
+//  * accepted aggregates and the points of reached leaves are staged in a
+//    per-warp pool in shared memory.  Entries every particle needs go to a
+//    list evaluated with broadcast reads; entries only some particles need go
+//    to per-lane index lists, evaluated transposed so that no lane idles on
+//    another lane's sources.
+constexpr int WC_THREADS = 128;
+constexpr int WC_WARPS = WC_THREADS / 32;
+constexpr int WC_STACK = 512;
+constexpr int WC_RESERVE = 3 * KEY_LEVELS + 3 * 16 + 4;   // growth a depth-first tail can still need
+constexpr int WC_POOL = 96;
+constexpr int WC_POP = 16;
 constexpr uint32_t AGG_REF = 0xffffffffu;
 
-struct WalkSmem {
-    int stk_node[WB_STACK];
-    unsigned stk_mask[WB_STACK];
-    float4 sA[WB_SRC];       // x_hi, y_hi, mass, charge
-    float4 sB[WB_SRC];       // x_lo, y_lo, vx, vy
-    float4 sC[WB_SRC];       // angVel, mu, L, ref bits (AGG_REF for aggregates)
-    unsigned sM[WB_SRC];     // lane mask
+template <bool NEEDC>
+struct WcSmem {
+    int stk_node[WC_STACK];
+    unsigned stk_mask[WC_STACK];
+    float4 a[WC_POOL];                 // x (hi), y (hi), mass, charge
+    float4 b[WC_POOL];                 // x (lo), y (lo), vx, vy
+    float4 c[NEEDC ? WC_POOL : 1];     // angVel, magMoment, angMomentum, -
+    uint32_t ref[WC_POOL];             // particle ref, AGG_REF for aggregates
+    uint8_t full[WC_POOL];             // pool indices every lane evaluates
+    uint8_t lst[WC_POOL][32];          // per-lane lists (column = lane) of partial entries
 };
 
 __device__ __forceinline__ int warp_incl_scan_i(int v) {
@@ -679,133 +682,201 @@ __device__ __forceinline__ int warp_incl_scan_i(int v) {
     }
     return v;
 }
-
-__device__ __forceinline__ void stage_point(const DevParams& P, const TreeBufs& T, WalkSmem& W, int e, int q, unsigned mask) {
-    const float4 pp = T.pt_pos[q];
-    const float2 pl = T.pt_lo[q];
-    const float4 pv = T.pt_vel[q];
-    const float2 pm = T.pt_mom[q];
-    const uint32_t ref = __float_as_uint(pv.w);
-    float ix, ixlo, iy, iylo;
-    point_image(P, pp.x, pp.y, pl.x, pl.y, ref_code(ref), ix, ixlo, iy, iylo);
-    W.sA[e] = make_float4(ix, iy, pp.z, pp.w);
-    W.sB[e] = make_float4(ixlo, iylo, pv.x, pv.y);
-    W.sC[e] = make_float4(pv.z, pm.x, pm.y, pv.w);
-    W.sM[e] = mask;
+__device__ __forceinline__ float warp_min_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_max_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ int warp_max_i(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
 }
 
 template <bool MAGGM, bool REL, bool BRK>
-__device__ __forceinline__ void eval_sources(const DevParams& P, const DevState& S, const ForceCtx& C,
-                                             const float* s_age, const float* s_segdt, const WalkSmem& W, int cnt,
-                                             const Tgt& t, Acc<MAGGM, BRK>& A, unsigned long long& inter, bool pe) {
-    const unsigned lane = threadIdx.x & 31;
-    for (int e = 0; e < cnt; e++) {
-        if (!((W.sM[e] >> lane) & 1u)) continue;
-        const float4 a = W.sA[e];
-        const float4 b = W.sB[e];
-        const float4 c = W.sC[e];
-        const uint32_t ref = __float_as_uint(c.w);
-        float rx, ry, svx, svy, sAng, sMu, sL;
-        SPos sp{ a.x, b.x, a.y, b.y };
-        bool dl = false;
-        if (ref == AGG_REF) {
-            displacement(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
-            svx = b.z; svy = b.w; sAng = 0.f; sMu = c.y; sL = c.z;
-        } else {
-            const int j = (int)ref_index(ref);
-            if (j == t.idx) continue;                                 // self and own ghosts (forces.js:648-649)
-            if (REL) {
-                Delayed d;
-                if (!delayed_state(P, S, C, s_age, s_segdt, j, t, d)) continue;
-                const uint32_t code = ref_code(ref);
-                float xj = 0.f, yj = 0.f;
-                if (code != CODE_IDENTITY && (code_mx(code) || code_my(code) || P.topology != GEON_TORUS)) {
-                    const float4 pj = S.pos[j];
-                    xj = pj.x; yj = pj.y;
-                }
-                delayed_disp(P, t, d, xj, yj, code, rx, ry, sp);
-                svx = d.vx; svy = d.vy;
-                const float rj = S.spin[j].z, rj2 = rj * rj;
-                sAng = d.angw * rsqrtf(1.f + d.angw * d.angw * rj2);
-                sMu = MAG_MOMENT_K * a.w * sAng * rj2;
-                sL = INERTIA_K * a.z * sAng * rj2;
-                dl = true;
-            } else {
-                displacement(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
-                svx = b.z; svy = b.w; sAng = c.x; sMu = c.y; sL = c.z;
+__device__ __forceinline__ void eval_entry(const DevParams& P, const DevState& S, const ForceCtx& C,
+                                           const float* s_age, const float* s_segdt, const WcSmem<MAGGM || REL>& W,
+                                           int e, const Tgt& t, Acc<MAGGM, BRK>& A, unsigned& inter, bool pe) {
+    const float4 a = W.a[e];
+    const float4 b = W.b[e];
+    const uint32_t ref = W.ref[e];
+    float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (MAGGM || REL) c = W.c[e];
+    float rx, ry, svx = b.z, svy = b.w, sAng = c.x, sMu = c.y, sL = c.z;
+    SPos sp{ a.x, b.x, a.y, b.y };
+    bool dl = false;
+    if (ref != AGG_REF) {
+        const int j = (int)ref_index(ref);
+        if (j == t.idx) return;                                       // self and own ghosts (forces.js:648-649)
+        if (REL) {                                                    // forces.js:652-672
+            Delayed d;
+            if (!delayed_state(P, S, C, s_age, s_segdt, j, t, d)) return;
+            const uint32_t code = ref_code(ref);
+            float xj = 0.f, yj = 0.f;
+            if (code != CODE_IDENTITY && (code_mx(code) || code_my(code) || P.topology != GEON_TORUS)) {
+                const float4 pj = S.pos[j];
+                xj = pj.x; yj = pj.y;
             }
+            delayed_disp(P, t, d, xj, yj, code, rx, ry, sp);
+            svx = d.vx; svy = d.vy;
+            const float rj = S.spin[j].z, rj2 = rj * rj;
+            sAng = d.angw * rsqrtf(1.f + d.angw * d.angw * rj2);
+            sMu = MAG_MOMENT_K * a.w * sAng * rj2;
+            sL = INERTIA_K * a.z * sAng * rj2;
+            dl = true;
+        } else {
+            displacement(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
         }
-        const bool yk = yukawa_in(P, rx, ry, sp, t);
-        pair_force<MAGGM, BRK>(P, t, rx, ry, svx, svy, a.z, a.w, sAng, sMu, sL, dl, yk, pe, A);
-        inter++;
+    } else {
+        displacement(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
+    }
+    const bool yk = yukawa_in(P, rx, ry, sp, t);
+    pair_force<MAGGM, BRK>(P, t, rx, ry, svx, svy, a.z, a.w, sAng, sMu, sL, dl, yk, pe, A);
+    inter++;
+}
+
+template <bool MAGGM, bool REL, bool BRK>
+__device__ __forceinline__ void flush_pool(const DevParams& P, const DevState& S, const ForceCtx& C,
+                                           const float* s_age, const float* s_segdt, WcSmem<MAGGM || REL>& W,
+                                           int& nfull, int& lcnt, int& npool, const Tgt& t, Acc<MAGGM, BRK>& A,
+                                           unsigned& inter, bool pe) {
+    __syncwarp();
+    const unsigned lane = threadIdx.x & 31;
+    const int total = nfull + warp_max_i(lcnt);
+    // full entries first (broadcast reads), then this lane's own list; two
+    // independent entries per iteration for instruction-level parallelism
+    for (int i = 0; i < total; i += 2) {
+        const int l0 = i - nfull, l1 = i + 1 - nfull;
+        const int e0 = l0 < 0 ? W.full[i] : (l0 < lcnt ? W.lst[l0][lane] : -1);
+        const int e1 = (i + 1 >= total) ? -1 : (l1 < 0 ? W.full[i + 1] : (l1 < lcnt ? W.lst[l1][lane] : -1));
+        if (e0 >= 0) eval_entry<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, e0, t, A, inter, pe);
+        if (e1 >= 0) eval_entry<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, e1, t, A, inter, pe);
+        A.tick();
+    }
+    __syncwarp();
+    nfull = 0; lcnt = 0; npool = 0;
+}
+
+template <bool NEEDC>
+__device__ __forceinline__ void stage_point(const TreeBufs& T, WcSmem<NEEDC>& W, int e, int q) {
+    const float4 pc = T.ps_c[q];
+    W.a[e] = T.ps_a[q];
+    W.b[e] = T.ps_b[q];
+    if (NEEDC) W.c[e] = pc;
+    W.ref[e] = __float_as_uint(pc.w);
+}
+
+// Adds entries [e0, e0+cnt) with lane mask m to the full list or the per-lane lists.
+template <bool NEEDC>
+__device__ __forceinline__ void list_entries(WcSmem<NEEDC>& W, unsigned m, unsigned active, int e0, int cnt,
+                                             int& nfull, int& lcnt) {
+    const unsigned lane = threadIdx.x & 31;
+    if (m == active) {
+        if ((int)lane < cnt) W.full[nfull + lane] = (uint8_t)(e0 + lane);
+        nfull += cnt;
+    } else if ((m >> lane) & 1u) {
+        for (int q = 0; q < cnt; q++) W.lst[lcnt + q][lane] = (uint8_t)(e0 + q);
+        lcnt += cnt;
     }
 }
 
 template <bool MAGGM, bool REL, bool BRK>
-__global__ void __launch_bounds__(WB_THREADS)
-walkb_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
-    extern __shared__ __align__(16) unsigned char wb_smem[];
-    WalkSmem* Wall = reinterpret_cast<WalkSmem*>(wb_smem);
-    float* s_age = reinterpret_cast<float*>(Wall + WB_WARPS);
+__global__ void __launch_bounds__(WC_THREADS, (MAGGM || REL || BRK) ? 3 : 5)
+walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
+    constexpr bool NEEDC = MAGGM || REL;
+    extern __shared__ __align__(16) unsigned char wc_smem[];
+    WcSmem<NEEDC>* Wall = reinterpret_cast<WcSmem<NEEDC>*>(wc_smem);
+    float* s_age = reinterpret_cast<float*>(Wall + WC_WARPS);
     float* s_segdt = s_age + HIST_LEN;
     if (REL) load_hist_tables(C, s_age, s_segdt);
     const int n = ctl->n;
     const int warp = threadIdx.x >> 5;
     const unsigned lane = threadIdx.x & 31;
-    WalkSmem& W = Wall[warp];
-    const int k0 = (blockIdx.x * WB_WARPS + warp) * 32 + (int)lane;
+    WcSmem<NEEDC>& W = Wall[warp];
+    const int k0 = (blockIdx.x * WC_WARPS + warp) * 32 + (int)lane;
     const bool valid = k0 < n;
     const unsigned active = __ballot_sync(0xffffffffu, valid);
     if (active == 0) return;
     Tgt t;
-    if (valid) t = load_target(S, T.tgt[k0]);
+    if (valid) { t = load_target(S, T.tgt[k0]); target_coupling(P, t); }
     else { t = Tgt{}; t.idx = -1; }
     Acc<MAGGM, BRK> A;
     A.init();
-    unsigned long long inter = 0;
+    unsigned inter = 0;
     const bool pe = C.pe != 0;
+    // bounding box of the warp's particles (padded beyond the rounding of hi + lo)
+    const float bx0 = warp_min_f(valid ? t.x : 3.0e38f), bx1 = warp_max_f(valid ? t.x : -3.0e38f);
+    const float by0 = warp_min_f(valid ? t.y : 3.0e38f), by1 = warp_max_f(valid ? t.y : -3.0e38f);
+    const float gcx = 0.5f * (bx0 + bx1), gcy = 0.5f * (by0 + by1);
+    const float ghx = 0.5f * (bx1 - bx0) * (1.f + 1e-6f) + 1e-6f * fabsf(gcx) + 1e-30f;
+    const float ghy = 0.5f * (by1 - by0) * (1.f + 1e-6f) + 1e-6f * fabsf(gcy) + 1e-30f;
+    const bool groupTests = !P.periodic || P.topology == GEON_TORUS;
+
     const int root = *d_root;
     const bool treeOk = (ctl->err & (ERR_NODE_OVERFLOW | ERR_BAD_INDEX)) == 0;
     const int nIntW = ctl->nInternal, nLeafW = ctl->nLeaves, nValidW = ctl->nValid;
-    const unsigned lt = lanemask_lt();
-    int top = 0, cnt = 0;
+    int top = 0, npool = 0, nfull = 0, lcnt = 0;
     if (root != ROOT_NONE && treeOk) {
         if (lane == 0) { W.stk_node[0] = root; W.stk_mask[0] = active; }
         top = 1;
     }
     __syncwarp();
     while (top > 0) {
-        // popping k entries and pushing up to 4 children each must fit the stack
-        const int k = min(min(32, top), (WB_STACK - top) / 3);
-        if (k <= 0) { if (lane == 0) atomicOr(&ctl->err, ERR_STACK_OVERFLOW); break; }
+        // wide pops while the stack has room; single pops (depth first) near the limit
+        int k = min(min(WC_POP, top), (WC_STACK - WC_RESERVE - top) / 3);
+        if (k < 1) k = 1;
+        if (top + 3 > WC_STACK) { if (lane == 0) atomicOr(&ctl->err, ERR_STACK_OVERFLOW); break; }
         int node = -1;
         unsigned mask = 0;
         if ((int)lane < k) { node = W.stk_node[top - k + lane]; mask = W.stk_mask[top - k + lane]; }
         __syncwarp();
         top -= k;
-        // fetch the popped node records, one per lane
-        bool isLeaf = false, skip = true;
+        // node records, one per lane; classification against the group box
+        int kind = 0;                          // 0 none, 1 leaf, 2 all accept, 3 all open, 4 mixed
         float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nc = make_float4(0.f, 0.f, 0.f, 0.f);
         int4 lm = make_int4(0, 0, 0, 0);
         if (node >= 0) {
             if (node & LEAF_REF) {
                 const int li = node & ~LEAF_REF;
                 if (li < nLeafW) {
-                    isLeaf = true;
                     lm = T.leaf_meta[li];
-                    na.z = T.leaf_a[li].z;
-                    skip = na.z < EPS_F || lm.x < 0 || lm.x + lm.y > nValidW;
+                    const float lmass = T.leaf_a[li].z;
+                    if (lmass >= EPS_F && lm.x >= 0 && lm.x + lm.y <= nValidW) kind = 1;   // forces.js:630,643
                 } else atomicOr(&ctl->err, ERR_BAD_INDEX);
             } else if (node < nIntW) {
                 na = T.int_a[node];
                 nc = T.int_c[node];
-                skip = na.z < EPS_F;                                  // forces.js:630
+                if (na.z >= EPS_F) {
+                    kind = 4;
+                    if (groupTests) {
+                        float dx, dy;
+                        if (P.periodic) {
+                            dx = wrap_axis_comp(na.x, gcx, nc.x, P.W, P.W_lo, P.halfW);
+                            dy = wrap_axis_comp(na.y, gcy, nc.y, P.H, P.H_lo, P.halfH);
+                        } else {
+                            dx = __fadd_rn(__fsub_rn(na.x, gcx), nc.x);
+                            dy = __fadd_rn(__fsub_rn(na.y, gcy), nc.y);
+                        }
+                        const float ax = fabsf(dx), ay = fabsf(dy);
+                        const bool wrapSafe = !P.periodic || (ax + ghx < 0.999f * P.halfW && ay + ghy < 0.999f * P.halfH);
+                        if (wrapSafe) {
+                            const float mnx = fmaxf(ax - ghx, 0.f), mny = fmaxf(ay - ghy, 0.f);
+                            const float mxx = ax + ghx, mxy = ay + ghy;
+                            const float dmin2 = mnx * mnx + mny * mny, dmax2 = mxx * mxx + mxy * mxy;
+                            if (nc.z < P.thetaSq * dmin2 * (1.f - 1e-5f)) kind = 2;
+                            else if (nc.z >= P.thetaSq * dmax2 * (1.f + 1e-5f)) kind = 3;
+                        }
+                    }
+                }
             } else atomicOr(&ctl->err, ERR_BAD_INDEX);
         }
-        // per-lane opening tests against each popped internal node (forces.js:680)
-        unsigned myAcc = 0, myOpen = 0;
-        const unsigned testMask = __ballot_sync(0xffffffffu, !skip && !isLeaf);
-        for (unsigned tm = testMask; tm; tm &= tm - 1) {
+        unsigned myAcc = kind == 2 ? mask : 0u, myOpen = kind == 3 ? mask : 0u;
+        for (unsigned tm = __ballot_sync(0xffffffffu, kind == 4); tm; tm &= tm - 1) {   // forces.js:680
             const int jj = __ffs(tm) - 1;
             const float cx = __shfl_sync(0xffffffffu, na.x, jj), cy = __shfl_sync(0xffffffffu, na.y, jj);
             const float clx = __shfl_sync(0xffffffffu, nc.x, jj), cly = __shfl_sync(0xffffffffu, nc.y, jj);
@@ -825,51 +896,54 @@ walkb_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
                 }
             }
             const unsigned acc = __ballot_sync(0xffffffffu, accept);
-            if ((int)lane == jj) { myAcc = acc; myOpen = msk & ~acc; }
+            if ((int)lane == jj) { myAcc = acc & msk; myOpen = msk & ~acc; }
         }
-        const unsigned leafMask = (isLeaf && !skip) ? mask : 0u;
+        const unsigned leafMask = kind == 1 ? mask : 0u;
         const bool bucket = leafMask && lm.y > LEAF_CAP;
         const int myPts = (leafMask && !bucket) ? lm.y : 0;
-        const unsigned aggBal = __ballot_sync(0xffffffffu, myAcc != 0);
-        const int ptsIncl = warp_incl_scan_i(myPts);
-        const int ptsTot = __shfl_sync(0xffffffffu, ptsIncl, 31);
-        if (cnt + __popc(aggBal) + ptsTot > WB_SRC) {
-            __syncwarp();
-            eval_sources<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, cnt, t, A, inter, pe);
-            __syncwarp();
-            cnt = 0;
-        }
+        const int myEnt = (myAcc ? 1 : 0) + myPts;
+        int incl = warp_incl_scan_i(myEnt);
+        const int tot = __shfl_sync(0xffffffffu, incl, 31);
+        if (npool + tot > WC_POOL)
+            flush_pool<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
+        const int e0 = npool + incl - myEnt;
         if (myAcc) {                                                  // forces.js:682-685
-            const int e = cnt + __popc(aggBal & lt);
             const float4 nb = T.int_b[node];
-            W.sA[e] = na;
-            W.sB[e] = make_float4(nc.x, nc.y, nb.x, nb.y);
-            W.sC[e] = make_float4(0.f, nb.z, nb.w, __uint_as_float(AGG_REF));
-            W.sM[e] = myAcc;
+            W.a[e0] = na;
+            W.b[e0] = make_float4(nc.x, nc.y, nb.x, nb.y);
+            if (NEEDC) W.c[e0] = make_float4(0.f, nb.z, nb.w, 0.f);
+            W.ref[e0] = AGG_REF;
         }
-        cnt += __popc(aggBal);
-        {                                                             // forces.js:643-679
-            const int base = cnt + ptsIncl - myPts;
-            for (int q = 0; q < myPts; q++) stage_point(P, T, W, base + q, lm.x + q, leafMask);
-            cnt += ptsTot;
+        const int p0 = e0 + (myAcc ? 1 : 0);
+        for (int q = 0; q < myPts; q++) stage_point<NEEDC>(T, W, p0 + q, lm.x + q);   // forces.js:643-679
+        npool += tot;
+        __syncwarp();
+        // route the new entries to the full list or the per-lane lists
+        for (unsigned gm = __ballot_sync(0xffffffffu, myAcc != 0); gm; gm &= gm - 1) {
+            const int jj = __ffs(gm) - 1;
+            list_entries<NEEDC>(W, __shfl_sync(0xffffffffu, myAcc, jj), active, __shfl_sync(0xffffffffu, e0, jj), 1, nfull, lcnt);
         }
-        for (unsigned bk = __ballot_sync(0xffffffffu, bucket); bk; bk &= bk - 1) {   // leaves deeper than the key
+        for (unsigned gm = __ballot_sync(0xffffffffu, myPts > 0); gm; gm &= gm - 1) {
+            const int jj = __ffs(gm) - 1;
+            list_entries<NEEDC>(W, __shfl_sync(0xffffffffu, leafMask, jj), active, __shfl_sync(0xffffffffu, p0, jj),
+                                __shfl_sync(0xffffffffu, myPts, jj), nfull, lcnt);
+        }
+        // leaves holding more than LEAF_CAP points (level-31 buckets)
+        for (unsigned bk = __ballot_sync(0xffffffffu, bucket); bk; bk &= bk - 1) {
             const int jj = __ffs(bk) - 1;
             const int bstart = __shfl_sync(0xffffffffu, lm.x, jj), bcount = __shfl_sync(0xffffffffu, lm.y, jj);
             const unsigned bmask = __shfl_sync(0xffffffffu, leafMask, jj);
             for (int b0 = 0; b0 < bcount; b0 += 32) {
                 const int chunk = min(32, bcount - b0);
-                if (cnt + chunk > WB_SRC) {
-                    __syncwarp();
-                    eval_sources<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, cnt, t, A, inter, pe);
-                    __syncwarp();
-                    cnt = 0;
-                }
-                if ((int)lane < chunk) stage_point(P, T, W, cnt + lane, bstart + b0 + lane, bmask);
-                cnt += chunk;
+                if (npool + chunk > WC_POOL)
+                    flush_pool<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
+                if ((int)lane < chunk) stage_point<NEEDC>(T, W, npool + lane, bstart + b0 + lane);
+                __syncwarp();
+                list_entries<NEEDC>(W, bmask, active, npool, chunk, nfull, lcnt);
+                npool += chunk;
             }
         }
-        // push children of the nodes some lanes must open (forces.js:686-692)
+        // children of nodes some lanes open (forces.js:686-692)
         int4 ch = make_int4(-1, -1, -1, -1);
         int myCh = 0;
         if (myOpen) {
@@ -888,12 +962,12 @@ walkb_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
         top += chTot;
         __syncwarp();
     }
-    __syncwarp();
-    eval_sources<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, cnt, t, A, inter, pe);
+    flush_pool<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
     finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter);
 }
 
-constexpr size_t WB_SMEM = sizeof(WalkSmem) * WB_WARPS + 2 * HIST_LEN * sizeof(float);
+template <bool MAGGM, bool REL>
+constexpr size_t wc_smem_bytes() { return sizeof(WcSmem<MAGGM || REL>) * WC_WARPS + 2 * HIST_LEN * sizeof(float); }
 
 // ---- pairwise O(N^2) sum (forces.js:94-125) -------------------------------------------------
 constexpr int DIRECT_THREADS = 256;
@@ -910,11 +984,11 @@ direct_kernel(DevParams P, DevState S, FrameCtl* ctl, ForceCtx C) {
     const int i = blockIdx.x * DIRECT_THREADS + threadIdx.x;
     const bool valid = i < n;
     Tgt t;
-    if (valid) t = load_target(S, i);
+    if (valid) { t = load_target(S, i); target_coupling(P, t); }
     else { t = Tgt{}; t.idx = -1; }
     Acc<MAGGM, BRK> A;
     A.init();
-    unsigned long long inter = 0;
+    unsigned inter = 0;
     const bool pe = C.pe != 0;
     for (int base = 0; base < n; base += DIRECT_THREADS) {
         const int j = base + threadIdx.x;
@@ -955,10 +1029,91 @@ direct_kernel(DevParams P, DevState S, FrameCtl* ctl, ForceCtx C) {
             const float sL = INERTIA_K * sp.z * sAng * sv.w;
             const bool yk = yukawa_in(P, rx, ry, spos, t);
             pair_force<MAGGM, BRK>(P, t, rx, ry, svx, svy, sp.z, sp.w, sAng, sMu, sL, dl, yk, pe, A);
+            A.tick();
             inter++;
         }
     }
     finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter);
+}
+
+// ---- pairwise forces for a subset of targets (no state change) -----------------------------
+// The O(N^2) sum of forces.js:94-125 evaluated for the listed particles only
+// and written to separate outputs: the exact reference against which the
+// Barnes-Hut force error is measured.
+template <bool MAGGM, bool REL>
+__global__ void __launch_bounds__(DIRECT_THREADS)
+direct_subset_kernel(DevParams P, DevState S, const FrameCtl* ctl, ForceCtx C, const int* __restrict__ idx, int k,
+                     float* __restrict__ out_fx, float* __restrict__ out_fy) {
+    __shared__ float4 s_pos[DIRECT_THREADS];
+    __shared__ float4 s_vel[DIRECT_THREADS];
+    __shared__ float2 s_lo[DIRECT_THREADS];
+    __shared__ float s_age[REL ? HIST_LEN : 1], s_segdt[REL ? HIST_LEN : 1];
+    if (REL) load_hist_tables(C, s_age, s_segdt);
+    const int n = ctl->n;
+    const int ti = blockIdx.x * DIRECT_THREADS + threadIdx.x;
+    const bool valid = ti < k && idx[ti] >= 0 && idx[ti] < n;
+    const int i = valid ? idx[ti] : -1;
+    Tgt t;
+    if (valid) { t = load_target(S, i); target_coupling(P, t); }
+    else { t = Tgt{}; t.idx = -1; }
+    Acc<MAGGM, false> A;
+    A.init();
+    for (int base = 0; base < n; base += DIRECT_THREADS) {
+        const int j = base + threadIdx.x;
+        __syncthreads();
+        if (j < n) {
+            const float4 sv = S.vel[j], ss = S.spin[j];
+            s_pos[threadIdx.x] = S.pos[j];
+            s_lo[threadIdx.x] = S.pos_lo[j];
+            s_vel[threadIdx.x] = make_float4(sv.z, sv.w, ss.y, ss.z * ss.z);
+        }
+        __syncthreads();
+        if (!valid) continue;
+        const int cnt = min(DIRECT_THREADS, n - base);
+        for (int jj = 0; jj < cnt; jj++) {
+            const int jg = base + jj;
+            if (jg == i) continue;
+            const float4 sp = s_pos[jj];
+            const float4 sv = s_vel[jj];
+            float rx, ry, svx, svy, sAng;
+            SPos spos;
+            bool dl = false;
+            if (REL) {
+                Delayed d;
+                if (!delayed_state(P, S, C, s_age, s_segdt, jg, t, d)) continue;
+                spos = SPos{ d.x, 0.f, d.y, 0.f };
+                rx = d.rx; ry = d.ry; svx = d.vx; svy = d.vy;
+                sAng = d.angw * rsqrtf(1.f + d.angw * d.angw * sv.w);
+                dl = true;
+            } else {
+                const float2 sl = s_lo[jj];
+                spos = SPos{ sp.x, sl.x, sp.y, sl.y };
+                displacement(P, t.x, t.y, sp.x, sl.x - t.xlo, sp.y, sl.y - t.ylo, rx, ry);
+                svx = sv.x; svy = sv.y; sAng = sv.z;
+            }
+            const float sMu = MAG_MOMENT_K * sp.w * sAng * sv.w;
+            const float sL = INERTIA_K * sp.z * sAng * sv.w;
+            const bool yk = yukawa_in(P, rx, ry, spos, t);
+            pair_force<MAGGM, false>(P, t, rx, ry, svx, svy, sp.z, sp.w, sAng, sMu, sL, dl, yk, false, A);
+            A.tick();
+        }
+    }
+    A.flush();
+    if (valid) { out_fx[ti] = A.get(Q_FX); out_fy[ti] = A.get(Q_FY); }
+}
+
+void direct_subset(const DevParams& P, const DevState& S, const FrameCtl* ctl, const ForceCtx& C, const int* idx,
+                   int k, float* fx, float* fy, cudaStream_t st, LaunchCounter& lc) {
+    const bool maggm = (P.toggles & (GEON_MAGNETIC | GEON_GRAVITOMAG | GEON_ONE_PN)) != 0;
+    const int blocks = std::max(1, (k + DIRECT_THREADS - 1) / DIRECT_THREADS);
+    if (maggm) {
+        if (P.rel) direct_subset_kernel<true, true><<<blocks, DIRECT_THREADS, 0, st>>>(P, S, ctl, C, idx, k, fx, fy);
+        else direct_subset_kernel<true, false><<<blocks, DIRECT_THREADS, 0, st>>>(P, S, ctl, C, idx, k, fx, fy);
+    } else {
+        if (P.rel) direct_subset_kernel<false, true><<<blocks, DIRECT_THREADS, 0, st>>>(P, S, ctl, C, idx, k, fx, fy);
+        else direct_subset_kernel<false, false><<<blocks, DIRECT_THREADS, 0, st>>>(P, S, ctl, C, idx, k, fx, fy);
+    }
+    lc.add(1);
 }
 
 // ---- 1PN-only passes (forces.js:445-610) ----------------------------------------------------
@@ -1049,9 +1204,9 @@ walk1pn_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_ro
             const int4 lm = T.leaf_meta[li];
             if (lm.x < 0 || lm.x + lm.y > nValidW) { if (lane == 0) atomicOr(&ctl->err, ERR_BAD_INDEX); continue; }
             for (int q = lm.x; q < lm.x + lm.y; q++) {               // forces.js:534-554
-                const float4 pp = T.pt_pos[q];
-                const float4 pv = T.pt_vel[q];
-                const uint32_t ref = __float_as_uint(pv.w);
+                const float4 pa = T.ps_a[q];
+                const float4 pb = T.ps_b[q];
+                const uint32_t ref = __float_as_uint(T.ps_c[q].w);
                 const int j = (int)ref_index(ref);
                 const uint32_t code = ref_code(ref);
                 if (!in || j == t.idx) continue;
@@ -1062,12 +1217,10 @@ walk1pn_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_ro
                     rx = d.rx; ry = d.ry;
                     svx = d.vx; svy = d.vy;
                 } else {
-                    const float2 pl = T.pt_lo[q];
-                    SPos sp;
-                    image_disp(P, t, pp.x, pp.y, pl.x, pl.y, code, rx, ry, sp);
-                    svx = pv.x; svy = pv.y;
+                    displacement(P, t.x, t.y, pa.x, pb.x - t.xlo, pa.y, pb.y - t.ylo, rx, ry);
+                    svx = pb.z; svy = pb.w;
                 }
-                accum_1pn(P, t, rx, ry, svx, svy, pp.z, pp.w, A.px, A.py);
+                accum_1pn(P, t, rx, ry, svx, svy, pa.z, pa.w, A.px, A.py);
                 A.tick();
             }
         } else {
@@ -1167,13 +1320,14 @@ static void launch_force(bool bh, const DevParams& P, const DevState& S, const T
         const int blocks = std::max(1, (n_cap + WALK_THREADS - 1) / WALK_THREADS);
         walk_kernel<MAGGM, REL, BRK><<<blocks, WALK_THREADS, 0, st>>>(P, S, T, d_root, ctl, C);
     } else if (bh) {
+        constexpr size_t smem = wc_smem_bytes<MAGGM, REL>();
         static bool attr = false;
         if (!attr) {
-            cudaFuncSetAttribute(walkb_kernel<MAGGM, REL, BRK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WB_SMEM);
+            cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             attr = true;
         }
-        const int blocks = std::max(1, (n_cap + WB_THREADS - 1) / WB_THREADS);
-        walkb_kernel<MAGGM, REL, BRK><<<blocks, WB_THREADS, WB_SMEM, st>>>(P, S, T, d_root, ctl, C);
+        const int blocks = std::max(1, (n_cap + WC_THREADS - 1) / WC_THREADS);
+        walkc_kernel<MAGGM, REL, BRK><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
     } else {
         const int blocks = std::max(1, (n_cap + DIRECT_THREADS - 1) / DIRECT_THREADS);
         direct_kernel<MAGGM, REL, BRK><<<blocks, DIRECT_THREADS, 0, st>>>(P, S, ctl, C);

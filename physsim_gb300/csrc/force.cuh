@@ -25,6 +25,11 @@ struct ForceCtx {
 void force_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
                 const ForceCtx& C, bool bh, int n_cap, cudaStream_t st, LaunchCounter& lc);
 
+// Pairwise forces (fx, fy) on the listed particles from all particles, into
+// separate outputs (device arrays of k floats); the state is not changed.
+void direct_subset(const DevParams& P, const DevState& S, const FrameCtl* ctl, const ForceCtx& C, const int* idx,
+                   int k, float* fx, float* fy, cudaStream_t st, LaunchCounter& lc);
+
 // 1PN-only pass (forces.js:578-610): writes S.f1pn.
 void onepn_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
                 const ForceCtx& C, bool bh, int n_cap, cudaStream_t st, LaunchCounter& lc);

@@ -41,10 +41,10 @@ struct TreeBufs {
     // sorted points
     uint64_t* skey;     // sorted keys (points to key or key_alt)
     uint32_t* sidx;     // sorted point indices
-    float4* pt_pos;     // x_j, y_j (particle, unshifted), mass, charge
-    float2* pt_lo;      // low parts of x_j, y_j
-    float4* pt_vel;     // vx, vy, angVel (after image flips), ref bits
-    float2* pt_mom;     // magMoment, angMomentum (fresh, after flips)
+    // sorted point records, ready to stage as force sources
+    float4* ps_a;       // image x (hi), image y (hi), mass, charge
+    float4* ps_b;       // image x (lo), image y (lo), vx, vy (image flips applied)
+    float4* ps_c;       // angVel (flipped), magMoment, angMomentum (current), ref bits
     int* lcp_a;         // lcp level with the previous key (-1 at 0)
     int* int_cnt;       // internal nodes started per point
     int* int_base;

@@ -195,16 +195,14 @@ __global__ void gather_kernel(DevParams P, DevState S, TreeBufs T, const FrameCt
         const bool fvx = code_fvx(code), fvy = code_fvy(code);
         const float sgn = (fvx || fvy) ? -1.f : 1.f;
         const float angVel = sgn * spn.y;
-        float4 pv;
-        pv.x = fvx ? -vel.z : vel.z;
-        pv.y = fvy ? -vel.w : vel.w;
-        pv.z = angVel;
-        pv.w = __uint_as_float(ref);
-        T.pt_pos[s] = pos;
-        T.pt_lo[s] = S.pos_lo[j];
-        T.pt_vel[s] = pv;
+        const float2 plo = S.pos_lo[j];
+        float ix, ixlo, iy, iylo;
+        point_image(P, pos.x, pos.y, plo.x, plo.y, code, ix, ixlo, iy, iylo);
         const float rsq = spn.z * spn.z;
-        T.pt_mom[s] = make_float2(MAG_MOMENT_K * pos.w * angVel * rsq, INERTIA_K * pos.z * angVel * rsq);
+        T.ps_a[s] = make_float4(ix, iy, pos.z, pos.w);
+        T.ps_b[s] = make_float4(ixlo, iylo, fvx ? -vel.z : vel.z, fvy ? -vel.w : vel.w);
+        T.ps_c[s] = make_float4(angVel, MAG_MOMENT_K * pos.w * angVel * rsq, INERTIA_K * pos.z * angVel * rsq,
+                                __uint_as_float(ref));
         T.real_flag[s] = (code == CODE_IDENTITY) ? 1 : 0;
         int a = -1, c = 0, lf = 0;
         if (s < nValid) {
@@ -237,7 +235,7 @@ __global__ void emit_kernel(DevParams P, TreeBufs T, FrameCtl* ctl) {
     const uint64_t* K = T.skey;
     int bucket = 0, maxl = 0;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nPts; s += gridDim.x * blockDim.x) {
-        if (T.real_flag[s]) T.tgt[T.tgt_base[s]] = (int)ref_index(__float_as_uint(T.pt_vel[s].w));
+        if (T.real_flag[s]) T.tgt[T.tgt_base[s]] = (int)ref_index(__float_as_uint(T.ps_c[s].w));
         if (s >= nValid) continue;
         const int a = T.lcp_a[s];
         const int c = T.int_cnt[s];
@@ -318,13 +316,6 @@ __global__ void link_kernel(DevParams P, TreeBufs T, FrameCtl* ctl, int* d_root)
 }
 
 // ---- bottom-up aggregation ---------------------------------------------------------
-// Image coordinate of a sorted point (v + vlo) as a compensated pair.
-__device__ __forceinline__ df image_coord(float v, float vlo, bool mirror, int shift, float L, float L_lo) {
-    df b = mirror ? df_add(df{ L, L_lo }, df{ -v, -vlo }) : df{ v, vlo };
-    if (shift == 0) return b;
-    return df_add(b, df{ shift * L, shift * L_lo });
-}
-
 // Aggregate accumulator.  Sums are compensated FP32 pairs; the centre of
 // mass is accumulated as mass-weighted offsets from a local origin (the first
 // point or child), so rounding of the total mass only perturbs the offset
@@ -383,27 +374,25 @@ __global__ void aggregate_kernel(DevParams P, DevState S, TreeBufs T, FrameCtl* 
         if (lm.x < 0 || lm.y < 1 || lm.x + lm.y > nValid || lm.w >= nInt) { atomicOr(&ctl->err, ERR_BAD_INDEX); continue; }
         for (int k = 0; k < lm.y; k++) {                     // quadtree.js:276-287
             const int s = lm.x + k;
-            const float4 pp = T.pt_pos[s];
-            const float4 pv = T.pt_vel[s];
-            const uint32_t ref = __float_as_uint(pv.w);
+            const float4 pa = T.ps_a[s];
+            const float4 pb = T.ps_b[s];
+            const float4 pc = T.ps_c[s];
+            const uint32_t ref = __float_as_uint(pc.w);
             const uint32_t j = ref_index(ref), code = ref_code(ref);
-            const float m = pp.z;
+            const float m = pa.z;
             const float4 vel = S.vel[j];
             const float wx = code_fvx(code) ? -vel.x : vel.x;
             const float wy = code_fvy(code) ? -vel.y : vel.y;
             float2 mom;
             if (code == CODE_IDENTITY) mom = S.mom[j];       // cached by the previous force pass
-            else mom = T.pt_mom[s];                          // ghosts: formed at ghost creation (integrator.js:193-194)
+            else mom = make_float2(pc.y, pc.z);              // ghosts: formed at ghost creation (integrator.js:193-194)
             g.mass = df_add(g.mass, df{ m, 0.f });
-            g.charge = df_add(g.charge, df{ pp.w, 0.f });
+            g.charge = df_add(g.charge, df{ pa.w, 0.f });
             g.mu = df_add(g.mu, df{ mom.x, 0.f });
             g.L = df_add(g.L, df{ mom.y, 0.f });
             g.px = df_add(g.px, two_prod(m, wx));
             g.py = df_add(g.py, two_prod(m, wy));
-            const float2 pl = T.pt_lo[s];
-            const df x = image_coord(pp.x, pl.x, code_mx(code), code_sx(code), P.W, P.W_lo);
-            const df y = image_coord(pp.y, pl.y, code_my(code), code_sy(code), P.H, P.H_lo);
-            agg_add_com(g, x, y, m);
+            agg_add_com(g, df{ pa.x, pb.x }, df{ pa.y, pb.y }, m);
         }
         agg_write(T.leaf_a, T.leaf_b, T.leaf_c, leaf, g, node_size2(P, lm.z), lm.z);
         // climb

@@ -111,6 +111,14 @@ class GeonSystem:
     def compute_1pn(self):
         self._ck(self.lib.geon_compute_1pn(self._h))
 
+    def direct_forces(self, idx) -> tuple:
+        """Pairwise (fx, fy) on the listed particles from all particles; state unchanged."""
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        fx = np.zeros(max(idx.size, 1), dtype=np.float32)
+        fy = np.zeros(max(idx.size, 1), dtype=np.float32)
+        self._ck(self.lib.geon_direct_forces(self._h, N.iptr(idx), idx.size, N.fptr(fx), N.fptr(fy)))
+        return fx[:idx.size], fy[:idx.size]
+
     def forces(self) -> dict:
         n = self.count()
         cap = max(n, 1)
