@@ -65,6 +65,7 @@ extern "C" {
 #define GEON_FLAG_BREAKDOWN   (1u << 1)  /* keep per-type force vectors (force breakdown) */
 #define GEON_FLAG_NO_GHOSTS   (1u << 2)  /* periodic BH without image ghosts (min-image only) */
 #define GEON_FLAG_SIMPLE_WALK (1u << 3)  /* one node per warp iteration (cross-check of the batched walk) */
+#define GEON_FLAG_LEARN       (1u << 4)  /* cell moments + learned far-field correction (when weights are set) */
 
 /* Physics parameters.  Mirrors the Physics fields that Physics.update reads
  * (src/integrator.js:65-107, :726-736) plus theta/softening, which the
@@ -239,6 +240,48 @@ int geon_compute_1pn(GeonHandle* h);
  * exact reference for measuring the Barnes-Hut force error on a subsample. */
 int geon_direct_forces(GeonHandle* h, const int32_t* idx, int32_t k, float* fx, float* fy);
 
+/* Training data of the learned far-field correction (no reference
+ * counterpart; the reference has plain monopole Barnes-Hut only).  Builds the
+ * tree with cell moments, walks it for the k listed target particles at the
+ * handle's theta, and for every (cell, target) aggregate interaction writes
+ * 9 mass-net features, 9 charge-net features, the exact member-sum residual
+ * (4: mass field x y, charge field x y, normalised) and the 2 scales
+ * (M / r_e^2, sum|q| / r_e^2), and (when pair_target is not NULL) the
+ * target particle of each pair.  Arrays hold `cap` records; *count receives
+ * the number of pairs found (records beyond cap are dropped). */
+int geon_learn_dataset(GeonHandle* h, const int32_t* targets, int32_t k, int32_t cap, float* feat_mass,
+                       float* feat_charge, float* residual, float* scales, int32_t* pair_target, int32_t* count);
+
+/* ---- learned far-field correction (no reference counterpart) --------------
+ * A 9 -> 64 -> 64 -> 2 GELU network (BF16 weights and activations, FP32
+ * accumulation on the tensor cores) maps the mass-net features of an
+ * accepted (cell, target) pair to the residual of its monopole term; the
+ * force pass adds m_i * (M / r_e^2) * net(features) for every pair.  Weight
+ * vector (FP32, GEON_MLP_NPARAM floats, nn.Linear layout W[out][in]):
+ *     W1[64][9] b1[64] W2[64][64] b2[64] W3[2][64] b3[2] */
+#define GEON_MLP_NPARAM 4930
+
+/* Sets the correction's weights (copied); NULL clears them.  The correction
+ * runs in Barnes-Hut force passes while GEON_FLAG_LEARN is set and weights
+ * are present.  n_param must be GEON_MLP_NPARAM. */
+int geon_learn_set_weights(GeonHandle* h, const float* weights, int32_t n_param);
+
+/* y[n][2] = net(x[n][9]) on the device (host arrays). */
+int geon_mlp_forward(GeonHandle* h, const float* weights, const float* x, int32_t n, float* y);
+
+/* Gradient of L = (1/n) sum_s wt_s |net(x_s) - t_s|^2 over all n samples
+ * (wt may be NULL: all 1), computed by the tensor-core backward pass:
+ * grad[GEON_MLP_NPARAM], *loss = L. */
+int geon_mlp_grad(GeonHandle* h, const float* weights, const float* x, const float* t, const float* wt, int32_t n,
+                  float* grad, double* loss);
+
+/* Trains the network in place with Adam (beta 0.9 / 0.999, eps 1e-8) for
+ * `steps` steps of `batch` samples drawn uniformly (seeded counter hash) from
+ * the n samples, with a cosine learning-rate schedule from lr to 0.
+ * loss_history[steps] (may be NULL) receives each step's batch loss. */
+int geon_mlp_train(GeonHandle* h, float* weights, const float* x, const float* t, const float* wt, int32_t n,
+                   int32_t steps, int32_t batch, float lr, uint64_t seed, double* loss_history);
+
 /* Copies `rows` rows (GEON_OUT_*) of per-particle force data, each `capacity`
  * floats, starting at row `first_row`. */
 int geon_download_forces(GeonHandle* h, int32_t first_row, int32_t rows,
@@ -287,6 +330,9 @@ typedef struct GeonProfile {
     int64_t tree_count, force_count, onepn_count, push_count;
     int64_t interactions;    /* pair evaluations summed over the profiled force passes */
     int64_t particle_substeps;
+    double learn_ms;         /* learned correction: pair collection + network        */
+    int64_t learn_count;
+    int64_t learn_pairs;     /* (cell, target) pairs corrected                        */
 } GeonProfile;
 
 /* enable = 1 clears the counters and starts recording; enable = 0 stops.

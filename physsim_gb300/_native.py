@@ -44,6 +44,8 @@ FLAG_PE = 1 << 0
 FLAG_BREAKDOWN = 1 << 1
 FLAG_NO_GHOSTS = 1 << 2
 FLAG_SIMPLE_WALK = 1 << 3
+FLAG_LEARN = 1 << 4
+MLP_NPARAM = 4930
 
 OUT_ROWS = 25
 OUT_NAMES = ["fx", "fy", "Bz", "Bgz", "dBzdx", "dBzdy", "dBgzdx", "dBgzdy", "tidal", "frameDrag",
@@ -103,7 +105,8 @@ class GeonTreeInfo(C.Structure):
 class GeonProfile(C.Structure):
     _fields_ = [("tree_ms", C.c_double), ("force_ms", C.c_double), ("onepn_ms", C.c_double), ("push_ms", C.c_double),
                 ("tree_count", C.c_int64), ("force_count", C.c_int64), ("onepn_count", C.c_int64),
-                ("push_count", C.c_int64), ("interactions", C.c_int64), ("particle_substeps", C.c_int64)]
+                ("push_count", C.c_int64), ("interactions", C.c_int64), ("particle_substeps", C.c_int64),
+                ("learn_ms", C.c_double), ("learn_count", C.c_int64), ("learn_pairs", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -147,6 +150,14 @@ SIGNATURES = {
     "geon_compute_forces": [_handle_t],
     "geon_compute_1pn": [_handle_t],
     "geon_direct_forces": [_handle_t, _P(C.c_int32), C.c_int32, _P(C.c_float), _P(C.c_float)],
+    "geon_learn_dataset": [_handle_t, _P(C.c_int32), C.c_int32, C.c_int32, _P(C.c_float), _P(C.c_float),
+                           _P(C.c_float), _P(C.c_float), _P(C.c_int32), _P(C.c_int32)],
+    "geon_learn_set_weights": [_handle_t, _P(C.c_float), C.c_int32],
+    "geon_mlp_forward": [_handle_t, _P(C.c_float), _P(C.c_float), C.c_int32, _P(C.c_float)],
+    "geon_mlp_grad": [_handle_t, _P(C.c_float), _P(C.c_float), _P(C.c_float), _P(C.c_float), C.c_int32,
+                      _P(C.c_float), _P(C.c_double)],
+    "geon_mlp_train": [_handle_t, _P(C.c_float), _P(C.c_float), _P(C.c_float), _P(C.c_float), C.c_int32, C.c_int32,
+                       C.c_int32, C.c_float, C.c_uint64, _P(C.c_double)],
     "geon_download_forces": [_handle_t, C.c_int32, C.c_int32, _P(C.c_float), C.c_int32],
     "geon_build_tree": [_handle_t, _P(GeonTreeInfo)],
     "geon_tree_leaves": [_handle_t, _P(C.c_int32), C.c_int32, _P(C.c_double), _P(C.c_double), _P(C.c_double),

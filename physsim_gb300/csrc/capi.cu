@@ -14,6 +14,8 @@
 #include <vector>
 #include "force.cuh"
 #include "push.cuh"
+#include "learn.cuh"
+#include "mlp.cuh"
 
 using namespace geon;
 
@@ -68,9 +70,11 @@ struct GeonHandle {
     DevArena arena;         // state + control
     DevArena tree_arena;    // tree buffers (reallocated when ghost capacity changes)
     DevArena hist_arena;    // history rings (allocated when relativity is first enabled)
+    DevArena learn_arena;   // learned-correction weights and pair buffer
     DevState S{}, S2{};
     TreeBufs T{};
     bool tree_periodic = false;
+    bool tree_moments = false;
     bool hist_alloc = false;
     FrameCtl* ctl = nullptr;
     FrameCtl* ctl_h = nullptr;     // pinned
@@ -91,6 +95,11 @@ struct GeonHandle {
     long long histTotal = 0;
     int lastSubsteps = 0;
     int nextId = 0;
+    // learned correction
+    float* learn_w = nullptr;       // [GEON_MLP_NPARAM] device weights (null: correction off)
+    LearnPair* pairs = nullptr;     // (cell, target) pairs of the current force pass
+    int* pair_cnt = nullptr;
+    int pair_cap = 0;
     LaunchCounter lc;
     std::string err;
     // profiling
@@ -100,7 +109,7 @@ struct GeonHandle {
     GeonProfile prof_acc{};
 };
 
-enum { PH_TREE = 0, PH_FORCE, PH_ONEPN, PH_PUSH };
+enum { PH_TREE = 0, PH_FORCE, PH_ONEPN, PH_PUSH, PH_LEARN };
 
 static cudaEvent_t get_event(GeonHandle* h) {
     if (!h->ev_pool.empty()) { cudaEvent_t e = h->ev_pool.back(); h->ev_pool.pop_back(); return e; }
@@ -131,6 +140,7 @@ static void prof_collect(GeonHandle* h) {
             case PH_TREE: h->prof_acc.tree_ms += ms; h->prof_acc.tree_count++; break;
             case PH_FORCE: h->prof_acc.force_ms += ms; h->prof_acc.force_count++; break;
             case PH_ONEPN: h->prof_acc.onepn_ms += ms; h->prof_acc.onepn_count++; break;
+            case PH_LEARN: h->prof_acc.learn_ms += ms; h->prof_acc.learn_count++; break;
             default: h->prof_acc.push_ms += ms; h->prof_acc.push_count++; break;
         }
         h->ev_pool.push_back(pe.second.first);
@@ -251,6 +261,7 @@ static int ensure_tree(GeonHandle* h) {
     T.leaf_a = A.alloc<float4>(T.cap_pts); T.leaf_b = A.alloc<float4>(T.cap_pts); T.leaf_c = A.alloc<float4>(T.cap_pts);
     T.leaf_meta = A.alloc<int4>(T.cap_pts); T.leaf_of = A.alloc<int>(T.cap_pts);
     if (A.failed) { A.free_all(); T = TreeBufs{}; return set_err(h, GEON_ERR_NOMEM, "tree allocation failed"); }
+    h->tree_moments = false;
     h->tree_periodic = per;
     return GEON_OK;
 }
@@ -392,19 +403,84 @@ static int read_ctl(GeonHandle* h) {
     CK(cudaStreamSynchronize(h->st));
     if (h->ctl_h->err) {
         const int e = h->ctl_h->err;
+        if (e & (ERR_MMA_TIMEOUT | ERR_AGG_TIMEOUT))
+            return set_err(h, GEON_ERR_TIMEOUT, std::string("device wait timed out, flag ") + std::to_string(e));
         return set_err(h, GEON_ERR_OVERFLOW, std::string("device overflow flag ") + std::to_string(e) +
                        ((e & ERR_NODE_OVERFLOW) ? " (node capacity)" : "") + ((e & ERR_STACK_OVERFLOW) ? " (walk stack)" : ""));
     }
     return GEON_OK;
 }
 
+// Cell moment arrays for the learned correction, allocated on first use.
+static int ensure_moments(GeonHandle* h) {
+    if (h->tree_moments) return GEON_OK;
+    TreeBufs& T = h->T;
+    DevArena& A = h->tree_arena;
+    T.int_m1 = A.alloc<float4>(T.cap_int); T.int_m2 = A.alloc<float4>(T.cap_int); T.int_m3 = A.alloc<float4>(T.cap_int);
+    T.leaf_m1 = A.alloc<float4>(T.cap_pts); T.leaf_m2 = A.alloc<float4>(T.cap_pts); T.leaf_m3 = A.alloc<float4>(T.cap_pts);
+    if (A.failed) return set_err(h, GEON_ERR_NOMEM, "moment allocation failed");
+    h->tree_moments = true;
+    return GEON_OK;
+}
+
 static int build_tree(GeonHandle* h) {
     int r = ensure_tree(h);
     if (r) return r;
+    h->T.mom_on = 0;
+    if (h->prm.flags & GEON_FLAG_LEARN) {
+        r = ensure_moments(h);
+        if (r) return r;
+        h->T.mom_on = 1;
+    }
     const int ps = prof_begin(h, PH_TREE);
     tree_build(h->P, h->S, h->T, h->ctl, h->d_root, h->n_cap, h->st, h->lc);
     prof_end(h, ps);
     CKL();
+    return GEON_OK;
+}
+
+static bool learn_active(const GeonHandle* h) {
+    return h->learn_w && (h->prm.flags & GEON_FLAG_LEARN) && h->T.mom_on && h->n > 0;
+}
+
+// Grows the pair buffer to hold at least `need` pairs (contents discarded).
+static int ensure_pairs(GeonHandle* h, long long need) {
+    if (need <= h->pair_cap) return GEON_OK;
+    const long long cap = std::min<long long>(INT_MAX, need + need / 4 + 4096);
+    if (h->pairs) { cudaStreamSynchronize(h->st); cudaFree(h->pairs); h->pairs = nullptr; h->pair_cap = 0; }
+    if (cudaMalloc(&h->pairs, (size_t)cap * sizeof(LearnPair)) != cudaSuccess) {
+        cudaGetLastError();
+        h->pairs = nullptr;
+        return set_err(h, GEON_ERR_NOMEM, "learned-correction pair buffer allocation failed");
+    }
+    h->pair_cap = (int)cap;
+    return GEON_OK;
+}
+
+// Learned far-field correction after a Barnes-Hut force pass: collect every
+// accepted (cell, target) pair of the walk (same opening rule), add the
+// network's correction to the forces, and redo the planner reductions the
+// force pass made from the uncorrected forces.
+static int learn_pass(GeonHandle* h) {
+    const int ps = prof_begin(h, PH_LEARN);
+    int found = 0;
+    for (int attempt = 0; attempt < 2; attempt++) {
+        learn_collect_pairs(h->P, h->S, h->T, h->d_root, h->ctl, h->T.tgt, h->n, h->pairs, h->pair_cap, h->pair_cnt,
+                            h->st, h->lc);
+        CKL();
+        CK(cudaMemcpyAsync(&found, h->pair_cnt, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        if (found <= h->pair_cap) break;
+        int r = ensure_pairs(h, found);
+        if (r) return r;
+    }
+    if (found > h->pair_cap) return set_err(h, GEON_ERR_OVERFLOW, "learned-correction pair buffer overflow");
+    mlp_correct(h->P, h->S, h->T, h->learn_w, h->pairs, found, &h->ctl->err, h->st, h->lc);
+    CKL();
+    launch_frame_scan(h->P, h->S, h->ctl, h->n_cap, h->st, h->lc);
+    CKL();
+    prof_end(h, ps);
+    if (h->prof) h->prof_acc.learn_pairs += found;
     return GEON_OK;
 }
 
@@ -416,6 +492,7 @@ static int run_force_pass(GeonHandle* h, bool rebuild) {
     force_pass(h->P, h->S, h->T, h->d_root, h->ctl, make_ctx(h), bh, h->n_cap, h->st, h->lc);
     prof_end(h, ps);
     CKL();
+    if (bh && learn_active(h)) return learn_pass(h);
     return GEON_OK;
 }
 
@@ -488,6 +565,8 @@ int geon_destroy(GeonHandle* h) {
     if (h->st) cudaStreamSynchronize(h->st);
     h->tree_arena.free_all();
     h->hist_arena.free_all();
+    h->learn_arena.free_all();
+    if (h->pairs) cudaFree(h->pairs);
     h->arena.free_all();
     prof_collect(h);
     for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
@@ -657,6 +736,168 @@ int geon_direct_forces(GeonHandle* h, const int32_t* idx, int32_t k, float* fx, 
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
     tmp.free_all();
     return cuda_check(h, e, "direct forces");
+}
+
+int geon_learn_dataset(GeonHandle* h, const int32_t* targets, int32_t k, int32_t cap, float* feat_mass,
+                       float* feat_charge, float* residual, float* scales, int32_t* pair_target, int32_t* count) {
+    if (!h || k < 0 || cap < 0 || (k > 0 && !targets) || (cap > 0 && (!feat_mass || !feat_charge || !residual || !scales)))
+        return GEON_ERR_ARG;
+    if (!(h->prm.toggles & GEON_BARNES_HUT)) return set_err(h, GEON_ERR_ARG, "the learned correction needs Barnes-Hut");
+    if (h->P.rel || (h->prm.toggles & (GEON_MAGNETIC | GEON_GRAVITOMAG | GEON_ONE_PN)))
+        return set_err(h, GEON_ERR_UNSUPPORTED, "the learned correction covers gravity, Coulomb and Yukawa without relativity");
+    if (count) *count = 0;
+    if (k == 0 || h->n == 0) return GEON_OK;
+    const uint32_t saved = h->prm.flags;
+    h->prm.flags |= GEON_FLAG_LEARN;
+    int r = build_tree(h);
+    h->prm.flags = saved;
+    if (r) return r;
+    DevArena tmp;
+    int* d_t = tmp.alloc<int>(k);
+    int* d_cnt = tmp.alloc<int>(1);
+    const int capd = std::max(cap, 1);
+    LearnPair* d_pairs = tmp.alloc<LearnPair>(capd);
+    float* d_fm = tmp.alloc<float>((size_t)capd * LF);
+    float* d_fc = tmp.alloc<float>((size_t)capd * LF);
+    float* d_res = tmp.alloc<float>((size_t)capd * 4);
+    float* d_sc = tmp.alloc<float>((size_t)capd * 2);
+    if (tmp.failed) { tmp.free_all(); return set_err(h, GEON_ERR_NOMEM, "dataset allocation failed"); }
+    cudaError_t e = cudaMemcpyAsync(d_t, targets, k * sizeof(int), cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess) {
+        learn_collect_pairs(h->P, h->S, h->T, h->d_root, h->ctl, d_t, k, d_pairs, cap, d_cnt, h->st, h->lc);
+        learn_residuals(h->P, h->S, h->T, d_pairs, d_cnt, cap, d_fm, d_fc, d_res, d_sc, h->st, h->lc);
+        e = cudaGetLastError();
+    }
+    int found = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&found, d_cnt, sizeof(int), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    const int m = std::min(found, cap);
+    if (e == cudaSuccess && m > 0) {
+        cudaMemcpyAsync(feat_mass, d_fm, (size_t)m * LF * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+        cudaMemcpyAsync(feat_charge, d_fc, (size_t)m * LF * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+        cudaMemcpyAsync(residual, d_res, (size_t)m * 4 * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+        e = cudaMemcpyAsync(scales, d_sc, (size_t)m * 2 * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+        if (e == cudaSuccess && pair_target) {
+            std::vector<LearnPair> hp(m);
+            e = cudaMemcpy(hp.data(), d_pairs, (size_t)m * sizeof(LearnPair), cudaMemcpyDeviceToHost);
+            for (int q = 0; q < m; q++) pair_target[q] = hp[q].target;
+        }
+    }
+    tmp.free_all();
+    if (count) *count = found;
+    r = cuda_check(h, e, "learned-correction dataset");
+    if (r) return r;
+    return read_ctl(h);
+}
+
+int geon_learn_set_weights(GeonHandle* h, const float* weights, int32_t n_param) {
+    if (!h) return GEON_ERR_ARG;
+    if (!weights) { h->learn_w = nullptr; return GEON_OK; }       // the buffer stays for reuse
+    if (n_param != MLP_NPARAM) return set_err(h, GEON_ERR_ARG, "n_param must be GEON_MLP_NPARAM");
+    static_assert(MLP_NPARAM == GEON_MLP_NPARAM, "weight count");
+    if (h->learn_arena.ptrs.empty()) {
+        float* w = h->learn_arena.alloc<float>(MLP_NPARAM);
+        int* c = h->learn_arena.alloc<int>(1);
+        if (h->learn_arena.failed) { h->learn_arena.free_all(); return set_err(h, GEON_ERR_NOMEM, "weight allocation failed"); }
+        (void)w; (void)c;
+    }
+    float* dw = static_cast<float*>(h->learn_arena.ptrs[0]);
+    h->pair_cnt = static_cast<int*>(h->learn_arena.ptrs[1]);
+    CK(cudaMemcpyAsync(dw, weights, MLP_NPARAM * sizeof(float), cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    h->learn_w = dw;
+    return GEON_OK;
+}
+
+// Device copies of a training set for the network entry points.
+struct MlpData {
+    DevArena A;
+    float* w = nullptr; float* x = nullptr; float* t = nullptr; float* wt = nullptr;
+    float* grad = nullptr; double* loss = nullptr;
+};
+static int mlp_upload(GeonHandle* h, MlpData& D, const float* weights, const float* x, const float* t, const float* wt,
+                      int n, int nloss) {
+    D.w = D.A.alloc<float>(MLP_NPARAM);
+    D.x = D.A.alloc<float>((size_t)n * LF);
+    if (t) D.t = D.A.alloc<float>((size_t)n * 2);
+    if (wt) D.wt = D.A.alloc<float>(n);
+    D.grad = D.A.alloc<float>(MLP_NPARAM);
+    D.loss = D.A.alloc<double>(std::max(nloss, 1));
+    if (D.A.failed) { D.A.free_all(); return set_err(h, GEON_ERR_NOMEM, "network buffer allocation failed"); }
+    cudaError_t e = cudaMemcpyAsync(D.w, weights, MLP_NPARAM * sizeof(float), cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(D.x, x, (size_t)n * LF * sizeof(float), cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess && t) e = cudaMemcpyAsync(D.t, t, (size_t)n * 2 * sizeof(float), cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess && wt) e = cudaMemcpyAsync(D.wt, wt, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(D.grad, 0, MLP_NPARAM * sizeof(float), h->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(D.loss, 0, std::max(nloss, 1) * sizeof(double), h->st);
+    if (e != cudaSuccess) { D.A.free_all(); return cuda_check(h, e, "network upload"); }
+    return GEON_OK;
+}
+
+int geon_mlp_forward(GeonHandle* h, const float* weights, const float* x, int32_t n, float* y) {
+    if (!h || !weights || n < 0 || (n > 0 && (!x || !y))) return GEON_ERR_ARG;
+    if (n == 0) return GEON_OK;
+    MlpData D;
+    int r = mlp_upload(h, D, weights, x, nullptr, nullptr, n, 0);
+    if (r) return r;
+    float* dy = D.A.alloc<float>((size_t)n * 2);
+    cudaError_t e = D.A.failed ? cudaErrorMemoryAllocation : cudaSuccess;
+    if (e == cudaSuccess) {
+        mlp_forward(D.w, D.x, n, dy, &h->ctl->err, h->st, h->lc);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(y, dy, (size_t)n * 2 * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    D.A.free_all();
+    r = cuda_check(h, e, "network forward");
+    return r ? r : read_ctl(h);
+}
+
+int geon_mlp_grad(GeonHandle* h, const float* weights, const float* x, const float* t, const float* wt, int32_t n,
+                  float* grad, double* loss) {
+    if (!h || !weights || !grad || n <= 0 || !x || !t) return GEON_ERR_ARG;
+    MlpData D;
+    int r = mlp_upload(h, D, weights, x, t, wt, n, 1);
+    if (r) return r;
+    mlp_grad(D.w, D.x, D.t, D.wt, n, n, 0ull, 0, D.grad, D.loss, &h->ctl->err, h->st, h->lc);
+    cudaError_t e = cudaGetLastError();
+    double l = 0.0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(grad, D.grad, MLP_NPARAM * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&l, D.loss, sizeof(double), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    D.A.free_all();
+    if (loss) *loss = l;
+    r = cuda_check(h, e, "network gradient");
+    return r ? r : read_ctl(h);
+}
+
+int geon_mlp_train(GeonHandle* h, float* weights, const float* x, const float* t, const float* wt, int32_t n,
+                   int32_t steps, int32_t batch, float lr, uint64_t seed, double* loss_history) {
+    if (!h || !weights || !x || !t || n <= 0 || steps < 0 || batch <= 0 || !(lr > 0.f)) return GEON_ERR_ARG;
+    if (steps == 0) return GEON_OK;
+    MlpData D;
+    int r = mlp_upload(h, D, weights, x, t, wt, n, steps);
+    if (r) return r;
+    float* m = D.A.alloc<float>(MLP_NPARAM);
+    float* v = D.A.alloc<float>(MLP_NPARAM);
+    cudaError_t e = D.A.failed ? cudaErrorMemoryAllocation : cudaSuccess;
+    if (e == cudaSuccess) e = cudaMemsetAsync(m, 0, MLP_NPARAM * sizeof(float), h->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(v, 0, MLP_NPARAM * sizeof(float), h->st);
+    const uint64_t sd = seed ? seed : 0x5DEECE66Dull;
+    for (int s = 0; s < steps && e == cudaSuccess; s++) {
+        const double lr_s = 0.5 * (double)lr * (1.0 + std::cos(3.141592653589793 * (double)s / (double)steps));
+        mlp_grad(D.w, D.x, D.t, D.wt, n, batch, sd, s, D.grad, D.loss + s, &h->ctl->err, h->st, h->lc);
+        mlp_adam(D.w, D.grad, m, v, (float)lr_s, 0.9f, 0.999f, 1e-8f, s + 1, h->st, h->lc);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(weights, D.w, MLP_NPARAM * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess && loss_history)
+        e = cudaMemcpyAsync(loss_history, D.loss, (size_t)steps * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    D.A.free_all();
+    r = cuda_check(h, e, "network training");
+    return r ? r : read_ctl(h);
 }
 
 int geon_download_forces(GeonHandle* h, int32_t first_row, int32_t rows, float* out, int32_t capacity) {

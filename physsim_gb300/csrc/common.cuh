@@ -32,6 +32,7 @@ constexpr int ERR_STACK_OVERFLOW = 1;
 constexpr int ERR_NODE_OVERFLOW = 2;
 constexpr int ERR_AGG_TIMEOUT = 4;
 constexpr int ERR_BAD_INDEX = 8;        // an index failed its bounds check (access skipped)
+constexpr int ERR_MMA_TIMEOUT = 16;     // a tensor-core completion wait ran out (kernel returned early)
 
 // ---- point references: particle index + periodic image code ----------------
 // code bits: [0,1] sx+1, [2,3] sy+1, [4] mirror x (x -> W - x), [5] mirror y,

@@ -1,0 +1,520 @@
+// mlp.cu — the learned-correction network on fifth-generation tensor cores.
+//
+// Network (learn.cuh): 9 -> 64 -> 64 -> 2 with GELU (tanh form) after the two
+// hidden layers; BF16 weights and activations, FP32 accumulation in TMEM.
+// A CTA of 128 threads (one warpgroup) processes tiles of 128 samples: thread
+// t owns sample row t, which is TMEM lane t.  Per layer the epilogue of the
+// previous layer writes BF16 activations to shared memory in the canonical
+// K-major layout (tc.cuh); thread 0 issues the tcgen05.mma chain and commits
+// it to an mbarrier; all threads wait (bounded) and read their accumulator
+// row back with tcgen05.ld.
+//
+// Training runs the same forward pass and then the backward pass on the
+// tensor cores too:
+//     dH2 = dY W3,   dZ2 = dH2 * gelu'(Z2),   dH1 = dZ2 W2,   dZ1 = dH1 * gelu'(Z1)
+// and the weight gradients as two GEMMs over the 128 samples of a tile
+// (K = samples), accumulated in TMEM across every tile a CTA processes:
+//     GA = [dZ2^T ; dZ1^T] [H1^T ; X'^T]^T     (128 x 80)
+//     GB = [H2^T ; 1]      [dY^T]^T            (128 x 16)
+// X' is the feature row with a constant 1 in column 9, so GA column 64+9
+// holds the bias gradients db2 (rows 0..63) and db1 (rows 64..127); the ones
+// row of GB gives db3.  The epilogues write the transposed operands with
+// scattered 2-byte stores.
+#include "mlp.cuh"
+#include "tc.cuh"
+
+#include <cuda_bf16.h>
+#include <algorithm>
+#include <cmath>
+
+namespace geon {
+
+using namespace tc;
+
+constexpr int MT = 128;          // samples per tile = threads per CTA = TMEM lanes
+constexpr int K1 = 16;           // layer-1 K: 9 features, a constant 1, zeros
+constexpr int N3 = 16;           // layer-3 N: 2 outputs, zeros
+constexpr int NGA = LH + K1;     // N of the GA gradient GEMM
+constexpr float GELU_C = 0.7978845608028654f;   // sqrt(2/pi)
+constexpr float GELU_A = 0.044715f;
+
+constexpr int OFF_W1 = 0;
+constexpr int OFF_B1 = OFF_W1 + LH * LF;
+constexpr int OFF_W2 = OFF_B1 + LH;
+constexpr int OFF_B2 = OFF_W2 + LH * LH;
+constexpr int OFF_W3 = OFF_B2 + LH;
+constexpr int OFF_B3 = OFF_W3 + LO * LH;
+static_assert(OFF_B3 + LO == MLP_NPARAM, "weight layout");
+
+// TMEM columns of the training CTA (512 allocated).
+constexpr uint32_t TC_Z1 = 0, TC_Z2 = 64, TC_Y = 128, TC_DH2 = 160, TC_DH1 = 224, TC_GA = 288, TC_GB = 384;
+static_assert(TC_GA + NGA <= TC_GB && TC_GB + N3 <= 512, "TMEM plan");
+
+__device__ __forceinline__ float tanh_approx(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float gelu(float x) {
+    const float u = GELU_C * fmaf(GELU_A * x, x * x, x);
+    return 0.5f * x * (1.f + tanh_approx(u));
+}
+__device__ __forceinline__ float gelu_grad(float x) {
+    const float x2 = x * x;
+    const float t = tanh_approx(GELU_C * fmaf(GELU_A * x, x2, x));
+    return 0.5f * (1.f + t) + 0.5f * x * (1.f - t * t) * GELU_C * fmaf(3.f * GELU_A, x2, 1.f);
+}
+
+// Forward operands, biases and the MMA barrier (every kernel of this file).
+struct NetSmem {
+    __align__(128) uint8_t w1[LH * K1 * 2];     // B of Z1 (N 64, K 16)
+    __align__(128) uint8_t w2[LH * LH * 2];     // B of Z2 (N 64, K 64)
+    __align__(128) uint8_t w3[N3 * LH * 2];     // B of Y  (N 16, K 64)
+    __align__(128) uint8_t x[MT * K1 * 2];      // A of Z1
+    __align__(128) uint8_t h1[MT * LH * 2];     // A of Z2
+    __align__(128) uint8_t h2[MT * LH * 2];     // A of Y
+    float b1[LH], b2[LH], b3[LO];
+    float red[MT / 32];
+    uint64_t bar;
+    uint32_t tmem;
+};
+// Training adds the backward operands.
+struct TrainSmem {
+    NetSmem f;
+    __align__(128) uint8_t w2t[LH * LH * 2];    // B of dH1 (N 64, K 64): W2^T
+    __align__(128) uint8_t w3t[LH * N3 * 2];    // B of dH2 (N 64, K 16): W3^T
+    __align__(128) uint8_t dy[MT * N3 * 2];     // A of dH2
+    __align__(128) uint8_t dz2[MT * LH * 2];    // A of dH1
+    __align__(128) uint8_t aga[MT * MT * 2];    // A of GA (128 rows, K = samples)
+    __align__(128) uint8_t bga[NGA * MT * 2];   // B of GA
+    __align__(128) uint8_t agb[MT * MT * 2];    // A of GB
+    __align__(128) uint8_t bgb[N3 * MT * 2];    // B of GB
+};
+
+__device__ __forceinline__ void put_bf16(uint8_t* buf, int r, int k, int K, float v) {
+    *reinterpret_cast<__nv_bfloat16*>(buf + kmajor_offset(r, k, K)) = __float2bfloat16_rn(v);
+}
+// Stores 8 consecutive values (k0 a multiple of 8) of row r as one 16-byte chunk.
+__device__ __forceinline__ void put8(uint8_t* buf, int r, int k0, int K, const float* v) {
+    uint4 u;
+    __nv_bfloat162 p;
+    p = __floats2bfloat162_rn(v[0], v[1]); u.x = *reinterpret_cast<uint32_t*>(&p);
+    p = __floats2bfloat162_rn(v[2], v[3]); u.y = *reinterpret_cast<uint32_t*>(&p);
+    p = __floats2bfloat162_rn(v[4], v[5]); u.z = *reinterpret_cast<uint32_t*>(&p);
+    p = __floats2bfloat162_rn(v[6], v[7]); u.w = *reinterpret_cast<uint32_t*>(&p);
+    *reinterpret_cast<uint4*>(buf + kmajor_offset(r, k0, K)) = u;
+}
+
+// Stages the FP32 weights as BF16 operands (zero padded) and FP32 biases.
+__device__ void stage_forward(NetSmem& s, const float* __restrict__ W) {
+    for (int i = threadIdx.x; i < LH * K1; i += blockDim.x) {
+        const int r = i / K1, k = i % K1;
+        put_bf16(s.w1, r, k, K1, k < LF ? W[OFF_W1 + r * LF + k] : 0.f);
+    }
+    for (int i = threadIdx.x; i < LH * LH; i += blockDim.x) put_bf16(s.w2, i / LH, i % LH, LH, W[OFF_W2 + i]);
+    for (int i = threadIdx.x; i < N3 * LH; i += blockDim.x) {
+        const int r = i / LH, k = i % LH;
+        put_bf16(s.w3, r, k, LH, r < LO ? W[OFF_W3 + r * LH + k] : 0.f);
+    }
+    for (int i = threadIdx.x; i < LH; i += blockDim.x) { s.b1[i] = W[OFF_B1 + i]; s.b2[i] = W[OFF_B2 + i]; }
+    if (threadIdx.x < LO) s.b3[threadIdx.x] = W[OFF_B3 + threadIdx.x];
+}
+
+__device__ void stage_backward(TrainSmem& s, const float* __restrict__ W) {
+    for (int i = threadIdx.x; i < LH * LH; i += blockDim.x) {
+        const int n = i / LH, k = i % LH;                       // W2^T[n][k] = W2[k][n]
+        put_bf16(s.w2t, n, k, LH, W[OFF_W2 + k * LH + n]);
+    }
+    for (int i = threadIdx.x; i < LH * N3; i += blockDim.x) {
+        const int n = i / N3, k = i % N3;                       // W3^T[n][k] = W3[k][n]
+        put_bf16(s.w3t, n, k, N3, k < LO ? W[OFF_W3 + k * LH + n] : 0.f);
+    }
+    // constant rows: GB's A operand has a row of ones (row 64) and zeros below;
+    // GB's B operand rows 2..15 stay zero
+    for (int i = threadIdx.x; i < (MT - LH) * MT; i += blockDim.x) {
+        const int r = LH + i / MT, k = i % MT;
+        put_bf16(s.agb, r, k, MT, r == LH ? 1.f : 0.f);
+    }
+    for (int i = threadIdx.x; i < (N3 - LO) * MT; i += blockDim.x) put_bf16(s.bgb, LO + i / MT, i % MT, MT, 0.f);
+}
+
+__device__ __forceinline__ void net_setup(NetSmem& s, uint32_t ncols) {
+    if (threadIdx.x == 0) {
+        mbar_init(&s.bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (threadIdx.x < 32) tmem_alloc(&s.tmem, ncols);
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+}
+
+// Makes this CTA's shared-memory writes visible to the tensor core, lets
+// thread 0 issue `issue()` and commit it, and waits for completion.  Returns
+// false (uniformly across the CTA) if `ok` was false or the wait timed out;
+// `phase` advances only on success so that a timed-out phase can be drained.
+template <class F>
+__device__ __forceinline__ bool mma_step(NetSmem& s, uint32_t& phase, bool ok, F&& issue) {
+    fence_proxy_async();
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    if (!ok) return false;
+    if (threadIdx.x == 0) {
+        issue();
+        commit(&s.bar);
+    }
+    const bool done = mbar_wait(&s.bar, phase);
+    const bool all = __syncthreads_and(done) != 0;
+    if (all) phase ^= 1u;
+    fence_after_sync();
+    return all;
+}
+
+__device__ __forceinline__ void net_teardown(NetSmem& s, bool ok, uint32_t phase, int* err, uint32_t ncols) {
+    if (!ok) {
+        if (threadIdx.x == 0) atomicOr(err, ERR_MMA_TIMEOUT);
+        mbar_wait(&s.bar, phase);          // drain the MMA still in flight before the columns are released
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    if (threadIdx.x < 32) tmem_dealloc(s.tmem, ncols);
+}
+
+// GELU epilogue of a 64-column accumulator into the next layer's A operand
+// (and, when training, into rows rowT0.. of a transposed operand).
+template <bool TR>
+__device__ __forceinline__ void hidden_epilogue(uint32_t tmem, uint32_t col, const float* bias, uint8_t* out,
+                                                uint8_t* outT, int rowT0) {
+    const int warp = threadIdx.x >> 5;
+    const int row = threadIdx.x;
+#pragma unroll
+    for (int c0 = 0; c0 < LH; c0 += 16) {
+        float v[16];
+        tmem_ld16(tmem_addr(tmem, warp, col + c0), v);
+#pragma unroll
+        for (int i = 0; i < 16; i++) v[i] = gelu(v[i] + bias[c0 + i]);
+        put8(out, row, c0, LH, v);
+        put8(out, row, c0 + 8, LH, v + 8);
+        if (TR) {
+#pragma unroll
+            for (int i = 0; i < 16; i++) put_bf16(outT, rowT0 + c0 + i, row, MT, v[i]);
+        }
+    }
+}
+
+__device__ __forceinline__ void stage_x(NetSmem& s, const float* f) {
+    put8(s.x, threadIdx.x, 0, K1, f);
+    put8(s.x, threadIdx.x, 8, K1, f + 8);
+}
+
+// Forward pass of the tile staged in s.x (128 TMEM columns); y0, y1 are this
+// thread's outputs.
+__device__ __forceinline__ bool tile_forward(NetSmem& s, uint32_t& phase, bool ok, float& y0, float& y1) {
+    const int warp = threadIdx.x >> 5;
+    ok = mma_step(s, phase, ok, [&] { gemm(s.tmem + 0, s.x, s.w1, LH, K1, false); });
+    hidden_epilogue<false>(s.tmem, 0, s.b1, s.h1, nullptr, 0);
+    ok = mma_step(s, phase, ok, [&] { gemm(s.tmem + 64, s.h1, s.w2, LH, LH, false); });
+    hidden_epilogue<false>(s.tmem, 64, s.b2, s.h2, nullptr, 0);
+    ok = mma_step(s, phase, ok, [&] { gemm(s.tmem + 0, s.h2, s.w3, N3, LH, false); });
+    float v[16];
+    tmem_ld16(tmem_addr(s.tmem, warp, 0), v);
+    y0 = v[0] + s.b3[0];
+    y1 = v[1] + s.b3[1];
+    return ok;
+}
+
+__global__ void __launch_bounds__(MT)
+mlp_forward_kernel(const float* __restrict__ W, const float* __restrict__ X, int n, float* __restrict__ Y, int* err) {
+    extern __shared__ __align__(1024) uint8_t fwd_smem_raw[];
+    NetSmem& s = *reinterpret_cast<NetSmem*>(fwd_smem_raw);
+    stage_forward(s, W);
+    net_setup(s, 128);
+    uint32_t phase = 0;
+    bool ok = true;
+    const int ntiles = (n + MT - 1) / MT;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int i = tile * MT + threadIdx.x;
+        float f[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) f[k] = (i < n && k < LF) ? X[(size_t)i * LF + k] : 0.f;
+        f[LF] = 1.f;
+        stage_x(s, f);
+        float y0, y1;
+        ok = tile_forward(s, phase, ok, y0, y1);
+        if (ok && i < n) { Y[(size_t)i * 2] = y0; Y[(size_t)i * 2 + 1] = y1; }
+    }
+    net_teardown(s, ok, phase, err, 128);
+}
+
+__global__ void __launch_bounds__(MT)
+mlp_correct_kernel(DevParams P, DevState S, TreeBufs T, const float* __restrict__ W, const LearnPair* __restrict__ pairs,
+                   int np, int* err) {
+    extern __shared__ __align__(1024) uint8_t cor_smem_raw[];
+    NetSmem& s = *reinterpret_cast<NetSmem*>(cor_smem_raw);
+    stage_forward(s, W);
+    net_setup(s, 128);
+    uint32_t phase = 0;
+    bool ok = true;
+    const int ntiles = (np + MT - 1) / MT;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int e = tile * MT + threadIdx.x;
+        float f[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) f[k] = 0.f;
+        float scale = 0.f;
+        int target = -1;
+        if (e < np) {
+            const LearnPair pr = pairs[e];
+            target = pr.target;
+            const float4 p = S.pos[pr.target];
+            const float2 pl = S.pos_lo[pr.target];
+            const float4 a = T.int_a[pr.node], c = T.int_c[pr.node];
+            float dx, dy;
+            displacement(P, p.x, p.y, a.x, c.x - pl.x, a.y, c.y - pl.y, dx, dy);
+            float fc[LF], sc;
+            pair_features(P, dx, dy, sqrtf(c.z), a.z, a.w, T.int_m1[pr.node], T.int_m2[pr.node], T.int_m3[pr.node],
+                          f, fc, scale, sc);
+            scale *= p.z;                                     // target mass
+        }
+        f[LF] = 1.f;
+        stage_x(s, f);
+        float y0, y1;
+        ok = tile_forward(s, phase, ok, y0, y1);
+        if (ok && target >= 0) {
+            float* fp = reinterpret_cast<float*>(&S.force[target]);
+            atomicAdd(fp, scale * y0);
+            atomicAdd(fp + 1, scale * y1);
+        }
+    }
+    net_teardown(s, ok, phase, err, 128);
+}
+
+// SplitMix64 finaliser (Steele, Lea, Flood 2014) of a (seed, step, j) counter,
+// mapped to [0, n) by a 32 x 32 -> 64-bit multiply.
+__device__ __forceinline__ int draw_sample(uint64_t seed, int step, int j, int n) {
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (((uint64_t)(uint32_t)step << 32) + (uint64_t)(uint32_t)j + 1ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (int)(((z >> 32) * (uint64_t)(uint32_t)n) >> 32);
+}
+
+__global__ void __launch_bounds__(MT, 1)
+mlp_train_kernel(const float* __restrict__ W, const float* __restrict__ X, const float* __restrict__ Tg,
+                 const float* __restrict__ wt, int n_data, int batch, uint64_t seed, int step,
+                 float* __restrict__ grad, double* loss, int* err) {
+    extern __shared__ __align__(1024) uint8_t tr_smem_raw[];
+    TrainSmem& s = *reinterpret_cast<TrainSmem*>(tr_smem_raw);
+    NetSmem& f = s.f;
+    stage_forward(f, W);
+    stage_backward(s, W);
+    net_setup(f, 512);
+    const int warp = threadIdx.x >> 5;
+    const int row = threadIdx.x;
+    const float invB = 1.f / (float)batch;
+    uint32_t phase = 0;
+    bool ok = true, first = true;
+    float lsum = 0.f;
+    const int ntiles = (batch + MT - 1) / MT;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int j = tile * MT + row;
+        const bool live = j < batch;
+        const int smp = !live ? -1 : (seed ? draw_sample(seed, step, j, n_data) : j);
+        float x[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) x[k] = 0.f;
+        float t0 = 0.f, t1 = 0.f, w = 0.f;
+        if (smp >= 0) {
+#pragma unroll
+            for (int k = 0; k < LF; k++) x[k] = X[(size_t)smp * LF + k];
+            t0 = Tg[(size_t)smp * 2];
+            t1 = Tg[(size_t)smp * 2 + 1];
+            w = wt ? wt[smp] : 1.f;
+        }
+        x[LF] = 1.f;
+        stage_x(f, x);
+#pragma unroll
+        for (int k = 0; k < K1; k++) put_bf16(s.bga, LH + k, row, MT, x[k]);
+        // forward
+        ok = mma_step(f, phase, ok, [&] { gemm(f.tmem + TC_Z1, f.x, f.w1, LH, K1, false); });
+        hidden_epilogue<true>(f.tmem, TC_Z1, f.b1, f.h1, s.bga, 0);
+        ok = mma_step(f, phase, ok, [&] { gemm(f.tmem + TC_Z2, f.h1, f.w2, LH, LH, false); });
+        hidden_epilogue<true>(f.tmem, TC_Z2, f.b2, f.h2, s.agb, 0);
+        ok = mma_step(f, phase, ok, [&] { gemm(f.tmem + TC_Y, f.h2, f.w3, N3, LH, false); });
+        {
+            float v[16];
+            tmem_ld16(tmem_addr(f.tmem, warp, TC_Y), v);
+            const float e0 = v[0] + f.b3[0] - t0, e1 = v[1] + f.b3[1] - t1;
+            lsum += w * (e0 * e0 + e1 * e1);
+            const float g = 2.f * w * invB;
+            float d[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++) d[k] = 0.f;
+            d[0] = g * e0;
+            d[1] = g * e1;
+            put8(s.dy, row, 0, N3, d);
+            put8(s.dy, row, 8, N3, d + 8);
+            put_bf16(s.bgb, 0, row, MT, d[0]);
+            put_bf16(s.bgb, 1, row, MT, d[1]);
+        }
+        // backward through layer 3 and the second GELU
+        ok = mma_step(f, phase, ok, [&] { gemm(f.tmem + TC_DH2, s.dy, s.w3t, LH, N3, false); });
+#pragma unroll
+        for (int c0 = 0; c0 < LH; c0 += 16) {
+            float dh[16], z[16];
+            tmem_ld16(tmem_addr(f.tmem, warp, TC_DH2 + c0), dh);
+            tmem_ld16(tmem_addr(f.tmem, warp, TC_Z2 + c0), z);
+#pragma unroll
+            for (int i = 0; i < 16; i++) dh[i] *= gelu_grad(z[i] + f.b2[c0 + i]);
+            put8(s.dz2, row, c0, LH, dh);
+            put8(s.dz2, row, c0 + 8, LH, dh + 8);
+#pragma unroll
+            for (int i = 0; i < 16; i++) put_bf16(s.aga, c0 + i, row, MT, dh[i]);
+        }
+        // backward through layer 2 and the first GELU
+        ok = mma_step(f, phase, ok, [&] { gemm(f.tmem + TC_DH1, s.dz2, s.w2t, LH, LH, false); });
+#pragma unroll
+        for (int c0 = 0; c0 < LH; c0 += 16) {
+            float dh[16], z[16];
+            tmem_ld16(tmem_addr(f.tmem, warp, TC_DH1 + c0), dh);
+            tmem_ld16(tmem_addr(f.tmem, warp, TC_Z1 + c0), z);
+#pragma unroll
+            for (int i = 0; i < 16; i++) put_bf16(s.aga, LH + c0 + i, row, MT, dh[i] * gelu_grad(z[i] + f.b1[c0 + i]));
+        }
+        // weight gradients of this tile, accumulated in TMEM
+        const bool acc = !first;
+        ok = mma_step(f, phase, ok, [&] {
+            gemm(f.tmem + TC_GA, s.aga, s.bga, NGA, MT, acc);
+            gemm(f.tmem + TC_GB, s.agb, s.bgb, N3, MT, acc);
+        });
+        first = false;
+    }
+    // loss
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if ((row & 31) == 0) f.red[warp] = lsum;
+    __syncthreads();
+    if (row == 0 && ok) atomicAdd(loss, (double)(f.red[0] + f.red[1] + f.red[2] + f.red[3]) * (double)invB);
+    // gradients: TMEM lane r holds row r of GA and of GB
+    if (ok && !first) {
+        const bool top = row < LH;
+        const int o = top ? row : row - LH;
+#pragma unroll
+        for (int c0 = 0; c0 < LH; c0 += 16) {
+            float v[16];
+            tmem_ld16(tmem_addr(f.tmem, warp, TC_GA + c0), v);
+            if (top) {
+#pragma unroll
+                for (int i = 0; i < 16; i++) atomicAdd(&grad[OFF_W2 + o * LH + c0 + i], v[i]);
+            }
+        }
+        {
+            float v[16];
+            tmem_ld16(tmem_addr(f.tmem, warp, TC_GA + LH), v);
+            if (top) {
+                atomicAdd(&grad[OFF_B2 + o], v[LF]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < LF; k++) atomicAdd(&grad[OFF_W1 + o * LF + k], v[k]);
+                atomicAdd(&grad[OFF_B1 + o], v[LF]);
+            }
+        }
+        {
+            float v[16];
+            tmem_ld16(tmem_addr(f.tmem, warp, TC_GB), v);
+            if (top) {
+                atomicAdd(&grad[OFF_W3 + row], v[0]);
+                atomicAdd(&grad[OFF_W3 + LH + row], v[1]);
+            } else if (row == LH) {
+                atomicAdd(&grad[OFF_B3], v[0]);
+                atomicAdd(&grad[OFF_B3 + 1], v[1]);
+            }
+        }
+    }
+    net_teardown(f, ok, phase, err, 512);
+}
+
+__global__ void mlp_adam_kernel(float* W, float* g, float* m, float* v, float lr, float b1, float b2, float eps,
+                                float c1, float c2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= MLP_NPARAM) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    W[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    g[i] = 0.f;
+}
+
+// ---- launchers ------------------------------------------------------------------
+static int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        n = v > 0 ? v : 1;
+    }
+    return n;
+}
+
+template <class K>
+static void allow_smem(K kernel, size_t bytes, bool& done) {
+    if (!done) {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        done = true;
+    }
+}
+
+constexpr size_t NET_SMEM = sizeof(NetSmem) + 1024;
+constexpr size_t TRAIN_SMEM = sizeof(TrainSmem) + 1024;
+static_assert(TRAIN_SMEM <= 227 * 1024, "training CTA exceeds shared memory");
+// one training CTA per SM: its 512 TMEM columns are the whole TMEM of the SM
+static_assert(2 * TRAIN_SMEM > 228 * 1024, "training CTAs must not share an SM");
+// at most four forward CTAs per SM: 4 x 128 TMEM columns
+static_assert(5 * NET_SMEM > 228 * 1024, "forward CTAs would oversubscribe TMEM");
+
+void mlp_forward(const float* W, const float* X, int n, float* Y, int* err, cudaStream_t st, LaunchCounter& lc) {
+    static bool attr = false;
+    allow_smem(mlp_forward_kernel, NET_SMEM, attr);
+    if (n <= 0) return;
+    const int tiles = (n + MT - 1) / MT;
+    const int blocks = std::max(1, std::min(tiles, sm_count() * 4));
+    mlp_forward_kernel<<<blocks, MT, NET_SMEM, st>>>(W, X, n, Y, err);
+    lc.add(1);
+}
+
+void mlp_correct(const DevParams& P, const DevState& S, const TreeBufs& T, const float* W, const LearnPair* pairs,
+                 int npairs, int* err, cudaStream_t st, LaunchCounter& lc) {
+    static bool attr = false;
+    allow_smem(mlp_correct_kernel, NET_SMEM, attr);
+    if (npairs <= 0) return;
+    const int tiles = (npairs + MT - 1) / MT;
+    const int blocks = std::max(1, std::min(tiles, sm_count() * 4));
+    mlp_correct_kernel<<<blocks, MT, NET_SMEM, st>>>(P, S, T, W, pairs, npairs, err);
+    lc.add(1);
+}
+
+void mlp_grad(const float* W, const float* X, const float* T, const float* wt, int n_data, int batch, uint64_t seed,
+              int step, float* grad, double* loss, int* err, cudaStream_t st, LaunchCounter& lc) {
+    static bool attr = false;
+    allow_smem(mlp_train_kernel, TRAIN_SMEM, attr);
+    if (batch <= 0 || n_data <= 0) return;
+    const int tiles = (batch + MT - 1) / MT;
+    const int blocks = std::max(1, std::min(tiles, sm_count()));
+    mlp_train_kernel<<<blocks, MT, TRAIN_SMEM, st>>>(W, X, T, wt, n_data, batch, seed, step, grad, loss, err);
+    lc.add(1);
+}
+
+void mlp_adam(float* W, float* grad, float* m, float* v, float lr, float beta1, float beta2, float eps, int t,
+              cudaStream_t st, LaunchCounter& lc) {
+    const float c1 = (float)(1.0 - std::pow((double)beta1, (double)t));
+    const float c2 = (float)(1.0 - std::pow((double)beta2, (double)t));
+    mlp_adam_kernel<<<(MLP_NPARAM + 255) / 256, 256, 0, st>>>(W, grad, m, v, lr, beta1, beta2, eps, c1, c2);
+    lc.add(1);
+}
+
+}  // namespace geon

@@ -64,6 +64,10 @@ struct TreeBufs {
     float4* leaf_a; float4* leaf_b; float4* leaf_c;
     int4*   leaf_meta;  // start, count, level, parent
     int*    leaf_of;    // [cap_pts] leaf of each sorted point
+    // higher moments about each node's centre of mass (learned correction only; null otherwise)
+    float4* int_m1; float4* int_m2; float4* int_m3;    // (Ixx, Ixy, Iyy, sum|q|), (Dx, Dy, Jxx, Jxy), (Jyy, -, -, -)
+    float4* leaf_m1; float4* leaf_m2; float4* leaf_m3;
+    int mom_on;         // compute the moments in this build
 };
 
 constexpr int LEAF_REF = 1 << 30;

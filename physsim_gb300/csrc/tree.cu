@@ -340,6 +340,44 @@ __device__ __forceinline__ void agg_add_com(Agg& g, df x, df y, float m) {
     g.sy = df_add(g.sy, two_prod(dy.hi + dy.lo, m));
 }
 
+// Higher moments about the node centre of mass: mass quadrupole I, charge
+// dipole D, charge quadrupole J (second moments, not trace-free), sum |q|.
+struct Mom {
+    float ixx, ixy, iyy, s, dx, dy, jxx, jxy, jyy;
+};
+__device__ __forceinline__ void mom_zero(Mom& m) { m = Mom{ 0, 0, 0, 0, 0, 0, 0, 0, 0 }; }
+__device__ __forceinline__ void mom_point(Mom& M, float m, float q, float dx, float dy) {
+    M.ixx += m * dx * dx; M.ixy += m * dx * dy; M.iyy += m * dy * dy;
+    M.dx += q * dx; M.dy += q * dy;
+    M.jxx += q * dx * dx; M.jxy += q * dx * dy; M.jyy += q * dy * dy;
+    M.s += fabsf(q);
+}
+// Adds a child's moments shifted by dx, dy (child COM minus parent COM).
+__device__ __forceinline__ void mom_child(Mom& M, float m, float q, const float4& c1, const float4& c2, const float4& c3,
+                                          float dx, float dy) {
+    M.ixx += c1.x + m * dx * dx; M.ixy += c1.y + m * dx * dy; M.iyy += c1.z + m * dy * dy;
+    M.s += c1.w;
+    M.dx += c2.x + q * dx; M.dy += c2.y + q * dy;
+    M.jxx += c2.z + 2.f * c2.x * dx + q * dx * dx;
+    M.jxy += c2.w + c2.x * dy + c2.y * dx + q * dx * dy;
+    M.jyy += c3.x + 2.f * c2.y * dy + q * dy * dy;
+}
+__device__ __forceinline__ void mom_write(float4* m1, float4* m2, float4* m3, int idx, const Mom& M) {
+    m1[idx] = make_float4(M.ixx, M.ixy, M.iyy, M.s);
+    m2[idx] = make_float4(M.dx, M.dy, M.jxx, M.jxy);
+    m3[idx] = make_float4(M.jyy, 0.f, 0.f, 0.f);
+}
+
+__device__ __forceinline__ void agg_com(const Agg& g, df& cx, df& cy) {
+    const float m = g.mass.hi + g.mass.lo;
+    if (m > 0.f) {
+        cx = df_add(g.ox, df{ (g.sx.hi + g.sx.lo) / m, 0.f });
+        cy = df_add(g.oy, df{ (g.sy.hi + g.sy.lo) / m, 0.f });
+    } else {
+        cx = df{ 0.f, 0.f }; cy = df{ 0.f, 0.f };
+    }
+}
+
 __device__ __forceinline__ void agg_write(float4* A, float4* B, float4* C, int idx, const Agg& g,
                                           float size2, int level) {
     const float m = g.mass.hi + g.mass.lo;
@@ -395,6 +433,19 @@ __global__ void aggregate_kernel(DevParams P, DevState S, TreeBufs T, FrameCtl* 
             agg_add_com(g, df{ pa.x, pb.x }, df{ pa.y, pb.y }, m);
         }
         agg_write(T.leaf_a, T.leaf_b, T.leaf_c, leaf, g, node_size2(P, lm.z), lm.z);
+        if (T.mom_on) {
+            df cx, cy;
+            agg_com(g, cx, cy);
+            Mom M; mom_zero(M);
+            for (int k = 0; k < lm.y; k++) {
+                const float4 pa = T.ps_a[lm.x + k];
+                const float4 pb = T.ps_b[lm.x + k];
+                const df ddx = df_add(df{ pa.x, pb.x }, df{ -cx.hi, -cx.lo });
+                const df ddy = df_add(df{ pa.y, pb.y }, df{ -cy.hi, -cy.lo });
+                mom_point(M, pa.z, pa.w, ddx.hi + ddx.lo, ddy.hi + ddy.lo);
+            }
+            mom_write(T.leaf_m1, T.leaf_m2, T.leaf_m3, leaf, M);
+        }
         // climb
         int node = lm.w;
         int guard = 0;
@@ -431,6 +482,32 @@ __global__ void aggregate_kernel(DevParams P, DevState S, TreeBufs T, FrameCtl* 
             }
             const int4 mm = T.int_meta[node];
             agg_write(T.int_a, T.int_b, T.int_c, node, h, node_size2(P, mm.x), mm.x);
+            if (T.mom_on) {
+                df px, py;
+                agg_com(h, px, py);
+                Mom M; mom_zero(M);
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int c = cs[q];
+                    if (c < 0) continue;
+                    float4 a, cc, c1, c2, c3;
+                    if (c & LEAF_REF) {
+                        const int li = c & ~LEAF_REF;
+                        if (li >= nLeaves) continue;
+                        a = __ldcg(&T.leaf_a[li]); cc = __ldcg(&T.leaf_c[li]);
+                        c1 = __ldcg(&T.leaf_m1[li]); c2 = __ldcg(&T.leaf_m2[li]); c3 = __ldcg(&T.leaf_m3[li]);
+                    } else {
+                        if (c >= nInt) continue;
+                        a = __ldcg(&T.int_a[c]); cc = __ldcg(&T.int_c[c]);
+                        c1 = __ldcg(&T.int_m1[c]); c2 = __ldcg(&T.int_m2[c]); c3 = __ldcg(&T.int_m3[c]);
+                    }
+                    if (!(a.z > 0.f)) continue;
+                    const df ddx = df_add(df{ a.x, cc.x }, df{ -px.hi, -px.lo });
+                    const df ddy = df_add(df{ a.y, cc.y }, df{ -py.hi, -py.lo });
+                    mom_child(M, a.z, a.w, c1, c2, c3, ddx.hi + ddx.lo, ddy.hi + ddy.lo);
+                }
+                mom_write(T.int_m1, T.int_m2, T.int_m3, node, M);
+            }
             node = mm.w;
         }
     }

@@ -119,6 +119,66 @@ class GeonSystem:
         self._ck(self.lib.geon_direct_forces(self._h, N.iptr(idx), idx.size, N.fptr(fx), N.fptr(fy)))
         return fx[:idx.size], fy[:idx.size]
 
+    def learn_dataset(self, targets, cap: int) -> dict:
+        """(cell, target) aggregate interactions of the listed targets with
+        features, exact residuals and scales (learned correction training data)."""
+        t = np.ascontiguousarray(targets, dtype=np.int32)
+        cap = int(cap)
+        fm = np.zeros((max(cap, 1), 9), dtype=np.float32)
+        fc = np.zeros((max(cap, 1), 9), dtype=np.float32)
+        res = np.zeros((max(cap, 1), 4), dtype=np.float32)
+        sc = np.zeros((max(cap, 1), 2), dtype=np.float32)
+        pt = np.zeros(max(cap, 1), dtype=np.int32)
+        cnt = C.c_int32()
+        self._ck(self.lib.geon_learn_dataset(self._h, N.iptr(t), t.size, cap, N.fptr(fm), N.fptr(fc), N.fptr(res),
+                                             N.fptr(sc), N.iptr(pt), C.byref(cnt)))
+        m = min(cnt.value, cap)
+        return {"count": cnt.value, "feat_mass": fm[:m], "feat_charge": fc[:m], "residual": res[:m], "scales": sc[:m],
+                "target": pt[:m]}
+
+    def learn_set_weights(self, weights):
+        """Weights of the learned correction (None clears them)."""
+        if weights is None:
+            self._ck(self.lib.geon_learn_set_weights(self._h, None, 0))
+            return
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        self._ck(self.lib.geon_learn_set_weights(self._h, N.fptr(w), w.size))
+
+    def mlp_forward(self, weights, x) -> np.ndarray:
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 9)
+        y = np.zeros((max(len(x), 1), 2), dtype=np.float32)
+        self._ck(self.lib.geon_mlp_forward(self._h, N.fptr(w), N.fptr(x), len(x), N.fptr(y)))
+        return y[:len(x)]
+
+    def mlp_grad(self, weights, x, t, wt=None) -> tuple:
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 9)
+        t = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, 2)
+        wp = None
+        if wt is not None:
+            wt = np.ascontiguousarray(wt, dtype=np.float32)
+            wp = N.fptr(wt)
+        g = np.zeros(N.MLP_NPARAM, dtype=np.float32)
+        loss = C.c_double()
+        self._ck(self.lib.geon_mlp_grad(self._h, N.fptr(w), N.fptr(x), N.fptr(t), wp, len(x), N.fptr(g),
+                                        C.byref(loss)))
+        return g, loss.value
+
+    def mlp_train(self, weights, x, t, steps: int, batch: int, lr: float, seed: int = 1, wt=None) -> tuple:
+        """Adam training on the device; returns (trained weights, per-step loss)."""
+        w = np.array(weights, dtype=np.float32, copy=True)
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 9)
+        t = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, 2)
+        wp = None
+        if wt is not None:
+            wt = np.ascontiguousarray(wt, dtype=np.float32)
+            wp = N.fptr(wt)
+        hist = np.zeros(max(int(steps), 1), dtype=np.float64)
+        self._ck(self.lib.geon_mlp_train(self._h, N.fptr(w), N.fptr(x), N.fptr(t), wp, len(x), int(steps), int(batch),
+                                         float(lr), int(seed), hist.ctypes.data_as(C.POINTER(C.c_double))))
+        return w, hist[:int(steps)]
+
     def forces(self) -> dict:
         n = self.count()
         cap = max(n, 1)
