@@ -246,7 +246,7 @@ int geon_direct_forces(GeonHandle* h, const int32_t* idx, int32_t k, float* fx, 
  * handle's theta, and for every (cell, target) aggregate interaction writes
  * 9 mass-net features, 9 charge-net features, the exact member-sum residual
  * (4: mass field x y, charge field x y, normalised) and the 2 scales
- * (M / r_e^2, sum|q| / r_e^2), and (when pair_target is not NULL) the
+ * (M s^2 / r_e^4, sum|q| / r_e^2; s the cell size), and (when pair_target is not NULL) the
  * target particle of each pair.  Arrays hold `cap` records; *count receives
  * the number of pairs found (records beyond cap are dropped). */
 int geon_learn_dataset(GeonHandle* h, const int32_t* targets, int32_t k, int32_t cap, float* feat_mass,
@@ -256,7 +256,7 @@ int geon_learn_dataset(GeonHandle* h, const int32_t* targets, int32_t k, int32_t
  * A 9 -> 64 -> 64 -> 2 GELU network (BF16 weights and activations, FP32
  * accumulation on the tensor cores) maps the mass-net features of an
  * accepted (cell, target) pair to the residual of its monopole term; the
- * force pass adds m_i * (M / r_e^2) * net(features) for every pair.  Weight
+ * force pass adds m_i * (M s^2 / r_e^4) * net(features) for every pair.  Weight
  * vector (FP32, GEON_MLP_NPARAM floats, nn.Linear layout W[out][in]):
  *     W1[64][9] b1[64] W2[64][64] b2[64] W3[2][64] b3[2] */
 #define GEON_MLP_NPARAM 4930

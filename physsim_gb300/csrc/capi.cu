@@ -97,9 +97,10 @@ struct GeonHandle {
     int nextId = 0;
     // learned correction
     float* learn_w = nullptr;       // [GEON_MLP_NPARAM] device weights (null: correction off)
-    LearnPair* pairs = nullptr;     // (cell, target) pairs of the current force pass
-    int* pair_cnt = nullptr;
-    int pair_cap = 0;
+    LearnPair* pairs = nullptr;     // (cell, target) pairs of one chunk of targets
+    unsigned long long* pair_cnt = nullptr;
+    long long pair_cap = 0;
+    double pairs_per_target = 0.0;  // largest ratio seen, sizes the target chunks
     LaunchCounter lc;
     std::string err;
     // profiling
@@ -443,17 +444,22 @@ static bool learn_active(const GeonHandle* h) {
     return h->learn_w && (h->prm.flags & GEON_FLAG_LEARN) && h->T.mom_on && h->n > 0;
 }
 
-// Grows the pair buffer to hold at least `need` pairs (contents discarded).
+// Largest pair buffer of the learned correction (pairs; 8 bytes each).  The
+// targets are processed in chunks that fit it.
+constexpr long long PAIR_CAP_MAX = 1ll << 28;
+
+// Grows the pair buffer to hold at least `need` (<= PAIR_CAP_MAX) pairs
+// (contents discarded).
 static int ensure_pairs(GeonHandle* h, long long need) {
     if (need <= h->pair_cap) return GEON_OK;
-    const long long cap = std::min<long long>(INT_MAX, need + need / 4 + 4096);
+    const long long cap = std::min<long long>(PAIR_CAP_MAX, need + need / 4 + 4096);
     if (h->pairs) { cudaStreamSynchronize(h->st); cudaFree(h->pairs); h->pairs = nullptr; h->pair_cap = 0; }
     if (cudaMalloc(&h->pairs, (size_t)cap * sizeof(LearnPair)) != cudaSuccess) {
         cudaGetLastError();
         h->pairs = nullptr;
         return set_err(h, GEON_ERR_NOMEM, "learned-correction pair buffer allocation failed");
     }
-    h->pair_cap = (int)cap;
+    h->pair_cap = cap;
     return GEON_OK;
 }
 
@@ -463,24 +469,40 @@ static int ensure_pairs(GeonHandle* h, long long need) {
 // force pass made from the uncorrected forces.
 static int learn_pass(GeonHandle* h) {
     const int ps = prof_begin(h, PH_LEARN);
-    int found = 0;
-    for (int attempt = 0; attempt < 2; attempt++) {
-        learn_collect_pairs(h->P, h->S, h->T, h->d_root, h->ctl, h->T.tgt, h->n, h->pairs, h->pair_cap, h->pair_cnt,
-                            h->st, h->lc);
+    const int n = h->n;
+    long long total = 0;
+    int k0 = 0;
+    while (k0 < n) {
+        // chunk of targets (in walk order) whose pairs should fit the buffer
+        long long chunk = n - k0;
+        const double est = h->pairs_per_target > 0 ? h->pairs_per_target * 1.1 : 4096.0;
+        chunk = std::min<long long>(chunk, std::max<long long>(1024, (long long)(PAIR_CAP_MAX / est)));
+        unsigned long long found = 0;
+        for (;;) {
+            learn_collect_pairs(h->P, h->S, h->T, h->d_root, h->ctl, h->T.tgt + k0, (int)chunk, h->pairs, h->pair_cap,
+                                h->pair_cnt, h->st, h->lc);
+            CKL();
+            CK(cudaMemcpyAsync(&found, h->pair_cnt, sizeof(found), cudaMemcpyDeviceToHost, h->st));
+            CK(cudaStreamSynchronize(h->st));
+            h->pairs_per_target = std::max(h->pairs_per_target, (double)found / (double)chunk);
+            if ((long long)found <= h->pair_cap) break;
+            if ((long long)found > PAIR_CAP_MAX) {                  // too many for one buffer: smaller chunk
+                if (chunk <= 1) return set_err(h, GEON_ERR_OVERFLOW, "learned-correction pairs of one target exceed the buffer");
+                chunk = std::max<long long>(1, chunk * PAIR_CAP_MAX / (long long)found / 2);
+                continue;
+            }
+            int r = ensure_pairs(h, (long long)found);
+            if (r) return r;
+        }
+        mlp_correct(h->P, h->S, h->T, h->learn_w, h->pairs, (int)found, &h->ctl->err, h->st, h->lc);
         CKL();
-        CK(cudaMemcpyAsync(&found, h->pair_cnt, sizeof(int), cudaMemcpyDeviceToHost, h->st));
-        CK(cudaStreamSynchronize(h->st));
-        if (found <= h->pair_cap) break;
-        int r = ensure_pairs(h, found);
-        if (r) return r;
+        total += (long long)found;
+        k0 += (int)chunk;
     }
-    if (found > h->pair_cap) return set_err(h, GEON_ERR_OVERFLOW, "learned-correction pair buffer overflow");
-    mlp_correct(h->P, h->S, h->T, h->learn_w, h->pairs, found, &h->ctl->err, h->st, h->lc);
-    CKL();
     launch_frame_scan(h->P, h->S, h->ctl, h->n_cap, h->st, h->lc);
     CKL();
     prof_end(h, ps);
-    if (h->prof) h->prof_acc.learn_pairs += found;
+    if (h->prof) h->prof_acc.learn_pairs += total;
     return GEON_OK;
 }
 
@@ -754,7 +776,7 @@ int geon_learn_dataset(GeonHandle* h, const int32_t* targets, int32_t k, int32_t
     if (r) return r;
     DevArena tmp;
     int* d_t = tmp.alloc<int>(k);
-    int* d_cnt = tmp.alloc<int>(1);
+    unsigned long long* d_cnt = tmp.alloc<unsigned long long>(1);
     const int capd = std::max(cap, 1);
     LearnPair* d_pairs = tmp.alloc<LearnPair>(capd);
     float* d_fm = tmp.alloc<float>((size_t)capd * LF);
@@ -768,9 +790,10 @@ int geon_learn_dataset(GeonHandle* h, const int32_t* targets, int32_t k, int32_t
         learn_residuals(h->P, h->S, h->T, d_pairs, d_cnt, cap, d_fm, d_fc, d_res, d_sc, h->st, h->lc);
         e = cudaGetLastError();
     }
-    int found = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&found, d_cnt, sizeof(int), cudaMemcpyDeviceToHost, h->st);
+    unsigned long long found64 = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&found64, d_cnt, sizeof(found64), cudaMemcpyDeviceToHost, h->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    const int found = (int)std::min<unsigned long long>(found64, (unsigned long long)INT_MAX);
     const int m = std::min(found, cap);
     if (e == cudaSuccess && m > 0) {
         cudaMemcpyAsync(feat_mass, d_fm, (size_t)m * LF * sizeof(float), cudaMemcpyDeviceToHost, h->st);
@@ -798,12 +821,12 @@ int geon_learn_set_weights(GeonHandle* h, const float* weights, int32_t n_param)
     static_assert(MLP_NPARAM == GEON_MLP_NPARAM, "weight count");
     if (h->learn_arena.ptrs.empty()) {
         float* w = h->learn_arena.alloc<float>(MLP_NPARAM);
-        int* c = h->learn_arena.alloc<int>(1);
+        unsigned long long* c = h->learn_arena.alloc<unsigned long long>(1);
         if (h->learn_arena.failed) { h->learn_arena.free_all(); return set_err(h, GEON_ERR_NOMEM, "weight allocation failed"); }
         (void)w; (void)c;
     }
     float* dw = static_cast<float*>(h->learn_arena.ptrs[0]);
-    h->pair_cnt = static_cast<int*>(h->learn_arena.ptrs[1]);
+    h->pair_cnt = static_cast<unsigned long long*>(h->learn_arena.ptrs[1]);
     CK(cudaMemcpyAsync(dw, weights, MLP_NPARAM * sizeof(float), cudaMemcpyHostToDevice, h->st));
     CK(cudaStreamSynchronize(h->st));
     h->learn_w = dw;
@@ -1198,3 +1221,4 @@ int geon_launch_count(GeonHandle* h, int64_t* count) {
 }
 
 }  // extern "C"
+

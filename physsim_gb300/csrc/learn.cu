@@ -17,7 +17,8 @@ constexpr int LC_WARPS = LC_THREADS / 32;
 
 __global__ void __launch_bounds__(LC_THREADS)
 collect_pairs_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl,
-                     const int* __restrict__ targets, int k, LearnPair* pairs, int cap, int* d_count) {
+                     const int* __restrict__ targets, int k, LearnPair* pairs, long long cap,
+                     unsigned long long* d_count) {
     __shared__ int s_node[LC_WARPS][WALK_STACK];
     __shared__ unsigned s_mask[LC_WARPS][WALK_STACK];
     const int warp = threadIdx.x >> 5;
@@ -65,12 +66,12 @@ collect_pairs_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict_
         }
         const unsigned acc = __ballot_sync(0xffffffffu, accept);
         if (acc) {
-            int base = 0;
-            if (lane == 0) base = atomicAdd(d_count, __popc(acc));
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(d_count, (unsigned long long)__popc(acc));
             base = __shfl_sync(0xffffffffu, base, 0);
             if (accept) {
-                const int pos = base + __popc(acc & lanemask_lt());
-                if (pos < cap) pairs[pos] = LearnPair{ node, i };
+                const unsigned long long pos = base + (unsigned long long)__popc(acc & lanemask_lt());
+                if (pos < (unsigned long long)cap) pairs[pos] = LearnPair{ node, i };
             }
         }
         const unsigned open = mask & ~acc;
@@ -113,8 +114,9 @@ __device__ __forceinline__ void source_fields(const DevParams& P, float rx, floa
 }
 
 __global__ void residual_kernel(DevParams P, DevState S, TreeBufs T, const LearnPair* __restrict__ pairs,
-                                const int* d_count, int cap, float* feat_m, float* feat_c, float* target, float* scales) {
-    const int np = min(*d_count, cap);
+                                const unsigned long long* d_count, int cap, float* feat_m, float* feat_c, float* target,
+                                float* scales) {
+    const int np = (int)min(*d_count, (unsigned long long)cap);
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < np; e += gridDim.x * blockDim.x) {
         const LearnPair pr = pairs[e];
         const int node = pr.node, i = pr.target;
@@ -152,15 +154,16 @@ __global__ void residual_kernel(DevParams P, DevState S, TreeBufs T, const Learn
 }
 
 void learn_collect_pairs(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
-                         const int* d_targets, int k, LearnPair* pairs, int cap, int* d_count,
+                         const int* d_targets, int k, LearnPair* pairs, long long cap, unsigned long long* d_count,
                          cudaStream_t st, LaunchCounter& lc) {
-    cudaMemsetAsync(d_count, 0, sizeof(int), st);
+    cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), st);
     const int blocks = std::max(1, (k + LC_THREADS - 1) / LC_THREADS);
     collect_pairs_kernel<<<blocks, LC_THREADS, 0, st>>>(P, S, T, d_root, ctl, d_targets, k, pairs, cap, d_count);
     lc.add(1);
 }
 
-void learn_residuals(const DevParams& P, const DevState& S, const TreeBufs& T, const LearnPair* pairs, const int* d_count,
+void learn_residuals(const DevParams& P, const DevState& S, const TreeBufs& T, const LearnPair* pairs,
+                     const unsigned long long* d_count,
                      int cap, float* feat_m, float* feat_c, float* target, float* scales, cudaStream_t st,
                      LaunchCounter& lc) {
     residual_kernel<<<152 * 8, 128, 0, st>>>(P, S, T, pairs, d_count, cap, feat_m, feat_c, target, scales);

@@ -4,11 +4,13 @@
 // For a Barnes-Hut interaction in which target i accepts cell c as one
 // aggregate (src/forces.js:680-685), the force is the monopole term at the
 // cell's centre of mass.  The correction adds
-//     m_i * (M / r_e^2) * g(x_mass) + q_i * (S / r_e^2) * e(x_charge)
-// where g and e are two small MLPs (9 -> 64 -> 64 -> 2, GELU) of dimensionless
-// features of the cell seen from the target, M the cell mass, S = sum |q|,
-// r_e^2 = |d|^2 + softening^2.  g corrects the mass-sourced field (gravity
-// and Yukawa), e the charge-sourced field (Coulomb).
+//     m_i * (M s^2 / r_e^4) * g(x_mass)
+// where g is a small MLP (9 -> 64 -> 64 -> 2, GELU) of dimensionless features
+// of the cell seen from the target, M the cell mass, s the cell size and
+// r_e^2 = |d|^2 + softening^2: the mass-sourced field (gravity and Yukawa).
+// The dataset also carries charge-net features with the scale S / r_e^2
+// (S = sum |q|) for the Coulomb field; measured, a charge net gains nothing
+// on the configurations here, so the force pass applies g only.
 #pragma once
 
 #include "state.cuh"
@@ -30,11 +32,15 @@ __device__ __forceinline__ void pair_features(const DevParams& P, float dx, floa
     const float ux = dx * inv, uy = dy * inv;
     const float sz = size * inv, so = P.soft * inv;
     fm[0] = ux; fm[1] = uy; fm[2] = sz; fm[3] = so;
-    const float iM = M > 0.f ? 1.f / M : 0.f;
-    fm[4] = m1.x * iM * inv2; fm[5] = m1.y * iM * inv2; fm[6] = m1.z * iM * inv2;
+    // second moments per unit mass in units of the cell size squared, and a
+    // scale with the quadrupole's fall-off M s^2 / r_e^4, so that features and
+    // targets stay O(1) from the largest to the smallest accepted cells
+    const float s2 = size * size;
+    const float iMs = (M > 0.f && s2 > 0.f) ? 1.f / (M * s2) : 0.f;
+    fm[4] = m1.x * iMs; fm[5] = m1.y * iMs; fm[6] = m1.z * iMs;
     fm[7] = P.yukOn ? P.yukMu * (re2 * inv) * (1.f / 6.f) : 0.f;
     fm[8] = P.yukOn ? r2 / P.yukCutSq : 0.f;
-    scale_m = M * inv2;
+    scale_m = M * s2 * inv2 * inv2;
     const float S = m1.w;
     const float iS = S > 0.f ? 1.f / S : 0.f;
     fc[0] = ux; fc[1] = uy; fc[2] = sz; fc[3] = so;
@@ -51,11 +57,14 @@ struct LearnPair { int node; int target; };
 // learn.cu
 // Collects the (cell, target) aggregate interactions of a Barnes-Hut walk for
 // the listed targets (device arrays), then computes features and the exact
-// member-sum residuals.  Returns the pair count through *d_count.
+// member-sum residuals.  Returns the pair count through *d_count (64-bit:
+// at small theta a million targets accept more than 2^31 cells); pairs at
+// positions >= cap are counted but not stored.
 void learn_collect_pairs(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
-                         const int* d_targets, int k, LearnPair* pairs, int cap, int* d_count,
+                         const int* d_targets, int k, LearnPair* pairs, long long cap, unsigned long long* d_count,
                          cudaStream_t st, LaunchCounter& lc);
-void learn_residuals(const DevParams& P, const DevState& S, const TreeBufs& T, const LearnPair* pairs, const int* d_count,
+void learn_residuals(const DevParams& P, const DevState& S, const TreeBufs& T, const LearnPair* pairs,
+                     const unsigned long long* d_count,
                      int cap, float* feat_m, float* feat_c, float* target, float* scales, cudaStream_t st,
                      LaunchCounter& lc);
 

@@ -13,7 +13,7 @@ constexpr int MLP_NPARAM = LH * LF + LH + LH * LH + LH + LO * LH + LO;   // 4930
 // Y[n][2] = net(X[n][9]) with device arrays.
 void mlp_forward(const float* W, const float* X, int n, float* Y, int* err, cudaStream_t st, LaunchCounter& lc);
 
-// Adds m_i * (M / r_e^2) * net(features) to S.force for every recorded (cell,
+// Adds m_i * (M s^2 / r_e^4) * net(features) to S.force for every recorded (cell,
 // target) pair; `npairs` is the number of valid entries of `pairs`.
 void mlp_correct(const DevParams& P, const DevState& S, const TreeBufs& T, const float* W, const LearnPair* pairs,
                  int npairs, int* err, cudaStream_t st, LaunchCounter& lc);
