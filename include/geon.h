@@ -240,6 +240,20 @@ int geon_compute_1pn(GeonHandle* h);
  * exact reference for measuring the Barnes-Hut force error on a subsample. */
 int geon_direct_forces(GeonHandle* h, const int32_t* idx, int32_t k, float* fx, float* fy);
 
+/* The same pairwise subset sum as geon_direct_forces, with no device
+ * allocation (no reference counterpart: the reference's JS path has no
+ * device memory to allocate).  For callers that must not call cudaMalloc /
+ * cudaFree during a run: the indices and outputs are staged in a fixed
+ * device array reserved when the library loads, one per device, so
+ *   - k is at most GEON_DIRECT_NOALLOC_MAX_K (larger k: GEON_ERR_ARG);
+ *   - the first call on a device sets up the array's address; make it before
+ *     any stream capture begins;
+ *   - no part of the array needs to start at zero;
+ *   - calls that overlap in time on one device race on the array: serialise
+ *     them (consecutive calls are safe; each waits for its stream). */
+#define GEON_DIRECT_NOALLOC_MAX_K 16384
+int geon_direct_forces_noalloc(GeonHandle* h, const int32_t* idx, int32_t k, float* fx, float* fy);
+
 /* Training data of the learned far-field correction (no reference
  * counterpart; the reference has plain monopole Barnes-Hut only).  Builds the
  * tree with cell moments, walks it for the k listed target particles at the

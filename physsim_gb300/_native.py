@@ -46,6 +46,7 @@ FLAG_NO_GHOSTS = 1 << 2
 FLAG_SIMPLE_WALK = 1 << 3
 FLAG_LEARN = 1 << 4
 MLP_NPARAM = 4930
+DIRECT_NOALLOC_MAX_K = 16384
 
 OUT_ROWS = 25
 OUT_NAMES = ["fx", "fy", "Bz", "Bgz", "dBzdx", "dBzdy", "dBgzdx", "dBgzdy", "tidal", "frameDrag",
@@ -150,6 +151,7 @@ SIGNATURES = {
     "geon_compute_forces": [_handle_t],
     "geon_compute_1pn": [_handle_t],
     "geon_direct_forces": [_handle_t, _P(C.c_int32), C.c_int32, _P(C.c_float), _P(C.c_float)],
+    "geon_direct_forces_noalloc": [_handle_t, _P(C.c_int32), C.c_int32, _P(C.c_float), _P(C.c_float)],
     "geon_learn_dataset": [_handle_t, _P(C.c_int32), C.c_int32, C.c_int32, _P(C.c_float), _P(C.c_float),
                            _P(C.c_float), _P(C.c_float), _P(C.c_int32), _P(C.c_int32)],
     "geon_learn_set_weights": [_handle_t, _P(C.c_float), C.c_int32],

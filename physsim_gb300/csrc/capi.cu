@@ -1222,3 +1222,88 @@ int geon_launch_count(GeonHandle* h, int64_t* count) {
 
 }  // extern "C"
 
+// =============================================================================================
+// geon_direct_forces_noalloc: the pairwise subset sum of geon_direct_forces
+// without any device allocation.
+//
+// geon_direct_forces allocates its index and output buffers with cudaMalloc
+// and releases them with cudaFree on every call.  Some callers cannot do that:
+// a host loop that samples the force error every frame while other streams
+// of the device are busy (cudaFree waits for the whole device and would stall
+// them), and embeddings that fix their device-memory footprint at start-up
+// and must not meet an allocation failure in the middle of a run.  This
+// variant stages the indices and the two output rows in one fixed array in
+// device global memory, reserved when the library is loaded, and allocates
+// nothing.
+//
+// Limits and rules:
+//   * at most GEON_DIRECT_NOALLOC_MAX_K targets per call (192 KiB of scratch:
+//     k indices, then k x forces, then k y forces, each row sized for the
+//     maximum); larger k is rejected with GEON_ERR_ARG;
+//   * the first call on a device does the setup (it looks up the array's
+//     device address with that device current and caches it per device), so
+//     make that first call before any stream capture begins;
+//   * nothing in the scratch has to start at zero: each call copies its k
+//     indices in before the kernel reads them, and the kernel writes all k
+//     outputs before they are copied out;
+//   * the array is one per device, shared by every handle on it: calls that
+//     overlap in time on the same device (from different host threads or
+//     handles) race on it and must be serialised by the caller.  Calls made
+//     one after another are safe, because each call waits for its stream
+//     before it returns.
+#include <mutex>
+
+static constexpr int NOALLOC_MAX_K = GEON_DIRECT_NOALLOC_MAX_K;
+static constexpr int NOALLOC_MAX_DEVICES = 64;
+static __device__ __align__(256) unsigned char g_direct_scratch[3 * NOALLOC_MAX_K * sizeof(float)];
+static void* g_direct_scratch_addr[NOALLOC_MAX_DEVICES] = {};
+static std::mutex g_direct_scratch_mu;
+
+// Device address of the scratch array on the device of h's stream.
+static int direct_scratch(GeonHandle* h, void** out) {
+    int dev = -1;
+    cudaError_t e = cudaStreamGetDevice(h->st, &dev);
+    if (e != cudaSuccess) return cuda_check(h, e, "cudaStreamGetDevice");
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return set_err(h, GEON_ERR_UNSUPPORTED, "device index beyond the scratch table");
+    std::lock_guard<std::mutex> lock(g_direct_scratch_mu);
+    if (!g_direct_scratch_addr[dev]) {
+        int cur = -1;
+        e = cudaGetDevice(&cur);
+        if (e == cudaSuccess && cur != dev) e = cudaSetDevice(dev);
+        void* p = nullptr;
+        if (e == cudaSuccess) e = cudaGetSymbolAddress(&p, g_direct_scratch);
+        if (cur >= 0 && cur != dev) cudaSetDevice(cur);
+        if (e != cudaSuccess) return cuda_check(h, e, "cudaGetSymbolAddress(direct-forces scratch)");
+        if (!p) return set_err(h, GEON_ERR_CUDA, "direct-forces scratch has no device address");
+        g_direct_scratch_addr[dev] = p;
+    }
+    *out = g_direct_scratch_addr[dev];
+    return GEON_OK;
+}
+
+extern "C" int geon_direct_forces_noalloc(GeonHandle* h, const int32_t* idx, int32_t k, float* fx, float* fy) {
+    if (!h || k < 0 || (k > 0 && (!idx || !fx || !fy))) return GEON_ERR_ARG;
+    if (k > NOALLOC_MAX_K)
+        return set_err(h, GEON_ERR_ARG, "geon_direct_forces_noalloc: k = " + std::to_string(k) +
+                       " exceeds GEON_DIRECT_NOALLOC_MAX_K = " + std::to_string(NOALLOC_MAX_K) +
+                       " (use geon_direct_forces for larger subsets)");
+    if (k == 0 || h->n == 0) return GEON_OK;
+    for (int i = 0; i < k; i++)
+        if (idx[i] < 0 || idx[i] >= h->n) return set_err(h, GEON_ERR_ARG, "index out of range");
+    void* base = nullptr;
+    int r = direct_scratch(h, &base);
+    if (r) return r;
+    int* d_idx = static_cast<int*>(base);
+    float* d_fx = reinterpret_cast<float*>(d_idx + NOALLOC_MAX_K);
+    float* d_fy = d_fx + NOALLOC_MAX_K;
+    cudaError_t e = cudaMemcpyAsync(d_idx, idx, k * sizeof(int), cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess && h->P.rel) { launch_hist_tables(h->hist_t, h->simTime, h->hist_age, h->hist_segdt, h->st, h->lc); e = cudaGetLastError(); }
+    if (e == cudaSuccess) {
+        direct_subset(h->P, h->S, h->ctl, make_ctx(h), d_idx, k, d_fx, d_fy, h->st, h->lc);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fx, d_fx, k * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fy, d_fy, k * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    return cuda_check(h, e, "direct forces (no allocation)");
+}
