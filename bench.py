@@ -65,6 +65,9 @@ def parse():
     ap.add_argument("--learn-steps", type=int, default=20000)
     ap.add_argument("--learn-batch", type=int, default=65536)
     ap.add_argument("--learn-train-n", type=int, default=262144, help="particles of the training snapshot")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--ensemble-systems", type=int, default=512)
+    ap.add_argument("--ensemble-frames", type=int, default=20)
     return ap.parse_args()
 
 
@@ -335,6 +338,82 @@ def run_learned(args, g, wl, idx, fx, fy, stream):
             "sweep": {str(k): v for k, v in sweep.items()}}
 
 
+def run_ensemble(args):
+    """Batched ensemble: 512 independent systems (N log-uniform in
+    [256, 16384], one Gaussian cluster each, gravity + Coulomb, torus,
+    theta 0.6) advanced together by one batched handle (frame = one CUDA
+    graph launch after the autotuner picked the mode), against looping the
+    plain per-system path (one handle per system, geon_update each).
+    Returns systems-frames/s and per-frame latency percentiles of both."""
+    from physsim_gb300 import workloads as W
+    from physsim_gb300.system import BatchSystem, GeonSystem
+
+    wl = W.ensemble(n_systems=args.ensemble_systems)
+    counts = wl.info["counts"]
+    nsys = len(counts)
+    b = BatchSystem(wl.params, counts)
+    b.upload(*[wl.state[k] for k in STATE_KEYS])
+    choice, tune_ms = b.autotune(wl.dt, frames=2)
+    b.upload(*[wl.state[k] for k in STATE_KEYS])
+    for _ in range(max(3, args.warmup)):
+        b.update(wl.dt)
+    b.synchronize()
+    lat = []
+    l0 = b.launch_count()
+    b.profile(True)
+    t0 = time.perf_counter()
+    for _ in range(args.ensemble_frames):
+        t = time.perf_counter()
+        b.update(wl.dt)                      # returns after the frame's summary read (synchronised)
+        lat.append(time.perf_counter() - t)
+    total = time.perf_counter() - t0
+    prof = b.profile(False)
+    launches = b.launch_count() - l0
+    steps = b.substeps()
+    b.close()
+    lat = np.array(lat) * 1e3
+    batched = {"value": nsys * args.ensemble_frames / total, "frames": args.ensemble_frames,
+               "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+               "particle_substeps_per_s": prof["particle_substeps"] / total,
+               "mode": {0: "launches, grouped walk", 1: "graph, grouped walk", 2: "launches, simple walk",
+                        3: "graph, simple walk"}[choice],
+               "autotune_ms_per_frame": {"launches+grouped": tune_ms[0], "graph+grouped": tune_ms[1],
+                                         "launches+simple": tune_ms[2], "graph+simple": tune_ms[3]},
+               "gpu_launches_per_frame": launches / args.ensemble_frames,
+               "substeps_last_frame": {"min": int(steps.min()), "max": int(steps.max()),
+                                       "mean": float(steps.mean())}}
+    # looping the plain per-system path: one handle per system, frames in turn
+    handles = []
+    for st in W.split_systems(wl):
+        g = GeonSystem(wl.params, st["x"].size)
+        g.upload(*[st[k] for k in STATE_KEYS])
+        handles.append(g)
+    for g in handles:
+        g.update(wl.dt)
+    loop_frames = max(1, min(3, args.ensemble_frames))
+    per = []
+    t0 = time.perf_counter()
+    for _ in range(loop_frames):
+        for g in handles:
+            t = time.perf_counter()
+            g.update(wl.dt)
+            per.append(time.perf_counter() - t)
+    total_l = time.perf_counter() - t0
+    for g in handles:
+        g.close()
+    per = np.array(per) * 1e3
+    frame_lat = per.reshape(loop_frames, nsys).sum(1)
+    looped = {"value": nsys * loop_frames / total_l, "frames": loop_frames,
+              "p50_ms": float(np.percentile(frame_lat, 50)), "p99_ms": float(np.percentile(frame_lat, 99)),
+              "system_frame_p50_ms": float(np.percentile(per, 50)),
+              "system_frame_p99_ms": float(np.percentile(per, 99))}
+    return {"workload": wl.name, "systems": nsys, "particles": int(counts.sum()), "unit": "systems-frames/s",
+            "theta": float(wl.params.theta), "forces": "gravity+coulomb+tidal", "boundary": "torus",
+            "batched": batched, "looped_per_system": looped,
+            "speedup": batched["value"] / looped["value"],
+            "latency_note": "p50/p99 of whole-ensemble frame latency (all systems advanced one frame)"}
+
+
 def run_native(args, ws, rank, local):
     import torch
     from physsim_gb300 import build, workloads as W
@@ -429,6 +508,9 @@ def run_native(args, ws, rank, local):
     learned = None
     if not args.no_learned and rank == 0:
         learned = run_learned(args, g, wl, idx, fx, fy, stream)
+    ensemble = None
+    if not args.no_ensemble and rank == 0:
+        ensemble = run_ensemble(args)
 
     # ---- roofline of the dominant kernel (the Barnes-Hut walk, FP32 pipe) ----
     pk = peaks()
@@ -484,6 +566,8 @@ def run_native(args, ws, rank, local):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if ensemble:
+        line["ensemble"] = ensemble
     if learned:
         line["learned"] = learned
         line["learned_vs_plain_at_target_error"] = learned["value"] / value if learned["reached_target"] else None

@@ -296,6 +296,35 @@ int geon_mlp_grad(GeonHandle* h, const float* weights, const float* x, const flo
 int geon_mlp_train(GeonHandle* h, float* weights, const float* x, const float* t, const float* wt, int32_t n,
                    int32_t steps, int32_t batch, float lr, uint64_t seed, double* loss_history);
 
+/* ---- batched systems -----------------------------------------------------
+ * One handle holding n_systems independent systems (up to 512) with the same
+ * parameters and their own particle counts, stepped together: geon_update
+ * advances every system by one frame, each with its own adaptive substeps
+ * (src/integrator.js:810-875).  The reference runs one system per Physics
+ * object; this is its per-system loop folded into one launch sequence.
+ * Particles are given system by system (counts[0] particles of system 0,
+ * then system 1, ...) through geon_upload_state with the total count.
+ * Supported: Barnes-Hut, loop or bounce boundary, no relativity / 1PN,
+ * no learned correction; geon_add_particles (other than the whole batch),
+ * geon_remove_particle, geon_direct_forces and geon_compute_1pn return
+ * GEON_ERR_UNSUPPORTED.  Trees use 27 Morton levels below the system id. */
+#define GEON_BATCH_MAX_SYSTEMS 512
+int geon_create_batch(const GeonParams* params, int32_t n_systems, const int32_t* counts, GeonHandle** out);
+
+/* Substeps each system took in the last frame (n_systems entries). */
+int geon_batch_substeps(GeonHandle* h, int32_t* steps, int32_t n_systems);
+
+/* Frame execution mode: use_graph = 1 runs each frame as one CUDA graph
+ * launch (the substep loop is a device-side WHILE node; default), 0 as
+ * individual launches with one host read per substep; simple_walk selects
+ * the one-node-per-step walk instead of the grouped walk. */
+int geon_batch_set_mode(GeonHandle* h, int32_t use_graph, int32_t simple_walk);
+
+/* Times `frames` frames of dt in each of the 4 modes (choice = use_graph +
+ * 2 * simple_walk; ms_per_frame[4] may be NULL), restores the state, and
+ * keeps the fastest mode. */
+int geon_batch_autotune(GeonHandle* h, double dt, int32_t frames, int32_t* choice, double* ms_per_frame);
+
 /* Copies `rows` rows (GEON_OUT_*) of per-particle force data, each `capacity`
  * floats, starting at row `first_row`. */
 int geon_download_forces(GeonHandle* h, int32_t first_row, int32_t rows,

@@ -47,6 +47,7 @@ FLAG_SIMPLE_WALK = 1 << 3
 FLAG_LEARN = 1 << 4
 MLP_NPARAM = 4930
 DIRECT_NOALLOC_MAX_K = 16384
+BATCH_MAX_SYSTEMS = 512
 
 OUT_ROWS = 25
 OUT_NAMES = ["fx", "fy", "Bz", "Bgz", "dBzdx", "dBzdy", "dBgzdx", "dBgzdy", "tidal", "frameDrag",
@@ -160,6 +161,10 @@ SIGNATURES = {
                       _P(C.c_float), _P(C.c_double)],
     "geon_mlp_train": [_handle_t, _P(C.c_float), _P(C.c_float), _P(C.c_float), _P(C.c_float), C.c_int32, C.c_int32,
                        C.c_int32, C.c_float, C.c_uint64, _P(C.c_double)],
+    "geon_create_batch": [_P(GeonParams), C.c_int32, _P(C.c_int32), _P(_handle_t)],
+    "geon_batch_substeps": [_handle_t, _P(C.c_int32), C.c_int32],
+    "geon_batch_set_mode": [_handle_t, C.c_int32, C.c_int32],
+    "geon_batch_autotune": [_handle_t, C.c_double, C.c_int32, _P(C.c_int32), _P(C.c_double)],
     "geon_download_forces": [_handle_t, C.c_int32, C.c_int32, _P(C.c_float), C.c_int32],
     "geon_build_tree": [_handle_t, _P(GeonTreeInfo)],
     "geon_tree_leaves": [_handle_t, _P(C.c_int32), C.c_int32, _P(C.c_double), _P(C.c_double), _P(C.c_double),

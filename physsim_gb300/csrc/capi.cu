@@ -16,6 +16,7 @@
 #include "push.cuh"
 #include "learn.cuh"
 #include "mlp.cuh"
+#include "batch.cuh"
 
 using namespace geon;
 
@@ -61,6 +62,27 @@ bool grid_exact(double c, double hw) {
 
 }  // namespace
 
+// Batched handle: device arrays of the per-system planner and the frame
+// graph (a WHILE conditional node over the substeps).
+struct Batch {
+    BatchDev dev{};
+    DevArena A;
+    std::vector<int> off;           // [nsys + 1] first particle of each system
+    std::vector<int> pad;           // [nsys] first walk slot of each system
+    int slots = 0;                  // padded walk slots
+    int* sys = nullptr;             // [n_cap] system of each particle
+    int* roots = nullptr;           // [nsys]
+    int* any_h = nullptr;           // pinned copy of dev.any_active
+    double* dt_h = nullptr;         // pinned frame dt
+    SysPlan* plan_h = nullptr;      // pinned copy of dev.plan
+    int use_graph = 1;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long graph_head = 0, graph_body = 0, graph_tail = 0;   // kernels per part of the graph
+    uint32_t graph_flags = 0;       // flags the graph was captured with
+    int last_max_steps = 0;
+};
+
 struct GeonHandle {
     GeonParams prm{};
     DevParams P{};
@@ -95,6 +117,9 @@ struct GeonHandle {
     long long histTotal = 0;
     int lastSubsteps = 0;
     int nextId = 0;
+    // batched systems (nsys > 0)
+    int nsys = 0;
+    Batch* batch = nullptr;
     // learned correction
     float* learn_w = nullptr;       // [GEON_MLP_NPARAM] device weights (null: correction off)
     LearnPair* pairs = nullptr;     // (cell, target) pairs of one chunk of targets
@@ -184,6 +209,9 @@ static void derive_params(GeonHandle* h) {
     P.ghosts = P.periodic && !(p.flags & GEON_FLAG_NO_GHOSTS);
     P.rel = (p.toggles & GEON_RELATIVITY) ? 1 : 0;
     P.n_cap = h->n_cap;
+    P.nsys = h->nsys;
+    P.keyTop = h->nsys ? 10 : 2;
+    P.keyLevels = h->nsys ? BATCH_KEY_LEVELS : KEY_LEVELS;
     P.Wd = p.domain_w; P.Hd = p.domain_h; P.offXd = p.off_x; P.offYd = p.off_y;
     P.W = (float)p.domain_w; P.H = (float)p.domain_h;
     P.W_lo = (float)(p.domain_w - (double)P.W); P.H_lo = (float)(p.domain_h - (double)P.H);
@@ -261,6 +289,7 @@ static int ensure_tree(GeonHandle* h) {
     T.int_child = A.alloc<int4>(T.cap_int); T.int_meta = A.alloc<int4>(T.cap_int); T.int_count = A.alloc<int>(T.cap_int);
     T.leaf_a = A.alloc<float4>(T.cap_pts); T.leaf_b = A.alloc<float4>(T.cap_pts); T.leaf_c = A.alloc<float4>(T.cap_pts);
     T.leaf_meta = A.alloc<int4>(T.cap_pts); T.leaf_of = A.alloc<int>(T.cap_pts);
+    T.roots = h->batch ? h->batch->roots : nullptr;
     if (A.failed) { A.free_all(); T = TreeBufs{}; return set_err(h, GEON_ERR_NOMEM, "tree allocation failed"); }
     h->tree_moments = false;
     h->tree_periodic = per;
@@ -589,6 +618,17 @@ int geon_destroy(GeonHandle* h) {
     h->hist_arena.free_all();
     h->learn_arena.free_all();
     if (h->pairs) cudaFree(h->pairs);
+    if (h->batch) {
+        Batch* B = h->batch;
+        if (B->exec) cudaGraphExecDestroy(B->exec);
+        if (B->graph) cudaGraphDestroy(B->graph);
+        if (B->any_h) cudaFreeHost(B->any_h);
+        if (B->dt_h) cudaFreeHost(B->dt_h);
+        if (B->plan_h) cudaFreeHost(B->plan_h);
+        B->A.free_all();
+        delete B;
+        h->batch = nullptr;
+    }
     h->arena.free_all();
     prof_collect(h);
     for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
@@ -599,12 +639,20 @@ int geon_destroy(GeonHandle* h) {
     return GEON_OK;
 }
 
+static int validate_batch_params(GeonHandle* h, const GeonParams& p);
+static void batch_drop_graph(Batch& B);
+
 int geon_set_params(GeonHandle* h, const GeonParams* params) {
     if (!h || !params) return GEON_ERR_ARG;
     GeonParams p = *params;
     if (p.max_substeps <= 0) p.max_substeps = 32;
     int r = validate_params(h, p);
     if (r) return r;
+    if (h->batch) {
+        r = validate_batch_params(h, p);
+        if (r) return r;
+        batch_drop_graph(*h->batch);
+    }
     h->prm = p;
     derive_params(h);
     r = ensure_history(h);
@@ -620,6 +668,8 @@ int geon_get_params(GeonHandle* h, GeonParams* out) {
 
 int geon_add_particles(GeonHandle* h, int32_t n, const float* soa, double creation_time, int32_t* first_index) {
     if (!h || (!soa && n > 0) || n < 0) return GEON_ERR_ARG;
+    if (h->batch && !(h->n == 0 && n == h->n_cap))
+        return set_err(h, GEON_ERR_UNSUPPORTED, "a batched handle takes its whole batch at once (geon_upload_state)");
     if (n == 0) { if (first_index) *first_index = h->n; return GEON_OK; }
     if ((long long)h->n + n > h->n_cap) return set_err(h, GEON_ERR_FULL, "particle capacity exhausted");
     const int cap = h->n_cap;
@@ -639,6 +689,7 @@ int geon_add_particles(GeonHandle* h, int32_t n, const float* soa, double creati
 
 int geon_remove_particle(GeonHandle* h, int32_t index) {
     if (!h || index < 0 || index >= h->n) return GEON_ERR_ARG;
+    if (h->batch) return set_err(h, GEON_ERR_UNSUPPORTED, "particles of a batched handle cannot be removed");
     std::vector<int> keep(h->n, 1);
     keep[index] = 0;
     CK(cudaMemcpyAsync(h->keep, keep.data(), h->n * sizeof(int), cudaMemcpyHostToDevice, h->st));
@@ -718,16 +769,19 @@ int geon_download_ids(GeonHandle* h, int32_t* ids, int32_t capacity, int32_t* n)
     return GEON_OK;
 }
 
+static int batch_forces(GeonHandle* h, bool all);
+
 int geon_compute_forces(GeonHandle* h) {
     if (!h) return GEON_ERR_ARG;
     if (h->n == 0) return GEON_OK;
-    int r = run_force_pass(h, true);
+    int r = h->batch ? batch_forces(h, true) : run_force_pass(h, true);
     if (r) return r;
     return read_ctl(h);
 }
 
 int geon_compute_1pn(GeonHandle* h) {
     if (!h) return GEON_ERR_ARG;
+    if (h->batch) return set_err(h, GEON_ERR_UNSUPPORTED, "batched handles run without 1PN");
     if (h->n == 0) return GEON_OK;
     const bool bh = bh_on(h);
     if (bh) { int r = build_tree(h); if (r) return r; }
@@ -739,6 +793,7 @@ int geon_compute_1pn(GeonHandle* h) {
 
 int geon_direct_forces(GeonHandle* h, const int32_t* idx, int32_t k, float* fx, float* fy) {
     if (!h || k < 0 || (k > 0 && (!idx || !fx || !fy))) return GEON_ERR_ARG;
+    if (h->batch) return set_err(h, GEON_ERR_UNSUPPORTED, "the pairwise subset sum would mix the systems of a batched handle");
     if (k == 0 || h->n == 0) return GEON_OK;
     for (int i = 0; i < k; i++)
         if (idx[i] < 0 || idx[i] >= h->n) return set_err(h, GEON_ERR_ARG, "index out of range");
@@ -765,6 +820,7 @@ int geon_learn_dataset(GeonHandle* h, const int32_t* targets, int32_t k, int32_t
     if (!h || k < 0 || cap < 0 || (k > 0 && !targets) || (cap > 0 && (!feat_mass || !feat_charge || !residual || !scales)))
         return GEON_ERR_ARG;
     if (!(h->prm.toggles & GEON_BARNES_HUT)) return set_err(h, GEON_ERR_ARG, "the learned correction needs Barnes-Hut");
+    if (h->batch) return set_err(h, GEON_ERR_UNSUPPORTED, "batched handles run without the learned correction");
     if (h->P.rel || (h->prm.toggles & (GEON_MAGNETIC | GEON_GRAVITOMAG | GEON_ONE_PN)))
         return set_err(h, GEON_ERR_UNSUPPORTED, "the learned correction covers gravity, Coulomb and Yukawa without relativity");
     if (count) *count = 0;
@@ -999,8 +1055,11 @@ int geon_interaction_count(GeonHandle* h, int64_t* count) {
     return GEON_OK;
 }
 
+static int batch_update(GeonHandle* h, double dt, int32_t* substeps);
+
 int geon_update(GeonHandle* h, double dt, int32_t* substeps) {
     if (!h) return GEON_ERR_ARG;
+    if (h->batch) return batch_update(h, dt, substeps);
     if (!(dt >= 0)) return set_err(h, GEON_ERR_ARG, "dt must be >= 0");
     int r;
     const GeonParams& p = h->prm;
@@ -1283,6 +1342,7 @@ static int direct_scratch(GeonHandle* h, void** out) {
 
 extern "C" int geon_direct_forces_noalloc(GeonHandle* h, const int32_t* idx, int32_t k, float* fx, float* fy) {
     if (!h || k < 0 || (k > 0 && (!idx || !fx || !fy))) return GEON_ERR_ARG;
+    if (h->batch) return set_err(h, GEON_ERR_UNSUPPORTED, "the pairwise subset sum would mix the systems of a batched handle");
     if (k > NOALLOC_MAX_K)
         return set_err(h, GEON_ERR_ARG, "geon_direct_forces_noalloc: k = " + std::to_string(k) +
                        " exceeds GEON_DIRECT_NOALLOC_MAX_K = " + std::to_string(NOALLOC_MAX_K) +
@@ -1307,3 +1367,358 @@ extern "C" int geon_direct_forces_noalloc(GeonHandle* h, const int32_t* idx, int
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
     return cuda_check(h, e, "direct forces (no allocation)");
 }
+
+// =============================================================================================
+// Batched systems: many independent systems with one parameter set in one
+// handle.  Particles are stored system by system; tree keys carry the system
+// id above a 27-level Morton code, so one sort, one node emission and one
+// walk serve every system, and no node mixes systems.  Each system keeps its
+// own adaptive substep schedule (the planner runs on the device); the frame
+// is captured once as a CUDA graph whose substep loop is a WHILE conditional
+// node, so a frame costs one graph launch and one read of the per-system
+// substep counts.
+static int validate_batch_params(GeonHandle* h, const GeonParams& p) {
+    if (!(p.toggles & GEON_BARNES_HUT))
+        return set_err(h, GEON_ERR_UNSUPPORTED, "batched systems need Barnes-Hut (a pairwise sum would mix systems)");
+    if (p.toggles & (GEON_RELATIVITY | GEON_ONE_PN))
+        return set_err(h, GEON_ERR_UNSUPPORTED, "batched systems run without relativity and 1PN (one history ring per handle)");
+    if (p.boundary_mode == GEON_BOUND_DESPAWN)
+        return set_err(h, GEON_ERR_UNSUPPORTED, "batched systems need the loop or bounce boundary (despawning would reorder systems)");
+    if (p.flags & GEON_FLAG_LEARN)
+        return set_err(h, GEON_ERR_UNSUPPORTED, "batched systems run without the learned correction");
+    return GEON_OK;
+}
+
+static void batch_drop_graph(Batch& B) {
+    if (B.exec) { cudaGraphExecDestroy(B.exec); B.exec = nullptr; }
+    if (B.graph) { cudaGraphDestroy(B.graph); B.graph = nullptr; }
+}
+
+static ForceCtx batch_ctx(GeonHandle* h, bool all) {
+    ForceCtx C = make_ctx(h);
+    Batch& B = *h->batch;
+    C.tgt_list = B.dev.tgt_pad;
+    C.tgt_count = B.slots;
+    C.roots = B.roots;
+    C.sys_dt = all ? nullptr : B.dev.sys_dt;
+    C.sys_accel = B.dev.sys_accel;
+    C.sys_cyc = B.dev.sys_cyc;
+    return C;
+}
+
+static PushFlags batch_push_flags(const GeonParams& p) {
+    const uint32_t tg = p.toggles;
+    const bool hasMag = tg & GEON_MAGNETIC, hasGM = tg & GEON_GRAVITOMAG, hasGrav = tg & GEON_GRAVITY;
+    PushFlags F{};
+    F.has1PN = 0;
+    F.needBoris = hasMag || hasGM || p.ext_bz != 0;
+    F.needSpinOrbit = (tg & GEON_SPIN_ORBIT) && (hasMag || hasGM);
+    F.needTorques = hasGrav;
+    return F;
+}
+
+// Tree, walk order and force pass: every system (all) or those stepping now.
+static int batch_forces(GeonHandle* h, bool all) {
+    int r = build_tree(h);
+    if (r) return r;
+    batch_targets(h->S, h->T, h->ctl, h->batch->dev, h->n, h->st, h->lc);
+    CKL();
+    const int ps = prof_begin(h, PH_FORCE);
+    force_pass(h->P, h->S, h->T, h->d_root, h->ctl, batch_ctx(h, all), true, h->n_cap, h->st, h->lc);
+    prof_end(h, ps);
+    CKL();
+    return GEON_OK;
+}
+
+// One substep of the systems the planner gave a substep (integrator.js:884-1348).
+static int batch_substep(GeonHandle* h) {
+    const int ps = prof_begin(h, PH_PUSH);
+    launch_push(h->P, h->S, h->ctl, 0.f, batch_push_flags(h->prm), h->n_cap, h->st, h->lc, h->batch->dev.sys_dt);
+    prof_end(h, ps);
+    CKL();
+    return batch_forces(h, false);
+}
+
+// Captures the frame: frame start + first planning step, then WHILE(some
+// system continues) { substep; planning step }, then the boundary.
+static int batch_build_graph(GeonHandle* h) {
+    Batch& B = *h->batch;
+    batch_drop_graph(B);
+    const GeonParams& p = h->prm;
+    const bool prof = h->prof;
+    h->prof = false;                       // no event nodes inside the graph
+    const long long lc0 = h->lc.n;
+    long long lc1 = lc0, lc2 = lc0, lc3 = lc0;
+    int r = GEON_OK;
+    cudaGraph_t g = nullptr;
+    cudaGraphConditionalHandle cond = 0;
+    std::vector<cudaGraphNode_t> deps;
+    cudaGraphNode_t cnode = nullptr;
+    cudaGraph_t body = nullptr;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&cond, g, 0, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(h->st, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        batch_frame_start(h->P, h->S, B.dev, h->n, h->st, h->lc);
+        batch_plan(h->P, B.dev, p.softening, p.max_substeps, (unsigned long long)cond, h->st, h->lc);
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t* d = nullptr;
+        size_t nd = 0;
+        cudaError_t e2 = cudaStreamGetCaptureInfo(h->st, &cs, nullptr, nullptr, &d, nullptr, &nd);
+        if (e2 == cudaSuccess && d) deps.assign(d, d + nd);
+        cudaGraph_t out = nullptr;
+        e = cudaStreamEndCapture(h->st, &out);
+        if (e == cudaSuccess) e = e2;
+    }
+    lc1 = h->lc.n;
+    if (e == cudaSuccess) {
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = cond;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        e = cudaGraphAddNode(&cnode, g, deps.data(), nullptr, deps.size(), &cp);
+        if (e == cudaSuccess) body = cp.conditional.phGraph_out[0];
+    }
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(h->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        r = batch_substep(h);
+        batch_plan(h->P, B.dev, p.softening, p.max_substeps, (unsigned long long)cond, h->st, h->lc);
+        cudaGraph_t out = nullptr;
+        e = cudaStreamEndCapture(h->st, &out);
+    }
+    lc2 = h->lc.n;
+    if (e == cudaSuccess && r == GEON_OK) e = cudaStreamBeginCaptureToGraph(h->st, g, &cnode, nullptr, 1, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess && r == GEON_OK) {
+        launch_boundary(h->P, h->S, h->ctl, h->keep, h->n_cap, h->st, h->lc);
+        cudaGraph_t out = nullptr;
+        e = cudaStreamEndCapture(h->st, &out);
+    }
+    lc3 = h->lc.n;
+    h->prof = prof;
+    h->lc.n = lc0;                          // captured kernels are counted when the graph runs
+    if (e == cudaSuccess && r == GEON_OK) e = cudaGraphInstantiate(&B.exec, g, 0);
+    if (e != cudaSuccess || r != GEON_OK) {
+        cudaGetLastError();
+        if (g) cudaGraphDestroy(g);
+        B.exec = nullptr;
+        if (r) return r;
+        return set_err(h, GEON_ERR_CUDA, std::string("frame graph capture failed: ") + cudaGetErrorString(e));
+    }
+    B.graph = g;
+    B.graph_head = lc1 - lc0;
+    B.graph_body = lc2 - lc1;
+    B.graph_tail = lc3 - lc2;
+    B.graph_flags = h->P.flags;
+    return GEON_OK;
+}
+
+static int batch_update(GeonHandle* h, double dt, int32_t* substeps) {
+    if (!(dt >= 0)) return set_err(h, GEON_ERR_ARG, "dt must be >= 0");
+    Batch& B = *h->batch;
+    const GeonParams& p = h->prm;
+    if (substeps) *substeps = 0;
+    if (h->n == 0) return GEON_OK;
+    int r;
+    if (!h->forcesInit) {                                                  // integrator.js:750-782
+        bootstrap_angvel_kernel<<<grid_for(h->n, 256), 256, 0, h->st>>>(h->P, h->S, h->ctl);
+        CKL();
+        h->lc.add(1);
+        r = batch_forces(h, true);
+        if (r) return r;
+        h->forcesInit = true;
+    }
+    *B.dt_h = dt;
+    CK(cudaMemcpyAsync(B.dev.frame_dt, B.dt_h, sizeof(double), cudaMemcpyHostToDevice, h->st));
+    const bool graph = B.use_graph != 0;
+    if (graph) {
+        if (!B.exec || B.graph_flags != h->P.flags) {
+            r = batch_build_graph(h);
+            if (r) return r;
+        }
+        CK(cudaGraphLaunch(B.exec, h->st));
+    } else {
+        batch_frame_start(h->P, h->S, B.dev, h->n, h->st, h->lc);
+        CKL();
+        for (int it = 0; it <= p.max_substeps; it++) {
+            batch_plan(h->P, B.dev, p.softening, p.max_substeps, 0ull, h->st, h->lc);
+            CKL();
+            CK(cudaMemcpyAsync(B.any_h, B.dev.any_active, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+            CK(cudaStreamSynchronize(h->st));
+            if (!*B.any_h) break;
+            r = batch_substep(h);
+            if (r) return r;
+        }
+        launch_boundary(h->P, h->S, h->ctl, h->keep, h->n_cap, h->st, h->lc);
+        CKL();
+    }
+    CK(cudaMemcpyAsync(B.plan_h, B.dev.plan, (size_t)B.dev.nsys * sizeof(SysPlan), cudaMemcpyDeviceToHost, h->st));
+    r = read_ctl(h);                                                       // synchronises
+    if (r) return r;
+    int mx = 0;
+    long long psub = 0;
+    for (int s = 0; s < B.dev.nsys; s++) {
+        mx = std::max(mx, B.plan_h[s].steps);
+        psub += (long long)(B.off[s + 1] - B.off[s]) * B.plan_h[s].steps;
+    }
+    if (graph) h->lc.add((int)(B.graph_head + (long long)mx * B.graph_body + B.graph_tail));
+    if (h->prof) h->prof_acc.particle_substeps += psub;
+    B.last_max_steps = mx;
+    h->lastSubsteps = mx;
+    h->simTime += dt;
+    if (substeps) *substeps = mx;
+    return GEON_OK;
+}
+
+// State arrays a frame changes, saved to / restored from the scratch copy S2
+// (the autotuner runs frames and then puts the state back).
+static int batch_snapshot(GeonHandle* h, bool save) {
+    const size_t n = (size_t)h->n_cap;
+    const DevState& a = save ? h->S : h->S2;
+    const DevState& b = save ? h->S2 : h->S;
+    struct { void* dst; const void* src; size_t bytes; } cp[] = {
+        { b.pos, a.pos, n * sizeof(float4) }, { b.pos_lo, a.pos_lo, n * sizeof(float2) },
+        { b.vel, a.vel, n * sizeof(float4) }, { b.spin, a.spin, n * sizeof(float4) },
+        { b.mom, a.mom, n * sizeof(float2) }, { b.force, a.force, n * sizeof(float4) },
+        { b.grad, a.grad, n * sizeof(float4) }, { b.torque, a.torque, n * sizeof(float4) },
+    };
+    for (auto& c : cp) CK(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return GEON_OK;
+}
+
+extern "C" {
+
+int geon_create_batch(const GeonParams* params, int32_t n_systems, const int32_t* counts, GeonHandle** out) {
+    if (!params || !counts || !out) return set_err(nullptr, GEON_ERR_ARG, "null argument");
+    if (n_systems < 1 || n_systems > BATCH_MAX_SYSTEMS)
+        return set_err(nullptr, GEON_ERR_ARG, "n_systems must be in [1, " + std::to_string(BATCH_MAX_SYSTEMS) + "]");
+    long long total = 0;
+    for (int s = 0; s < n_systems; s++) {
+        if (counts[s] < 1) return set_err(nullptr, GEON_ERR_ARG, "every system needs at least one particle");
+        total += counts[s];
+    }
+    if (total > (long long)REF_INDEX_MASK) return set_err(nullptr, GEON_ERR_ARG, "batch too large");
+    GeonParams p = *params;
+    if (p.max_substeps <= 0) p.max_substeps = 32;
+    *out = nullptr;
+    GeonHandle* h = nullptr;
+    int r = geon_create(&p, (int32_t)total, &h);
+    if (r) return r;
+    r = validate_batch_params(h, h->prm);
+    if (r) { g_err = h->err; geon_destroy(h); return r; }
+    Batch* B = new Batch();
+    h->batch = B;
+    h->nsys = n_systems;
+    B->off.assign(n_systems + 1, 0);
+    B->pad.assign(n_systems, 0);
+    int slots = 0;
+    for (int s = 0; s < n_systems; s++) {
+        B->off[s + 1] = B->off[s] + counts[s];
+        B->pad[s] = slots;
+        slots += (counts[s] + 31) / 32 * 32;
+    }
+    B->slots = slots;
+    DevArena& A = B->A;
+    B->sys = A.alloc<int>(total);
+    B->roots = A.alloc<int>(n_systems);
+    int* d_off = A.alloc<int>(n_systems + 1);
+    int* d_pad = A.alloc<int>(n_systems);
+    BatchDev& D = B->dev;
+    D.nsys = n_systems;
+    D.plan = A.alloc<SysPlan>(n_systems);
+    D.sys_dt = A.alloc<double>(n_systems);
+    D.sys_accel = A.alloc<unsigned long long>(n_systems);
+    D.sys_cyc = A.alloc<unsigned long long>(n_systems);
+    D.sys_off = d_off;
+    D.pad_off = d_pad;
+    D.tgt_pad = A.alloc<int>(slots);
+    D.any_active = A.alloc<int>(1);
+    D.frame_dt = A.alloc<double>(1);
+    bool ok = !A.failed;
+    ok = ok && cudaMallocHost(&B->any_h, sizeof(int)) == cudaSuccess;
+    ok = ok && cudaMallocHost(&B->dt_h, sizeof(double)) == cudaSuccess;
+    ok = ok && cudaMallocHost(&B->plan_h, (size_t)n_systems * sizeof(SysPlan)) == cudaSuccess;
+    if (!ok) { g_err = "batch allocation failed"; geon_destroy(h); return GEON_ERR_NOMEM; }
+    std::vector<int> sys(total);
+    for (int s = 0; s < n_systems; s++)
+        for (int i = B->off[s]; i < B->off[s + 1]; i++) sys[i] = s;
+    cudaError_t e = cudaMemcpy(B->sys, sys.data(), total * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_off, B->off.data(), (n_systems + 1) * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_pad, B->pad.data(), n_systems * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(D.tgt_pad, 0xFF, (size_t)slots * sizeof(int));          // padding = -1
+    if (e == cudaSuccess) e = cudaMemset(D.plan, 0, (size_t)n_systems * sizeof(SysPlan));
+    if (e == cudaSuccess) e = cudaMemset(D.sys_dt, 0, (size_t)n_systems * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(B->roots, 0xFF, (size_t)n_systems * sizeof(int));
+    if (e != cudaSuccess) { g_err = std::string("batch setup: ") + cudaGetErrorString(e); geon_destroy(h); return GEON_ERR_CUDA; }
+    h->S.sys = B->sys;
+    h->S2.sys = B->sys;
+    h->T.roots = B->roots;
+    derive_params(h);
+    *out = h;
+    return GEON_OK;
+}
+
+int geon_batch_substeps(GeonHandle* h, int32_t* steps, int32_t n_systems) {
+    if (!h || !steps) return GEON_ERR_ARG;
+    if (!h->batch) return set_err(h, GEON_ERR_ARG, "not a batched handle");
+    if (n_systems < h->batch->dev.nsys) return set_err(h, GEON_ERR_ARG, "output array too small");
+    for (int s = 0; s < h->batch->dev.nsys; s++) steps[s] = h->batch->plan_h[s].steps;
+    return GEON_OK;
+}
+
+int geon_batch_set_mode(GeonHandle* h, int32_t use_graph, int32_t simple_walk) {
+    if (!h) return GEON_ERR_ARG;
+    if (!h->batch) return set_err(h, GEON_ERR_ARG, "not a batched handle");
+    h->batch->use_graph = use_graph ? 1 : 0;
+    if (simple_walk) h->prm.flags |= GEON_FLAG_SIMPLE_WALK;
+    else h->prm.flags &= ~GEON_FLAG_SIMPLE_WALK;
+    derive_params(h);
+    batch_drop_graph(*h->batch);
+    return GEON_OK;
+}
+
+int geon_batch_autotune(GeonHandle* h, double dt, int32_t frames, int32_t* choice, double* ms_per_frame) {
+    if (!h || frames < 1 || !(dt >= 0)) return GEON_ERR_ARG;
+    if (!h->batch) return set_err(h, GEON_ERR_ARG, "not a batched handle");
+    if (h->n == 0) return set_err(h, GEON_ERR_ARG, "empty batch");
+    Batch& B = *h->batch;
+    int r = batch_snapshot(h, true);
+    if (r) return r;
+    const double t0 = h->simTime;
+    const bool init0 = h->forcesInit;
+    cudaEvent_t a = get_event(h), b = get_event(h);
+    double best = 1e300;
+    int bestc = 0;
+    for (int c = 0; c < 4; c++) {
+        r = geon_batch_set_mode(h, c & 1, (c >> 1) & 1);
+        if (r) break;
+        r = batch_snapshot(h, false);
+        if (r) break;
+        h->simTime = t0;
+        h->forcesInit = init0;
+        r = batch_update(h, dt, nullptr);                 // warm-up (captures the graph)
+        if (r) break;
+        CK(cudaEventRecord(a, h->st));
+        for (int f = 0; f < frames && !r; f++) r = batch_update(h, dt, nullptr);
+        if (r) break;
+        CK(cudaEventRecord(b, h->st));
+        CK(cudaEventSynchronize(b));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        const double per = ms / frames;
+        if (ms_per_frame) ms_per_frame[c] = per;
+        if (per < best) { best = per; bestc = c; }
+    }
+    h->ev_pool.push_back(a);
+    h->ev_pool.push_back(b);
+    const int r2 = geon_batch_set_mode(h, bestc & 1, (bestc >> 1) & 1);
+    const int r3 = batch_snapshot(h, false);
+    h->simTime = t0;
+    h->forcesInit = init0;
+    if (choice) *choice = bestc;
+    (void)B;
+    return r ? r : (r2 ? r2 : r3);
+}
+
+}  // extern "C"

@@ -77,7 +77,15 @@ struct DevParams {
     // external fields (integrator.js:553-593)
     float extGx, extGy, extEx, extEy, extBz;
     float friction;
+    // batched systems: nsys > 0 when one handle holds several independent
+    // systems; tree keys are then (system << 54) | 27-level Morton code
+    int nsys;
+    int keyTop;            // key bits above the Morton code (2: invalid flag + spare; 10 batched)
+    int keyLevels;         // Morton levels in a key (31; 27 batched)
 };
+
+constexpr int BATCH_MAX_SYSTEMS = 512;   // 9 system bits above a 54-bit Morton code
+constexpr int BATCH_KEY_LEVELS = 27;
 
 // ---- frame control block in device memory --------------------------------------
 struct FrameCtl {

@@ -410,7 +410,7 @@ __device__ __forceinline__ void delayed_disp(const DevParams& P, const Tgt& t, c
 template <bool MAGGM, bool BRK>
 __device__ __forceinline__ void finalize_target(const DevParams& P, const DevState& S, const ForceCtx& C,
                                                 FrameCtl* ctl, const Tgt& t, bool valid, Acc<MAGGM, BRK>& A,
-                                                unsigned inter32) {
+                                                unsigned inter32, int sysId = -1) {
     unsigned long long inter = inter32;
     A.flush();
     double aSq = 0.0, wc = 0.0;
@@ -496,8 +496,13 @@ __device__ __forceinline__ void finalize_target(const DevParams& P, const DevSta
         inter += __shfl_xor_sync(0xffffffffu, inter, o);
     }
     if ((threadIdx.x & 31) == 0) {
-        atomic_max_pos_double(&ctl->maxAccelSqBits, aSq);
-        atomic_max_pos_double(&ctl->maxCycBits, wc);
+        if (C.sys_accel && sysId >= 0) {       // batched: the warp's targets are one system
+            atomic_max_pos_double(&C.sys_accel[sysId], aSq);
+            atomic_max_pos_double(&C.sys_cyc[sysId], wc);
+        } else {
+            atomic_max_pos_double(&ctl->maxAccelSqBits, aSq);
+            atomic_max_pos_double(&ctl->maxCycBits, wc);
+        }
         if (inter) atomicAdd(&ctl->interactions, inter);
     }
 }
@@ -510,6 +515,22 @@ __device__ __forceinline__ void load_hist_tables(const ForceCtx& C, float* s_age
     __syncthreads();
 }
 
+// Target in slot k of the walk order: T.tgt[k] (k < n) for one system.  For
+// batched handles the slots come from the per-system list padded to whole
+// warps, and systems whose substep is over sit the pass out.  Returns -1 for
+// an empty slot; sysId receives the system (batched) or -1.
+__device__ __forceinline__ int walk_target(const DevState& S, const TreeBufs& T, const FrameCtl* ctl,
+                                           const ForceCtx& C, int k, int& sysId) {
+    sysId = -1;
+    if (!C.tgt_list) return k < ctl->n ? T.tgt[k] : -1;
+    if (k >= C.tgt_count) return -1;
+    const int i = C.tgt_list[k];
+    if (i < 0) return -1;
+    sysId = S.sys[i];
+    if (C.sys_dt && !(C.sys_dt[sysId] > 0.0)) return -1;
+    return i;
+}
+
 // ---- Barnes-Hut walk (forces.js:622-694) -----------------------------------------------------
 template <bool MAGGM, bool REL, bool BRK>
 __global__ void __launch_bounds__(WALK_THREADS)
@@ -518,21 +539,23 @@ walk_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root,
     __shared__ unsigned s_mask[WALK_WARPS][WALK_STACK];
     __shared__ float s_age[REL ? HIST_LEN : 1], s_segdt[REL ? HIST_LEN : 1];
     if (REL) load_hist_tables(C, s_age, s_segdt);
-    const int n = ctl->n;
     const int warp = threadIdx.x >> 5;
     const unsigned lane = threadIdx.x & 31;
     const int k = (blockIdx.x * WALK_WARPS + warp) * 32 + (int)lane;
-    const bool valid = k < n;
+    int sysId;
+    const int ti = walk_target(S, T, ctl, C, k, sysId);
+    const bool valid = ti >= 0;
     const unsigned active = __ballot_sync(0xffffffffu, valid);
     if (active == 0) return;
+    if (C.roots) sysId = __shfl_sync(0xffffffffu, sysId, __ffs(active) - 1);
     Tgt t;
-    if (valid) { t = load_target(S, T.tgt[k]); target_coupling(P, t); }
+    if (valid) { t = load_target(S, ti); target_coupling(P, t); }
     else { t = Tgt{}; t.idx = -1; }
     Acc<MAGGM, BRK> A;
     A.init();
     unsigned inter = 0;
     const bool pe = C.pe != 0;
-    const int root = *d_root;
+    const int root = C.roots ? C.roots[sysId] : *d_root;
     const bool treeOk = (ctl->err & (ERR_NODE_OVERFLOW | ERR_BAD_INDEX)) == 0;
     const int nIntW = ctl->nInternal, nLeafW = ctl->nLeaves, nValidW = ctl->nValid;
     int top = 0;
@@ -637,7 +660,7 @@ walk_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root,
             }
         }
     }
-    finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter);
+    finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter, sysId);
 }
 
 // ---- batched Barnes-Hut walk ----------------------------------------------------------------
@@ -794,16 +817,18 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
     float* s_age = reinterpret_cast<float*>(Wall + WC_WARPS);
     float* s_segdt = s_age + HIST_LEN;
     if (REL) load_hist_tables(C, s_age, s_segdt);
-    const int n = ctl->n;
     const int warp = threadIdx.x >> 5;
     const unsigned lane = threadIdx.x & 31;
     WcSmem<NEEDC>& W = Wall[warp];
     const int k0 = (blockIdx.x * WC_WARPS + warp) * 32 + (int)lane;
-    const bool valid = k0 < n;
+    int sysId;
+    const int ti = walk_target(S, T, ctl, C, k0, sysId);
+    const bool valid = ti >= 0;
     const unsigned active = __ballot_sync(0xffffffffu, valid);
     if (active == 0) return;
+    if (C.roots) sysId = __shfl_sync(0xffffffffu, sysId, __ffs(active) - 1);
     Tgt t;
-    if (valid) { t = load_target(S, T.tgt[k0]); target_coupling(P, t); }
+    if (valid) { t = load_target(S, ti); target_coupling(P, t); }
     else { t = Tgt{}; t.idx = -1; }
     Acc<MAGGM, BRK> A;
     A.init();
@@ -817,7 +842,7 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
     const float ghy = 0.5f * (by1 - by0) * (1.f + 1e-6f) + 1e-6f * fabsf(gcy) + 1e-30f;
     const bool groupTests = !P.periodic || P.topology == GEON_TORUS;
 
-    const int root = *d_root;
+    const int root = C.roots ? C.roots[sysId] : *d_root;
     const bool treeOk = (ctl->err & (ERR_NODE_OVERFLOW | ERR_BAD_INDEX)) == 0;
     const int nIntW = ctl->nInternal, nLeafW = ctl->nLeaves, nValidW = ctl->nValid;
     int top = 0, npool = 0, nfull = 0, lcnt = 0;
@@ -963,7 +988,7 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
         __syncwarp();
     }
     flush_pool<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
-    finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter);
+    finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter, sysId);
 }
 
 template <bool MAGGM, bool REL>
@@ -1316,8 +1341,9 @@ __global__ void clear_reductions_kernel(FrameCtl* ctl) {
 template <bool MAGGM, bool REL, bool BRK>
 static void launch_force(bool bh, const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root,
                          FrameCtl* ctl, const ForceCtx& C, int n_cap, cudaStream_t st) {
+    const int slots = C.tgt_list ? C.tgt_count : n_cap;      // walk slots (batched: padded per system)
     if (bh && (P.flags & GEON_FLAG_SIMPLE_WALK)) {
-        const int blocks = std::max(1, (n_cap + WALK_THREADS - 1) / WALK_THREADS);
+        const int blocks = std::max(1, (slots + WALK_THREADS - 1) / WALK_THREADS);
         walk_kernel<MAGGM, REL, BRK><<<blocks, WALK_THREADS, 0, st>>>(P, S, T, d_root, ctl, C);
     } else if (bh) {
         constexpr size_t smem = wc_smem_bytes<MAGGM, REL>();
@@ -1326,7 +1352,7 @@ static void launch_force(bool bh, const DevParams& P, const DevState& S, const T
             cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             attr = true;
         }
-        const int blocks = std::max(1, (n_cap + WC_THREADS - 1) / WC_THREADS);
+        const int blocks = std::max(1, (slots + WC_THREADS - 1) / WC_THREADS);
         walkc_kernel<MAGGM, REL, BRK><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
     } else {
         const int blocks = std::max(1, (n_cap + DIRECT_THREADS - 1) / DIRECT_THREADS);

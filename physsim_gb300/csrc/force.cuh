@@ -16,6 +16,13 @@ struct ForceCtx {
     int pe;                   // accumulate potential energy
     int brk;                  // keep per-type vectors
     int bounce;               // boundary == BOUNCE (wall forces)
+    // batched handles (all null for one system)
+    const int* tgt_list;      // targets, each system's run padded to whole warps (-1 = padding)
+    int tgt_count;
+    const int* roots;         // root of each system
+    const double* sys_dt;     // substep of each system; systems with dt <= 0 sit this pass out
+    unsigned long long* sys_accel;   // per-system planner maxima (double bits)
+    unsigned long long* sys_cyc;
 };
 
 // Force pass: resetForces + computeAllForces (+ external fields, bounce

@@ -67,13 +67,20 @@ __global__ void clear_planner_kernel(FrameCtl* ctl) {
 }
 
 // ---- substep push -----------------------------------------------------------------------
-__global__ void push_kernel(DevParams P, DevState S, const FrameCtl* ctl, float dtSub, PushFlags F) {
+__global__ void push_kernel(DevParams P, DevState S, const FrameCtl* ctl, float dtSub0, PushFlags F,
+                            const double* __restrict__ sys_dt) {
     const int n = ctl->n;
     const bool rel = P.rel != 0;
     const bool mag = on(P, GEON_MAGNETIC), gm = on(P, GEON_GRAVITOMAG), grav = on(P, GEON_GRAVITY);
     const bool hasExtBz = P.extBz != 0.f;
-    const float halfDt = dtSub * 0.5f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float dtSub = dtSub0;
+        if (sys_dt) {                           // batched: the substep of this particle's system
+            const double d = sys_dt[S.sys[i]];
+            if (!(d > 0.0)) continue;
+            dtSub = (float)d;
+        }
+        const float halfDt = dtSub * 0.5f;
         float4 pos = S.pos[i];
         float2 plo = S.pos_lo[i];
         float4 vel = S.vel[i];                  // wx, wy, vx, vy
@@ -380,8 +387,8 @@ void launch_frame_scan(const DevParams& P, const DevState& S, FrameCtl* ctl, int
     lc.add(2);
 }
 void launch_push(const DevParams& P, const DevState& S, const FrameCtl* ctl, float dtSub, const PushFlags& F,
-                 int n_cap, cudaStream_t st, LaunchCounter& lc) {
-    push_kernel<<<grid_for(n_cap, 256), 256, 0, st>>>(P, S, ctl, dtSub, F);
+                 int n_cap, cudaStream_t st, LaunchCounter& lc, const double* sys_dt) {
+    push_kernel<<<grid_for(n_cap, 256), 256, 0, st>>>(P, S, ctl, dtSub, F, sys_dt);
     lc.add(1);
 }
 void launch_vv_kick(const DevParams& P, const DevState& S, const FrameCtl* ctl, float halfDt, int n_cap,

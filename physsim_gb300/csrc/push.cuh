@@ -13,8 +13,10 @@ struct PushFlags {
 };
 
 void launch_frame_scan(const DevParams& P, const DevState& S, FrameCtl* ctl, int n_cap, cudaStream_t st, LaunchCounter& lc);
+// sys_dt (batched handles): per-system substep; particles of systems with
+// dt <= 0 are left alone.  Null: every particle advances by dtSub.
 void launch_push(const DevParams& P, const DevState& S, const FrameCtl* ctl, float dtSub, const PushFlags& F,
-                 int n_cap, cudaStream_t st, LaunchCounter& lc);
+                 int n_cap, cudaStream_t st, LaunchCounter& lc, const double* sys_dt = nullptr);
 void launch_vv_kick(const DevParams& P, const DevState& S, const FrameCtl* ctl, float halfDt, int n_cap,
                     cudaStream_t st, LaunchCounter& lc);
 void launch_hist_tables(const double* hist_t, double simTime, float* age, float* segdt, cudaStream_t st, LaunchCounter& lc);

@@ -25,6 +25,7 @@ struct DevState {
     float4* hist;     // history ring [n_cap][256]: x, y, vx, vy
     float*  hist_angw;// [n_cap][256]
     int*    hist_cnt; // samples held per particle
+    int*    sys;      // system of each particle (batched handles; null otherwise)
 };
 
 // Quadtree over particles + ghosts.
@@ -68,6 +69,7 @@ struct TreeBufs {
     float4* int_m1; float4* int_m2; float4* int_m3;    // (Ixx, Ixy, Iyy, sum|q|), (Dx, Dy, Jxx, Jxy), (Jyy, -, -, -)
     float4* leaf_m1; float4* leaf_m2; float4* leaf_m3;
     int mom_on;         // compute the moments in this build
+    int* roots;         // [nsys] root of each system (batched handles; null otherwise)
 };
 
 constexpr int LEAF_REF = 1 << 30;

@@ -33,15 +33,22 @@
 
 namespace geon {
 
-__device__ __forceinline__ int lcp_level(uint64_t a, uint64_t b) {
+// Common-prefix length in levels of two valid keys: the Morton code sits
+// below `top` bits (the invalid flag, and in batched handles the system id);
+// keys that differ above it share no node (-1).
+__device__ __forceinline__ int lcp_level(uint64_t a, uint64_t b, int top, int levels) {
     uint64_t x = a ^ b;
-    if (x == 0) return KEY_LEVELS;
-    int lz = __clzll((long long)x);          // keys use bits [0, 62)
-    return (lz - 2) >> 1;
+    if (x == 0) return levels;
+    int lz = __clzll((long long)x);
+    if (lz < top) return -1;
+    return (lz - top) >> 1;
+}
+__device__ __forceinline__ int lcp_level(const DevParams& P, uint64_t a, uint64_t b) {
+    return lcp_level(a, b, P.keyTop, P.keyLevels);
 }
 
-__device__ __forceinline__ uint32_t key_digit(uint64_t k, int level) {   // level 1..31
-    return (uint32_t)(k >> (2 * (KEY_LEVELS - level))) & 3u;
+__device__ __forceinline__ uint32_t key_digit(uint64_t k, int level, int levels) {   // level 1..levels
+    return (uint32_t)(k >> (2 * (levels - level))) & 3u;
 }
 
 // ---------------------------------------------------------------------------
@@ -170,6 +177,10 @@ __global__ void key_kernel(DevParams P, DevState S, TreeBufs T, FrameCtl* ctl) {
                 k |= (uint64_t)((qx >> b) & 1u) << (2 * b);
                 k |= (uint64_t)((qy >> b) & 1u) << (2 * b + 1);
             }
+            if (P.nsys) {      // batched: the first 27 routing levels below the system id
+                k = ((uint64_t)S.sys[ref_index(ref)] << (2 * BATCH_KEY_LEVELS)) |
+                    (k >> (2 * (KEY_LEVELS - BATCH_KEY_LEVELS)));
+            }
             key = k;
             valid++;
         }
@@ -207,12 +218,12 @@ __global__ void gather_kernel(DevParams P, DevState S, TreeBufs T, const FrameCt
         int a = -1, c = 0, lf = 0;
         if (s < nValid) {
             const uint64_t k = K[s];
-            a = (s == 0) ? -1 : lcp_level(K[s - 1], k);
-            const int b = (s + 4 < nValid) ? lcp_level(k, K[s + 4]) : -1;
-            c = max(0, min(b, KEY_LEVELS - 1) - a);
+            a = (s == 0) ? -1 : lcp_level(P, K[s - 1], k);
+            const int b = (s + 4 < nValid) ? lcp_level(P, k, K[s + 4]) : -1;
+            c = max(0, min(b, P.keyLevels - 1) - a);
             int m = -1;
-            for (int jj = max(0, s - 4); jj <= s && jj + 4 < nValid; jj++) m = max(m, lcp_level(K[jj], K[jj + 4]));
-            const int L = min(m + 1, KEY_LEVELS);
+            for (int jj = max(0, s - 4); jj <= s && jj + 4 < nValid; jj++) m = max(m, lcp_level(P, K[jj], K[jj + 4]));
+            const int L = min(m + 1, P.keyLevels);
             lf = (a < L) ? 1 : 0;
         }
         T.lcp_a[s] = a;
@@ -221,10 +232,10 @@ __global__ void gather_kernel(DevParams P, DevState S, TreeBufs T, const FrameCt
     }
 }
 
-__device__ __forceinline__ int leaf_level_of(const uint64_t* K, int s, int nValid) {
+__device__ __forceinline__ int leaf_level_of(const DevParams& P, const uint64_t* K, int s, int nValid) {
     int m = -1;
-    for (int jj = max(0, s - 4); jj <= s && jj + 4 < nValid; jj++) m = max(m, lcp_level(K[jj], K[jj + 4]));
-    return min(m + 1, KEY_LEVELS);
+    for (int jj = max(0, s - 4); jj <= s && jj + 4 < nValid; jj++) m = max(m, lcp_level(P, K[jj], K[jj + 4]));
+    return min(m + 1, P.keyLevels);
 }
 
 __global__ void emit_kernel(DevParams P, TreeBufs T, FrameCtl* ctl) {
@@ -243,11 +254,11 @@ __global__ void emit_kernel(DevParams P, TreeBufs T, FrameCtl* ctl) {
             const int base = T.int_base[s];
             for (int k = 0; k < c; k++) T.int_meta[base + k] = make_int4(a + 1 + k, s, 0, -1);
         }
-        const int L = leaf_level_of(K, s, nValid);
+        const int L = leaf_level_of(P, K, s, nValid);
         const int lb = T.leaf_base[s];
         if (T.leaf_flag[s]) {
             int cnt = 1;
-            while (s + cnt < nValid && lcp_level(K[s], K[s + cnt]) >= L) cnt++;
+            while (s + cnt < nValid && lcp_level(P, K[s], K[s + cnt]) >= L) cnt++;
             T.leaf_meta[lb] = make_int4(s, cnt, L, -1);
             if (cnt > LEAF_CAP) bucket++;
             maxl = max(maxl, L);
@@ -261,10 +272,10 @@ __global__ void emit_kernel(DevParams P, TreeBufs T, FrameCtl* ctl) {
 }
 
 // First index in [lo, hi) whose digit at `level` is >= d (digits non-decreasing there).
-__device__ __forceinline__ int lower_digit(const uint64_t* K, int lo, int hi, int level, uint32_t d) {
+__device__ __forceinline__ int lower_digit(const uint64_t* K, int lo, int hi, int level, int levels, uint32_t d) {
     while (lo < hi) {
         int mid = (lo + hi) >> 1;
-        if (key_digit(K[mid], level) < d) lo = mid + 1; else hi = mid;
+        if (key_digit(K[mid], level, levels) < d) lo = mid + 1; else hi = mid;
     }
     return lo;
 }
@@ -285,19 +296,20 @@ __global__ void link_kernel(DevParams P, TreeBufs T, FrameCtl* ctl, int* d_root)
         const uint64_t ks = K[s];
         while (lo < hi) {
             int mid = (lo + hi) >> 1;
-            if (lcp_level(ks, K[mid]) >= d) lo = mid + 1; else hi = mid;
+            if (lcp_level(P, ks, K[mid]) >= d) lo = mid + 1; else hi = mid;
         }
         const int e = lo;
-        const int b1 = lower_digit(K, s, e, d + 1, 1u);
-        const int b2 = lower_digit(K, b1, e, d + 1, 2u);
-        const int b3 = lower_digit(K, b2, e, d + 1, 3u);
+        const int LV = P.keyLevels;
+        const int b1 = lower_digit(K, s, e, d + 1, LV, 1u);
+        const int b2 = lower_digit(K, b1, e, d + 1, LV, 2u);
+        const int b3 = lower_digit(K, b2, e, d + 1, LV, 3u);
         const int bounds[5] = { s, b1, b2, b3, e };
         int ch[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const int cs = bounds[q], ce = bounds[q + 1];
             if (ce <= cs) { ch[q] = -1; continue; }
-            if (ce - cs > LEAF_CAP && d + 1 <= KEY_LEVELS - 1) {
+            if (ce - cs > LEAF_CAP && d + 1 <= LV - 1) {
                 const int ci = T.int_base[cs] + (d + 1 - T.lcp_a[cs] - 1);
                 if (ci <= node || ci >= nInt) { atomicOr(&ctl->err, ERR_BAD_INDEX); ch[q] = -1; continue; }
                 ch[q] = ci;
@@ -312,6 +324,29 @@ __global__ void link_kernel(DevParams P, TreeBufs T, FrameCtl* ctl, int* d_root)
         T.int_child[node] = make_int4(ch[0], ch[1], ch[2], ch[3]);
         T.int_meta[node].z = e;
         T.int_count[node] = 0;
+    }
+}
+
+// Batched handles: the root of every system.  The first sorted point of a
+// system shares no prefix with its predecessor (lcp -1), so the first node
+// it starts is the system's level-0 node; a system of at most 4 points is a
+// single leaf.  Systems without points keep ROOT_NONE.
+__global__ void batch_roots_kernel(DevParams P, TreeBufs T, const FrameCtl* ctl) {
+    const int nValid = ctl->nValid;
+    const int nInt = min(ctl->nInternal, T.cap_int), nLeaves = ctl->nLeaves;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nValid; s += gridDim.x * blockDim.x) {
+        if (T.lcp_a[s] != -1) continue;
+        const int sys = (int)(T.skey[s] >> (2 * BATCH_KEY_LEVELS));
+        if (sys < 0 || sys >= P.nsys) continue;
+        int root = ROOT_NONE;
+        if (T.int_cnt[s] > 0) {
+            const int ni = T.int_base[s];
+            if (ni >= 0 && ni < nInt) root = ni;
+        } else {
+            const int li = T.leaf_base[s];
+            if (li >= 0 && li < nLeaves) root = LEAF_REF | li;
+        }
+        T.roots[sys] = root;
     }
 }
 
@@ -538,8 +573,14 @@ void tree_build(const DevParams& P, const DevState& S, TreeBufs& T, FrameCtl* ct
     exclusive_scan(T.real_flag, T.tgt_base, T.cap_pts, &ctl->nPts, nullptr, T.scan_tmp, st, &lc);
     emit_kernel<<<grid_for(T.cap_pts, TH), TH, 0, st>>>(P, T, ctl);
     link_kernel<<<grid_for(T.cap_int, TH), TH, 0, st>>>(P, T, ctl, d_root);
+    lc.add(2);
+    if (P.nsys) {
+        cudaMemsetAsync(T.roots, 0xFF, (size_t)P.nsys * sizeof(int), st);      // ROOT_NONE
+        batch_roots_kernel<<<grid_for(T.cap_pts, TH), TH, 0, st>>>(P, T, ctl);
+        lc.add(1);
+    }
     aggregate_kernel<<<grid_for(T.cap_pts, TH), TH, 0, st>>>(P, S, T, ctl);
-    lc.add(3);
+    lc.add(1);
 }
 
 // ---- leaf dump for membership tests ----------------------------------------------------
@@ -555,7 +596,7 @@ __global__ void leaf_dump_kernel(DevParams P, TreeBufs T, const FrameCtl* ctl, i
         const uint64_t k = T.skey[lm.x];
         double cx = P.rootX, cy = P.rootY, hw = P.rootW, hh = P.rootH;
         for (int lv = 1; lv <= lm.z; lv++) {                 // quadtree.js:119-131
-            const uint32_t dg = key_digit(k, lv);
+            const uint32_t dg = key_digit(k, lv, P.keyLevels);
             hw = hw / 2; hh = hh / 2;
             cx = (dg & 1u) ? cx + hw : cx - hw;
             cy = (dg & 2u) ? cy + hh : cy - hh;

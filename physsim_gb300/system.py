@@ -244,3 +244,35 @@ class GeonSystem:
         c = C.c_int64()
         self._ck(self.lib.geon_launch_count(self._h, C.byref(c)))
         return c.value
+
+
+class BatchSystem(GeonSystem):
+    """Many independent systems with one parameter set in one handle
+    (``geon_create_batch``).  State arrays are concatenated system by system;
+    ``update`` advances every system by one frame."""
+
+    def __init__(self, params: N.GeonParams, counts):
+        self.lib = N.load()
+        self._h = C.c_void_p()
+        self.counts = np.ascontiguousarray(counts, dtype=np.int32)
+        rc = self.lib.geon_create_batch(C.byref(params), int(self.counts.size), N.iptr(self.counts), C.byref(self._h))
+        if rc < 0:
+            raise N.GeonError(rc, self.lib.geon_last_error(None).decode())
+        self.capacity = int(self.counts.sum())
+        self.offsets = np.concatenate([[0], np.cumsum(self.counts)]).astype(np.int64)
+
+    def substeps(self) -> np.ndarray:
+        out = np.zeros(self.counts.size, dtype=np.int32)
+        self._ck(self.lib.geon_batch_substeps(self._h, N.iptr(out), out.size))
+        return out
+
+    def set_mode(self, use_graph: bool = True, simple_walk: bool = False):
+        self._ck(self.lib.geon_batch_set_mode(self._h, int(use_graph), int(simple_walk)))
+
+    def autotune(self, dt: float, frames: int = 2) -> tuple:
+        """Times the four modes, keeps the fastest; returns (choice, ms per frame of each)."""
+        ch = C.c_int32()
+        ms = np.zeros(4, dtype=np.float64)
+        self._ck(self.lib.geon_batch_autotune(self._h, float(dt), int(frames), C.byref(ch),
+                                              ms.ctypes.data_as(C.POINTER(C.c_double))))
+        return ch.value, ms

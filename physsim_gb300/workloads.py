@@ -104,6 +104,43 @@ def clusters_torus(n: int = 65536, seed: int = 2, barnes_hut: bool = True, relat
     return Workload("clusters_torus_n%d" % n, p, st, 1 / 60, 100, {"box": L})
 
 
+def ensemble(n_systems: int = 512, seed: int = 5, n_min: int = 256, n_max: int = 16384, box: float = 100.0,
+             sigma: float = 10.0, theta: float = 0.6, softening: float = 8.0) -> Workload:
+    """Batched ensemble: n_systems independent systems, N log-uniform in
+    [n_min, n_max] (seeded), each one Gaussian cluster (sigma 10) at a uniform
+    centre of a box x box torus; lognormal(0, 0.5) masses, quantised charges,
+    spin U[-0.5, 0.5], proper velocity N(0, 0.05^2); gravity + Coulomb,
+    Barnes-Hut theta 0.6.  The state is concatenated system by system;
+    info["counts"] holds the particles of each system."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    counts = np.exp(rng.uniform(np.log(n_min), np.log(n_max), n_systems)).astype(np.int64)
+    counts = np.clip(counts, n_min, n_max)
+    parts = {k: [] for k in ("x", "y", "wx", "wy", "m", "q", "spin")}
+    for c in counts:
+        c = int(c)
+        cx, cy = rng.random(2) * box
+        parts["x"].append(np.mod(cx + rng.normal(0, sigma, c), box))
+        parts["y"].append(np.mod(cy + rng.normal(0, sigma, c), box))
+        parts["wx"].append(rng.normal(0, 0.05, c))
+        parts["wy"].append(rng.normal(0, 0.05, c))
+        parts["m"].append(rng.lognormal(0.0, 0.5, c))
+        parts["q"].append(_charges(rng, c))
+        parts["spin"].append(rng.uniform(-0.5, 0.5, c))
+    cat = {k: np.concatenate(v) for k, v in parts.items()}
+    m32 = _f32(cat["m"])
+    st = _pack(cat["x"], cat["y"], cat["wx"], cat["wy"], cat["m"], cat["q"], spin_to_angw(cat["spin"], m32))
+    p = N.make_params(toggles=N.GRAVITY | N.COULOMB | N.BARNES_HUT, boundary_mode=N.BOUND_LOOP, topology=N.TORUS,
+                      domain_w=box, domain_h=box, theta=theta, softening=softening)
+    return Workload("ensemble_%dx[%d,%d]" % (n_systems, n_min, n_max), p, st, 1 / 60, 10,
+                    {"counts": counts.astype(np.int32), "box": box})
+
+
+def split_systems(wl: Workload) -> list:
+    """The systems of an ensemble as separate state dicts."""
+    off = np.concatenate([[0], np.cumsum(wl.info["counts"])])
+    return [{k: v[off[s]:off[s + 1]] for k, v in wl.state.items()} for s in range(len(off) - 1)]
+
+
 def plummer_disk(n: int = 1 << 20, seed: int = 3, theta: float = 0.5, softening: float = 8.0,
                  a: float = 50.0, background: float = 0.05) -> Workload:
     """Large plain BH: 2-D Plummer-like disk (surface density (1+r^2/a^2)^-2,

@@ -37,8 +37,10 @@ def rel(a, b):
 @pytest.mark.parametrize("name", CASES)
 def test_gpu_matches_golden(name, gpu_lib):
     from physsim_gb300.system import GeonSystem
+    from physsim_gb300 import _native as N
     wl, hist = cases()[name]
     ref = load(name)
+    wl.params.flags |= N.FLAG_PE            # the oracle always sums the potential energy
     g = GeonSystem(wl.params, wl.n)
     g.upload(*[wl.state[k] for k in STATE_KEYS])
     if hist is not None:
