@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--learn-batch", type=int, default=65536)
     ap.add_argument("--learn-train-n", type=int, default=262144, help="particles of the training snapshot")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other configurations (small disk, torus full force set, theta sweep)")
     ap.add_argument("--ensemble-systems", type=int, default=512)
     ap.add_argument("--ensemble-frames", type=int, default=20)
     return ap.parse_args()
@@ -414,6 +416,91 @@ def run_ensemble(args):
             "latency_note": "p50/p99 of whole-ensemble frame latency (all systems advanced one frame)"}
 
 
+def time_frames(g, dt, frames, warmup, stream):
+    """Device time of `frames` frames after `warmup` frames: (seconds,
+    substeps, per-frame latencies in ms from host clocks around each
+    synchronised frame)."""
+    import torch
+    for _ in range(warmup):
+        g.update(dt)
+    g.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    lat = []
+    sub = 0
+    e0.record(stream)
+    for _ in range(frames):
+        t = time.perf_counter()
+        sub += g.update(dt)
+        g.synchronize()
+        lat.append(1e3 * (time.perf_counter() - t))
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / 1e3, sub, np.array(lat)
+
+
+def run_configs(args, g_big, wl_big, idx, fx, fy, fp32_peak):
+    """The other measured configurations: the small disk (latency), the
+    torus with the full force set (BH and pairwise), and the theta sweep of
+    the large disk (error, throughput and FP32 roofline per theta)."""
+    import torch
+    from physsim_gb300 import _native as N, workloads as W
+    from physsim_gb300.system import GeonSystem
+    out = {}
+    # small disk: N = 2048, gravity + Coulomb + relativity, softening 0.1, 10 frames
+    wl = W.small_disk(2048)
+    g = GeonSystem(wl.params, wl.n)
+    g.upload(*[wl.state[k] for k in STATE_KEYS])
+    st = torch.cuda.ExternalStream(g.stream_ptr())
+    secs, sub, lat = time_frames(g, wl.dt, 10, 3, st)
+    out["small_disk_n2048"] = {"value": wl.n * sub / secs, "unit": UNIT, "frames": 10, "substeps": sub,
+                               "frame_ms_p50": float(np.percentile(lat, 50)),
+                               "frame_ms_p99": float(np.percentile(lat, 99)),
+                               "note": "fresh particles: no history yet, so no near-field forces under signal delay"}
+    g.close()
+    # torus, full force set with relativity and a warmed history; BH theta 0.5 and the pairwise sum
+    for bh in (True, False):
+        wl = W.clusters_torus(65536, barnes_hut=bh)
+        g = GeonSystem(wl.params, wl.n)
+        g.upload(*[wl.state[k] for k in STATE_KEYS])
+        hist = W.straight_line_history(wl.state, 64, 0.0, 64 / 60)
+        g.upload_history(*hist)
+        g.set_sim_time(0.0)
+        st = torch.cuda.ExternalStream(g.stream_ptr())
+        frames = 3 if bh else 1
+        secs, sub, lat = time_frames(g, wl.dt, frames, 1, st)
+        g.profile(True)
+        g.compute_forces()
+        pr = g.profile(False)
+        out["clusters_torus_n65536_" + ("bh" if bh else "pairwise")] = {
+            "value": wl.n * sub / secs, "unit": UNIT, "frames": frames, "substeps": sub,
+            "force_pass_ms": (pr["tree_ms"] + pr["force_ms"]) / max(pr["force_count"], 1),
+            "interactions_per_pass": g.interactions() if bh else wl.n * (wl.n - 1),
+            "forces": "gravity+coulomb+yukawa+magnetic+gravitomagnetic+1PN+spin-orbit, relativity, 64-sample history"}
+        g.close()
+    # theta sweep of the large disk
+    sweep = {}
+    p = g_big.params()
+    for th in (0.3, 0.5, 0.7, 0.9):
+        p.theta = th
+        g_big.set_params(p)
+        g_big.upload(*[np.ascontiguousarray(wl_big.state[k], dtype=np.float32) for k in STATE_KEYS])
+        e = force_error(g_big, idx, fx, fy)
+        st = torch.cuda.ExternalStream(g_big.stream_ptr())
+        g_big.profile(True)
+        secs, sub, _ = time_frames(g_big, wl_big.dt, 3, 1, st)
+        pr = g_big.profile(False)
+        walk_ms = pr["force_ms"] / max(pr["force_count"], 1)
+        inter = pr["interactions"] / max(pr["force_count"], 1)
+        tf = inter * FLOP_PER_INTERACTION_GCY / (walk_ms / 1e3) / 1e12
+        sweep[str(th)] = {"rms_rel_force_error": e, "value": wl_big.n * sub / secs, "unit": UNIT,
+                          "walk_ms": walk_ms, "tree_ms": pr["tree_ms"] / max(pr["tree_count"], 1),
+                          "interactions_per_particle": inter / wl_big.n, "walk_tflops": tf,
+                          "walk_frac_of_fp32_peak": tf / fp32_peak if fp32_peak else None}
+    out["plummer_disk_n1048576_theta_sweep"] = sweep
+    return out
+
+
 def run_native(args, ws, rank, local):
     import torch
     from physsim_gb300 import build, workloads as W
@@ -511,6 +598,9 @@ def run_native(args, ws, rank, local):
     ensemble = None
     if not args.no_ensemble and rank == 0:
         ensemble = run_ensemble(args)
+    configs = None
+    if not args.no_configs and rank == 0:
+        configs = run_configs(args, g, wl, idx, fx, fy, measured_fp32_peak(g))
 
     # ---- roofline of the dominant kernel (the Barnes-Hut walk, FP32 pipe) ----
     pk = peaks()
@@ -568,6 +658,8 @@ def run_native(args, ws, rank, local):
         line["cpu_baseline"] = cpu
     if ensemble:
         line["ensemble"] = ensemble
+    if configs:
+        line["configs"] = configs
     if learned:
         line["learned"] = learned
         line["learned_vs_plain_at_target_error"] = learned["value"] / value if learned["reached_target"] else None

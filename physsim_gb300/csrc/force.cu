@@ -242,14 +242,32 @@ __device__ __forceinline__ void exact_disp(const DevParams& P, double ox, double
 // A source position as unevaluated (hi, lo) pairs, converted to FP64 only in guard paths.
 struct SPos { float x, xlo, y, ylo; };
 
+// FP64 re-test of the Yukawa cutoff inside the FP32 guard band (rarely taken).
+__device__ __forceinline__ bool yukawa_in_exact(const DevParams& P, const SPos& sp, double tx, double ty) {
+    double dx, dy;
+    exact_disp(P, tx, ty, (double)sp.x + (double)sp.xlo, (double)sp.y + (double)sp.ylo, dx, dy);
+    return dx * dx + dy * dy < P.yukCutSqD;
+}
+
 __device__ __forceinline__ bool yukawa_in(const DevParams& P, float rx, float ry, const SPos& sp, const Tgt& t) {
     if (!P.yukOn) return false;
     const float rr = __fmaf_rn(rx, rx, ry * ry);
     const float cut = P.yukCutSq;
     if (fabsf(rr - cut) > 1e-6f * cut) return rr < cut;
-    double dx, dy;
-    exact_disp(P, t.xd(), t.yd(), (double)sp.x + (double)sp.xlo, (double)sp.y + (double)sp.ylo, dx, dy);
-    return dx * dx + dy * dy < P.yukCutSqD;
+    return yukawa_in_exact(P, sp, t.xd(), t.yd());
+}
+
+// Displacement with the topology class fixed at compile time: PER false is
+// the open box (no wrap code at all), PER true the runtime periodic case.
+template <bool PER>
+__device__ __forceinline__ void displacement_p(const DevParams& P, float ox, float oy, float sx, float sx_lo,
+                                               float sy, float sy_lo, float& rx, float& ry) {
+    if (!PER) {
+        rx = __fadd_rn(__fsub_rn(sx, ox), sx_lo);
+        ry = __fadd_rn(__fsub_rn(sy, oy), sy_lo);
+    } else {
+        displacement(P, ox, oy, sx, sx_lo, sy, sy_lo, rx, ry);
+    }
 }
 
 // ---- signal delay (signal-delay.js:16-221) ----------------------------------------------
@@ -721,7 +739,7 @@ __device__ __forceinline__ int warp_max_i(int v) {
     return v;
 }
 
-template <bool MAGGM, bool REL, bool BRK>
+template <bool MAGGM, bool REL, bool BRK, bool PER>
 __device__ __forceinline__ void eval_entry(const DevParams& P, const DevState& S, const ForceCtx& C,
                                            const float* s_age, const float* s_segdt, const WcSmem<MAGGM || REL>& W,
                                            int e, const Tgt& t, Acc<MAGGM, BRK>& A, unsigned& inter, bool pe) {
@@ -753,17 +771,17 @@ __device__ __forceinline__ void eval_entry(const DevParams& P, const DevState& S
             sL = INERTIA_K * a.z * sAng * rj2;
             dl = true;
         } else {
-            displacement(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
+            displacement_p<PER>(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
         }
     } else {
-        displacement(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
+        displacement_p<PER>(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
     }
     const bool yk = yukawa_in(P, rx, ry, sp, t);
     pair_force<MAGGM, BRK>(P, t, rx, ry, svx, svy, a.z, a.w, sAng, sMu, sL, dl, yk, pe, A);
     inter++;
 }
 
-template <bool MAGGM, bool REL, bool BRK>
+template <bool MAGGM, bool REL, bool BRK, bool PER>
 __device__ __forceinline__ void flush_pool(const DevParams& P, const DevState& S, const ForceCtx& C,
                                            const float* s_age, const float* s_segdt, WcSmem<MAGGM || REL>& W,
                                            int& nfull, int& lcnt, int& npool, const Tgt& t, Acc<MAGGM, BRK>& A,
@@ -777,8 +795,8 @@ __device__ __forceinline__ void flush_pool(const DevParams& P, const DevState& S
         const int l0 = i - nfull, l1 = i + 1 - nfull;
         const int e0 = l0 < 0 ? W.full[i] : (l0 < lcnt ? W.lst[l0][lane] : -1);
         const int e1 = (i + 1 >= total) ? -1 : (l1 < 0 ? W.full[i + 1] : (l1 < lcnt ? W.lst[l1][lane] : -1));
-        if (e0 >= 0) eval_entry<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, e0, t, A, inter, pe);
-        if (e1 >= 0) eval_entry<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, e1, t, A, inter, pe);
+        if (e0 >= 0) eval_entry<MAGGM, REL, BRK, PER>(P, S, C, s_age, s_segdt, W, e0, t, A, inter, pe);
+        if (e1 >= 0) eval_entry<MAGGM, REL, BRK, PER>(P, S, C, s_age, s_segdt, W, e1, t, A, inter, pe);
         A.tick();
     }
     __syncwarp();
@@ -787,11 +805,23 @@ __device__ __forceinline__ void flush_pool(const DevParams& P, const DevState& S
 
 template <bool NEEDC>
 __device__ __forceinline__ void stage_point(const TreeBufs& T, WcSmem<NEEDC>& W, int e, int q) {
-    const float4 pc = T.ps_c[q];
     W.a[e] = T.ps_a[q];
     W.b[e] = T.ps_b[q];
-    if (NEEDC) W.c[e] = pc;
-    W.ref[e] = __float_as_uint(pc.w);
+    if (NEEDC) {
+        const float4 pc = T.ps_c[q];
+        W.c[e] = pc;
+        W.ref[e] = __float_as_uint(pc.w);
+    } else {
+        W.ref[e] = __float_as_uint(reinterpret_cast<const float*>(T.ps_c + q)[3]);
+    }
+}
+
+// FP64 opening test (forces.js:680) inside the FP32 guard band (rarely taken).
+__device__ __forceinline__ bool accept_exact(const DevParams& P, double tx, double ty, double sx, double sy, float lvl) {
+    double dx, dy;
+    exact_disp(P, tx, ty, sx, sy, dx, dy);
+    const double size = 2.0 * ldexp(P.rootW, -(int)lvl);
+    return size * size < P.thetaSqD * (dx * dx + dy * dy);
 }
 
 // Adds entries [e0, e0+cnt) with lane mask m to the full list or the per-lane lists.
@@ -808,7 +838,7 @@ __device__ __forceinline__ void list_entries(WcSmem<NEEDC>& W, unsigned m, unsig
     }
 }
 
-template <bool MAGGM, bool REL, bool BRK>
+template <bool MAGGM, bool REL, bool BRK, bool PER>
 __global__ void __launch_bounds__(WC_THREADS, (MAGGM || REL || BRK) ? 3 : 5)
 walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
     constexpr bool NEEDC = MAGGM || REL;
@@ -880,7 +910,7 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
                     kind = 4;
                     if (groupTests) {
                         float dx, dy;
-                        if (P.periodic) {
+                        if (PER && P.periodic) {
                             dx = wrap_axis_comp(na.x, gcx, nc.x, P.W, P.W_lo, P.halfW);
                             dy = wrap_axis_comp(na.y, gcy, nc.y, P.H, P.H_lo, P.halfH);
                         } else {
@@ -888,7 +918,7 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
                             dy = __fadd_rn(__fsub_rn(na.y, gcy), nc.y);
                         }
                         const float ax = fabsf(dx), ay = fabsf(dy);
-                        const bool wrapSafe = !P.periodic || (ax + ghx < 0.999f * P.halfW && ay + ghy < 0.999f * P.halfH);
+                        const bool wrapSafe = !PER || !P.periodic || (ax + ghx < 0.999f * P.halfW && ay + ghy < 0.999f * P.halfH);
                         if (wrapSafe) {
                             const float mnx = fmaxf(ax - ghx, 0.f), mny = fmaxf(ay - ghy, 0.f);
                             const float mxx = ax + ghx, mxy = ay + ghy;
@@ -910,15 +940,11 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
             bool accept = false;
             if ((msk >> lane) & 1u) {
                 float rx, ry;
-                displacement(P, t.x, t.y, cx, clx - t.xlo, cy, cly - t.ylo, rx, ry);
+                displacement_p<PER>(P, t.x, t.y, cx, clx - t.xlo, cy, cly - t.ylo, rx, ry);
                 const float rhs = P.thetaSq * __fmaf_rn(rx, rx, ry * ry);
                 accept = s2 < rhs;
-                if (fabsf(rhs - s2) <= 1e-6f * s2) {
-                    double dx, dy;
-                    exact_disp(P, t.xd(), t.yd(), (double)cx + (double)clx, (double)cy + (double)cly, dx, dy);
-                    const double size = 2.0 * ldexp(P.rootW, -(int)lvl);
-                    accept = size * size < P.thetaSqD * (dx * dx + dy * dy);
-                }
+                if (fabsf(rhs - s2) <= 1e-6f * s2)
+                    accept = accept_exact(P, t.xd(), t.yd(), (double)cx + (double)clx, (double)cy + (double)cly, lvl);
             }
             const unsigned acc = __ballot_sync(0xffffffffu, accept);
             if ((int)lane == jj) { myAcc = acc & msk; myOpen = msk & ~acc; }
@@ -930,7 +956,7 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
         int incl = warp_incl_scan_i(myEnt);
         const int tot = __shfl_sync(0xffffffffu, incl, 31);
         if (npool + tot > WC_POOL)
-            flush_pool<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
+            flush_pool<MAGGM, REL, BRK, PER>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
         const int e0 = npool + incl - myEnt;
         if (myAcc) {                                                  // forces.js:682-685
             const float4 nb = T.int_b[node];
@@ -961,7 +987,7 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
             for (int b0 = 0; b0 < bcount; b0 += 32) {
                 const int chunk = min(32, bcount - b0);
                 if (npool + chunk > WC_POOL)
-                    flush_pool<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
+                    flush_pool<MAGGM, REL, BRK, PER>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
                 if ((int)lane < chunk) stage_point<NEEDC>(T, W, npool + lane, bstart + b0 + lane);
                 __syncwarp();
                 list_entries<NEEDC>(W, bmask, active, npool, chunk, nfull, lcnt);
@@ -987,7 +1013,7 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
         top += chTot;
         __syncwarp();
     }
-    flush_pool<MAGGM, REL, BRK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
+    flush_pool<MAGGM, REL, BRK, PER>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
     finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter, sysId);
 }
 
@@ -1349,11 +1375,13 @@ static void launch_force(bool bh, const DevParams& P, const DevState& S, const T
         constexpr size_t smem = wc_smem_bytes<MAGGM, REL>();
         static bool attr = false;
         if (!attr) {
-            cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             attr = true;
         }
         const int blocks = std::max(1, (slots + WC_THREADS - 1) / WC_THREADS);
-        walkc_kernel<MAGGM, REL, BRK><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+        if (P.periodic) walkc_kernel<MAGGM, REL, BRK, true><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+        else walkc_kernel<MAGGM, REL, BRK, false><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
     } else {
         const int blocks = std::max(1, (n_cap + DIRECT_THREADS - 1) / DIRECT_THREADS);
         direct_kernel<MAGGM, REL, BRK><<<blocks, DIRECT_THREADS, 0, st>>>(P, S, ctl, C);
