@@ -838,7 +838,10 @@ __device__ __forceinline__ void list_entries(WcSmem<NEEDC>& W, unsigned m, unsig
     }
 }
 
-template <bool MAGGM, bool REL, bool BRK, bool PER>
+// NOPE: the potential-energy sums are off at compile time (the common case
+// of a force pass that only integrates), which keeps their code out of the
+// evaluation loop.
+template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE = false>
 __global__ void __launch_bounds__(WC_THREADS, (MAGGM || REL || BRK) ? 3 : 5)
 walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
     constexpr bool NEEDC = MAGGM || REL;
@@ -863,7 +866,7 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
     Acc<MAGGM, BRK> A;
     A.init();
     unsigned inter = 0;
-    const bool pe = C.pe != 0;
+    const bool pe = NOPE ? false : (C.pe != 0);
     // bounding box of the warp's particles (padded beyond the rounding of hi + lo)
     const float bx0 = warp_min_f(valid ? t.x : 3.0e38f), bx1 = warp_max_f(valid ? t.x : -3.0e38f);
     const float by0 = warp_min_f(valid ? t.y : 3.0e38f), by1 = warp_max_f(valid ? t.y : -3.0e38f);
@@ -1374,14 +1377,23 @@ static void launch_force(bool bh, const DevParams& P, const DevState& S, const T
     } else if (bh) {
         constexpr size_t smem = wc_smem_bytes<MAGGM, REL>();
         static bool attr = false;
+        constexpr bool PLAIN = !MAGGM && !REL && !BRK;
         if (!attr) {
             cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK, false, PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK, true, PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             attr = true;
         }
         const int blocks = std::max(1, (slots + WC_THREADS - 1) / WC_THREADS);
-        if (P.periodic) walkc_kernel<MAGGM, REL, BRK, true><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
-        else walkc_kernel<MAGGM, REL, BRK, false><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+        const bool lean = PLAIN && !C.pe;
+        if (P.periodic) {
+            if (lean) walkc_kernel<MAGGM, REL, BRK, true, PLAIN><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+            else walkc_kernel<MAGGM, REL, BRK, true><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+        } else {
+            if (lean) walkc_kernel<MAGGM, REL, BRK, false, PLAIN><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+            else walkc_kernel<MAGGM, REL, BRK, false><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+        }
     } else {
         const int blocks = std::max(1, (n_cap + DIRECT_THREADS - 1) / DIRECT_THREADS);
         direct_kernel<MAGGM, REL, BRK><<<blocks, DIRECT_THREADS, 0, st>>>(P, S, ctl, C);
