@@ -972,15 +972,29 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
         for (int q = 0; q < myPts; q++) stage_point<NEEDC>(T, W, p0 + q, lm.x + q);   // forces.js:643-679
         npool += tot;
         __syncwarp();
-        // route the new entries to the full list or the per-lane lists
-        for (unsigned gm = __ballot_sync(0xffffffffu, myAcc != 0); gm; gm &= gm - 1) {
-            const int jj = __ffs(gm) - 1;
-            list_entries<NEEDC>(W, __shfl_sync(0xffffffffu, myAcc, jj), active, __shfl_sync(0xffffffffu, e0, jj), 1, nfull, lcnt);
-        }
-        for (unsigned gm = __ballot_sync(0xffffffffu, myPts > 0); gm; gm &= gm - 1) {
-            const int jj = __ffs(gm) - 1;
-            list_entries<NEEDC>(W, __shfl_sync(0xffffffffu, leafMask, jj), active, __shfl_sync(0xffffffffu, p0, jj),
-                                __shfl_sync(0xffffffffu, myPts, jj), nfull, lcnt);
+        // route the new entries: those every particle needs go to the full
+        // list, placed in parallel by a prefix sum; the others go, source by
+        // source, to the per-lane lists of the particles that need them
+        {
+            const bool accFull = myAcc != 0 && myAcc == active;
+            const bool ptsFull = myPts > 0 && leafMask == active;
+            const int myFull = (accFull ? 1 : 0) + (ptsFull ? myPts : 0);
+            const int fincl = warp_incl_scan_i(myFull);
+            int fp = nfull + fincl - myFull;
+            if (accFull) W.full[fp++] = (uint8_t)e0;
+            if (ptsFull)
+                for (int q = 0; q < myPts; q++) W.full[fp++] = (uint8_t)(p0 + q);
+            nfull += __shfl_sync(0xffffffffu, fincl, 31);
+            for (unsigned gm = __ballot_sync(0xffffffffu, myAcc != 0 && !accFull); gm; gm &= gm - 1) {
+                const int jj = __ffs(gm) - 1;
+                list_entries<NEEDC>(W, __shfl_sync(0xffffffffu, myAcc, jj), active, __shfl_sync(0xffffffffu, e0, jj), 1,
+                                    nfull, lcnt);
+            }
+            for (unsigned gm = __ballot_sync(0xffffffffu, myPts > 0 && !ptsFull); gm; gm &= gm - 1) {
+                const int jj = __ffs(gm) - 1;
+                list_entries<NEEDC>(W, __shfl_sync(0xffffffffu, leafMask, jj), active, __shfl_sync(0xffffffffu, p0, jj),
+                                    __shfl_sync(0xffffffffu, myPts, jj), nfull, lcnt);
+            }
         }
         // leaves holding more than LEAF_CAP points (level-31 buckets)
         for (unsigned bk = __ballot_sync(0xffffffffu, bucket); bk; bk &= bk - 1) {
