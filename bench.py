@@ -40,8 +40,8 @@ UNIT = "particle-substeps/s"
 # FLOPs per pair interaction (FMA = 2; rsqrt/rcp/ex2 = 1): gravity 20, Coulomb 6,
 # tidal torque 16, Yukawa 16.
 FLOP_PER_INTERACTION_GCY = 58
-# DRAM bytes of one walk launch at N = 1M, theta 0.0955 (ncu, read 571.3 MB + write 184.9 MB)
-WALK_TRAFFIC_BYTES = 756.2e6
+# DRAM bytes of one walk launch at N = 1M, theta 0.0955 (ncu, read 576.0 MB + write 186.0 MB)
+WALK_TRAFFIC_BYTES = 762.0e6
 STATE_KEYS = ("x", "y", "wx", "wy", "mass", "charge", "angw")
 
 
@@ -301,7 +301,7 @@ def run_learned(args, g, wl, idx, fx, fy, stream):
             g.compute_forces()
         pr = g.profile(False)
         ms = (pr["tree_ms"] + pr["force_ms"] + pr["learn_ms"]) / max(pr["force_count"], 1)
-        sweep[th] = {"rms_rel_force_error": e, "force_pass_ms": ms,
+        sweep[th] = {"rms_rel_force_error": e, "force_pass_ms": ms, "train_targets": tr["targets"],
                      "learn_ms": pr["learn_ms"] / max(pr["learn_count"], 1),
                      "pairs_per_particle": pr["learn_pairs"] / max(pr["learn_count"], 1) / wl.n,
                      "train_pairs": tr["pairs"], "train_s": train_s,

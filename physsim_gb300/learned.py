@@ -33,9 +33,12 @@ def train_correction(system, targets, steps: int = 20000, batch: int = 65536, lr
     """Builds the residual dataset of `targets` on `system` at its current
     theta and trains the network on the device.  Returns the weights, the
     per-step losses and the dataset size."""
+    targets = np.asarray(targets, dtype=np.int32)
     ds = system.learn_dataset(targets, cap)
-    if ds["count"] > cap:
-        raise RuntimeError(f"dataset of {ds['count']} pairs exceeds cap {cap}")
+    while ds["count"] > cap:                 # small theta: fewer targets so that the pairs fit
+        keep = max(1, int(len(targets) * cap / ds["count"] * 0.9))
+        targets = targets[np.linspace(0, len(targets) - 1, keep).astype(np.int64)]
+        ds = system.learn_dataset(targets, cap)
     w, hist = system.mlp_train(init_weights(init_seed), ds["feat_mass"], ds["residual"][:, 0:2], steps=steps,
                                batch=batch, lr=lr, seed=seed)
-    return {"weights": w, "loss": hist, "pairs": int(ds["count"])}
+    return {"weights": w, "loss": hist, "pairs": int(ds["count"]), "targets": int(len(targets))}
