@@ -297,13 +297,14 @@ def run_learned(args, g, wl, idx, fx, fy, stream):
         e = force_error(g, idx, fx, fy)
         g.synchronize()
         g.profile(True)
-        for _ in range(2):
+        passes = 2
+        for _ in range(passes):
             g.compute_forces()
         pr = g.profile(False)
-        ms = (pr["tree_ms"] + pr["force_ms"] + pr["learn_ms"]) / max(pr["force_count"], 1)
+        ms = (pr["tree_ms"] + pr["force_ms"] + pr["learn_ms"]) / passes
         sweep[th] = {"rms_rel_force_error": e, "force_pass_ms": ms, "train_targets": tr["targets"],
-                     "learn_ms": pr["learn_ms"] / max(pr["learn_count"], 1),
-                     "pairs_per_particle": pr["learn_pairs"] / max(pr["learn_count"], 1) / wl.n,
+                     "walk_ms": pr["force_ms"] / passes, "network_ms": pr["learn_ms"] / passes,
+                     "pairs_per_particle": pr["learn_pairs"] / passes / wl.n,
                      "train_pairs": tr["pairs"], "train_s": train_s,
                      "final_loss": float(np.mean(tr["loss"][-100:]))}
         key = (e > args.target_error, -th if e <= args.target_error else e)

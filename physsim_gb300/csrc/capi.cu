@@ -492,45 +492,58 @@ static int ensure_pairs(GeonHandle* h, long long need) {
     return GEON_OK;
 }
 
-// Learned far-field correction after a Barnes-Hut force pass: collect every
-// accepted (cell, target) pair of the walk (same opening rule), add the
-// network's correction to the forces, and redo the planner reductions the
-// force pass made from the uncorrected forces.
-static int learn_pass(GeonHandle* h) {
-    const int ps = prof_begin(h, PH_LEARN);
+// Barnes-Hut force pass with the learned far-field correction.  The targets
+// are processed in chunks (in walk order) whose pairs fit the pair buffer:
+// the walk of a chunk computes its forces and records every accepted
+// (cell, particle) pair, then the network adds its correction to those
+// particles.  The planner reductions are redone from the corrected forces.
+static int learned_force_pass(GeonHandle* h) {
     const int n = h->n;
     long long total = 0;
     int k0 = 0;
+    bool first = true;
     while (k0 < n) {
-        // chunk of targets (in walk order) whose pairs should fit the buffer
         long long chunk = n - k0;
         const double est = h->pairs_per_target > 0 ? h->pairs_per_target * 1.1 : 4096.0;
-        chunk = std::min<long long>(chunk, std::max<long long>(1024, (long long)(PAIR_CAP_MAX / est)));
-        unsigned long long found = 0;
+        chunk = std::min<long long>(chunk, std::max<long long>(1024, (long long)(PAIR_CAP_MAX / est) / 32 * 32));
+        unsigned long long found = 0, inter0 = 0;
+        CK(cudaMemcpyAsync(&inter0, &h->ctl->interactions, sizeof(inter0), cudaMemcpyDeviceToHost, h->st));
         for (;;) {
-            learn_collect_pairs(h->P, h->S, h->T, h->d_root, h->ctl, h->T.tgt + k0, (int)chunk, h->pairs, h->pair_cap,
-                                h->pair_cnt, h->st, h->lc);
+            CK(cudaMemsetAsync(h->pair_cnt, 0, sizeof(unsigned long long), h->st));
+            ForceCtx C = make_ctx(h);
+            C.tgt_list = h->T.tgt + k0;
+            C.tgt_count = (int)chunk;
+            C.pairs = reinterpret_cast<int2*>(h->pairs);
+            C.pair_cap = h->pair_cap;
+            C.pair_count = h->pair_cnt;
+            const int ps = prof_begin(h, PH_FORCE);
+            force_pass(h->P, h->S, h->T, h->d_root, h->ctl, C, true, h->n_cap, h->st, h->lc, first);
+            prof_end(h, ps);
             CKL();
             CK(cudaMemcpyAsync(&found, h->pair_cnt, sizeof(found), cudaMemcpyDeviceToHost, h->st));
             CK(cudaStreamSynchronize(h->st));
             h->pairs_per_target = std::max(h->pairs_per_target, (double)found / (double)chunk);
             if ((long long)found <= h->pair_cap) break;
-            if ((long long)found > PAIR_CAP_MAX) {                  // too many for one buffer: smaller chunk
-                if (chunk <= 1) return set_err(h, GEON_ERR_OVERFLOW, "learned-correction pairs of one target exceed the buffer");
-                chunk = std::max<long long>(1, chunk * PAIR_CAP_MAX / (long long)found / 2);
+            // redo the chunk with room for its pairs (its forces are simply rewritten)
+            if (!first) CK(cudaMemcpyAsync(&h->ctl->interactions, &inter0, sizeof(inter0), cudaMemcpyHostToDevice, h->st));
+            if ((long long)found > PAIR_CAP_MAX) {
+                if (chunk <= 32) return set_err(h, GEON_ERR_OVERFLOW, "learned-correction pairs of one warp exceed the buffer");
+                chunk = std::max<long long>(32, chunk * PAIR_CAP_MAX / (long long)found / 2 / 32 * 32);
                 continue;
             }
             int r = ensure_pairs(h, (long long)found);
             if (r) return r;
         }
+        const int pl = prof_begin(h, PH_LEARN);
         mlp_correct(h->P, h->S, h->T, h->learn_w, h->pairs, (int)found, &h->ctl->err, h->st, h->lc);
+        prof_end(h, pl);
         CKL();
         total += (long long)found;
         k0 += (int)chunk;
+        first = false;
     }
     launch_frame_scan(h->P, h->S, h->ctl, h->n_cap, h->st, h->lc);
     CKL();
-    prof_end(h, ps);
     if (h->prof) h->prof_acc.learn_pairs += total;
     return GEON_OK;
 }
@@ -539,11 +552,11 @@ static int run_force_pass(GeonHandle* h, bool rebuild) {
     const bool bh = bh_on(h);
     if (bh && rebuild) { int r = build_tree(h); if (r) return r; }
     if (h->P.rel) { launch_hist_tables(h->hist_t, h->simTime, h->hist_age, h->hist_segdt, h->st, h->lc); CKL(); }
+    if (bh && learn_active(h)) return learned_force_pass(h);
     const int ps = prof_begin(h, PH_FORCE);
     force_pass(h->P, h->S, h->T, h->d_root, h->ctl, make_ctx(h), bh, h->n_cap, h->st, h->lc);
     prof_end(h, ps);
     CKL();
-    if (bh && learn_active(h)) return learn_pass(h);
     return GEON_OK;
 }
 
@@ -839,10 +852,15 @@ int geon_learn_dataset(GeonHandle* h, const int32_t* targets, int32_t k, int32_t
     float* d_fc = tmp.alloc<float>((size_t)capd * LF);
     float* d_res = tmp.alloc<float>((size_t)capd * 4);
     float* d_sc = tmp.alloc<float>((size_t)capd * 2);
+    LearnPair* d_sorted = tmp.alloc<LearnPair>(capd);
+    int* d_nsorted = tmp.alloc<int>(1);
+    void* d_sort_tmp = tmp.alloc<char>(learn_sort_scratch_bytes(capd));
     if (tmp.failed) { tmp.free_all(); return set_err(h, GEON_ERR_NOMEM, "dataset allocation failed"); }
     cudaError_t e = cudaMemcpyAsync(d_t, targets, k * sizeof(int), cudaMemcpyHostToDevice, h->st);
     if (e == cudaSuccess) {
         learn_collect_pairs(h->P, h->S, h->T, h->d_root, h->ctl, d_t, k, d_pairs, cap, d_cnt, h->st, h->lc);
+        learn_sort_pairs(d_pairs, d_cnt, capd, d_sorted, d_nsorted, d_sort_tmp, h->st, h->lc);
+        d_pairs = d_sorted;
         learn_residuals(h->P, h->S, h->T, d_pairs, d_cnt, cap, d_fm, d_fc, d_res, d_sc, h->st, h->lc);
         e = cudaGetLastError();
     }
@@ -894,6 +912,7 @@ struct MlpData {
     DevArena A;
     float* w = nullptr; float* x = nullptr; float* t = nullptr; float* wt = nullptr;
     float* grad = nullptr; double* loss = nullptr;
+    float* part = nullptr; double* loss_part = nullptr;   // per-CTA gradient slots
 };
 static int mlp_upload(GeonHandle* h, MlpData& D, const float* weights, const float* x, const float* t, const float* wt,
                       int n, int nloss) {
@@ -903,6 +922,8 @@ static int mlp_upload(GeonHandle* h, MlpData& D, const float* weights, const flo
     if (wt) D.wt = D.A.alloc<float>(n);
     D.grad = D.A.alloc<float>(MLP_NPARAM);
     D.loss = D.A.alloc<double>(std::max(nloss, 1));
+    D.part = D.A.alloc<float>(mlp_grad_scratch_floats());
+    D.loss_part = D.A.alloc<double>(mlp_grad_scratch_ctas());
     if (D.A.failed) { D.A.free_all(); return set_err(h, GEON_ERR_NOMEM, "network buffer allocation failed"); }
     cudaError_t e = cudaMemcpyAsync(D.w, weights, MLP_NPARAM * sizeof(float), cudaMemcpyHostToDevice, h->st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(D.x, x, (size_t)n * LF * sizeof(float), cudaMemcpyHostToDevice, h->st);
@@ -939,7 +960,7 @@ int geon_mlp_grad(GeonHandle* h, const float* weights, const float* x, const flo
     MlpData D;
     int r = mlp_upload(h, D, weights, x, t, wt, n, 1);
     if (r) return r;
-    mlp_grad(D.w, D.x, D.t, D.wt, n, n, 0ull, 0, D.grad, D.loss, &h->ctl->err, h->st, h->lc);
+    mlp_grad(D.w, D.x, D.t, D.wt, n, n, 0ull, 0, D.grad, D.loss, D.part, D.loss_part, &h->ctl->err, h->st, h->lc);
     cudaError_t e = cudaGetLastError();
     double l = 0.0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(grad, D.grad, MLP_NPARAM * sizeof(float), cudaMemcpyDeviceToHost, h->st);
@@ -966,7 +987,8 @@ int geon_mlp_train(GeonHandle* h, float* weights, const float* x, const float* t
     const uint64_t sd = seed ? seed : 0x5DEECE66Dull;
     for (int s = 0; s < steps && e == cudaSuccess; s++) {
         const double lr_s = 0.5 * (double)lr * (1.0 + std::cos(3.141592653589793 * (double)s / (double)steps));
-        mlp_grad(D.w, D.x, D.t, D.wt, n, batch, sd, s, D.grad, D.loss + s, &h->ctl->err, h->st, h->lc);
+        mlp_grad(D.w, D.x, D.t, D.wt, n, batch, sd, s, D.grad, D.loss + s, D.part, D.loss_part, &h->ctl->err, h->st,
+                 h->lc);
         mlp_adam(D.w, D.grad, m, v, (float)lr_s, 0.9f, 0.999f, 1e-8f, s + 1, h->st, h->lc);
         e = cudaGetLastError();
     }

@@ -544,7 +544,7 @@ __device__ __forceinline__ int walk_target(const DevState& S, const TreeBufs& T,
     if (k >= C.tgt_count) return -1;
     const int i = C.tgt_list[k];
     if (i < 0) return -1;
-    sysId = S.sys[i];
+    sysId = S.sys ? S.sys[i] : -1;
     if (C.sys_dt && !(C.sys_dt[sysId] > 0.0)) return -1;
     return i;
 }
@@ -840,8 +840,9 @@ __device__ __forceinline__ void list_entries(WcSmem<NEEDC>& W, unsigned m, unsig
 
 // NOPE: the potential-energy sums are off at compile time (the common case
 // of a force pass that only integrates), which keeps their code out of the
-// evaluation loop.
-template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE = false>
+// evaluation loop.  EMIT: record the accepted (cell, particle) pairs for the
+// learned correction.
+template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE = false, bool EMIT = false>
 __global__ void __launch_bounds__(WC_THREADS, (MAGGM || REL || BRK) ? 3 : 5)
 walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
     constexpr bool NEEDC = MAGGM || REL;
@@ -951,6 +952,28 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
             }
             const unsigned acc = __ballot_sync(0xffffffffu, accept);
             if ((int)lane == jj) { myAcc = acc & msk; myOpen = msk & ~acc; }
+        }
+        if (EMIT) {                                                   // learned correction: (cell, particle) pairs
+            const int myCnt = __popc(myAcc);
+            const int pincl = warp_incl_scan_i(myCnt);
+            const int ptot = __shfl_sync(0xffffffffu, pincl, 31);
+            if (ptot) {
+                unsigned long long base = 0;
+                if (lane == 31) base = atomicAdd(C.pair_count, (unsigned long long)ptot);
+                base = __shfl_sync(0xffffffffu, base, 31);
+                // one accepted cell at a time, each accepting particle writes its
+                // own pair: the pairs of a cell are one contiguous write
+                for (unsigned om = __ballot_sync(0xffffffffu, myAcc != 0); om; om &= om - 1) {
+                    const int jj = __ffs(om) - 1;
+                    const unsigned m = __shfl_sync(0xffffffffu, myAcc, jj);
+                    const int nd = __shfl_sync(0xffffffffu, node, jj);
+                    const int off = __shfl_sync(0xffffffffu, pincl - myCnt, jj);
+                    if ((m >> lane) & 1u) {
+                        const unsigned long long pos = base + (unsigned long long)(off + __popc(m & lanemask_lt()));
+                        if (pos < (unsigned long long)C.pair_cap) C.pairs[pos] = make_int2(nd, ti);
+                    }
+                }
+            }
         }
         const unsigned leafMask = kind == 1 ? mask : 0u;
         const bool bucket = leafMask && lm.y > LEAF_CAP;
@@ -1401,7 +1424,23 @@ static void launch_force(bool bh, const DevParams& P, const DevState& S, const T
         }
         const int blocks = std::max(1, (slots + WC_THREADS - 1) / WC_THREADS);
         const bool lean = PLAIN && !C.pe;
-        if (P.periodic) {
+        if (PLAIN && C.pair_count) {               // learned correction (plain forces only)
+            static bool eattr = false;
+            if (!eattr) {
+                cudaFuncSetAttribute(walkc_kernel<false, false, false, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                cudaFuncSetAttribute(walkc_kernel<false, false, false, true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                cudaFuncSetAttribute(walkc_kernel<false, false, false, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                cudaFuncSetAttribute(walkc_kernel<false, false, false, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                eattr = true;
+            }
+            if (P.periodic) {
+                if (lean) walkc_kernel<false, false, false, true, true, true><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+                else walkc_kernel<false, false, false, true, false, true><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+            } else {
+                if (lean) walkc_kernel<false, false, false, false, true, true><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+                else walkc_kernel<false, false, false, false, false, true><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+            }
+        } else if (P.periodic) {
             if (lean) walkc_kernel<MAGGM, REL, BRK, true, PLAIN><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
             else walkc_kernel<MAGGM, REL, BRK, true><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
         } else {
@@ -1415,8 +1454,8 @@ static void launch_force(bool bh, const DevParams& P, const DevState& S, const T
 }
 
 void force_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
-                const ForceCtx& C, bool bh, int n_cap, cudaStream_t st, LaunchCounter& lc) {
-    clear_reductions_kernel<<<1, 1, 0, st>>>(ctl);
+                const ForceCtx& C, bool bh, int n_cap, cudaStream_t st, LaunchCounter& lc, bool clear) {
+    if (clear) clear_reductions_kernel<<<1, 1, 0, st>>>(ctl);
     const bool maggm = (P.toggles & (GEON_MAGNETIC | GEON_GRAVITOMAG | GEON_ONE_PN)) != 0;
     const bool rel = P.rel != 0;
     const bool brk = C.brk != 0;
@@ -1427,7 +1466,7 @@ void force_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const 
         if (rel) { if (brk) launch_force<false, true, true>(bh, P, S, T, d_root, ctl, C, n_cap, st); else launch_force<false, true, false>(bh, P, S, T, d_root, ctl, C, n_cap, st); }
         else     { if (brk) launch_force<false, false, true>(bh, P, S, T, d_root, ctl, C, n_cap, st); else launch_force<false, false, false>(bh, P, S, T, d_root, ctl, C, n_cap, st); }
     }
-    lc.add(2);
+    lc.add(clear ? 2 : 1);
 }
 
 void onepn_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,

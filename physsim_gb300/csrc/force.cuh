@@ -23,14 +23,21 @@ struct ForceCtx {
     const double* sys_dt;     // substep of each system; systems with dt <= 0 sit this pass out
     unsigned long long* sys_accel;   // per-system planner maxima (double bits)
     unsigned long long* sys_cyc;
+    // learned correction: the walk records every accepted (cell, target)
+    // pair as (node, particle); pairs at positions >= pair_cap are counted only
+    int2* pairs;
+    long long pair_cap;
+    unsigned long long* pair_count;
 };
 
 // Force pass: resetForces + computeAllForces (+ external fields, bounce
 // walls) for every particle, with the max-acceleration / cyclotron
 // reductions for the substep planner.  `bh` selects the tree walk (tree must
 // be built) or the pairwise sum.
+// clear = false keeps the planner reductions and the interaction counter of
+// earlier passes (a force pass split over target chunks).
 void force_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
-                const ForceCtx& C, bool bh, int n_cap, cudaStream_t st, LaunchCounter& lc);
+                const ForceCtx& C, bool bh, int n_cap, cudaStream_t st, LaunchCounter& lc, bool clear = true);
 
 // Pairwise forces (fx, fy) on the listed particles from all particles, into
 // separate outputs (device arrays of k floats); the state is not changed.

@@ -153,6 +153,46 @@ __global__ void residual_kernel(DevParams P, DevState S, TreeBufs T, const Learn
     }
 }
 
+// Deterministic order of the collected pairs: (target, node) keys sorted
+// with the stable radix sort, then the records permuted.
+__global__ void pair_keys_kernel(const LearnPair* __restrict__ pairs, const unsigned long long* d_count, int cap,
+                                 int* d_n, uint64_t* keys, uint32_t* vals) {
+    const int n = (int)min(*d_count, (unsigned long long)cap);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *d_n = n;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const LearnPair p = pairs[e];
+        keys[e] = ((uint64_t)(uint32_t)p.target << 32) | (uint64_t)(uint32_t)p.node;
+        vals[e] = (uint32_t)e;
+    }
+}
+__global__ void pair_permute_kernel(const LearnPair* __restrict__ in, const uint32_t* __restrict__ order,
+                                    const int* d_n, LearnPair* __restrict__ out) {
+    const int n = *d_n;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) out[e] = in[order[e]];
+}
+
+size_t learn_sort_scratch_bytes(int cap) {
+    const size_t c = (size_t)std::max(cap, 1);
+    return c * (2 * sizeof(uint64_t) + 2 * sizeof(uint32_t)) + radix_temp_bytes(std::max(cap, 1)) + 256;
+}
+
+void learn_sort_pairs(const LearnPair* pairs, const unsigned long long* d_count, int cap, LearnPair* out, int* d_n,
+                      void* scratch, cudaStream_t st, LaunchCounter& lc) {
+    const size_t c = (size_t)std::max(cap, 1);
+    char* p = static_cast<char*>(scratch);
+    uint64_t* keys = reinterpret_cast<uint64_t*>(p); p += c * sizeof(uint64_t);
+    uint64_t* keys_alt = reinterpret_cast<uint64_t*>(p); p += c * sizeof(uint64_t);
+    uint32_t* vals = reinterpret_cast<uint32_t*>(p); p += c * sizeof(uint32_t);
+    uint32_t* vals_alt = reinterpret_cast<uint32_t*>(p); p += c * sizeof(uint32_t);
+    p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(p) + 255) & ~(uintptr_t)255);
+    const int blocks = 152 * 8;
+    pair_keys_kernel<<<blocks, 256, 0, st>>>(pairs, d_count, cap, d_n, keys, vals);
+    lc.add(1);
+    const int which = radix_sort_pairs(keys, vals, keys_alt, vals_alt, (int)c, d_n, 64, p, st, &lc);
+    pair_permute_kernel<<<blocks, 256, 0, st>>>(pairs, which ? vals_alt : vals, d_n, out);
+    lc.add(1);
+}
+
 void learn_collect_pairs(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
                          const int* d_targets, int k, LearnPair* pairs, long long cap, unsigned long long* d_count,
                          cudaStream_t st, LaunchCounter& lc) {

@@ -63,6 +63,12 @@ struct LearnPair { int node; int target; };
 void learn_collect_pairs(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
                          const int* d_targets, int k, LearnPair* pairs, long long cap, unsigned long long* d_count,
                          cudaStream_t st, LaunchCounter& lc);
+// Writes the first min(*d_count, cap) pairs to `out` in (target, node)
+// order (so that datasets do not depend on the collection's timing); *d_n
+// receives their number.  `scratch` holds learn_sort_scratch_bytes(cap).
+size_t learn_sort_scratch_bytes(int cap);
+void learn_sort_pairs(const LearnPair* pairs, const unsigned long long* d_count, int cap, LearnPair* out, int* d_n,
+                      void* scratch, cudaStream_t st, LaunchCounter& lc);
 void learn_residuals(const DevParams& P, const DevState& S, const TreeBufs& T, const LearnPair* pairs,
                      const unsigned long long* d_count,
                      int cap, float* feat_m, float* feat_c, float* target, float* scales, cudaStream_t st,

@@ -24,6 +24,7 @@
 #include "tc.cuh"
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <algorithm>
 #include <cmath>
 
@@ -59,6 +60,22 @@ __device__ __forceinline__ float gelu(float x) {
     const float u = GELU_C * fmaf(GELU_A * x, x * x, x);
     return 0.5f * x * (1.f + tanh_approx(u));
 }
+// Two GELUs in packed FP16 arithmetic (inference): 0.5 x (1 + tanh(x (c + c a x^2))),
+// returning the FP16 pair that the next layer reads.  The packed math halves
+// the CUDA-core instructions of the epilogue, which bound the inference
+// kernel; FP16 keeps 11 significant bits, more than the BF16 of training.
+__device__ __forceinline__ uint32_t gelu2_f16(float x0, float x1) {
+    const __half2 x = __floats2half2_rn(x0, x1);
+    const __half2 x2 = __hmul2(x, x);
+    const __half2 p = __hfma2(x2, __float2half2_rn(GELU_C * GELU_A), __float2half2_rn(GELU_C));
+    const __half2 u = __hmul2(p, x);
+    uint32_t ui = *reinterpret_cast<const uint32_t*>(&u), ti;
+    asm("tanh.approx.f16x2 %0, %1;" : "=r"(ti) : "r"(ui));
+    const __half2 t = *reinterpret_cast<const __half2*>(&ti);
+    const __half2 hx = __hmul2(x, __float2half2_rn(0.5f));
+    const __half2 g = __hfma2(t, hx, hx);
+    return *reinterpret_cast<const uint32_t*>(&g);
+}
 __device__ __forceinline__ float gelu_grad(float x) {
     const float x2 = x * x;
     const float t = tanh_approx(GELU_C * fmaf(GELU_A * x, x2, x));
@@ -78,6 +95,22 @@ struct NetSmem {
     uint64_t bar;
     uint32_t tmem;
 };
+// Inference CTA: the second hidden layer reuses the first layer's activation
+// buffer and accumulator columns (GEMM 2 has consumed layer 1 before the
+// epilogue overwrites it), so a CTA needs 33 KB of shared memory and 64 TMEM
+// columns and six CTAs share an SM.
+struct InfSmem {
+    __align__(128) uint8_t w1[LH * K1 * 2];
+    __align__(128) uint8_t w2[LH * LH * 2];
+    __align__(128) uint8_t w3[N3 * LH * 2];
+    __align__(128) uint8_t x[MT * K1 * 2];
+    __align__(128) uint8_t h[MT * LH * 2];      // A of Z2, then A of Y
+    float b1[LH], b2[LH], b3[LO];
+    uint64_t bar;
+    uint32_t tmem;
+};
+constexpr uint32_t INF_COLS = 64;
+
 // Training adds the backward operands.
 struct TrainSmem {
     NetSmem f;
@@ -106,7 +139,8 @@ __device__ __forceinline__ void put8(uint8_t* buf, int r, int k0, int K, const f
 }
 
 // Stages the FP32 weights as BF16 operands (zero padded) and FP32 biases.
-__device__ void stage_forward(NetSmem& s, const float* __restrict__ W) {
+template <class SM>
+__device__ void stage_forward(SM& s, const float* __restrict__ W) {
     for (int i = threadIdx.x; i < LH * K1; i += blockDim.x) {
         const int r = i / K1, k = i % K1;
         put_bf16(s.w1, r, k, K1, k < LF ? W[OFF_W1 + r * LF + k] : 0.f);
@@ -138,7 +172,8 @@ __device__ void stage_backward(TrainSmem& s, const float* __restrict__ W) {
     for (int i = threadIdx.x; i < (N3 - LO) * MT; i += blockDim.x) put_bf16(s.bgb, LO + i / MT, i % MT, MT, 0.f);
 }
 
-__device__ __forceinline__ void net_setup(NetSmem& s, uint32_t ncols) {
+template <class SM>
+__device__ __forceinline__ void net_setup(SM& s, uint32_t ncols) {
     if (threadIdx.x == 0) {
         mbar_init(&s.bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -153,8 +188,8 @@ __device__ __forceinline__ void net_setup(NetSmem& s, uint32_t ncols) {
 // thread 0 issue `issue()` and commit it, and waits for completion.  Returns
 // false (uniformly across the CTA) if `ok` was false or the wait timed out;
 // `phase` advances only on success so that a timed-out phase can be drained.
-template <class F>
-__device__ __forceinline__ bool mma_step(NetSmem& s, uint32_t& phase, bool ok, F&& issue) {
+template <class SM, class F>
+__device__ __forceinline__ bool mma_step(SM& s, uint32_t& phase, bool ok, F&& issue) {
     fence_proxy_async();
     fence_before_sync();
     __syncthreads();
@@ -171,7 +206,8 @@ __device__ __forceinline__ bool mma_step(NetSmem& s, uint32_t& phase, bool ok, F
     return all;
 }
 
-__device__ __forceinline__ void net_teardown(NetSmem& s, bool ok, uint32_t phase, int* err, uint32_t ncols) {
+template <class SM>
+__device__ __forceinline__ void net_teardown(SM& s, bool ok, uint32_t phase, int* err, uint32_t ncols) {
     if (!ok) {
         if (threadIdx.x == 0) atomicOr(err, ERR_MMA_TIMEOUT);
         mbar_wait(&s.bar, phase);          // drain the MMA still in flight before the columns are released
@@ -204,20 +240,67 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t tmem, uint32_t col, con
     }
 }
 
-__device__ __forceinline__ void stage_x(NetSmem& s, const float* f) {
+template <class SM>
+__device__ __forceinline__ void stage_x(SM& s, const float* f) {
     put8(s.x, threadIdx.x, 0, K1, f);
     put8(s.x, threadIdx.x, 8, K1, f + 8);
 }
 
-// Forward pass of the tile staged in s.x (128 TMEM columns); y0, y1 are this
-// thread's outputs.
-__device__ __forceinline__ bool tile_forward(NetSmem& s, uint32_t& phase, bool ok, float& y0, float& y1) {
+// ---- inference in FP16 operands ----------------------------------------------------
+__device__ __forceinline__ void put_f16(uint8_t* buf, int r, int k, int K, float v) {
+    *reinterpret_cast<__half*>(buf + kmajor_offset(r, k, K)) = __float2half_rn(v);
+}
+__device__ __forceinline__ void put8_f16(uint8_t* buf, int r, int k0, int K, const float* v) {
+    uint4 u;
+    __half2 p;
+    p = __floats2half2_rn(v[0], v[1]); u.x = *reinterpret_cast<uint32_t*>(&p);
+    p = __floats2half2_rn(v[2], v[3]); u.y = *reinterpret_cast<uint32_t*>(&p);
+    p = __floats2half2_rn(v[4], v[5]); u.z = *reinterpret_cast<uint32_t*>(&p);
+    p = __floats2half2_rn(v[6], v[7]); u.w = *reinterpret_cast<uint32_t*>(&p);
+    *reinterpret_cast<uint4*>(buf + kmajor_offset(r, k0, K)) = u;
+}
+__device__ void stage_forward_f16(InfSmem& s, const float* __restrict__ W) {
+    for (int i = threadIdx.x; i < LH * K1; i += blockDim.x) {
+        const int r = i / K1, k = i % K1;
+        put_f16(s.w1, r, k, K1, k < LF ? W[OFF_W1 + r * LF + k] : 0.f);
+    }
+    for (int i = threadIdx.x; i < LH * LH; i += blockDim.x) put_f16(s.w2, i / LH, i % LH, LH, W[OFF_W2 + i]);
+    for (int i = threadIdx.x; i < N3 * LH; i += blockDim.x) {
+        const int r = i / LH, k = i % LH;
+        put_f16(s.w3, r, k, LH, r < LO ? W[OFF_W3 + r * LH + k] : 0.f);
+    }
+    for (int i = threadIdx.x; i < LH; i += blockDim.x) { s.b1[i] = W[OFF_B1 + i]; s.b2[i] = W[OFF_B2 + i]; }
+    if (threadIdx.x < LO) s.b3[threadIdx.x] = W[OFF_B3 + threadIdx.x];
+}
+__device__ __forceinline__ void stage_x_f16(InfSmem& s, const float* f) {
+    put8_f16(s.x, threadIdx.x, 0, K1, f);
+    put8_f16(s.x, threadIdx.x, 8, K1, f + 8);
+}
+// GELU epilogue of a 64-column accumulator into the next layer's FP16 operand.
+__device__ __forceinline__ void hidden_epilogue_f16(uint32_t tmem, const float* bias, uint8_t* out) {
     const int warp = threadIdx.x >> 5;
-    ok = mma_step(s, phase, ok, [&] { gemm(s.tmem + 0, s.x, s.w1, LH, K1, false); });
-    hidden_epilogue<false>(s.tmem, 0, s.b1, s.h1, nullptr, 0);
-    ok = mma_step(s, phase, ok, [&] { gemm(s.tmem + 64, s.h1, s.w2, LH, LH, false); });
-    hidden_epilogue<false>(s.tmem, 64, s.b2, s.h2, nullptr, 0);
-    ok = mma_step(s, phase, ok, [&] { gemm(s.tmem + 0, s.h2, s.w3, N3, LH, false); });
+    const int row = threadIdx.x;
+#pragma unroll
+    for (int c0 = 0; c0 < LH; c0 += 16) {
+        float v[16];
+        tmem_ld16(tmem_addr(tmem, warp, c0), v);
+        uint32_t g[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) g[i] = gelu2_f16(v[2 * i] + bias[c0 + 2 * i], v[2 * i + 1] + bias[c0 + 2 * i + 1]);
+        *reinterpret_cast<uint4*>(out + kmajor_offset(row, c0, LH)) = make_uint4(g[0], g[1], g[2], g[3]);
+        *reinterpret_cast<uint4*>(out + kmajor_offset(row, c0 + 8, LH)) = make_uint4(g[4], g[5], g[6], g[7]);
+    }
+}
+
+// Forward pass of the tile staged in s.x (FP16 operands; 64 TMEM columns,
+// reused by every layer); y0, y1 are this thread's outputs.
+__device__ __forceinline__ bool tile_forward(InfSmem& s, uint32_t& phase, bool ok, float& y0, float& y1) {
+    const int warp = threadIdx.x >> 5;
+    ok = mma_step(s, phase, ok, [&] { gemm(s.tmem + 0, s.x, s.w1, LH, K1, false, true); });
+    hidden_epilogue_f16(s.tmem, s.b1, s.h);
+    ok = mma_step(s, phase, ok, [&] { gemm(s.tmem + 0, s.h, s.w2, LH, LH, false, true); });
+    hidden_epilogue_f16(s.tmem, s.b2, s.h);
+    ok = mma_step(s, phase, ok, [&] { gemm(s.tmem + 0, s.h, s.w3, N3, LH, false, true); });
     float v[16];
     tmem_ld16(tmem_addr(s.tmem, warp, 0), v);
     y0 = v[0] + s.b3[0];
@@ -228,9 +311,9 @@ __device__ __forceinline__ bool tile_forward(NetSmem& s, uint32_t& phase, bool o
 __global__ void __launch_bounds__(MT)
 mlp_forward_kernel(const float* __restrict__ W, const float* __restrict__ X, int n, float* __restrict__ Y, int* err) {
     extern __shared__ __align__(1024) uint8_t fwd_smem_raw[];
-    NetSmem& s = *reinterpret_cast<NetSmem*>(fwd_smem_raw);
-    stage_forward(s, W);
-    net_setup(s, 128);
+    InfSmem& s = *reinterpret_cast<InfSmem*>(fwd_smem_raw);
+    stage_forward_f16(s, W);
+    net_setup(s, INF_COLS);
     uint32_t phase = 0;
     bool ok = true;
     const int ntiles = (n + MT - 1) / MT;
@@ -240,21 +323,21 @@ mlp_forward_kernel(const float* __restrict__ W, const float* __restrict__ X, int
 #pragma unroll
         for (int k = 0; k < 16; k++) f[k] = (i < n && k < LF) ? X[(size_t)i * LF + k] : 0.f;
         f[LF] = 1.f;
-        stage_x(s, f);
+        stage_x_f16(s, f);
         float y0, y1;
         ok = tile_forward(s, phase, ok, y0, y1);
         if (ok && i < n) { Y[(size_t)i * 2] = y0; Y[(size_t)i * 2 + 1] = y1; }
     }
-    net_teardown(s, ok, phase, err, 128);
+    net_teardown(s, ok, phase, err, INF_COLS);
 }
 
 __global__ void __launch_bounds__(MT)
 mlp_correct_kernel(DevParams P, DevState S, TreeBufs T, const float* __restrict__ W, const LearnPair* __restrict__ pairs,
                    int np, int* err) {
     extern __shared__ __align__(1024) uint8_t cor_smem_raw[];
-    NetSmem& s = *reinterpret_cast<NetSmem*>(cor_smem_raw);
-    stage_forward(s, W);
-    net_setup(s, 128);
+    InfSmem& s = *reinterpret_cast<InfSmem*>(cor_smem_raw);
+    stage_forward_f16(s, W);
+    net_setup(s, INF_COLS);
     uint32_t phase = 0;
     bool ok = true;
     const int ntiles = (np + MT - 1) / MT;
@@ -279,7 +362,7 @@ mlp_correct_kernel(DevParams P, DevState S, TreeBufs T, const float* __restrict_
             scale *= p.z;                                     // target mass
         }
         f[LF] = 1.f;
-        stage_x(s, f);
+        stage_x_f16(s, f);
         float y0, y1;
         ok = tile_forward(s, phase, ok, y0, y1);
         if (ok && target >= 0) {
@@ -288,7 +371,7 @@ mlp_correct_kernel(DevParams P, DevState S, TreeBufs T, const float* __restrict_
             atomicAdd(fp + 1, scale * y1);
         }
     }
-    net_teardown(s, ok, phase, err, 128);
+    net_teardown(s, ok, phase, err, INF_COLS);
 }
 
 // SplitMix64 finaliser (Steele, Lea, Flood 2014) of a (seed, step, j) counter,
@@ -304,7 +387,10 @@ __device__ __forceinline__ int draw_sample(uint64_t seed, int step, int j, int n
 __global__ void __launch_bounds__(MT, 1)
 mlp_train_kernel(const float* __restrict__ W, const float* __restrict__ X, const float* __restrict__ Tg,
                  const float* __restrict__ wt, int n_data, int batch, uint64_t seed, int step,
-                 float* __restrict__ grad, double* loss, int* err) {
+                 float* __restrict__ part_all, double* __restrict__ loss_part, int* err) {
+    // this CTA's gradient slot: every element is written exactly once (summed
+    // over the CTAs in a fixed order afterwards, so training is reproducible)
+    float* __restrict__ grad = part_all + (size_t)blockIdx.x * MLP_NPARAM;
     extern __shared__ __align__(1024) uint8_t tr_smem_raw[];
     TrainSmem& s = *reinterpret_cast<TrainSmem*>(tr_smem_raw);
     NetSmem& f = s.f;
@@ -396,9 +482,11 @@ mlp_train_kernel(const float* __restrict__ W, const float* __restrict__ X, const
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
     if ((row & 31) == 0) f.red[warp] = lsum;
     __syncthreads();
-    if (row == 0 && ok) atomicAdd(loss, (double)(f.red[0] + f.red[1] + f.red[2] + f.red[3]) * (double)invB);
+    if (row == 0) loss_part[blockIdx.x] = ok ? (double)(f.red[0] + f.red[1] + f.red[2] + f.red[3]) * (double)invB : 0.0;
     // gradients: TMEM lane r holds row r of GA and of GB
-    if (ok && !first) {
+    if (!ok || first) {
+        for (int i = row; i < MLP_NPARAM; i += MT) grad[i] = 0.f;
+    } else {
         const bool top = row < LH;
         const int o = top ? row : row - LH;
 #pragma unroll
@@ -407,33 +495,49 @@ mlp_train_kernel(const float* __restrict__ W, const float* __restrict__ X, const
             tmem_ld16(tmem_addr(f.tmem, warp, TC_GA + c0), v);
             if (top) {
 #pragma unroll
-                for (int i = 0; i < 16; i++) atomicAdd(&grad[OFF_W2 + o * LH + c0 + i], v[i]);
+                for (int i = 0; i < 16; i++) grad[OFF_W2 + o * LH + c0 + i] = v[i];
             }
         }
         {
             float v[16];
             tmem_ld16(tmem_addr(f.tmem, warp, TC_GA + LH), v);
             if (top) {
-                atomicAdd(&grad[OFF_B2 + o], v[LF]);
+                grad[OFF_B2 + o] = v[LF];
             } else {
 #pragma unroll
-                for (int k = 0; k < LF; k++) atomicAdd(&grad[OFF_W1 + o * LF + k], v[k]);
-                atomicAdd(&grad[OFF_B1 + o], v[LF]);
+                for (int k = 0; k < LF; k++) grad[OFF_W1 + o * LF + k] = v[k];
+                grad[OFF_B1 + o] = v[LF];
             }
         }
         {
             float v[16];
             tmem_ld16(tmem_addr(f.tmem, warp, TC_GB), v);
             if (top) {
-                atomicAdd(&grad[OFF_W3 + row], v[0]);
-                atomicAdd(&grad[OFF_W3 + LH + row], v[1]);
+                grad[OFF_W3 + row] = v[0];
+                grad[OFF_W3 + LH + row] = v[1];
             } else if (row == LH) {
-                atomicAdd(&grad[OFF_B3], v[0]);
-                atomicAdd(&grad[OFF_B3 + 1], v[1]);
+                grad[OFF_B3] = v[0];
+                grad[OFF_B3 + 1] = v[1];
             }
         }
     }
     net_teardown(f, ok, phase, err, 512);
+}
+
+// grad += sum over the CTAs of their slots, loss += sum of their losses, in CTA order.
+__global__ void mlp_reduce_kernel(const float* __restrict__ part, const double* __restrict__ loss_part, int nb,
+                                  float* __restrict__ grad, double* loss) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < MLP_NPARAM) {
+        float acc = 0.f;
+        for (int b = 0; b < nb; b++) acc += part[(size_t)b * MLP_NPARAM + i];
+        grad[i] += acc;
+    }
+    if (i == 0) {
+        double l = 0.0;
+        for (int b = 0; b < nb; b++) l += loss_part[b];
+        *loss += l;
+    }
 }
 
 __global__ void mlp_adam_kernel(float* W, float* g, float* m, float* v, float lr, float b1, float b2, float eps,
@@ -469,20 +573,20 @@ static void allow_smem(K kernel, size_t bytes, bool& done) {
     }
 }
 
-constexpr size_t NET_SMEM = sizeof(NetSmem) + 1024;
+constexpr size_t NET_SMEM = sizeof(InfSmem) + 1024;
 constexpr size_t TRAIN_SMEM = sizeof(TrainSmem) + 1024;
 static_assert(TRAIN_SMEM <= 227 * 1024, "training CTA exceeds shared memory");
 // one training CTA per SM: its 512 TMEM columns are the whole TMEM of the SM
 static_assert(2 * TRAIN_SMEM > 228 * 1024, "training CTAs must not share an SM");
-// at most four forward CTAs per SM: 4 x 128 TMEM columns
-static_assert(5 * NET_SMEM > 228 * 1024, "forward CTAs would oversubscribe TMEM");
+// at most eight inference CTAs per SM: 8 x 64 TMEM columns
+static_assert(9 * NET_SMEM > 228 * 1024, "inference CTAs would oversubscribe TMEM");
 
 void mlp_forward(const float* W, const float* X, int n, float* Y, int* err, cudaStream_t st, LaunchCounter& lc) {
     static bool attr = false;
     allow_smem(mlp_forward_kernel, NET_SMEM, attr);
     if (n <= 0) return;
     const int tiles = (n + MT - 1) / MT;
-    const int blocks = std::max(1, std::min(tiles, sm_count() * 4));
+    const int blocks = std::max(1, std::min(tiles, sm_count() * 6));
     mlp_forward_kernel<<<blocks, MT, NET_SMEM, st>>>(W, X, n, Y, err);
     lc.add(1);
 }
@@ -493,20 +597,25 @@ void mlp_correct(const DevParams& P, const DevState& S, const TreeBufs& T, const
     allow_smem(mlp_correct_kernel, NET_SMEM, attr);
     if (npairs <= 0) return;
     const int tiles = (npairs + MT - 1) / MT;
-    const int blocks = std::max(1, std::min(tiles, sm_count() * 4));
+    const int blocks = std::max(1, std::min(tiles, sm_count() * 6));
     mlp_correct_kernel<<<blocks, MT, NET_SMEM, st>>>(P, S, T, W, pairs, npairs, err);
     lc.add(1);
 }
 
+size_t mlp_grad_scratch_floats() { return (size_t)sm_count() * MLP_NPARAM; }
+int mlp_grad_scratch_ctas() { return sm_count(); }
+
 void mlp_grad(const float* W, const float* X, const float* T, const float* wt, int n_data, int batch, uint64_t seed,
-              int step, float* grad, double* loss, int* err, cudaStream_t st, LaunchCounter& lc) {
+              int step, float* grad, double* loss, float* part, double* loss_part, int* err, cudaStream_t st,
+              LaunchCounter& lc) {
     static bool attr = false;
     allow_smem(mlp_train_kernel, TRAIN_SMEM, attr);
     if (batch <= 0 || n_data <= 0) return;
     const int tiles = (batch + MT - 1) / MT;
     const int blocks = std::max(1, std::min(tiles, sm_count()));
-    mlp_train_kernel<<<blocks, MT, TRAIN_SMEM, st>>>(W, X, T, wt, n_data, batch, seed, step, grad, loss, err);
-    lc.add(1);
+    mlp_train_kernel<<<blocks, MT, TRAIN_SMEM, st>>>(W, X, T, wt, n_data, batch, seed, step, part, loss_part, err);
+    mlp_reduce_kernel<<<(MLP_NPARAM + 255) / 256, 256, 0, st>>>(part, loss_part, blocks, grad, loss);
+    lc.add(2);
 }
 
 void mlp_adam(float* W, float* grad, float* m, float* v, float lr, float beta1, float beta2, float eps, int t,

@@ -24,8 +24,14 @@ void mlp_correct(const DevParams& P, const DevState& S, const TreeBufs& T, const
 // of the data; otherwise sample j of step `step` is drawn uniformly from the
 // n_data samples by a counter-based hash of (seed, step, j).  `wt` may be null
 // (all weights 1).
+// The sum over the CTAs is taken in a fixed order from per-CTA slots in
+// `part` (mlp_grad_scratch_floats() floats) and `loss_part`
+// (mlp_grad_scratch_ctas() doubles), so the result does not depend on timing.
 void mlp_grad(const float* W, const float* X, const float* T, const float* wt, int n_data, int batch, uint64_t seed,
-              int step, float* grad, double* loss, int* err, cudaStream_t st, LaunchCounter& lc);
+              int step, float* grad, double* loss, float* part, double* loss_part, int* err, cudaStream_t st,
+              LaunchCounter& lc);
+size_t mlp_grad_scratch_floats();
+int mlp_grad_scratch_ctas();
 
 // One Adam update of W from `grad` (then zeroed); m and v are the moment
 // vectors, t the 1-based step number.

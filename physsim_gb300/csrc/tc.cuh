@@ -44,6 +44,10 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
+// The same with FP16 A and B (format code 0).
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
 
 // ---- TMEM -----------------------------------------------------------------
 // Executed by one full warp.  The allocated address is written to *slot.
@@ -66,11 +70,13 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64
                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
                  :: "r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"((uint32_t)(accum ? 1 : 0)) : "memory");
 }
-// D[128 x N] (+)= A[128 x K] * B[N x K]^T, K a multiple of 16.  Issued by one thread.
-__device__ __forceinline__ void gemm(uint32_t d_tmem, const void* A, const void* B, int N, int K, bool accum) {
+// D[128 x N] (+)= A[128 x K] * B[N x K]^T, K a multiple of 16, A and B both
+// BF16 (or both FP16 with f16 set).  Issued by one thread.
+__device__ __forceinline__ void gemm(uint32_t d_tmem, const void* A, const void* B, int N, int K, bool accum,
+                                     bool f16 = false) {
     const uint32_t a0 = smem_u32(A), b0 = smem_u32(B);
     const uint32_t sbo = (uint32_t)K * 16u;
-    const uint32_t id = idesc_bf16(128, N);
+    const uint32_t id = f16 ? idesc_f16(128, N) : idesc_bf16(128, N);
     for (int k = 0; k < K; k += 16) {
         const uint32_t step = (uint32_t)(k >> 3) * LBO;
         mma_bf16(d_tmem, make_desc(a0 + step, LBO, sbo), make_desc(b0 + step, LBO, sbo), id, accum || k > 0);
