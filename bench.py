@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--learn-steps", type=int, default=20000)
     ap.add_argument("--learn-batch", type=int, default=65536)
     ap.add_argument("--learn-train-n", type=int, default=262144, help="particles of the training snapshot")
+    ap.add_argument("--learn-unweighted", action="store_true",
+                    help="plain MSE instead of weighting pairs by their share of the relative force error")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the other configurations (small disk, torus full force set, theta sweep)")
@@ -287,7 +289,8 @@ def run_learned(args, g, wl, idx, fx, fy, stream):
         q.theta = th
         gt.set_params(q)
         t0 = time.perf_counter()
-        tr = train_correction(gt, tt, steps=args.learn_steps, batch=args.learn_batch)
+        tr = train_correction(gt, tt, steps=args.learn_steps, batch=args.learn_batch,
+                              mass=None if args.learn_unweighted else wt.state["mass"])
         train_s = time.perf_counter() - t0
         p = g.params()
         p.theta = th
