@@ -325,6 +325,24 @@ int geon_batch_set_mode(GeonHandle* h, int32_t use_graph, int32_t simple_walk);
  * keeps the fastest mode. */
 int geon_batch_autotune(GeonHandle* h, double dt, int32_t frames, int32_t* choice, double* ms_per_frame);
 
+/* Potential heat map (Heatmap.update, src/heatmap.js:133-206, with the
+ * tree walk treePotential of :38-101 and the box blur _blur of :278-302):
+ * gravitational, electric and Yukawa potential at the centres of a grid x
+ * grid lattice of cells of cell_w x cell_h whose corner is (left, top)
+ * (the reference derives them from the camera, heatmap.js:136-142).  With
+ * Barnes-Hut on the tree is rebuilt at the current state and walked;
+ * otherwise the pairwise sum runs.  fields: bit 0 gravity, 1 electric,
+ * 2 Yukawa (each only when its force is on); blur != 0 smooths each computed
+ * field.  Outputs are host arrays of grid*grid floats, row-major (y, x); a
+ * field not computed is zero.  The colour mapping and canvas are UI and
+ * not part of the path; dead particles (not held by this path) are not
+ * included. */
+#define GEON_HEAT_GRAVITY  1u
+#define GEON_HEAT_ELECTRIC 2u
+#define GEON_HEAT_YUKAWA   4u
+int geon_heatmap(GeonHandle* h, double left, double top, double cell_w, double cell_h, int32_t grid, uint32_t fields,
+                 int32_t blur, float* grav, float* elec, float* yuk);
+
 /* Copies `rows` rows (GEON_OUT_*) of per-particle force data, each `capacity`
  * floats, starting at row `first_row`. */
 int geon_download_forces(GeonHandle* h, int32_t first_row, int32_t rows,

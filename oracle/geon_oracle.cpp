@@ -782,6 +782,129 @@ struct Sim {
         }
     }
 
+    // ---- potential heat map (heatmap.js) ----
+    // treePotential (heatmap.js:38-101) at (wx, wy): aggregates at the node's
+    // centre of mass without minimum image, leaf points skip ghosts and use
+    // the signal-delayed position when useDelay; no Yukawa cutoff.
+    void treePotential(double wx, double wy, bool doG, bool doE, bool doY, bool useDelay, std::vector<int>& stack,
+                       double& g, double& e, double& yk) const {
+        const QuadTree& t = tree;
+        const double thetaSq = prm.theta * prm.theta;
+        const double softSq = prm.softening * prm.softening;
+        const double mu = prm.yukawa_mu;
+        const bool per = periodic();
+        stack.clear();
+        stack.push_back(root);
+        while (!stack.empty()) {
+            const int nodeIdx = stack.back(); stack.pop_back();
+            if (t.totalMass[nodeIdx] == 0 && t.totalCharge[nodeIdx] == 0) continue;
+            const double dx = t.comX[nodeIdx] - wx, dy = t.comY[nodeIdx] - wy;
+            const double dSq = dx * dx + dy * dy;
+            const double size = t.bw[nodeIdx] * 2;
+            if (!t.divided[nodeIdx] && t.pointCount[nodeIdx] > 0) {
+                double gP = 0, eP = 0, yP = 0;
+                for (int i = 0; i < t.pointCount[nodeIdx]; i++) {
+                    const int other = t.points[nodeIdx * QT_CAPACITY + i];
+                    if (other >= nReal()) continue;                 // ghosts: periodic images (heatmap.js:60)
+                    const Particle& q = ps[other];
+                    double pdx, pdy;
+                    if (useDelay) {
+                        if (q.h.count < 2) continue;
+                        Delayed ret;
+                        if (!getDelayedState(q, wx, wy, ret)) continue;
+                        if (per) {
+                            const Vec d = minImage(wx, wy, ret.x, ret.y, prm.topology, prm.domain_w, prm.domain_h,
+                                                   prm.domain_w * 0.5, prm.domain_h * 0.5);
+                            pdx = d.x; pdy = d.y;
+                        } else { pdx = ret.x - wx; pdy = ret.y - wy; }
+                    } else { pdx = q.x - wx; pdy = q.y - wy; }
+                    const double rSq = pdx * pdx + pdy * pdy + softSq;
+                    const double invR = 1 / std::sqrt(rSq);
+                    if (doG) gP -= q.mass * invR;
+                    if (doE) eP += q.charge * invR;
+                    if (doY) { const double r = 1 / invR; yP -= YUKAWA_COUPLING * q.mass * std::exp(-mu * r) * invR; }
+                }
+                g += gP; e += eP; yk += yP;
+            } else if (t.divided[nodeIdx] && (size * size < thetaSq * dSq)) {
+                const double invR = 1 / std::sqrt(dSq + softSq);
+                if (doG) g -= t.totalMass[nodeIdx] * invR;
+                if (doE) e += t.totalCharge[nodeIdx] * invR;
+                if (doY) { const double r = 1 / invR; yk -= YUKAWA_COUPLING * t.totalMass[nodeIdx] * std::exp(-mu * r) * invR; }
+            } else if (t.divided[nodeIdx]) {
+                stack.push_back(t.nw[nodeIdx]); stack.push_back(t.ne[nodeIdx]);
+                stack.push_back(t.sw[nodeIdx]); stack.push_back(t.se[nodeIdx]);
+            }
+        }
+    }
+
+    // Heatmap.update's grid loop (heatmap.js:152-206, without dead
+    // particles): G x G sample points at cell centres of the view rectangle.
+    void heatmap(double left, double top, double cellW, double cellH, int G, bool doG, bool doE, bool doY,
+                 double* gOut, double* eOut, double* yOut) {
+        const bool useTree = (prm.toggles & GEON_BARNES_HUT) != 0;
+        const bool useDelay = (prm.toggles & GEON_RELATIVITY) != 0;
+        if (useTree) buildTree();
+        const double softSq = prm.softening * prm.softening;
+        const double mu = prm.yukawa_mu;
+        const double cutSq = doY ? (6 / mu) * (6 / mu) : INF;          // heatmap.js:149
+        const bool per = periodic();
+        const int n = nReal();
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nThreads)
+        for (int idx = 0; idx < G * G; idx++) {
+            const int gy = idx / G, gx = idx % G;
+            const double wy = top + (gy + 0.5) * cellH;
+            const double wx = left + (gx + 0.5) * cellW;
+            double g = 0, e = 0, yk = 0;
+            if (useTree && root >= 0) {
+                std::vector<int> stack;
+                treePotential(wx, wy, doG, doE, doY, useDelay, stack, g, e, yk);
+            } else {
+                for (int i = 0; i < n; i++) {
+                    const Particle& q = ps[i];
+                    double dx, dy;
+                    if (useDelay) {
+                        if (q.h.count < 2) continue;
+                        Delayed ret;
+                        if (!getDelayedState(q, wx, wy, ret)) continue;
+                        if (per) {
+                            const Vec d = minImage(wx, wy, ret.x, ret.y, prm.topology, prm.domain_w, prm.domain_h,
+                                                   prm.domain_w * 0.5, prm.domain_h * 0.5);
+                            dx = d.x; dy = d.y;
+                        } else { dx = ret.x - wx; dy = ret.y - wy; }
+                    } else if (per) {
+                        const Vec d = minImage(wx, wy, q.x, q.y, prm.topology, prm.domain_w, prm.domain_h,
+                                               prm.domain_w * 0.5, prm.domain_h * 0.5);
+                        dx = d.x; dy = d.y;
+                    } else { dx = q.x - wx; dy = q.y - wy; }
+                    const double rSq = dx * dx + dy * dy + softSq;
+                    const double invR = 1 / std::sqrt(rSq);
+                    if (doG) g -= q.mass * invR;
+                    if (doE) e += q.charge * invR;
+                    if (doY && rSq < cutSq) { const double r = 1 / invR; yk -= YUKAWA_COUPLING * q.mass * std::exp(-mu * r) * invR; }
+                }
+            }
+            gOut[idx] = g; eOut[idx] = e; yOut[idx] = yk;
+        }
+    }
+
+    // Heatmap._blur (heatmap.js:278-302): separable 3 x 3 box blur, clamp to edge.
+    static void blur(double* arr, int G) {
+        std::vector<double> t((size_t)G * G);
+        for (int y = 0; y < G; y++) {
+            const int row = y * G;
+            for (int x = 0; x < G; x++) {
+                const double l = x > 0 ? arr[row + x - 1] : arr[row];
+                const double r = x < G - 1 ? arr[row + x + 1] : arr[row + G - 1];
+                t[row + x] = (l + arr[row + x] + r) * (1.0 / 3);
+            }
+        }
+        const int lastRow = (G - 1) * G;
+        for (int y = 0; y < G; y++) {
+            const int rA = y > 0 ? (y - 1) * G : 0, rC = y * G, rB = y < G - 1 ? (y + 1) * G : lastRow;
+            for (int x = 0; x < G; x++) arr[rC + x] = (t[rA + x] + t[rC + x] + t[rB + x]) * (1.0 / 3);
+        }
+    }
+
     // ---- resetForces (forces.js:31-54) ----
     static void resetOne(Particle& p) {
         p.fx = p.fy = 0;
@@ -1371,6 +1494,24 @@ int oracle_get_forces(void* h, double* out, int cap) {
         for (int r = 0; r < GEON_OUT_ROWS; r++) out[(size_t)r * cap + i] = v[r];
     }
     return n;
+}
+
+// Potential heat map (heatmap.js:152-206, 278-302): fields bit 1 gravity,
+// 2 electric, 4 Yukawa (each also needs its force toggle); blur != 0 applies
+// the 3 x 3 box blur to each computed field.  Outputs G*G doubles each.
+void oracle_heatmap(void* h, double left, double top, double cell_w, double cell_h, int G, unsigned fields, int blur,
+                    double* g, double* e, double* y) {
+    Sim* s = static_cast<Sim*>(h);
+    const unsigned tg = s->prm.toggles;
+    const bool doG = (fields & 1u) && (tg & GEON_GRAVITY);
+    const bool doE = (fields & 2u) && (tg & GEON_COULOMB);
+    const bool doY = (fields & 4u) && (tg & GEON_YUKAWA);
+    s->heatmap(left, top, cell_w, cell_h, G, doG, doE, doY, g, e, y);
+    if (blur) {
+        if (doG) Sim::blur(g, G);
+        if (doE) Sim::blur(e, G);
+        if (doY) Sim::blur(y, G);
+    }
 }
 
 // Build the tree at the current positions; returns the number of tree points.

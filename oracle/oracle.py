@@ -77,6 +77,7 @@ def load() -> C.CDLL:
         "oracle_min_image": ([d, d, d, d, i, d, d, P(d)], None),
         "oracle_delayed_state": ([v, i, d, d, P(d)], i),
         "oracle_compute_forces_subset": ([v, P(C.c_int), i], C.c_longlong),
+        "oracle_heatmap": ([v, d, d, d, d, i, C.c_uint, i, P(d), P(d), P(d)], None),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -233,6 +234,13 @@ class OracleSim:
         out = np.zeros(5)
         ok = self.lib.oracle_delayed_state(self._h, src, ox, oy, _dp(out))
         return out if ok else None
+
+    def heatmap(self, left, top, cell_w, cell_h, grid, fields=7, blur=True) -> dict:
+        """Potential grids (heatmap.js:152-206, 278-302), grid x grid each."""
+        out = [np.zeros(grid * grid) for _ in range(3)]
+        self.lib.oracle_heatmap(self._h, left, top, cell_w, cell_h, grid, fields, 1 if blur else 0,
+                                *[_dp(a) for a in out])
+        return {k: a.reshape(grid, grid) for k, a in zip(("gravity", "electric", "yukawa"), out)}
 
     def set_forces_init(self, v: bool):
         self.lib.oracle_set_forces_init(self._h, 1 if v else 0)

@@ -165,6 +165,8 @@ SIGNATURES = {
     "geon_batch_substeps": [_handle_t, _P(C.c_int32), C.c_int32],
     "geon_batch_set_mode": [_handle_t, C.c_int32, C.c_int32],
     "geon_batch_autotune": [_handle_t, C.c_double, C.c_int32, _P(C.c_int32), _P(C.c_double)],
+    "geon_heatmap": [_handle_t, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_uint32, C.c_int32,
+                     _P(C.c_float), _P(C.c_float), _P(C.c_float)],
     "geon_download_forces": [_handle_t, C.c_int32, C.c_int32, _P(C.c_float), C.c_int32],
     "geon_build_tree": [_handle_t, _P(GeonTreeInfo)],
     "geon_tree_leaves": [_handle_t, _P(C.c_int32), C.c_int32, _P(C.c_double), _P(C.c_double), _P(C.c_double),

@@ -1001,6 +1001,39 @@ int geon_mlp_train(GeonHandle* h, float* weights, const float* x, const float* t
     return r ? r : read_ctl(h);
 }
 
+int geon_heatmap(GeonHandle* h, double left, double top, double cell_w, double cell_h, int32_t grid, uint32_t fields,
+                 int32_t blur, float* grav, float* elec, float* yuk) {
+    if (!h || grid < 1 || grid > 4096 || !grav || !elec || !yuk) return GEON_ERR_ARG;
+    if (h->batch) return set_err(h, GEON_ERR_UNSUPPORTED, "the heat map covers one system");
+    const uint32_t tg = h->prm.toggles;
+    const bool doG = (fields & 1u) && (tg & GEON_GRAVITY);
+    const bool doE = (fields & 2u) && (tg & GEON_COULOMB);
+    const bool doY = (fields & 4u) && (tg & GEON_YUKAWA);
+    const bool tree = bh_on(h) && h->n > 0;
+    if (tree) { int r = build_tree(h); if (r) return r; }
+    const size_t gg = (size_t)grid * grid;
+    DevArena tmp;
+    float* d_g = tmp.alloc<float>(gg);
+    float* d_e = tmp.alloc<float>(gg);
+    float* d_y = tmp.alloc<float>(gg);
+    float* d_t = tmp.alloc<float>(gg);
+    if (tmp.failed) { tmp.free_all(); return set_err(h, GEON_ERR_NOMEM, "heat map allocation failed"); }
+    cudaError_t e = cudaSuccess;
+    if (h->P.rel) { launch_hist_tables(h->hist_t, h->simTime, h->hist_age, h->hist_segdt, h->st, h->lc); e = cudaGetLastError(); }
+    if (e == cudaSuccess) {
+        heatmap_pass(h->P, h->S, h->T, h->d_root, h->ctl, make_ctx(h), left, top, cell_w, cell_h, grid, doG, doE, doY,
+                     tree, blur != 0, d_g, d_e, d_y, d_t, h->st, h->lc);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(grav, d_g, gg * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(elec, d_e, gg * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(yuk, d_y, gg * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    tmp.free_all();
+    int r = cuda_check(h, e, "heat map");
+    return r ? r : read_ctl(h);
+}
+
 int geon_download_forces(GeonHandle* h, int32_t first_row, int32_t rows, float* out, int32_t capacity) {
     if (!h || !out || first_row < 0 || rows <= 0 || first_row + rows > GEON_OUT_ROWS || capacity < 0) return GEON_ERR_ARG;
     const int cnt = std::min(h->n, capacity);

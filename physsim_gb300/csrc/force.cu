@@ -1207,6 +1207,166 @@ void direct_subset(const DevParams& P, const DevState& S, const FrameCtl* ctl, c
     lc.add(1);
 }
 
+// ---- potential heat map (heatmap.js:38-101, 152-206) ---------------------------------------------
+// One thread per grid point.  Tree mode follows treePotential: a node is
+// skipped only when both its mass and charge are zero; aggregates use the
+// centre of mass without minimum image; leaves evaluate their real points
+// (ghosts are skipped), signal-delayed when relativity is on; no Yukawa
+// cutoff.  Pairwise mode follows the grid loop's direct branch: minimum
+// image, Yukawa cutoff on r^2 + softening^2 < (6/mu)^2.
+constexpr int HM_THREADS = 128;
+constexpr int HM_STACK = 128;       // depth 31 needs at most 3 * 31 + 4 entries
+
+__device__ __forceinline__ void potential_terms(const DevParams& P, float rx, float ry, float m, float q,
+                                                bool doG, bool doE, bool doY, bool cut, CAcc& g, CAcc& e, CAcc& y) {
+    const float rSq = __fmaf_rn(rx, rx, ry * ry) + P.softSq;
+    const float invR = rsqrtf(rSq);
+    if (doG) g.add(-m * invR);
+    if (doE) e.add(q * invR);
+    if (doY) {
+        bool in = true;
+        if (cut) {                                          // heatmap.js:185 (pairwise branch only)
+            const float c = P.yukCutSq;
+            in = fabsf(rSq - c) > 1e-6f * c ? rSq < c
+                                            : ((double)rx * rx + (double)ry * ry + (double)P.softSq < P.yukCutSqD);
+        }
+        if (in) {
+            const float r = rSq * invR;
+            y.add(-YUKAWA_COUPLING * m * __expf(-P.yukMu * r) * invR);
+        }
+    }
+}
+
+template <bool REL>
+__global__ void __launch_bounds__(HM_THREADS)
+heatmap_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C,
+               double left, double top, double cw, double chh, int G, int doG_, int doE_, int doY_, int useTree,
+               float* __restrict__ gOut, float* __restrict__ eOut, float* __restrict__ yOut) {
+    __shared__ float s_age[REL ? HIST_LEN : 1], s_segdt[REL ? HIST_LEN : 1];
+    if (REL) load_hist_tables(C, s_age, s_segdt);
+    const bool doG = doG_ != 0, doE = doE_ != 0, doY = doY_ != 0;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= G * G) return;
+    const int gy = idx / G, gx = idx % G;
+    const double wy = top + (gy + 0.5) * chh, wx = left + (gx + 0.5) * cw;
+    Tgt o{};
+    o.x = (float)wx; o.xlo = (float)(wx - (double)o.x);
+    o.y = (float)wy; o.ylo = (float)(wy - (double)o.y);
+    o.idx = -1;
+    CAcc g, e, y;
+    g.init(); e.init(); y.init();
+    const int n = ctl->n;
+    if (useTree) {
+        int stack[HM_STACK];
+        int sp = 0;
+        const int root = *d_root;
+        const int nInt = ctl->nInternal, nLeaf = ctl->nLeaves, nValid = ctl->nValid;
+        if (root != ROOT_NONE && !(ctl->err & (ERR_NODE_OVERFLOW | ERR_BAD_INDEX))) stack[sp++] = root;
+        while (sp > 0) {
+            const int node = stack[--sp];
+            if (node & LEAF_REF) {
+                const int li = node & ~LEAF_REF;
+                if (li < 0 || li >= nLeaf) { atomicOr(&ctl->err, ERR_BAD_INDEX); continue; }
+                const float4 la = T.leaf_a[li];
+                if (la.z == 0.f && la.w == 0.f) continue;
+                const int4 lm = T.leaf_meta[li];
+                if (lm.x < 0 || lm.x + lm.y > nValid) { atomicOr(&ctl->err, ERR_BAD_INDEX); continue; }
+                for (int q = lm.x; q < lm.x + lm.y; q++) {
+                    const uint32_t ref = __float_as_uint(T.ps_c[q].w);
+                    if (ref_code(ref) != CODE_IDENTITY) continue;            // heatmap.js:60
+                    const float4 pa = T.ps_a[q];
+                    float rx, ry;
+                    if (REL) {
+                        const int j = (int)ref_index(ref);
+                        Delayed d;
+                        if (!delayed_state(P, S, C, s_age, s_segdt, j, o, d)) continue;
+                        rx = d.rx; ry = d.ry;
+                    } else {
+                        const float4 pb = T.ps_b[q];
+                        rx = __fadd_rn(__fsub_rn(pa.x, o.x), pb.x - o.xlo);
+                        ry = __fadd_rn(__fsub_rn(pa.y, o.y), pb.y - o.ylo);
+                    }
+                    potential_terms(P, rx, ry, pa.z, pa.w, doG, doE, doY, false, g, e, y);
+                }
+            } else {
+                if (node < 0 || node >= nInt) { atomicOr(&ctl->err, ERR_BAD_INDEX); continue; }
+                const float4 a = T.int_a[node];
+                if (a.z == 0.f && a.w == 0.f) continue;
+                const float4 c = T.int_c[node];
+                const float dx = __fadd_rn(__fsub_rn(a.x, o.x), c.x - o.xlo);
+                const float dy = __fadd_rn(__fsub_rn(a.y, o.y), c.y - o.ylo);
+                const float rhs = P.thetaSq * __fmaf_rn(dx, dx, dy * dy);
+                bool accept = c.z < rhs;
+                if (fabsf(rhs - c.z) <= 1e-6f * c.z) {
+                    const double ddx = ((double)a.x + (double)c.x) - wx, ddy = ((double)a.y + (double)c.y) - wy;
+                    const double size = 2.0 * ldexp(P.rootW, -(int)c.w);
+                    accept = size * size < P.thetaSqD * (ddx * ddx + ddy * ddy);
+                }
+                if (accept) {
+                    potential_terms(P, dx, dy, a.z, a.w, doG, doE, doY, false, g, e, y);
+                } else {
+                    const int4 ch = T.int_child[node];
+                    if (sp + 4 > HM_STACK) { atomicOr(&ctl->err, ERR_STACK_OVERFLOW); break; }
+                    if (ch.x >= 0) stack[sp++] = ch.x;
+                    if (ch.y >= 0) stack[sp++] = ch.y;
+                    if (ch.z >= 0) stack[sp++] = ch.z;
+                    if (ch.w >= 0) stack[sp++] = ch.w;
+                }
+            }
+        }
+    } else {
+        for (int i = 0; i < n; i++) {
+            float rx, ry;
+            const float4 p = S.pos[i];
+            if (REL) {
+                Delayed d;
+                if (!delayed_state(P, S, C, s_age, s_segdt, i, o, d)) continue;
+                rx = d.rx; ry = d.ry;
+            } else {
+                const float2 pl = S.pos_lo[i];
+                displacement(P, o.x, o.y, p.x, pl.x - o.xlo, p.y, pl.y - o.ylo, rx, ry);
+            }
+            potential_terms(P, rx, ry, p.z, p.w, doG, doE, doY, true, g, e, y);
+        }
+    }
+    gOut[idx] = g.value();
+    eOut[idx] = e.value();
+    yOut[idx] = y.value();
+}
+
+// Heatmap._blur (heatmap.js:278-302): 3 x 3 box blur, clamp to edge, as two passes.
+__global__ void blur_kernel(const float* __restrict__ in, float* __restrict__ out, int G, int horizontal) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= G * G) return;
+    const int yy = idx / G, xx = idx % G;
+    float a, b, c;
+    if (horizontal) {
+        a = in[yy * G + max(xx - 1, 0)]; b = in[idx]; c = in[yy * G + min(xx + 1, G - 1)];
+    } else {
+        a = in[max(yy - 1, 0) * G + xx]; b = in[idx]; c = in[min(yy + 1, G - 1) * G + xx];
+    }
+    out[idx] = (a + b + c) * (1.f / 3.f);
+}
+
+void heatmap_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
+                  const ForceCtx& C, double left, double top, double cw, double ch, int G, bool doG, bool doE, bool doY,
+                  bool useTree, bool blur, float* g, float* e, float* y, float* tmp, cudaStream_t st, LaunchCounter& lc) {
+    const int blocks = (G * G + HM_THREADS - 1) / HM_THREADS;
+    if (P.rel) heatmap_kernel<true><<<blocks, HM_THREADS, 0, st>>>(P, S, T, d_root, ctl, C, left, top, cw, ch, G, doG, doE, doY, useTree, g, e, y);
+    else heatmap_kernel<false><<<blocks, HM_THREADS, 0, st>>>(P, S, T, d_root, ctl, C, left, top, cw, ch, G, doG, doE, doY, useTree, g, e, y);
+    lc.add(1);
+    if (blur) {
+        float* fields[3] = { g, e, y };
+        const bool on3[3] = { doG, doE, doY };
+        for (int f = 0; f < 3; f++) {
+            if (!on3[f]) continue;
+            blur_kernel<<<blocks, HM_THREADS, 0, st>>>(fields[f], tmp, G, 1);
+            blur_kernel<<<blocks, HM_THREADS, 0, st>>>(tmp, fields[f], G, 0);
+            lc.add(2);
+        }
+    }
+}
+
 // ---- 1PN-only passes (forces.js:445-610) ----------------------------------------------------
 __device__ __forceinline__ void accum_1pn(const DevParams& P, const Tgt& t, float rx, float ry, float svx, float svy,
                                           float sm, float sq, float& ox, float& oy) {

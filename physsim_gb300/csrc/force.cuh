@@ -34,6 +34,13 @@ struct ForceCtx {
 // walls) for every particle, with the max-acceleration / cyclotron
 // reductions for the substep planner.  `bh` selects the tree walk (tree must
 // be built) or the pairwise sum.
+// Potential heat map on a G x G grid of cell centres (heatmap.js:152-206):
+// tree walk (useTree, tree built) or pairwise sum; optional 3 x 3 box blur
+// of each computed field (tmp: G*G floats).  Device outputs of G*G floats.
+void heatmap_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
+                  const ForceCtx& C, double left, double top, double cw, double ch, int G, bool doG, bool doE, bool doY,
+                  bool useTree, bool blur, float* g, float* e, float* y, float* tmp, cudaStream_t st, LaunchCounter& lc);
+
 // clear = false keeps the planner reductions and the interaction counter of
 // earlier passes (a force pass split over target chunks).
 void force_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,

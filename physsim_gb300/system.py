@@ -179,6 +179,14 @@ class GeonSystem:
                                          float(lr), int(seed), hist.ctypes.data_as(C.POINTER(C.c_double))))
         return w, hist[:int(steps)]
 
+    def heatmap(self, left: float, top: float, cell_w: float, cell_h: float, grid: int, fields: int = 7,
+                blur: bool = True) -> dict:
+        """Gravitational, electric and Yukawa potential grids (grid x grid)."""
+        out = [np.zeros(grid * grid, dtype=np.float32) for _ in range(3)]
+        self._ck(self.lib.geon_heatmap(self._h, float(left), float(top), float(cell_w), float(cell_h), int(grid),
+                                       int(fields), 1 if blur else 0, *[N.fptr(a) for a in out]))
+        return {k: a.reshape(grid, grid) for k, a in zip(("gravity", "electric", "yukawa"), out)}
+
     def forces(self) -> dict:
         n = self.count()
         cap = max(n, 1)
