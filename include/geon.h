@@ -211,6 +211,13 @@ int geon_download_state_f64(GeonHandle* h, double* soa, int32_t rows, int32_t ca
 int geon_reset(GeonHandle* h);
 
 /* GPUPhysics.getParticleCount() (src/gpu/gpu-physics.js:4287). */
+/* geon_upload_state from double precision (the reference's save files hold
+ * doubles, save-load.js:94-98): positions are kept as compensated FP32
+ * pairs (hi + lo), so a state written by geon_download_state_f64 comes back
+ * exactly; the other rows are rounded to FP32.  `soa` holds GEON_ST_ROWS_IN
+ * rows of n doubles. */
+int geon_upload_state_f64(GeonHandle* h, int32_t n, const double* soa, double sim_time);
+
 int geon_particle_count(GeonHandle* h, int32_t* n);
 
 /* Physics.update(particles, dt, ...) (src/integrator.js:726-1825), the

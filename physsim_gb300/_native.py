@@ -146,6 +146,7 @@ SIGNATURES = {
     "geon_download_ids": [_handle_t, _P(C.c_int32), C.c_int32, _P(C.c_int32)],
     "geon_download_state_f64": [_handle_t, _P(C.c_double), C.c_int32, C.c_int32, _P(C.c_int32)],
     "geon_reset": [_handle_t],
+    "geon_upload_state_f64": [_handle_t, C.c_int32, _P(C.c_double), C.c_double],
     "geon_particle_count": [_handle_t, _P(C.c_int32)],
     "geon_update": [_handle_t, C.c_double, _P(C.c_int32)],
     "geon_synchronize": [_handle_t],

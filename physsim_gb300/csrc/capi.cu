@@ -299,8 +299,9 @@ static int ensure_tree(GeonHandle* h) {
 // ---- small kernels local to the driver --------------------------------------------------------
 __global__ void set_n_kernel(FrameCtl* ctl, int n) { ctl->n = n; }
 
+// rows: x, y, wx, wy, mass, charge, angw (and, with with_lo, the low parts of x, y)
 __global__ void init_particles_kernel(DevParams P, DevState S, const float* __restrict__ rows, int cap, int first, int k,
-                                      double ctime, int id0) {
+                                      double ctime, int id0, int with_lo) {
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < k; t += gridDim.x * blockDim.x) {
         const float x = rows[t], y = rows[cap + t], wx = rows[2 * cap + t], wy = rows[3 * cap + t];
         const float m = rows[4 * cap + t], q = rows[5 * cap + t], angw = rows[6 * cap + t];
@@ -313,7 +314,7 @@ __global__ void init_particles_kernel(DevParams P, DevState S, const float* __re
             angVel = angw / sqrtf(1.f + angw * angw * r * r);             // relativity.js:7-9
         }
         S.pos[i] = make_float4(x, y, m, q);
-        S.pos_lo[i] = make_float2(0.f, 0.f);
+        S.pos_lo[i] = with_lo ? make_float2(rows[7 * cap + t], rows[8 * cap + t]) : make_float2(0.f, 0.f);
         S.vel[i] = make_float4(wx, wy, vx, vy);
         S.spin[i] = make_float4(angw, angVel, r, 1.f / m);
         S.mom[i] = make_float2(0.f, 0.f);                                   // particle.js:53-54
@@ -688,7 +689,7 @@ int geon_add_particles(GeonHandle* h, int32_t n, const float* soa, double creati
     const int cap = h->n_cap;
     for (int r = 0; r < GEON_ST_ROWS_IN; r++)
         CK(cudaMemcpyAsync(h->staging + (size_t)r * cap, soa + (size_t)r * n, n * sizeof(float), cudaMemcpyHostToDevice, h->st));
-    init_particles_kernel<<<grid_for(n, 256), 256, 0, h->st>>>(h->P, h->S, h->staging, cap, h->n, n, creation_time, h->nextId);
+    init_particles_kernel<<<grid_for(n, 256), 256, 0, h->st>>>(h->P, h->S, h->staging, cap, h->n, n, creation_time, h->nextId, 0);
     CKL();
     h->lc.add(1);
     if (first_index) *first_index = h->n;
@@ -735,6 +736,40 @@ int geon_upload_state(GeonHandle* h, int32_t n, const float* soa, double sim_tim
     h->simTime = sim_time;
     // loaded particles are treated as always existing (save-load.js:231)
     return geon_add_particles(h, n, soa, -INFINITY, nullptr);
+}
+
+int geon_upload_state_f64(GeonHandle* h, int32_t n, const double* soa, double sim_time) {
+    if (!h || n < 0 || (n > 0 && !soa)) return GEON_ERR_ARG;
+    if (n > h->n_cap) return set_err(h, GEON_ERR_FULL, "particle capacity exhausted");
+    if (h->batch && n != h->n_cap)
+        return set_err(h, GEON_ERR_UNSUPPORTED, "a batched handle takes its whole batch at once (geon_upload_state)");
+    int r = geon_reset(h);
+    if (r) return r;
+    h->simTime = sim_time;
+    if (n == 0) return GEON_OK;
+    const int cap = h->n_cap;
+    std::vector<float> rows((size_t)9 * n);
+    for (int i = 0; i < n; i++) {
+        for (int c = 0; c < 2; c++) {                      // positions as hi + lo pairs
+            const double v = soa[(size_t)c * n + i];
+            const float hi = (float)v;
+            rows[(size_t)c * n + i] = hi;
+            rows[(size_t)(7 + c) * n + i] = (float)(v - (double)hi);
+        }
+        for (int c = 2; c < GEON_ST_ROWS_IN; c++) rows[(size_t)c * n + i] = (float)soa[(size_t)c * n + i];
+    }
+    for (int c = 0; c < 9; c++)
+        CK(cudaMemcpyAsync(h->staging + (size_t)c * cap, rows.data() + (size_t)c * n, n * sizeof(float),
+                           cudaMemcpyHostToDevice, h->st));
+    init_particles_kernel<<<grid_for(n, 256), 256, 0, h->st>>>(h->P, h->S, h->staging, cap, 0, n, -INFINITY, h->nextId, 1);
+    CKL();
+    h->lc.add(1);
+    h->n = n;
+    h->nextId += n;
+    set_n_kernel<<<1, 1, 0, h->st>>>(h->ctl, h->n);
+    h->lc.add(1);
+    CK(cudaStreamSynchronize(h->st));
+    return GEON_OK;
 }
 
 int geon_particle_count(GeonHandle* h, int32_t* n) {

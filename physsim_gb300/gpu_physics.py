@@ -79,6 +79,7 @@ class GeonGPUPhysics:
                          ext_electric_angle=0.0, ext_bz=0.0)
         self._bounceFriction = 0.4
         self._sys: GeonSystem | None = None
+        self._meta = {}             # particle id -> (baseMass, antimatter), kept for the save format
         self._stats = None
         self._selected = -1
         self._ready = False
@@ -166,8 +167,10 @@ class GeonGPUPhysics:
         (_, _), (wx, wy) = set_velocity(float(_get(p, "vx", 0.0)), float(_get(p, "vy", 0.0)))
         q = quantise_charge(float(_get(p, "charge", 0.0)))
         try:
-            return self._sys.add([_get(p, "x")], [_get(p, "y")], [wx], [wy], [m], [q],
+            slot = self._sys.add([_get(p, "x")], [_get(p, "y")], [wx], [wy], [m], [q],
                                  [float(_get(p, "angw", 0.0))], creation_time=self.simTime)
+            self._meta[int(self._sys.ids()[slot])] = (m, bool(_get(p, "antimatter", False)))
+            return slot
         except N.GeonError as e:
             if e.code == N.GEON_ERR_FULL:
                 return -1
@@ -190,33 +193,94 @@ class GeonGPUPhysics:
             return 0
         return self._sys.update(dt)
 
-    # -- save / load (gpu-physics.js:3749-3972; save format save-load.js:89-120) --------------
+    # -- save / load (save format save-load.js:89-120; loading :129-229) ------------------------
+    # The toggle names of the saved state (save-load.js:106-111) and their bits.
+    _SAVE_TOGGLES = [("gravityEnabled", N.GRAVITY), ("bosonInterEnabled", 0), ("coulombEnabled", N.COULOMB),
+                     ("magneticEnabled", N.MAGNETIC), ("gravitomagEnabled", N.GRAVITOMAG),
+                     ("relativityEnabled", N.RELATIVITY), ("barnesHutEnabled", N.BARNES_HUT),
+                     ("radiationEnabled", N.RADIATION), ("blackHoleEnabled", N.BLACK_HOLE),
+                     ("disintegrationEnabled", 0), ("spinOrbitEnabled", N.SPIN_ORBIT), ("onePNEnabled", N.ONE_PN),
+                     ("yukawaEnabled", N.YUKAWA), ("axionEnabled", N.AXION), ("expansionEnabled", 0),
+                     ("higgsEnabled", N.HIGGS)]
+    COL_NAMES = ["pass", "bounce", "merge"]
+
     def serialize(self, sim=None) -> dict:
-        st = self._sys.state()
-        parts = [{"x": float(st["x"][i]), "y": float(st["y"][i]), "wx": float(st["wx"][i]),
-                  "wy": float(st["wy"][i]), "mass": float(st["mass"][i]), "baseMass": float(st["mass"][i]),
-                  "charge": float(st["charge"][i]), "angw": float(st["angw"][i]), "antimatter": False}
-                 for i in range(st["x"].size)]
-        return {"version": 1, "particles": parts, "toggles": {},
-                "settings": {"boundary": BOUND_NAMES[self.boundaryMode], "topology": TOPO_NAMES[self.topologyMode]},
-                "yukawaMu": self._yukawaMu, "simTime": self.simTime}
+        """The reference's save state (version 1, save-load.js:91-127): particles
+        with position, proper velocity, mass, base mass, charge, angw and the
+        antimatter flag; the 16 physics toggles; settings; external fields.
+        `sim` (optional) supplies speedScale and camera as the reference reads
+        them from the Simulation.  simTime is added (the reference's GPU path
+        keeps it on the device)."""
+        st = self._sys.state(f64=True)
+        n = st["x"].size
+        ids = self._sys.ids() if n else []
+        parts = []
+        for i in range(n):
+            base, anti = self._meta.get(int(ids[i]), (float(st["mass"][i]), False))
+            parts.append({"x": float(st["x"][i]), "y": float(st["y"][i]), "wx": float(st["wx"][i]),
+                          "wy": float(st["wy"][i]), "mass": float(st["mass"][i]), "baseMass": float(base),
+                          "charge": float(st["charge"][i]), "angw": float(st["angw"][i]), "antimatter": bool(anti)})
+        toggles = {name: bool(bit and (self._toggles & bit)) for name, bit in self._SAVE_TOGGLES}
+        settings = {"collision": self.COL_NAMES[int(self._collisionMode) % 3] if isinstance(self._collisionMode, int)
+                    else str(self._collisionMode),
+                    "boundary": BOUND_NAMES[self.boundaryMode], "topology": TOPO_NAMES[self.topologyMode],
+                    "speed": float(_get(sim, "speedScale", 1.0)) if sim is not None else 1.0,
+                    "friction": self._bounceFriction}
+        state = {"version": 1, "particles": parts, "toggles": toggles, "settings": settings,
+                 "yukawaMu": self._yukawaMu, "axionMass": None, "hubbleParam": None, "higgsMass": None,
+                 "extGravity": self._ext["ext_gravity"], "extGravityAngle": self._ext["ext_gravity_angle"],
+                 "extElectric": self._ext["ext_electric"], "extElectricAngle": self._ext["ext_electric_angle"],
+                 "extBz": self._ext["ext_bz"], "simTime": self.simTime}
+        cam = _get(sim, "camera", None) if sim is not None else None
+        if cam is not None:
+            state["camera"] = {"x": _get(cam, "x", 0.0), "y": _get(cam, "y", 0.0), "zoom": _get(cam, "zoom", 1.0)}
+        return state
 
     def deserialize(self, state: dict, sim=None) -> bool:
+        """loadState (save-load.js:129-229): restores toggles, external fields,
+        friction and the boundary / topology / collision settings, then the
+        particles (at most maxParticles; loaded particles always existed,
+        :212; coordinate velocity from w as :220-223 derive it)."""
         if not state or state.get("version") != 1:
             return False
-        parts = state.get("particles", [])[: self.maxParticles]
-        cols = {k: np.array([float(p.get(k, 0.0) or 0.0) for p in parts]) for k in ("x", "y", "wx", "wy", "charge", "angw")}
-        cols["mass"] = np.array([float(p.get("mass") or 1.0) for p in parts])
-        if "yukawaMu" in state:
+        tg = state.get("toggles") or {}
+        if tg:
+            t = 0
+            for name, bit in self._SAVE_TOGGLES:
+                if bit and tg.get(name, False):
+                    t |= bit
+            self._toggles = t
+        for key, name in (("ext_gravity", "extGravity"), ("ext_gravity_angle", "extGravityAngle"),
+                          ("ext_electric", "extElectric"), ("ext_electric_angle", "extElectricAngle"),
+                          ("ext_bz", "extBz")):
+            if state.get(name) is not None:
+                self._ext[key] = float(state[name])
+        if state.get("yukawaMu") is not None:
             self._yukawaMu = float(state["yukawaMu"])
-            self._sync()
-        self._sys.upload(cols["x"], cols["y"], cols["wx"], cols["wy"], cols["mass"], cols["charge"], cols["angw"],
-                         sim_time=float(state.get("simTime", 0.0)))
+        st = state.get("settings") or {}
+        if st.get("friction") is not None:
+            self._bounceFriction = float(st["friction"])
+        if st.get("boundary") in BOUND_NAMES:
+            self.boundaryMode = BOUND_NAMES.index(st["boundary"])
+        if st.get("topology") in TOPO_NAMES:
+            self.topologyMode = TOPO_NAMES.index(st["topology"])
+        col = "bounce" if st.get("collision") == "repel" else st.get("collision", "pass")   # save-load.js:180
+        if col in self.COL_NAMES:
+            self._collisionMode = self.COL_NAMES.index(col)
+        self._sync()
+        parts = (state.get("particles") or [])[: self.maxParticles]
+        f = lambda k, d=0.0: np.array([float(pp.get(k, d) if pp.get(k, d) is not None else d) for pp in parts])
+        self._sys.upload_f64(f("x"), f("y"), f("wx"), f("wy"), f("mass", 1.0), f("charge"), f("angw"),
+                             sim_time=float(state.get("simTime", 0.0) or 0.0))
+        ids = self._sys.ids() if parts else []
+        self._meta = {int(ids[i]): (float(pp.get("baseMass", pp.get("mass", 1.0)) or 1.0), bool(pp.get("antimatter", False)))
+                      for i, pp in enumerate(parts)}
         return True
 
     def reset(self):
         self._sys.reset()
         self._stats = None
+        self._meta = {}
 
     # -- stats (gpu-physics.js:4146-4283) ----------------------------------------------------
     def requestStats(self, selectedGpuIdx: int = -1):

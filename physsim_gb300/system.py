@@ -68,6 +68,13 @@ class GeonSystem:
         rows, n = self._rows(x, y, wx, wy, mass, charge, angw)
         self._ck(self.lib.geon_upload_state(self._h, n, N.fptr(rows), sim_time))
 
+    def upload_f64(self, x, y, wx, wy, mass, charge, angw, sim_time: float = 0.0):
+        """upload() from doubles: positions keep their compensated low parts."""
+        cols = [np.asarray(a, dtype=np.float64).ravel() for a in (x, y, wx, wy, mass, charge, angw)]
+        n = cols[0].size
+        rows = np.ascontiguousarray(np.stack(cols)) if n else np.zeros((7, 1))
+        self._ck(self.lib.geon_upload_state_f64(self._h, n, N.dptr(rows), sim_time))
+
     def count(self) -> int:
         n = C.c_int32()
         self._ck(self.lib.geon_particle_count(self._h, C.byref(n)))
