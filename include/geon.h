@@ -89,8 +89,15 @@ typedef struct GeonParams {
     double   ext_electric_angle;
     double   ext_bz;           /* Physics.extBz                                       */
     int32_t  max_substeps;     /* MAX_SUBSTEPS (32)                                   */
-    int32_t  reserved;
+    int32_t  collision_mode;   /* GEON_COL_*: the collisionMode argument of Physics.update */
 } GeonParams;
+
+/* collision modes (src/config.js:10-12).  GEON_COL_MERGE runs handleCollisions
+ * (src/collisions.js:24-107) after the tree rebuild of every substep; the
+ * bounce mode's contact forces are not part of this library. */
+#define GEON_COL_PASS   0
+#define GEON_COL_MERGE  1
+#define GEON_COL_BOUNCE 2   /* unsupported */
 
 /* Conserved quantities in FP64 (src/energy.js:11-62 passes 1-2, and the
  * potential energy of the last force pass, src/forces.js:26). */

@@ -42,6 +42,7 @@
 #include <string>
 #include <limits>
 #include <algorithm>
+#include <array>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -55,6 +56,7 @@ constexpr double EPS = 1e-12;                // config.js:30
 constexpr double INERTIA_K = 0.4;            // config.js:52
 constexpr double MAG_MOMENT_K = 0.2;         // config.js:53
 constexpr double TIDAL_STRENGTH = 64;        // config.js:54
+constexpr double BOSON_CHARGE = 0.1;         // config.js:75
 constexpr double YUKAWA_COUPLING = 14;       // config.js:80
 constexpr int    QT_CAPACITY = 4;            // config.js:59
 constexpr int    HISTORY_SIZE = 256;         // config.js:120
@@ -94,6 +96,9 @@ struct Particle {                              // particle.js:15-92 (fields on t
     double creationTime = -INF, deathTime = INF;
     double axMod = 1, yukMod = 1, higgsMod = 1;
     double pe = 0;                             // this particle's share of _peAccum
+    double baseMass = 1;                       // particle.js:48 (scaled by annihilation, summed by merges)
+    bool antimatter = false;                   // particle.js:50
+    bool dead = false;                         // removed by a collision this substep, still a tree source
     History h;
 
     void setMass(double m) {                   // Particle.updateColor (particle.js:110-121), non-BH
@@ -294,6 +299,10 @@ struct Sim {
     int64_t interactions = 0;
     int nextId = 0;
     int nThreads = 1;
+    int nTree = 0;                             // particles in the last tree (ghost points start there)
+    // collision results of the last update (collisions.js:24-107)
+    std::vector<std::array<double, 6>> events; // type (1 annihilation, 2 merge), x, y, energy, px, py
+    int nMerges = 0, nAnnihilations = 0, nSpawned = 0, nRemovedCol = 0;
     std::string err;
 
     bool on(uint32_t bit) const { return (prm.toggles & bit) != 0; }
@@ -314,8 +323,8 @@ struct Sim {
     // tree point accessors
     int nReal() const { return (int)ps.size(); }
     void ptPos(int i, double& x, double& y) const {
-        if (i < nReal()) { x = ps[i].x; y = ps[i].y; }
-        else { x = ghosts[i - nReal()].x; y = ghosts[i - nReal()].y; }
+        if (i < nTree) { x = ps[i].x; y = ps[i].y; }
+        else { x = ghosts[i - nTree].x; y = ghosts[i - nTree].y; }
     }
 
     // ---- ghosts (integrator.js:176-244) ----
@@ -396,12 +405,12 @@ struct Sim {
                 for (int i = 0; i < cnt; i++) {
                     int pt = t.points[idx * QT_CAPACITY + i];
                     double pm, q, mu, L, x, y, wx, wy;
-                    if (pt < nReal()) {
+                    if (pt < nTree) {
                         const Particle& p = ps[pt];
                         pm = p.mass; q = p.charge; mu = p.magMoment; L = p.angMomentum;
                         x = p.x; y = p.y; wx = p.wx; wy = p.wy;
                     } else {
-                        const Ghost& g = ghosts[pt - nReal()];
+                        const Ghost& g = ghosts[pt - nTree];
                         pm = g.mass; q = g.charge; mu = g.magMoment; L = g.angMomentum;
                         x = g.x; y = g.y; wx = g.wx; wy = g.wy;
                     }
@@ -432,10 +441,11 @@ struct Sim {
     }
 
     int buildTree() {
+        nTree = nReal();
         if (periodic() && !(prm.flags & GEON_FLAG_NO_GHOSTS)) generateGhosts(); else ghosts.clear();
         const double bxr = prm.off_x + prm.domain_w / 2, byr = prm.off_y + prm.domain_h / 2;  // integrator.js:727-730
         const double bwr = prm.domain_w * 2, bhr = prm.domain_h * 2;
-        int nPts = nReal() + (int)ghosts.size();
+        int nPts = nTree + (int)ghosts.size();
         tree.count = 0;
         tree.overflow = false;
         // Guard against the reference's unbounded subdivision on >= 5 coincident points.
@@ -448,6 +458,157 @@ struct Sim {
         calculateMassDistribution(r);
         root = r;
         return r;
+    }
+
+    // ---- QuadTreePool.query (quadtree.js:372-404): points in the closed box
+    // (rx +/- rw, ry +/- rh), depth first with children pushed NW, NE, SW, SE.
+    void query(double rx, double ry, double rw, double rh, std::vector<int>& found, std::vector<int>& qs) const {
+        const QuadTree& t = tree;
+        found.clear();
+        if (root < 0) return;
+        qs.clear();
+        qs.push_back(root);
+        while (!qs.empty()) {
+            const int ni = qs.back(); qs.pop_back();
+            if (rx - rw > t.bx[ni] + t.bw[ni] || rx + rw < t.bx[ni] - t.bw[ni] ||     // _intersects, quadtree.js:112-117
+                ry - rh > t.by[ni] + t.bh[ni] || ry + rh < t.by[ni] - t.bh[ni]) continue;
+            if (!t.divided[ni]) {
+                for (int i = 0; i < t.pointCount[ni]; i++) {
+                    const int pt = t.points[ni * QT_CAPACITY + i];
+                    double x, y; ptPos(pt, x, y);
+                    if (x >= rx - rw && x <= rx + rw && y >= ry - rh && y <= ry + rh) found.push_back(pt);
+                }
+            } else {
+                qs.push_back(t.nw[ni]); qs.push_back(t.ne[ni]);
+                qs.push_back(t.sw[ni]); qs.push_back(t.se[ni]);
+            }
+        }
+    }
+
+    // ---- merge collisions (collisions.js:24-158, integrator.js:1350-1381) ----
+    static double particleKE(const Particle& p) {                 // collisions.js:17-20
+        const double wSq = p.wx * p.wx + p.wy * p.wy;
+        return wSq / (std::sqrt(1 + wSq) + 1) * p.mass;
+    }
+    struct Spawn { double x, y, wx, wy, mass, baseMass, charge, angw, ke; bool antimatter; };
+    static Spawn resolveMerge(Particle& p1, Particle& p2, double miDx, double miDy) {   // collisions.js:110-158
+        Spawn s;
+        const double totalMass = p1.mass + p2.mass;
+        s.wx = (p1.mass * p1.wx + p2.mass * p2.wx) / totalMass;
+        s.wy = (p1.mass * p1.wy + p2.mass * p2.wy) / totalMass;
+        const double p2x = p1.x + miDx, p2y = p1.y + miDy;
+        s.x = (p1.x * p1.mass + p2x * p2.mass) / totalMass;
+        s.y = (p1.y * p1.mass + p2y * p2.mass) / totalMass;
+        const double dx1 = p1.x - s.x, dy1 = p1.y - s.y;
+        const double dx2 = p2x - s.x, dy2 = p2y - s.y;
+        const double Lorb = dx1 * (p1.mass * p1.wy) - dy1 * (p1.mass * p1.wx)
+                          + dx2 * (p2.mass * p2.wy) - dy2 * (p2.mass * p2.wx);
+        const double Lspin = INERTIA_K * p1.mass * p1.radius * p1.radius * p1.angw
+                           + INERTIA_K * p2.mass * p2.radius * p2.radius * p2.angw;
+        const double newRadius = std::cbrt(totalMass);
+        const double newI = INERTIA_K * totalMass * newRadius * newRadius;
+        s.angw = newI > EPS ? (Lorb + Lspin) / newI : 0;
+        s.baseMass = p1.baseMass + p2.baseMass;
+        s.charge = p1.charge + p2.charge;
+        s.antimatter = p1.antimatter;
+        s.mass = totalMass;
+        const double wSq = s.wx * s.wx + s.wy * s.wy;
+        s.ke = wSq / (std::sqrt(1 + wSq) + 1) * totalMass;
+        p1.mass = 0; p2.mass = 0;                   // both die; charge, radius, velocity stay as they were
+        p1.baseMass = 0; p2.baseMass = 0;
+        return s;
+    }
+
+    // handleCollisions in COL_MERGE mode over the tree just built.  Removed
+    // particles are flagged `dead` and spawns are appended; the particle list is
+    // compacted after the substep's force pass (compactDead), which leaves the
+    // force pass exactly as the reference runs it: the removed particles are no
+    // longer targets but remain in the tree with their live fields, and the
+    // spawns are targets but not in the tree.
+    void handleCollisions() {
+        const bool per = periodic();
+        const int topo = prm.topology;
+        const double W = prm.domain_w, H = prm.domain_h;
+        const int n = nReal();
+        std::vector<int> cand, qs;
+        std::vector<Spawn> spawns;
+        int ann = 0;
+        for (int ci = 0; ci < n; ci++) {
+            Particle& p1 = ps[ci];
+            if (p1.mass == 0) continue;
+            query(p1.x, p1.y, p1.radius * 2, p1.radius * 2, cand, qs);
+            for (int pt : cand) {
+                const bool isGhost = pt >= nTree;
+                const int r2 = isGhost ? ghosts[pt - nTree].orig : pt;
+                Particle& p2 = ps[r2];
+                if (r2 == ci || p2.mass == 0 || p1.id >= p2.id) continue;
+                double qx, qy; ptPos(pt, qx, qy);
+                double dx, dy;
+                if (per) { Vec d = minImage(p1.x, p1.y, qx, qy, topo, W, H, W * 0.5, H * 0.5); dx = d.x; dy = d.y; }
+                else { dx = qx - p1.x; dy = qy - p1.y; }
+                const double distSq = dx * dx + dy * dy;
+                const double minDist = p1.radius + p2.radius;
+                if (!(distSq < minDist * minDist)) continue;
+                if (p1.antimatter != p2.antimatter) {             // collisions.js:60-80
+                    const double a = std::min(p1.mass, p2.mass);
+                    const double f1 = a / p1.mass, f2 = a / p2.mass;
+                    const double ke = f1 * particleKE(p1) + f2 * particleKE(p2);
+                    events.push_back({ 1.0, p1.x + dx * 0.5, p1.y + dy * 0.5, 2 * a + ke,
+                                       (p1.wx + p2.wx) * a, (p1.wy + p2.wy) * a });
+                    ann++;
+                    const double m1 = p1.mass, m2 = p2.mass;
+                    p1.mass -= a; p2.mass -= a;
+                    if (m1 > 0) p1.baseMass *= p1.mass / m1;
+                    if (m2 > 0) p2.baseMass *= p2.mass / m2;
+                    p1.setMass(p1.mass);                          // updateColor (particle.js:110-121)
+                    p2.setMass(p2.mass);
+                } else {                                          // collisions.js:81-91
+                    const double keBefore = particleKE(p1) + particleKE(p2);
+                    Spawn s = resolveMerge(p1, p2, dx, dy);
+                    const double keLost = std::max(0.0, keBefore - s.ke);
+                    if (keLost > 0) events.push_back({ 2.0, s.x, s.y, keLost, 0.0, 0.0 });
+                    spawns.push_back(s);
+                }
+            }
+        }
+        nAnnihilations += ann;
+        nMerges += (int)spawns.size();
+        if (ann == 0 && spawns.empty()) return;
+        for (int i = 0; i < n; i++)                                // collisions.js:96-104
+            if (ps[i].mass == 0) { ps[i].dead = true; nRemovedCol++; }
+        const bool rel = relOn();
+        for (const Spawn& s : spawns) {                            // integrator.js:1363-1381, main.js:504-523
+            Particle q;
+            q.id = nextId++;
+            q.x = s.x; q.y = s.y;
+            q.setMass(s.mass);
+            q.baseMass = s.baseMass;
+            const double cq = s.charge / BOSON_CHARGE;             // Math.round: nearest, ties up
+            double rq = std::floor(cq);
+            if (cq - rq >= 0.5) rq += 1;
+            q.charge = rq * BOSON_CHARGE;
+            q.antimatter = s.antimatter;
+            q.creationTime = simTime;
+            q.wx = s.wx; q.wy = s.wy;
+            q.angw = s.angw;
+            q.angVel = rel ? angwToAngVel(q.angw, q.radius) : q.angw;
+            const double invG = rel ? 1 / std::sqrt(1 + s.wx * s.wx + s.wy * s.wy) : 1;
+            q.vx = s.wx * invG; q.vy = s.wy * invG;
+            if (per) wrapPosition(q, topo, W, H);
+            ps.push_back(q);
+            nSpawned++;
+        }
+    }
+
+    // Drops the particles removed by this substep's collisions, keeping order.
+    void compactDead() {
+        size_t w = 0;
+        for (size_t i = 0; i < ps.size(); i++) {
+            if (ps[i].dead) continue;
+            if (w != i) ps[w] = std::move(ps[i]);
+            w++;
+        }
+        ps.resize(w);
     }
 
     // ---- signal-delay.js ----
@@ -732,20 +893,20 @@ struct Sim {
                 for (int i = 0; i < t.pointCount[nodeIdx]; i++) {
                     int other = t.points[nodeIdx * QT_CAPACITY + i];
                     if (other == pi) continue;
-                    const bool isGhost = other >= nReal();
-                    const int realIdx = isGhost ? ghosts[other - nReal()].orig : other;
+                    const bool isGhost = other >= nTree;
+                    const int realIdx = isGhost ? ghosts[other - nTree].orig : other;
                     if (isGhost && realIdx == pi) continue;
                     const Particle& real = ps[realIdx];
                     double sx, sy, svx, svy, sAngVel, sMag, sAng, oMass, oCharge;
                     bool delayed;
-                    if (isGhost) { const Ghost& g = ghosts[other - nReal()]; oMass = g.mass; oCharge = g.charge; }
+                    if (isGhost) { const Ghost& g = ghosts[other - nTree]; oMass = g.mass; oCharge = g.charge; }
                     else { oMass = real.mass; oCharge = real.charge; }
                     if (useSignalDelay) {
                         if (real.h.count < 2) continue;
                         Delayed ret;
                         if (!getDelayedState(real, px, py, ret)) continue;
                         if (isGhost) {
-                            const Ghost& g = ghosts[other - nReal()];
+                            const Ghost& g = ghosts[other - nTree];
                             sx = ret.x + (g.x - real.x); sy = ret.y + (g.y - real.y);
                         } else { sx = ret.x; sy = ret.y; }
                         svx = ret.vx; svy = ret.vy;
@@ -756,7 +917,7 @@ struct Sim {
                         delayed = true;
                     } else {
                         if (isGhost) {
-                            const Ghost& g = ghosts[other - nReal()];
+                            const Ghost& g = ghosts[other - nTree];
                             sx = g.x; sy = g.y; svx = g.vx; svy = g.vy;
                             sAngVel = g.angVel; sMag = g.magMoment; sAng = g.angMomentum;
                         } else {
@@ -805,7 +966,7 @@ struct Sim {
                 double gP = 0, eP = 0, yP = 0;
                 for (int i = 0; i < t.pointCount[nodeIdx]; i++) {
                     const int other = t.points[nodeIdx * QT_CAPACITY + i];
-                    if (other >= nReal()) continue;                 // ghosts: periodic images (heatmap.js:60)
+                    if (other >= nTree) continue;                   // ghosts: periodic images (heatmap.js:60)
                     const Particle& q = ps[other];
                     double pdx, pdy;
                     if (useDelay) {
@@ -923,8 +1084,12 @@ struct Sim {
         const Toggles tg = toggles();
         const int n = nReal();
         for (auto& p : ps) p.pe = 0;
+        // Particles removed by this substep's collisions are no longer in the
+        // particle list: they are neither targets nor re-cached, but stay tree
+        // sources with their live fields (collisions.js:98-107).
         for (int i = 0; i < n; i++) {                        // forces.js:71-76
             Particle& p = ps[i];
+            if (p.dead) continue;
             const double rSq = p.bodyRadiusSq;
             p.magMoment = MAG_MOMENT_K * p.charge * p.angVel * rSq;
             p.angMomentum = INERTIA_K * p.mass * p.angVel * rSq;
@@ -940,7 +1105,7 @@ struct Sim {
                     std::vector<int> stack;
                     stack.reserve(256);
 #pragma omp for schedule(dynamic, 64)
-                    for (int i = 0; i < n; i++) calculateForce(i, tg, useSignalDelay, cutSq, stack, inter);
+                    for (int i = 0; i < n; i++) if (!ps[i].dead) calculateForce(i, tg, useSignalDelay, cutSq, stack, inter);
                 }
             }
         } else {
@@ -949,8 +1114,9 @@ struct Sim {
 #pragma omp parallel for num_threads(nThreads) schedule(dynamic, 16) reduction(+:inter)
             for (int i = 0; i < n; i++) {
                 Particle& p = ps[i];
+                if (p.dead) continue;
                 for (int j = 0; j < n; j++) {
-                    if (i == j) continue;
+                    if (i == j || ps[j].dead) continue;
                     const Particle& o = ps[j];
                     double sx, sy, svx, svy, sAngVel, sMag, sAng;
                     if (useSignalDelay) {
@@ -974,7 +1140,7 @@ struct Sim {
         }
         interactions = inter;
         double s = 0;
-        for (auto& p : ps) s += p.pe;
+        for (auto& p : ps) if (!p.dead) s += p.pe;
         pe = s * 0.5;                                        // forces.js:26
     }
 
@@ -1048,8 +1214,8 @@ struct Sim {
                 for (int i = 0; i < t.pointCount[nodeIdx]; i++) {
                     int other = t.points[nodeIdx * QT_CAPACITY + i];
                     if (other == pi) continue;
-                    const bool isGhost = other >= nReal();
-                    const int realIdx = isGhost ? ghosts[other - nReal()].orig : other;
+                    const bool isGhost = other >= nTree;
+                    const int realIdx = isGhost ? ghosts[other - nTree].orig : other;
                     if (isGhost && realIdx == pi) continue;
                     const Particle& real = ps[realIdx];
                     double sx, sy, svx, svy, oMass, oCharge;
@@ -1060,7 +1226,7 @@ struct Sim {
                         sx = ret.x; sy = ret.y; svx = ret.vx; svy = ret.vy;
                         oMass = real.mass; oCharge = real.charge;
                     } else {
-                        const Ghost& g = ghosts[other - nReal()];
+                        const Ghost& g = ghosts[other - nTree];
                         sx = g.x; sy = g.y; svx = g.vx; svy = g.vy;
                         oMass = g.mass; oCharge = g.charge;
                     }
@@ -1166,6 +1332,8 @@ struct Sim {
 
     // ---- Physics.update (integrator.js:726-1825), in-scope part ----
     int update(double dt) {
+        events.clear();
+        nMerges = nAnnihilations = nSpawned = nRemovedCol = 0;
         const int n0 = nReal();
         const bool relOn_ = relOn();
         const Toggles tg = toggles();
@@ -1174,7 +1342,7 @@ struct Sim {
             forcePass(true);
             forcesInit = true;
         }
-        const int n = nReal();
+        int n = nReal();
         const bool hasGrav = on(GEON_GRAVITY), hasMagnetic = on(GEON_MAGNETIC), hasGM = on(GEON_GRAVITOMAG);
         const bool hasExtBz = prm.ext_bz != 0;
         double dtRemain = dt;
@@ -1309,10 +1477,13 @@ struct Sim {
                 }
             }
             if (!haveVVTree) buildTree();                            // integrator.js:1340-1347
+            const bool merge = prm.collision_mode == GEON_COL_MERGE;
+            if (merge) handleCollisions();                           // integrator.js:1350-1381
             resetForces();                                           // integrator.js:1490-1493
             computeAllForces();
             applyExternalFields();
             if (prm.boundary_mode == GEON_BOUND_BOUNCE) applyBoundaryForces();
+            if (merge) { compactDead(); n = nReal(); }
         }
         lastSubsteps = totalSteps;
         if (relOn_ && n > 0 && ++histStride >= HISTORY_STRIDE) {    // integrator.js:1550-1565
@@ -1392,6 +1563,7 @@ int oracle_add_particles(void* h, int n, const double* x, const double* y, const
         p.id = s->nextId++;
         p.x = x[i]; p.y = y[i];
         p.setMass(mass[i]);
+        p.baseMass = mass[i];
         p.charge = charge[i];
         p.wx = wx[i]; p.wy = wy[i];
         if (rel) {
@@ -1407,6 +1579,34 @@ int oracle_add_particles(void* h, int n, const double* x, const double* y, const
 }
 
 int oracle_count(void* h) { return (int)static_cast<Sim*>(h)->ps.size(); }
+
+// Antimatter flags and base masses of the first n particles (null: unchanged).
+void oracle_set_matter(void* h, int n, const int* antimatter, const double* base_mass) {
+    Sim* s = static_cast<Sim*>(h);
+    for (int i = 0; i < n && i < (int)s->ps.size(); i++) {
+        if (antimatter) s->ps[i].antimatter = antimatter[i] != 0;
+        if (base_mass) s->ps[i].baseMass = base_mass[i];
+    }
+}
+int oracle_get_matter(void* h, int* antimatter, double* base_mass, int cap) {
+    Sim* s = static_cast<Sim*>(h);
+    const int n = std::min(cap, (int)s->ps.size());
+    for (int i = 0; i < n; i++) { antimatter[i] = s->ps[i].antimatter ? 1 : 0; base_mass[i] = s->ps[i].baseMass; }
+    return n;
+}
+// Collision events of the last update, 6 doubles each (type, x, y, energy,
+// px, py); returns the number of events (all of them, even beyond cap).
+int oracle_collision_events(void* h, double* out, int cap) {
+    Sim* s = static_cast<Sim*>(h);
+    for (int k = 0; k < (int)s->events.size() && k < cap; k++)
+        for (int c = 0; c < 6; c++) out[(size_t)k * 6 + c] = s->events[k][c];
+    return (int)s->events.size();
+}
+// merges, annihilations, spawned particles, removed particles of the last update
+void oracle_collision_counts(void* h, int* out) {
+    Sim* s = static_cast<Sim*>(h);
+    out[0] = s->nMerges; out[1] = s->nAnnihilations; out[2] = s->nSpawned; out[3] = s->nRemovedCol;
+}
 void oracle_set_sim_time(void* h, double t) { static_cast<Sim*>(h)->simTime = t; }
 double oracle_sim_time(void* h) { return static_cast<Sim*>(h)->simTime; }
 int oracle_last_substeps(void* h) { return static_cast<Sim*>(h)->lastSubsteps; }
@@ -1519,7 +1719,7 @@ int oracle_build_tree(void* h, int* n_nodes) {
     Sim* s = static_cast<Sim*>(h);
     s->buildTree();
     if (n_nodes) *n_nodes = s->tree.count;
-    return s->nReal() + (int)s->ghosts.size();
+    return s->nTree + (int)s->ghosts.size();
 }
 int oracle_tree_overflow(void* h) { return static_cast<Sim*>(h)->tree.overflow ? 1 : 0; }
 
@@ -1540,6 +1740,20 @@ int oracle_tree_leaves(void* h, int* leaf_of_point, int n_points, double* lbx, d
         nl++;
     }
     return nl;
+}
+// Storage slot of each tree point inside its leaf (-1 if dropped): the order
+// in which QuadTreePool.query reports a leaf's points (quadtree.js:386-393).
+void oracle_tree_leaf_slots(void* h, int* slot_of_point, int n_points) {
+    Sim* s = static_cast<Sim*>(h);
+    const QuadTree& t = s->tree;
+    for (int i = 0; i < n_points; i++) slot_of_point[i] = -1;
+    for (int idx = 0; idx < t.count; idx++) {
+        if (t.divided[idx]) continue;
+        for (int k = 0; k < t.pointCount[idx]; k++) {
+            const int pt = t.points[idx * QT_CAPACITY + k];
+            if (pt >= 0 && pt < n_points) slot_of_point[pt] = k;
+        }
+    }
 }
 // Ghost originals in generation order.
 int oracle_ghost_origins(void* h, int* orig, int cap) {

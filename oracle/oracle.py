@@ -78,6 +78,11 @@ def load() -> C.CDLL:
         "oracle_delayed_state": ([v, i, d, d, P(d)], i),
         "oracle_compute_forces_subset": ([v, P(C.c_int), i], C.c_longlong),
         "oracle_heatmap": ([v, d, d, d, d, i, C.c_uint, i, P(d), P(d), P(d)], None),
+        "oracle_set_matter": ([v, i, P(C.c_int), P(d)], None),
+        "oracle_tree_leaf_slots": ([v, P(C.c_int), i], None),
+        "oracle_get_matter": ([v, P(C.c_int), P(d), i], i),
+        "oracle_collision_events": ([v, P(d), i], i),
+        "oracle_collision_counts": ([v, P(C.c_int)], None),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -184,6 +189,12 @@ class OracleSim:
         nl = self.lib.oracle_tree_leaves(self._h, _ip(lop), n_points, _dp(bx), _dp(by), _dp(bw), _ip(lv), cap)
         return lop[:n_points], bx[:nl], by[:nl], bw[:nl], lv[:nl]
 
+    def leaf_slots(self, n_points: int) -> np.ndarray:
+        """Storage slot of each tree point in its leaf (insertion history order)."""
+        out = np.zeros(max(n_points, 1), dtype=np.int32)
+        self.lib.oracle_tree_leaf_slots(self._h, _ip(out), n_points)
+        return out[:n_points]
+
     def ghost_origins(self) -> np.ndarray:
         n = self.lib.oracle_ghost_origins(self._h, None, 0)
         out = np.zeros(max(n, 1), dtype=np.int32)
@@ -241,6 +252,33 @@ class OracleSim:
         self.lib.oracle_heatmap(self._h, left, top, cell_w, cell_h, grid, fields, 1 if blur else 0,
                                 *[_dp(a) for a in out])
         return {k: a.reshape(grid, grid) for k, a in zip(("gravity", "electric", "yukawa"), out)}
+
+    def set_matter(self, antimatter=None, base_mass=None):
+        """Antimatter flags / base masses of the particles (None: unchanged)."""
+        n = self.count()
+        am = None if antimatter is None else np.ascontiguousarray(antimatter, dtype=np.int32)
+        bm = None if base_mass is None else np.ascontiguousarray(base_mass, dtype=np.float64)
+        self.lib.oracle_set_matter(self._h, n, None if am is None else _ip(am), None if bm is None else _dp(bm))
+
+    def matter(self) -> dict:
+        n = self.count()
+        am = np.zeros(max(n, 1), dtype=np.int32)
+        bm = np.zeros(max(n, 1))
+        self.lib.oracle_get_matter(self._h, _ip(am), _dp(bm), max(n, 1))
+        return {"antimatter": am[:n].astype(bool), "base_mass": bm[:n]}
+
+    def collision_events(self) -> np.ndarray:
+        """Events of the last update: rows (type, x, y, energy, px, py);
+        type 1 annihilation, 2 merge."""
+        k = self.lib.oracle_collision_events(self._h, None, 0)
+        out = np.zeros((max(k, 1), 6))
+        self.lib.oracle_collision_events(self._h, _dp(out), k)
+        return out[:k]
+
+    def collision_counts(self) -> dict:
+        out = np.zeros(4, dtype=np.int32)
+        self.lib.oracle_collision_counts(self._h, _ip(out))
+        return dict(zip(("merges", "annihilations", "spawned", "removed"), out.tolist()))
 
     def set_forces_init(self, v: bool):
         self.lib.oracle_set_forces_init(self._h, 1 if v else 0)

@@ -39,6 +39,7 @@ BARNES_HUT = 1 << 14
 
 BOUND_DESPAWN, BOUND_BOUNCE, BOUND_LOOP = 0, 1, 2
 TORUS, KLEIN, RP2 = 0, 1, 2
+COL_PASS, COL_MERGE, COL_BOUNCE = 0, 1, 2
 
 FLAG_PE = 1 << 0
 FLAG_BREAKDOWN = 1 << 1
@@ -78,7 +79,7 @@ class GeonParams(C.Structure):
         ("ext_electric_angle", C.c_double),
         ("ext_bz", C.c_double),
         ("max_substeps", C.c_int32),
-        ("reserved", C.c_int32),
+        ("collision_mode", C.c_int32),
     ]
 
 
@@ -117,11 +118,12 @@ class GeonProfile(C.Structure):
 def make_params(toggles=GRAVITY | COULOMB, flags=0, boundary_mode=BOUND_DESPAWN, topology=TORUS,
                 domain_w=100.0, domain_h=100.0, off_x=0.0, off_y=0.0, theta=0.5, softening=8.0,
                 yukawa_mu=0.15, bounce_friction=0.4, ext_gravity=0.0, ext_gravity_angle=np.pi * 0.5,
-                ext_electric=0.0, ext_electric_angle=0.0, ext_bz=0.0, max_substeps=32) -> GeonParams:
+                ext_electric=0.0, ext_electric_angle=0.0, ext_bz=0.0, max_substeps=32,
+                collision_mode=COL_PASS) -> GeonParams:
     """GeonParams with the reference's defaults (src/config.js, src/integrator.js:65-99)."""
     return GeonParams(toggles, flags, boundary_mode, topology, domain_w, domain_h, off_x, off_y, theta,
                       softening, yukawa_mu, bounce_friction, ext_gravity, ext_gravity_angle, ext_electric,
-                      ext_electric_angle, ext_bz, max_substeps, 0)
+                      ext_electric_angle, ext_bz, max_substeps, collision_mode)
 
 
 class GeonError(RuntimeError):
