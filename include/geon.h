@@ -357,6 +357,47 @@ int geon_batch_autotune(GeonHandle* h, double dt, int32_t frames, int32_t* choic
 int geon_heatmap(GeonHandle* h, double left, double top, double cell_w, double cell_h, int32_t grid, uint32_t fields,
                  int32_t blur, float* grav, float* elec, float* yuk);
 
+/* ---- merge collisions (GeonParams.collision_mode = GEON_COL_MERGE) ------
+ * handleCollisions (src/collisions.js:24-158) runs after every substep's
+ * tree rebuild, as Physics.update does (src/integrator.js:1350-1381):
+ * overlapping particles merge (mass, proper momentum and charge add, orbital
+ * plus spin angular momentum becomes spin) or, for matter against
+ * antimatter, annihilate the smaller mass.  Merged particles are appended
+ * after the survivors with new ids and creation time now, as
+ * Simulation.addParticle makes them (main.js:504-523).  The annihilation
+ * photons and field excitations the reference emits from these events are
+ * not part of this library; the events are returned instead. */
+
+/* Antimatter flags (0 / 1) and base masses (Particle.antimatter, .baseMass,
+ * src/particle.js:48-50) of particles [first, first + count); either array
+ * may be NULL to leave that field.  Particles start as matter with
+ * base mass = mass (GPUPhysics.addParticle's antimatter field,
+ * src/gpu/gpu-physics.js:1857-1870). */
+int geon_set_matter(GeonHandle* h, int32_t first, int32_t count, const int32_t* antimatter, const float* base_mass);
+int geon_get_matter(GeonHandle* h, int32_t* antimatter, float* base_mass, int32_t capacity, int32_t* n);
+
+/* Collision counts of the last geon_update. */
+typedef struct GeonCollisionInfo {
+    int32_t merges;          /* merged pairs (each appends one particle)                 */
+    int32_t annihilations;   /* matter-antimatter contacts                               */
+    int32_t spawned;         /* particles appended                                       */
+    int32_t removed;         /* particles whose mass reached zero                        */
+    int32_t candidates;      /* overlap candidates examined                              */
+    int32_t events;          /* events stored for geon_collision_events (<= 65536)       */
+    int32_t events_dropped;  /* events beyond that                                       */
+    int32_t order_approx;    /* 1 if a leaf at the 31-level depth cap held > 4 points:
+                                its candidates were taken in insertion-index order       */
+} GeonCollisionInfo;
+int geon_collision_info(GeonHandle* h, GeonCollisionInfo* out);
+
+/* The last geon_update's events, the arrays handleCollisions returns
+ * (collisions.js:9-14): rows of 6 doubles (type, x, y, energy, px, py),
+ * type 1 = annihilation (energy 2 m + kinetic, the photon burst of
+ * integrator.js:1387-1393) and 2 = merge (kinetic energy lost, the field
+ * excitation of integrator.js:1394-1414; px = py = 0).  Copies
+ * min(events, capacity) rows; `n` receives the number stored. */
+int geon_collision_events(GeonHandle* h, double* events, int32_t capacity, int32_t* n);
+
 /* Copies `rows` rows (GEON_OUT_*) of per-particle force data, each `capacity`
  * floats, starting at row `first_row`. */
 int geon_download_forces(GeonHandle* h, int32_t first_row, int32_t rows,

@@ -105,6 +105,15 @@ class GeonTreeInfo(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class GeonCollisionInfo(C.Structure):
+    _fields_ = [(k, C.c_int32) for k in
+                ("merges", "annihilations", "spawned", "removed", "candidates", "events", "events_dropped",
+                 "order_approx")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class GeonProfile(C.Structure):
     _fields_ = [("tree_ms", C.c_double), ("force_ms", C.c_double), ("onepn_ms", C.c_double), ("push_ms", C.c_double),
                 ("tree_count", C.c_int64), ("force_count", C.c_int64), ("onepn_count", C.c_int64),
@@ -170,6 +179,10 @@ SIGNATURES = {
     "geon_batch_autotune": [_handle_t, C.c_double, C.c_int32, _P(C.c_int32), _P(C.c_double)],
     "geon_heatmap": [_handle_t, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_uint32, C.c_int32,
                      _P(C.c_float), _P(C.c_float), _P(C.c_float)],
+    "geon_set_matter": [_handle_t, C.c_int32, C.c_int32, _P(C.c_int32), _P(C.c_float)],
+    "geon_get_matter": [_handle_t, _P(C.c_int32), _P(C.c_float), C.c_int32, _P(C.c_int32)],
+    "geon_collision_info": [_handle_t, _P(GeonCollisionInfo)],
+    "geon_collision_events": [_handle_t, _P(C.c_double), C.c_int32, _P(C.c_int32)],
     "geon_download_forces": [_handle_t, C.c_int32, C.c_int32, _P(C.c_float), C.c_int32],
     "geon_build_tree": [_handle_t, _P(GeonTreeInfo)],
     "geon_tree_leaves": [_handle_t, _P(C.c_int32), C.c_int32, _P(C.c_double), _P(C.c_double), _P(C.c_double),

@@ -17,6 +17,7 @@
 #include "learn.cuh"
 #include "mlp.cuh"
 #include "batch.cuh"
+#include "collide.cuh"
 
 using namespace geon;
 
@@ -87,9 +88,12 @@ struct GeonHandle {
     GeonParams prm{};
     DevParams P{};
     int n_cap = 0;
+    int slots = 0;          // particle slots of S / S2: n_cap, or 2 n_cap once merge collisions are on
     int n = 0;
     cudaStream_t st = nullptr;
-    DevArena arena;         // state + control
+    DevArena arena;         // control
+    DevArena state_arena;   // S, S2 and the compaction buffers (reallocated when slots grow)
+    DevArena col_arena;     // merge-collision buffers (allocated when the merge mode is first used)
     DevArena tree_arena;    // tree buffers (reallocated when ghost capacity changes)
     DevArena hist_arena;    // history rings (allocated when relativity is first enabled)
     DevArena learn_arena;   // learned-correction weights and pair buffer
@@ -117,6 +121,14 @@ struct GeonHandle {
     long long histTotal = 0;
     int lastSubsteps = 0;
     int nextId = 0;
+    // merge collisions
+    CollBufs col{};
+    CollCtl* col_h = nullptr;       // pinned copy of col.cc
+    int col_cap_int = 0;            // tree node capacity the collision buffers were sized for
+    bool col_alloc = false;
+    bool col_tgt_active = false;    // the next force pass walks col.tgt2
+    int col_tgt_count = 0;
+    GeonCollisionInfo col_info{};
     // batched systems (nsys > 0)
     int nsys = 0;
     Batch* batch = nullptr;
@@ -196,6 +208,10 @@ static int validate_params(GeonHandle* h, const GeonParams& p) {
     if (!(p.theta >= 0)) return set_err(h, GEON_ERR_ARG, "theta must be >= 0");
     if (!(p.softening > 0)) return set_err(h, GEON_ERR_ARG, "softening must be > 0");
     if ((p.toggles & GEON_YUKAWA) && !(p.yukawa_mu > 0)) return set_err(h, GEON_ERR_ARG, "yukawa_mu must be > 0");
+    if (p.collision_mode < GEON_COL_PASS || p.collision_mode > GEON_COL_BOUNCE) return set_err(h, GEON_ERR_ARG, "collision_mode out of range");
+    if (p.collision_mode == GEON_COL_BOUNCE) return set_err(h, GEON_ERR_UNSUPPORTED, "the bounce collision mode (contact forces) is not part of this library");
+    if (p.collision_mode == GEON_COL_MERGE && (p.flags & GEON_FLAG_LEARN))
+        return set_err(h, GEON_ERR_UNSUPPORTED, "merge collisions and the learned correction cannot be combined");
     return GEON_OK;
 }
 
@@ -208,7 +224,7 @@ static void derive_params(GeonHandle* h) {
     P.periodic = p.boundary_mode == GEON_BOUND_LOOP;
     P.ghosts = P.periodic && !(p.flags & GEON_FLAG_NO_GHOSTS);
     P.rel = (p.toggles & GEON_RELATIVITY) ? 1 : 0;
-    P.n_cap = h->n_cap;
+    P.n_cap = h->slots;
     P.nsys = h->nsys;
     P.keyTop = h->nsys ? 10 : 2;
     P.keyLevels = h->nsys ? BATCH_KEY_LEVELS : KEY_LEVELS;
@@ -244,8 +260,57 @@ static void fill_state(DevArena& A, DevState& S, int cap) {
     S.spin = A.alloc<float4>(cap); S.mom = A.alloc<float2>(cap); S.force = A.alloc<float4>(cap);
     S.grad = A.alloc<float4>(cap); S.torque = A.alloc<float4>(cap); S.f1pn = A.alloc<float2>(cap);
     S.f1pnOld = A.alloc<float2>(cap); S.brk = A.alloc<float>((size_t)12 * cap); S.ctime = A.alloc<double>(cap);
-    S.id = A.alloc<int>(cap); S.hist_cnt = A.alloc<int>(cap);
+    S.id = A.alloc<int>(cap); S.hist_cnt = A.alloc<int>(cap); S.matter = A.alloc<float2>(cap);
     S.hist = nullptr; S.hist_angw = nullptr;
+}
+
+static bool merge_on(const GeonHandle* h) { return h->prm.collision_mode == GEON_COL_MERGE; }
+
+// Particle slots needed: a merge spawns its particle into a new slot while the
+// two it replaces stay in place until the end of the substep (each spawn
+// removes at least one particle, so 2 n_cap slots always suffice).
+static int slots_wanted(const GeonHandle* h) { return merge_on(h) ? 2 * h->n_cap : h->n_cap; }
+
+// (Re)allocates S, S2 and the compaction buffers with `slots` slots, keeping
+// the first n particles (every per-particle row; the history rings live in
+// their own arena and are not moved).
+static int alloc_state(GeonHandle* h, int slots) {
+    DevArena A;
+    DevState S{}, S2{};
+    fill_state(A, S, slots);
+    fill_state(A, S2, slots);
+    int* keep = A.alloc<int>(slots);
+    int* dst = A.alloc<int>(slots);
+    int* tmp = A.alloc<int>(scan_temp_ints(slots) + 16);
+    if (A.failed) { A.free_all(); return set_err(h, GEON_ERR_NOMEM, "state allocation failed"); }
+    cudaMemsetAsync(S.hist_cnt, 0, (size_t)slots * sizeof(int), h->st);
+    cudaMemsetAsync(S.brk, 0, (size_t)12 * slots * sizeof(float), h->st);
+    const size_t n = (size_t)h->n;
+    if (h->slots > 0 && n > 0) {
+        const DevState& O = h->S;
+        auto cp = [&](void* d, const void* s, size_t bytes) { return cudaMemcpyAsync(d, s, bytes, cudaMemcpyDeviceToDevice, h->st); };
+        cudaError_t e = cudaSuccess;
+        e = e ? e : cp(S.pos, O.pos, n * sizeof(float4));   e = e ? e : cp(S.pos_lo, O.pos_lo, n * sizeof(float2));
+        e = e ? e : cp(S.vel, O.vel, n * sizeof(float4));   e = e ? e : cp(S.spin, O.spin, n * sizeof(float4));
+        e = e ? e : cp(S.mom, O.mom, n * sizeof(float2));   e = e ? e : cp(S.force, O.force, n * sizeof(float4));
+        e = e ? e : cp(S.grad, O.grad, n * sizeof(float4)); e = e ? e : cp(S.torque, O.torque, n * sizeof(float4));
+        e = e ? e : cp(S.f1pn, O.f1pn, n * sizeof(float2)); e = e ? e : cp(S.f1pnOld, O.f1pnOld, n * sizeof(float2));
+        e = e ? e : cp(S.ctime, O.ctime, n * sizeof(double)); e = e ? e : cp(S.id, O.id, n * sizeof(int));
+        e = e ? e : cp(S.hist_cnt, O.hist_cnt, n * sizeof(int)); e = e ? e : cp(S.matter, O.matter, n * sizeof(float2));
+        for (int r = 0; r < 12 && !e; r++) e = cp(S.brk + (size_t)r * slots, O.brk + (size_t)r * h->slots, n * sizeof(float));
+        if (!e) e = cudaStreamSynchronize(h->st);
+        if (e) { A.free_all(); return cuda_check(h, e, "state copy"); }
+    }
+    S.hist = h->S.hist; S.hist_angw = h->S.hist_angw; S.sys = h->S.sys;
+    S2.hist = h->S2.hist; S2.hist_angw = h->S2.hist_angw; S2.sys = h->S2.sys;
+    if (h->slots > 0) cudaStreamSynchronize(h->st);
+    h->state_arena.free_all();
+    h->state_arena.ptrs.swap(A.ptrs);
+    h->S = S; h->S2 = S2;
+    h->keep = keep; h->dst = dst; h->cscan_tmp = tmp;
+    h->slots = slots;
+    h->P.n_cap = slots;
+    return GEON_OK;
 }
 
 static int ensure_history(GeonHandle* h) {
@@ -326,6 +391,7 @@ __global__ void init_particles_kernel(DevParams P, DevState S, const float* __re
         S.ctime[i] = ctime;
         S.id[i] = id0 + t;
         S.hist_cnt[i] = 0;
+        S.matter[i] = make_float2(m, 0.f);                                  // baseMass = mass, matter
         for (int rr = 0; rr < 12; rr++) S.brk[(size_t)rr * P.n_cap + i] = 0.f;
     }
 }
@@ -426,6 +492,10 @@ static ForceCtx make_ctx(GeonHandle* h) {
     C.pe = (h->prm.flags & GEON_FLAG_PE) ? 1 : 0;
     C.brk = (h->prm.flags & GEON_FLAG_BREAKDOWN) ? 1 : 0;
     C.bounce = h->prm.boundary_mode == GEON_BOUND_BOUNCE;
+    if (h->col_tgt_active) {            // force pass right after merge collisions
+        C.tgt_list = h->col.tgt2;
+        C.tgt_count = h->col_tgt_count;
+    }
     return C;
 }
 
@@ -561,12 +631,118 @@ static int run_force_pass(GeonHandle* h, bool rebuild) {
     return GEON_OK;
 }
 
-static int compact(GeonHandle* h) {
-    const int n = h->n;
+static int compact(GeonHandle* h, int n_slots = -1) {
+    const int n = n_slots < 0 ? h->n : n_slots;
     exclusive_scan(h->keep, h->dst, n, nullptr, nullptr, h->cscan_tmp, h->st, &h->lc);
-    launch_compact(h->S, h->S2, h->keep, h->dst, n, h->n_cap, h->hist_alloc, true, h->st, h->lc);
+    launch_compact(h->S, h->S2, h->keep, h->dst, n, h->slots, h->hist_alloc, true, h->st, h->lc);
     CKL();
     std::swap(h->S, h->S2);
+    return GEON_OK;
+}
+
+// ---- merge collisions (collide.cu) ------------------------------------------------------------
+// Buffers sized for the particle capacity and the tree's node capacity.
+static int ensure_collide(GeonHandle* h) {
+    if (h->col_alloc && h->col_cap_int == h->T.cap_int) return GEON_OK;
+    CK(cudaStreamSynchronize(h->st));
+    h->col_arena.free_all();
+    h->col_arena.failed = false;
+    h->col_alloc = false;
+    DevArena& A = h->col_arena;
+    CollBufs& B = h->col;
+    B = CollBufs{};
+    const int cap = h->n_cap;
+    B.cc = A.alloc<CollCtl>(1);
+    B.cnt = A.alloc<int>(cap);
+    B.off = A.alloc<int>(cap);
+    B.cap = (int)std::min<long long>((long long)cap * 8 + 4096, 1ll << 28);
+    B.cand = A.alloc<int2>(B.cap);
+    B.inv = A.alloc<int>(cap);
+    B.min5 = A.alloc<int>((size_t)h->T.cap_int * 5);
+    B.m5cnt = A.alloc<int>(h->T.cap_int);
+    B.tflag = A.alloc<int>(cap);
+    B.tpos = A.alloc<int>(cap);
+    B.tgt2 = A.alloc<int>((size_t)2 * cap);
+    B.events = A.alloc<double>((size_t)COL_EVENT_CAP * 6);
+    B.scan_tmp = A.alloc<int>(scan_temp_ints(cap) + 16);
+    if (A.failed) { A.free_all(); B = CollBufs{}; return set_err(h, GEON_ERR_NOMEM, "collision buffer allocation failed"); }
+    if (!h->col_h && cudaMallocHost(&h->col_h, sizeof(CollCtl)) != cudaSuccess) {
+        h->col_h = nullptr;
+        return set_err(h, GEON_ERR_NOMEM, "pinned allocation failed");
+    }
+    CK(cudaMemsetAsync(B.cc, 0, sizeof(CollCtl), h->st));
+    h->col_cap_int = h->T.cap_int;
+    h->col_alloc = true;
+    return GEON_OK;
+}
+
+// handleCollisions for one substep, over the tree just built
+// (integrator.js:1350-1381).  With Barnes-Hut the removed particles stay in
+// their slots (they are still tree sources) and the spawns sit in slots n,
+// n+1, ...: the force pass then walks the collision target list and
+// collide_finish compacts after it.  The pairwise sum reads its sources from
+// the particle slots, so there the compaction happens at once.  `spawned`
+// stays -1 when no compaction is pending.
+static int collide_step(GeonHandle* h, int& spawned, int& removed) {
+    spawned = -1;
+    removed = 0;
+    int r = ensure_collide(h);
+    if (r) return r;
+    CollBufs& B = h->col;
+    const int n = h->n;
+    collide_detect(h->P, h->S, h->T, h->d_root, h->ctl, B, h->n_cap, h->st, h->lc);
+    CKL();
+    collide_resolve(h->P, h->S, h->T, h->ctl, B, h->keep, n, h->slots, h->simTime, h->nextId, h->n_cap, h->st, h->lc);
+    CKL();
+    CK(cudaMemcpyAsync(h->col_h, B.cc, sizeof(CollCtl), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    const CollCtl c = *h->col_h;
+    if (c.err & (COL_ERR_CAND_OVERFLOW | COL_ERR_SLOTS | COL_ERR_QUERY)) {
+        std::string why = (c.err & COL_ERR_CAND_OVERFLOW) ? "more overlap candidates than " + std::to_string(B.cap) :
+                          (c.err & COL_ERR_SLOTS) ? "no slot for a merged particle" : "tree query failed";
+        return set_err(h, GEON_ERR_OVERFLOW, "merge collisions: " + why);
+    }
+    GeonCollisionInfo& I = h->col_info;
+    I.merges += c.merges;
+    I.annihilations += c.annihilations;
+    I.spawned += c.spawned;
+    I.removed += c.removed;
+    I.candidates += c.total;
+    I.events = c.events;
+    I.events_dropped = c.events_dropped;
+    I.order_approx |= (c.err & COL_ERR_ORDER) ? 1 : 0;
+    if (c.spawned + c.annihilations == 0) return GEON_OK;
+    h->nextId += c.spawned;
+    if (bh_on(h)) {
+        collide_targets(h->S, h->T, h->ctl, B, n, c.spawned, h->n_cap, h->st, h->lc);
+        CKL();
+        h->col_tgt_active = true;
+        h->col_tgt_count = n - c.removed + c.spawned;
+        set_n_kernel<<<1, 1, 0, h->st>>>(h->ctl, n + c.spawned);
+        h->lc.add(1);
+        spawned = c.spawned;
+        removed = c.removed;
+        return GEON_OK;
+    }
+    r = compact(h, n + c.spawned);
+    if (r) return r;
+    h->n = n - c.removed + c.spawned;
+    set_n_kernel<<<1, 1, 0, h->st>>>(h->ctl, h->n);
+    h->lc.add(1);
+    return GEON_OK;
+}
+
+// Compaction after the force pass that followed the collisions (keep flags
+// were written by the resolution): removed particles leave, spawns follow the
+// survivors in spawn order (collisions.js:96-104, integrator.js:1363-1371).
+static int collide_finish(GeonHandle* h, int spawned, int removed) {
+    h->col_tgt_active = false;
+    const int n = h->n;
+    int r = compact(h, n + spawned);
+    if (r) return r;
+    h->n = n - removed + spawned;
+    set_n_kernel<<<1, 1, 0, h->st>>>(h->ctl, h->n);
+    h->lc.add(1);
     return GEON_OK;
 }
 
@@ -592,16 +768,11 @@ int geon_create(const GeonParams* params, int32_t max_particles, GeonHandle** ou
         g_err = "cudaStreamCreate failed"; delete h; return GEON_ERR_CUDA;
     }
     DevArena& A = h->arena;
-    fill_state(A, h->S, h->n_cap);
-    fill_state(A, h->S2, h->n_cap);
     h->ctl = A.alloc<FrameCtl>(1);
     h->d_root = A.alloc<int>(1);
     h->hist_t = A.alloc<double>(HIST_LEN);
     h->hist_age = A.alloc<float>(HIST_LEN);
     h->hist_segdt = A.alloc<float>(HIST_LEN);
-    h->keep = A.alloc<int>(h->n_cap);
-    h->dst = A.alloc<int>(h->n_cap);
-    h->cscan_tmp = A.alloc<int>(scan_temp_ints(h->n_cap) + 16);
     h->staging = A.alloc<float>((size_t)GEON_ST_ROWS * h->n_cap);
     h->staging_d = A.alloc<double>((size_t)GEON_ST_ROWS * h->n_cap);
     h->stats_d = A.alloc<double>(16);
@@ -615,8 +786,8 @@ int geon_create(const GeonParams* params, int32_t max_particles, GeonHandle** ou
     }
     cudaMemsetAsync(h->ctl, 0, sizeof(FrameCtl), h->st);
     cudaMemsetAsync(h->hist_t, 0, HIST_LEN * sizeof(double), h->st);
-    cudaMemsetAsync(h->S.hist_cnt, 0, h->n_cap * sizeof(int), h->st);
-    cudaMemsetAsync(h->S.brk, 0, (size_t)12 * h->n_cap * sizeof(float), h->st);
+    r = alloc_state(h, slots_wanted(h));
+    if (r) { g_err = h->err; geon_destroy(h); return r; }
     r = ensure_history(h);
     if (!r) r = ensure_tree(h);
     if (r) { g_err = h->err; geon_destroy(h); return r; }
@@ -631,6 +802,9 @@ int geon_destroy(GeonHandle* h) {
     h->tree_arena.free_all();
     h->hist_arena.free_all();
     h->learn_arena.free_all();
+    h->state_arena.free_all();
+    h->col_arena.free_all();
+    if (h->col_h) cudaFreeHost(h->col_h);
     if (h->pairs) cudaFree(h->pairs);
     if (h->batch) {
         Batch* B = h->batch;
@@ -669,6 +843,10 @@ int geon_set_params(GeonHandle* h, const GeonParams* params) {
     }
     h->prm = p;
     derive_params(h);
+    if (h->slots < slots_wanted(h)) {
+        r = alloc_state(h, slots_wanted(h));
+        if (r) return r;
+    }
     r = ensure_history(h);
     if (r) return r;
     return ensure_tree(h);
@@ -1036,6 +1214,68 @@ int geon_mlp_train(GeonHandle* h, float* weights, const float* x, const float* t
     return r ? r : read_ctl(h);
 }
 
+__global__ void set_matter_kernel(DevState S, int first, int count, const float* __restrict__ rows, int has_anti,
+                                  int has_base) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+        float2 m = S.matter[first + t];
+        if (has_anti) m.y = rows[t] != 0.f ? 1.f : 0.f;
+        if (has_base) m.x = rows[count + t];
+        S.matter[first + t] = m;
+    }
+}
+
+int geon_set_matter(GeonHandle* h, int32_t first, int32_t count, const int32_t* antimatter, const float* base_mass) {
+    if (!h || first < 0 || count < 0 || (long long)first + count > h->n)
+        return set_err(h, GEON_ERR_ARG, "matter range outside the particles");
+    if (count == 0 || (!antimatter && !base_mass)) return GEON_OK;
+    std::vector<float> rows((size_t)2 * count, 0.f);
+    for (int t = 0; t < count; t++) {
+        if (antimatter) rows[t] = antimatter[t] ? 1.f : 0.f;
+        if (base_mass) rows[count + t] = base_mass[t];
+    }
+    // the staging area holds GEON_ST_ROWS x n_cap floats >= 2 * count
+    CK(cudaMemcpyAsync(h->staging, rows.data(), rows.size() * sizeof(float), cudaMemcpyHostToDevice, h->st));
+    set_matter_kernel<<<grid_for(count, 256), 256, 0, h->st>>>(h->S, first, count, h->staging, antimatter ? 1 : 0,
+                                                               base_mass ? 1 : 0);
+    CKL();
+    h->lc.add(1);
+    CK(cudaStreamSynchronize(h->st));
+    return GEON_OK;
+}
+
+int geon_get_matter(GeonHandle* h, int32_t* antimatter, float* base_mass, int32_t capacity, int32_t* n) {
+    if (!h || capacity < 0 || !n) return GEON_ERR_ARG;
+    const int cnt = std::min(capacity, h->n);
+    *n = h->n;
+    if (cnt == 0) return GEON_OK;
+    std::vector<float2> m(cnt);
+    CK(cudaMemcpyAsync(m.data(), h->S.matter, cnt * sizeof(float2), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    for (int i = 0; i < cnt; i++) {
+        if (antimatter) antimatter[i] = m[i].y != 0.f ? 1 : 0;
+        if (base_mass) base_mass[i] = m[i].x;
+    }
+    return GEON_OK;
+}
+
+int geon_collision_info(GeonHandle* h, GeonCollisionInfo* out) {
+    if (!h || !out) return GEON_ERR_ARG;
+    *out = h->col_info;
+    return GEON_OK;
+}
+
+int geon_collision_events(GeonHandle* h, double* events, int32_t capacity, int32_t* n) {
+    if (!h || !n || capacity < 0 || (capacity > 0 && !events)) return GEON_ERR_ARG;
+    const int stored = h->col_info.events;
+    *n = stored;
+    const int cnt = std::min(capacity, stored);
+    if (cnt > 0) {
+        CK(cudaMemcpyAsync(events, h->col.events, (size_t)cnt * 6 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+    }
+    return GEON_OK;
+}
+
 int geon_heatmap(GeonHandle* h, double left, double top, double cell_w, double cell_h, int32_t grid, uint32_t fields,
                  int32_t blur, float* grav, float* elec, float* yuk) {
     if (!h || grid < 1 || grid > 4096 || !grav || !elec || !yuk) return GEON_ERR_ARG;
@@ -1076,7 +1316,7 @@ int geon_download_forces(GeonHandle* h, int32_t first_row, int32_t rows, float* 
         // staging holds GEON_ST_ROWS rows of n_cap floats: pack in chunks of that many rows
         for (int r0 = 0; r0 < rows; r0 += GEON_ST_ROWS) {
             const int rr = std::min(GEON_ST_ROWS, rows - r0);
-            pack_forces_kernel<<<grid_for(cnt, 256), 256, 0, h->st>>>(h->S, cnt, first_row + r0, rr, h->n_cap, h->n_cap, h->staging);
+            pack_forces_kernel<<<grid_for(cnt, 256), 256, 0, h->st>>>(h->S, cnt, first_row + r0, rr, h->n_cap, h->slots, h->staging);
             CKL();
             h->lc.add(1);
             for (int r = 0; r < rr; r++)
@@ -1161,6 +1401,15 @@ int geon_update(GeonHandle* h, double dt, int32_t* substeps) {
     const bool bh = bh_on(h);
     const int maxSub = p.max_substeps;
     const double EPS = 1e-12;
+    const bool merge = merge_on(h);
+    h->col_tgt_active = false;
+    h->col_info = GeonCollisionInfo{};
+    if (merge) {
+        r = ensure_tree(h);
+        if (!r) r = ensure_collide(h);
+        if (r) return r;
+        CK(cudaMemsetAsync(h->col.cc, 0, sizeof(CollCtl), h->st));
+    }
     if (!h->forcesInit && h->n > 0) {                                      // integrator.js:750-782
         bootstrap_angvel_kernel<<<grid_for(h->n, 256), 256, 0, h->st>>>(h->P, h->S, h->ctl);
         CKL();
@@ -1218,10 +1467,17 @@ int geon_update(GeonHandle* h, double dt, int32_t* substeps) {
             launch_vv_kick(h->P, h->S, h->ctl, (float)(dtSub * 0.5), h->n_cap, h->st, h->lc);
             CKL();
         }
+        int colSpawned = -1, colRemoved = 0;
+        if (merge) {                                                       // integrator.js:1340-1381
+            if (!haveTree) { r = build_tree(h); if (r) return r; haveTree = true; }
+            r = collide_step(h, colSpawned, colRemoved);
+            if (r) { h->col_tgt_active = false; return r; }
+        }
         r = run_force_pass(h, !haveTree);                                  // integrator.js:1336-1348, 1489-1493
-        if (r) return r;
+        if (r) { h->col_tgt_active = false; return r; }
         r = read_ctl(h);
-        if (r) return r;
+        if (r) { h->col_tgt_active = false; return r; }
+        if (colSpawned >= 0) { r = collide_finish(h, colSpawned, colRemoved); if (r) return r; }
         if (h->prof) h->prof_acc.interactions += (int64_t)h->ctl_h->interactions;
         curAccel = bits_to_double(h->ctl_h->maxAccelSqBits);
         curCyc = bits_to_double(h->ctl_h->maxCycBits);
@@ -1476,6 +1732,8 @@ static int validate_batch_params(GeonHandle* h, const GeonParams& p) {
         return set_err(h, GEON_ERR_UNSUPPORTED, "batched systems need the loop or bounce boundary (despawning would reorder systems)");
     if (p.flags & GEON_FLAG_LEARN)
         return set_err(h, GEON_ERR_UNSUPPORTED, "batched systems run without the learned correction");
+    if (p.collision_mode != GEON_COL_PASS)
+        return set_err(h, GEON_ERR_UNSUPPORTED, "batched systems run without merge collisions (spawns would reorder systems)");
     return GEON_OK;
 }
 

@@ -284,7 +284,10 @@ __global__ void boundary_kernel(DevParams P, DevState S, FrameCtl* ctl, int* kee
     if ((threadIdx.x & 31) == 0 && removed) atomicAdd(&ctl->nRemoved, removed);
 }
 
-// Stable compaction: particle i moves to slot dst[i] when keep[i].
+// Stable compaction: particle i moves to slot dst[i] when keep[i].  `n_cap`
+// is the row stride of the force-breakdown rows.  History rings are copied
+// only for particles holding samples (a ring without samples is never read),
+// so slots beyond the ring capacity (merge spawns) are never touched there.
 __global__ void compact_kernel(DevState S, DevState D, const int* keep, const int* dst, int n, int n_cap,
                                int with_hist, int with_brk) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -293,11 +296,13 @@ __global__ void compact_kernel(DevState S, DevState D, const int* keep, const in
         D.pos[d] = S.pos[i]; D.pos_lo[d] = S.pos_lo[i]; D.vel[d] = S.vel[i]; D.spin[d] = S.spin[i];
         D.mom[d] = S.mom[i]; D.force[d] = S.force[i]; D.grad[d] = S.grad[i]; D.torque[d] = S.torque[i];
         D.f1pn[d] = S.f1pn[i]; D.f1pnOld[d] = S.f1pnOld[i]; D.ctime[d] = S.ctime[i]; D.id[d] = S.id[i];
-        D.hist_cnt[d] = S.hist_cnt[i];
+        D.matter[d] = S.matter[i];
+        const int hc = S.hist_cnt[i];
+        D.hist_cnt[d] = hc;
         if (with_brk) {
             for (int r = 0; r < 12; r++) D.brk[(size_t)r * n_cap + d] = S.brk[(size_t)r * n_cap + i];
         }
-        if (with_hist) {
+        if (with_hist && hc > 0) {
             const float4* hs = S.hist + (size_t)i * HIST_LEN;
             float4* hd = D.hist + (size_t)d * HIST_LEN;
             for (int k = 0; k < HIST_LEN; k++) hd[k] = hs[k];

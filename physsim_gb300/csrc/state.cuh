@@ -26,6 +26,7 @@ struct DevState {
     float*  hist_angw;// [n_cap][256]
     int*    hist_cnt; // samples held per particle
     int*    sys;      // system of each particle (batched handles; null otherwise)
+    float2* matter;   // baseMass, antimatter (1 or 0) (particle.js:48-50; merge collisions)
 };
 
 // Quadtree over particles + ghosts.

@@ -14,12 +14,17 @@ authoritative semantics:
     numbers it is given as w directly.
   * removeParticle removes the slot at once and later slots shift down (the
     CPU path's array compaction); ids from getParticleIds() stay stable.
-  * Scalar fields, bosons, collisions, heatmap, trails and rendering are not
-    part of this library; their GPUPhysics methods are inert stubs.
+  * Merge collisions run on the device with the CPU path's sequential
+    semantics (collisions.js:24-158); the annihilation photons and field
+    excitations they would emit are returned as events (collisionEvents)
+    instead.  The bounce mode's contact forces are not part of this library.
+  * Scalar fields, bosons, heatmap, trails and rendering are not part of
+    this library; their GPUPhysics methods are inert stubs.
 """
 from __future__ import annotations
 
 import math
+import warnings
 from typing import Any
 
 import numpy as np
@@ -79,7 +84,6 @@ class GeonGPUPhysics:
                          ext_electric_angle=0.0, ext_bz=0.0)
         self._bounceFriction = 0.4
         self._sys: GeonSystem | None = None
-        self._meta = {}             # particle id -> (baseMass, antimatter), kept for the save format
         self._stats = None
         self._selected = -1
         self._ready = False
@@ -101,7 +105,17 @@ class GeonGPUPhysics:
         return N.make_params(toggles=self._toggles, flags=self._flags, boundary_mode=self.boundaryMode,
                              topology=self.topologyMode, domain_w=self.domainW, domain_h=self.domainH,
                              off_x=self.offX, off_y=self.offY, theta=self._theta, softening=self._softening,
-                             yukawa_mu=self._yukawaMu, bounce_friction=self._bounceFriction, **self._ext)
+                             yukawa_mu=self._yukawaMu, bounce_friction=self._bounceFriction,
+                             collision_mode=self._library_collision_mode(), **self._ext)
+
+    def _library_collision_mode(self) -> int:
+        """Merge runs on the device; bounce (contact forces, integrator.js:669-684)
+        is not part of the library: the setting is kept for saving, the run
+        proceeds without contact forces and says so."""
+        if self._collisionMode == N.COL_BOUNCE:
+            warnings.warn("bounce collisions (contact forces) are not simulated by this backend", RuntimeWarning)
+            return N.COL_PASS
+        return int(self._collisionMode)
 
     def _sync(self):
         if self._sys:
@@ -129,8 +143,8 @@ class GeonGPUPhysics:
             if v is not None:
                 self._ext[key] = float(v)
         cm = _get(physics, "collisionMode", None)
-        if cm is not None:
-            self._collisionMode = cm
+        if cm is not None:          # COL_* number or the settings string (config.js:10-14)
+            self._collisionMode = self.COL_NAMES.index(cm) if cm in self.COL_NAMES else int(cm) if isinstance(cm, int) else 0
         self._sync()
 
     def setBoundary(self, boundaryMode: int, topologyMode: int = 0):
@@ -169,7 +183,8 @@ class GeonGPUPhysics:
         try:
             slot = self._sys.add([_get(p, "x")], [_get(p, "y")], [wx], [wy], [m], [q],
                                  [float(_get(p, "angw", 0.0))], creation_time=self.simTime)
-            self._meta[int(self._sys.ids()[slot])] = (m, bool(_get(p, "antimatter", False)))
+            if _get(p, "antimatter", False):
+                self._sys.set_matter(antimatter=[1], first=slot)
             return slot
         except N.GeonError as e:
             if e.code == N.GEON_ERR_FULL:
@@ -202,7 +217,7 @@ class GeonGPUPhysics:
                      ("disintegrationEnabled", 0), ("spinOrbitEnabled", N.SPIN_ORBIT), ("onePNEnabled", N.ONE_PN),
                      ("yukawaEnabled", N.YUKAWA), ("axionEnabled", N.AXION), ("expansionEnabled", 0),
                      ("higgsEnabled", N.HIGGS)]
-    COL_NAMES = ["pass", "bounce", "merge"]
+    COL_NAMES = ["pass", "merge", "bounce"]        # COL_PASS, COL_MERGE, COL_BOUNCE (config.js:10-12)
 
     def serialize(self, sim=None) -> dict:
         """The reference's save state (version 1, save-load.js:91-127): particles
@@ -213,10 +228,10 @@ class GeonGPUPhysics:
         keeps it on the device)."""
         st = self._sys.state(f64=True)
         n = st["x"].size
-        ids = self._sys.ids() if n else []
+        mt = self._sys.matter()
         parts = []
         for i in range(n):
-            base, anti = self._meta.get(int(ids[i]), (float(st["mass"][i]), False))
+            base, anti = mt["base_mass"][i], mt["antimatter"][i]
             parts.append({"x": float(st["x"][i]), "y": float(st["y"][i]), "wx": float(st["wx"][i]),
                           "wy": float(st["wy"][i]), "mass": float(st["mass"][i]), "baseMass": float(base),
                           "charge": float(st["charge"][i]), "angw": float(st["angw"][i]), "antimatter": bool(anti)})
@@ -264,7 +279,7 @@ class GeonGPUPhysics:
             self.boundaryMode = BOUND_NAMES.index(st["boundary"])
         if st.get("topology") in TOPO_NAMES:
             self.topologyMode = TOPO_NAMES.index(st["topology"])
-        col = "bounce" if st.get("collision") == "repel" else st.get("collision", "pass")   # save-load.js:180
+        col = "bounce" if st.get("collision") == "repel" else st.get("collision", "pass")   # save-load.js:183-184
         if col in self.COL_NAMES:
             self._collisionMode = self.COL_NAMES.index(col)
         self._sync()
@@ -272,15 +287,21 @@ class GeonGPUPhysics:
         f = lambda k, d=0.0: np.array([float(pp.get(k, d) if pp.get(k, d) is not None else d) for pp in parts])
         self._sys.upload_f64(f("x"), f("y"), f("wx"), f("wy"), f("mass", 1.0), f("charge"), f("angw"),
                              sim_time=float(state.get("simTime", 0.0) or 0.0))
-        ids = self._sys.ids() if parts else []
-        self._meta = {int(ids[i]): (float(pp.get("baseMass", pp.get("mass", 1.0)) or 1.0), bool(pp.get("antimatter", False)))
-                      for i, pp in enumerate(parts)}
+        if parts:
+            self._sys.set_matter(antimatter=np.array([1 if pp.get("antimatter", False) else 0 for pp in parts]),
+                                 base_mass=f("baseMass", 0.0) + np.where([pp.get("baseMass") is None for pp in parts],
+                                                                      f("mass", 1.0), 0.0))
         return True
 
     def reset(self):
         self._sys.reset()
         self._stats = None
-        self._meta = {}
+
+    def collisionEvents(self) -> np.ndarray:
+        """Events of the last update (rows type, x, y, energy, px, py; type 1
+        annihilation, 2 merge): what handleCollisions returns to the caller
+        for photon bursts and field excitations (integrator.js:1383-1414)."""
+        return self._sys.collision_events()
 
     # -- stats (gpu-physics.js:4146-4283) ----------------------------------------------------
     def requestStats(self, selectedGpuIdx: int = -1):

@@ -194,6 +194,39 @@ class GeonSystem:
                                        int(fields), 1 if blur else 0, *[N.fptr(a) for a in out]))
         return {k: a.reshape(grid, grid) for k, a in zip(("gravity", "electric", "yukawa"), out)}
 
+    def set_matter(self, antimatter=None, base_mass=None, first: int = 0):
+        """Antimatter flags / base masses of particles first, first+1, ... (None: unchanged)."""
+        arrs = [a for a in (antimatter, base_mass) if a is not None]
+        if not arrs:
+            return
+        k = len(arrs[0])
+        am = None if antimatter is None else np.ascontiguousarray(antimatter, dtype=np.int32)
+        bm = None if base_mass is None else np.ascontiguousarray(base_mass, dtype=np.float32)
+        self._ck(self.lib.geon_set_matter(self._h, int(first), int(k), None if am is None else N.iptr(am),
+                                          None if bm is None else N.fptr(bm)))
+
+    def matter(self) -> dict:
+        n = self.count()
+        am = np.zeros(max(n, 1), dtype=np.int32)
+        bm = np.zeros(max(n, 1), dtype=np.float32)
+        cnt = C.c_int32()
+        self._ck(self.lib.geon_get_matter(self._h, N.iptr(am), N.fptr(bm), max(n, 1), C.byref(cnt)))
+        return {"antimatter": am[:n].astype(bool), "base_mass": bm[:n]}
+
+    def collision_info(self) -> dict:
+        info = N.GeonCollisionInfo()
+        self._ck(self.lib.geon_collision_info(self._h, C.byref(info)))
+        return info.as_dict()
+
+    def collision_events(self) -> np.ndarray:
+        """Events of the last update: rows (type, x, y, energy, px, py);
+        type 1 annihilation, 2 merge."""
+        cnt = C.c_int32()
+        self._ck(self.lib.geon_collision_events(self._h, None, 0, C.byref(cnt)))
+        out = np.zeros((max(cnt.value, 1), 6))
+        self._ck(self.lib.geon_collision_events(self._h, N.dptr(out), cnt.value, C.byref(cnt)))
+        return out[:cnt.value]
+
     def forces(self) -> dict:
         n = self.count()
         cap = max(n, 1)

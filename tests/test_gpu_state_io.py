@@ -74,9 +74,10 @@ def test_loads_a_reference_format_file(gpu_lib):
              "higgsMass": 0.5, "extGravity": 0.0, "extGravityAngle": 1.0, "extElectric": 0.2,
              "extElectricAngle": 0.5, "extBz": 0.01}
     b = backend(cap=50)
-    assert b.deserialize(state)
+    with pytest.warns(RuntimeWarning, match="bounce"):
+        assert b.deserialize(state)
     assert b.getParticleCount() == 50                       # capacity caps the load (save-load.js:204)
-    assert b._collisionMode == 1 and b.boundaryMode == 1 and b.topologyMode == 1
+    assert b._collisionMode == N.COL_BOUNCE and b.boundaryMode == 1 and b.topologyMode == 1
     p = b._params()
     assert p.toggles & N.RELATIVITY and p.toggles & N.MAGNETIC and not p.toggles & N.BARNES_HUT
     assert p.bounce_friction == 0.7 and p.yukawa_mu == 0.3 and p.ext_electric == 0.2 and p.ext_bz == 0.01
