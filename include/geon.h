@@ -449,6 +449,8 @@ typedef struct GeonProfile {
     double learn_ms;         /* learned correction: pair collection + network        */
     int64_t learn_count;
     int64_t learn_pairs;     /* (cell, target) pairs corrected                        */
+    double collide_ms;       /* merge collisions: detection, resolution, target list  */
+    int64_t collide_count;
 } GeonProfile;
 
 /* enable = 1 clears the counters and starts recording; enable = 0 stops.

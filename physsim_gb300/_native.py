@@ -118,7 +118,8 @@ class GeonProfile(C.Structure):
     _fields_ = [("tree_ms", C.c_double), ("force_ms", C.c_double), ("onepn_ms", C.c_double), ("push_ms", C.c_double),
                 ("tree_count", C.c_int64), ("force_count", C.c_int64), ("onepn_count", C.c_int64),
                 ("push_count", C.c_int64), ("interactions", C.c_int64), ("particle_substeps", C.c_int64),
-                ("learn_ms", C.c_double), ("learn_count", C.c_int64), ("learn_pairs", C.c_int64)]
+                ("learn_ms", C.c_double), ("learn_count", C.c_int64), ("learn_pairs", C.c_int64),
+                ("collide_ms", C.c_double), ("collide_count", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

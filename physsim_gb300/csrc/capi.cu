@@ -147,7 +147,7 @@ struct GeonHandle {
     GeonProfile prof_acc{};
 };
 
-enum { PH_TREE = 0, PH_FORCE, PH_ONEPN, PH_PUSH, PH_LEARN };
+enum { PH_TREE = 0, PH_FORCE, PH_ONEPN, PH_PUSH, PH_LEARN, PH_COLLIDE };
 
 static cudaEvent_t get_event(GeonHandle* h) {
     if (!h->ev_pool.empty()) { cudaEvent_t e = h->ev_pool.back(); h->ev_pool.pop_back(); return e; }
@@ -179,6 +179,7 @@ static void prof_collect(GeonHandle* h) {
             case PH_FORCE: h->prof_acc.force_ms += ms; h->prof_acc.force_count++; break;
             case PH_ONEPN: h->prof_acc.onepn_ms += ms; h->prof_acc.onepn_count++; break;
             case PH_LEARN: h->prof_acc.learn_ms += ms; h->prof_acc.learn_count++; break;
+            case PH_COLLIDE: h->prof_acc.collide_ms += ms; h->prof_acc.collide_count++; break;
             default: h->prof_acc.push_ms += ms; h->prof_acc.push_count++; break;
         }
         h->ev_pool.push_back(pe.second.first);
@@ -655,16 +656,34 @@ static int ensure_collide(GeonHandle* h) {
     B.cc = A.alloc<CollCtl>(1);
     B.cnt = A.alloc<int>(cap);
     B.off = A.alloc<int>(cap);
-    B.cap = (int)std::min<long long>((long long)cap * 8 + 4096, 1ll << 28);
+    B.cap = (int)std::min<long long>((long long)cap * 4 + 4096, 1ll << 28);
     B.cand = A.alloc<int2>(B.cap);
+    B.uf = A.alloc<int>(cap);
+    B.skey = A.alloc<uint64_t>(B.cap); B.skey_alt = A.alloc<uint64_t>(B.cap);
+    B.sval = A.alloc<uint32_t>(B.cap); B.sval_alt = A.alloc<uint32_t>(B.cap);
+    B.sort_tmp = A.alloc<char>(radix_temp_bytes(B.cap));
+    int bits = 1;
+    while ((1ll << bits) < (long long)cap) bits++;
+    B.sort_bits = 32 + bits;
+    B.rec = A.alloc<PairRec>(B.cap);
+    B.kind = A.alloc<int>(B.cap);
+    B.sflag = A.alloc<int>(B.cap); B.spos = A.alloc<int>(B.cap);
+    B.eflag = A.alloc<int>(B.cap); B.epos = A.alloc<int>(B.cap);
     B.inv = A.alloc<int>(cap);
     B.min5 = A.alloc<int>((size_t)h->T.cap_int * 5);
+    B.ibox = A.alloc<float4>(h->T.cap_int);
+    B.lbox = A.alloc<float4>(h->T.cap_pts);
     B.m5cnt = A.alloc<int>(h->T.cap_int);
     B.tflag = A.alloc<int>(cap);
     B.tpos = A.alloc<int>(cap);
+    B.tk = A.alloc<int>(cap);
+    B.acnt = A.alloc<int>(cap);
+    B.abefore = A.alloc<int>(cap);
+    B.amin = A.alloc<int>(cap);
+    B.anch = A.alloc<int>(B.cap);
     B.tgt2 = A.alloc<int>((size_t)2 * cap);
     B.events = A.alloc<double>((size_t)COL_EVENT_CAP * 6);
-    B.scan_tmp = A.alloc<int>(scan_temp_ints(cap) + 16);
+    B.scan_tmp = A.alloc<int>(scan_temp_ints(std::max(cap, B.cap)) + 16);
     if (A.failed) { A.free_all(); B = CollBufs{}; return set_err(h, GEON_ERR_NOMEM, "collision buffer allocation failed"); }
     if (!h->col_h && cudaMallocHost(&h->col_h, sizeof(CollCtl)) != cudaSuccess) {
         h->col_h = nullptr;
@@ -690,16 +709,31 @@ static int collide_step(GeonHandle* h, int& spawned, int& removed) {
     if (r) return r;
     CollBufs& B = h->col;
     const int n = h->n;
+    const int pc = prof_begin(h, PH_COLLIDE);
     collide_detect(h->P, h->S, h->T, h->d_root, h->ctl, B, h->n_cap, h->st, h->lc);
-    CKL();
-    collide_resolve(h->P, h->S, h->T, h->ctl, B, h->keep, n, h->slots, h->simTime, h->nextId, h->n_cap, h->st, h->lc);
     CKL();
     CK(cudaMemcpyAsync(h->col_h, B.cc, sizeof(CollCtl), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
+    const int total = h->col_h->total;
+    if (h->col_h->err & COL_ERR_QUERY) { prof_end(h, pc); return set_err(h, GEON_ERR_OVERFLOW, "merge collisions: tree query failed"); }
+    if (total > B.cap) {
+        prof_end(h, pc);
+        return set_err(h, GEON_ERR_OVERFLOW, "merge collisions: " + std::to_string(total) +
+                       " overlap candidates, more than the " + std::to_string(B.cap) + " the buffers hold");
+    }
+    if (total == 0) {                                     // nothing touches: no resolution, no compaction
+        prof_end(h, pc);
+        h->col_info.order_approx |= (h->col_h->err & COL_ERR_ORDER) ? 1 : 0;
+        return GEON_OK;
+    }
+    collide_resolve(h->P, h->S, h->T, h->ctl, B, h->keep, n, total, h->slots, h->simTime, h->nextId, h->st, h->lc);
+    CKL();
+    prof_end(h, pc);
+    CK(cudaMemcpyAsync(h->col_h, B.cc, sizeof(CollCtl), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
     const CollCtl c = *h->col_h;
-    if (c.err & (COL_ERR_CAND_OVERFLOW | COL_ERR_SLOTS | COL_ERR_QUERY)) {
-        std::string why = (c.err & COL_ERR_CAND_OVERFLOW) ? "more overlap candidates than " + std::to_string(B.cap) :
-                          (c.err & COL_ERR_SLOTS) ? "no slot for a merged particle" : "tree query failed";
+    if (c.err & (COL_ERR_SLOTS | COL_ERR_QUERY)) {
+        std::string why = (c.err & COL_ERR_SLOTS) ? "no slot for a merged particle" : "pair components failed";
         return set_err(h, GEON_ERR_OVERFLOW, "merge collisions: " + why);
     }
     GeonCollisionInfo& I = h->col_info;
@@ -714,7 +748,7 @@ static int collide_step(GeonHandle* h, int& spawned, int& removed) {
     if (c.spawned + c.annihilations == 0) return GEON_OK;
     h->nextId += c.spawned;
     if (bh_on(h)) {
-        collide_targets(h->S, h->T, h->ctl, B, n, c.spawned, h->n_cap, h->st, h->lc);
+        collide_targets(h->S, h->T, h->ctl, B, n, total, c.spawned, h->n_cap, h->st, h->lc);
         CKL();
         h->col_tgt_active = true;
         h->col_tgt_count = n - c.removed + c.spawned;

@@ -141,6 +141,30 @@ def split_systems(wl: Workload) -> list:
     return [{k: v[off[s]:off[s + 1]] for k, v in wl.state.items()} for s in range(len(off) - 1)]
 
 
+def sparse_field(n: int = 65536, seed: int = 9, box: float | None = None, anti_frac: float = 0.05,
+                 theta: float = 0.5) -> Workload:
+    """Merge-collision workload: n particles uniform over a square box whose
+    side grows as sqrt(n) (2000 at n = 65536: mean spacing about 8, so about
+    one particle in ten touches a neighbour at radius cbrt(m) ~ 1 in the
+    first substep), lognormal(0, 0.5) masses, w ~ N(0, 0.05^2) per axis,
+    charges as the other workloads, a fraction `anti_frac` of antimatter
+    (info['antimatter']); gravity + Coulomb, Barnes-Hut, softening 8, merge
+    collisions, despawn boundary."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    L = box if box is not None else 2000.0 * np.sqrt(n / 65536.0)
+    x = rng.random(n) * L
+    y = rng.random(n) * L
+    m = rng.lognormal(0.0, 0.5, n)
+    q = _charges(rng, n)
+    wx = rng.normal(0, 0.05, n)
+    wy = rng.normal(0, 0.05, n)
+    anti = (rng.random(n) < anti_frac).astype(np.int32)
+    st = _pack(x, y, wx, wy, m, q, np.zeros(n))
+    p = N.make_params(toggles=N.GRAVITY | N.COULOMB | N.BARNES_HUT, boundary_mode=N.BOUND_DESPAWN, domain_w=L,
+                      domain_h=L, theta=theta, softening=8.0, collision_mode=N.COL_MERGE)
+    return Workload("sparse_field_n%d" % n, p, st, 1 / 60, 10, {"box": L, "antimatter": anti})
+
+
 def plummer_disk(n: int = 1 << 20, seed: int = 3, theta: float = 0.5, softening: float = 8.0,
                  a: float = 50.0, background: float = 0.05) -> Workload:
     """Large plain BH: 2-D Plummer-like disk (surface density (1+r^2/a^2)^-2,
