@@ -502,7 +502,76 @@ def run_configs(args, g_big, wl_big, idx, fx, fy, fp32_peak):
                           "interactions_per_particle": inter / wl_big.n, "walk_tflops": tf,
                           "walk_frac_of_fp32_peak": tf / fp32_peak if fp32_peak else None}
     out["plummer_disk_n1048576_theta_sweep"] = sweep
+    out["sparse_field_merge"] = run_merge()
     return out
+
+
+def run_merge():
+    """Merge collisions (collision_mode = merge) on the sparse field: the
+    first frame resolves the initial overlaps (about a tenth of the
+    particles), later frames a few dozen merges each.  Per size: the first
+    frame, steady-state throughput with merges and without (pass mode, same
+    start), the collision phase per substep; at N = 65536 the CPU baseline of
+    the first frame (the FP64 oracle on all host threads)."""
+    import torch
+    from physsim_gb300 import _native as N, workloads as W
+    from physsim_gb300.system import GeonSystem
+    res = {}
+    for n in (1 << 16, 1 << 20):
+        wl = W.sparse_field(n)
+        entry = {"n": n, "box": wl.info["box"], "antimatter_fraction": 0.05, "theta": wl.params.theta}
+        for mode in ("merge", "pass"):
+            p = wl.params
+            p.collision_mode = N.COL_MERGE if mode == "merge" else N.COL_PASS
+            g = GeonSystem(p, n)
+            g.upload(*[wl.state[k] for k in STATE_KEYS])
+            g.set_matter(antimatter=wl.info["antimatter"])
+            g.compute_forces()
+            st = torch.cuda.ExternalStream(g.stream_ptr())
+            if mode == "merge":
+                g.synchronize()
+                g.profile(True)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                g.update(wl.dt)
+                e1.record(st)
+                e1.synchronize()
+                pr = g.profile(False)
+                entry["first_frame_ms"] = e0.elapsed_time(e1)
+                entry["first_frame_collide_ms"] = pr["collide_ms"]
+                entry["first_frame"] = g.collision_info()
+            g.profile(True)
+            secs, sub, lat = time_frames(g, wl.dt, 10, 2, st)
+            pr = g.profile(False)
+            entry[mode] = {"value": g.count() * sub / secs, "unit": UNIT, "frames": 10, "substeps": sub,
+                           "frame_ms_p50": float(np.percentile(lat, 50)),
+                           "force_ms": pr["force_ms"] / max(pr["force_count"], 1),
+                           "tree_ms": pr["tree_ms"] / max(pr["tree_count"], 1),
+                           "collide_ms_per_substep": pr["collide_ms"] / max(pr["collide_count"], 1)
+                           if mode == "merge" else 0.0,
+                           "particles": g.count()}
+            if mode == "merge":
+                entry[mode]["last_frame"] = g.collision_info()
+            g.close()
+        if n == 1 << 16:
+            from oracle import oracle
+            o = oracle.OracleSim(wl.params, threads=oracle.max_threads())
+            p = wl.params
+            p.collision_mode = N.COL_MERGE
+            o.set_params(p)
+            o.add(*[wl.state[k] for k in STATE_KEYS])
+            o.set_matter(antimatter=wl.info["antimatter"])
+            o.compute_forces()
+            o.set_forces_init(True)
+            t0 = time.perf_counter()
+            o.update(wl.dt)
+            entry["cpu_baseline"] = {"first_frame_s": time.perf_counter() - t0, "cores": oracle.max_threads(),
+                                     "kind": "port", "collisions": o.collision_counts(),
+                                     "sample": "the same first frame in the FP64 restatement of the reference "
+                                               "(tree, handleCollisions, force pass)"}
+            o.close()
+        res["n%d" % n] = entry
+    return res
 
 
 def run_native(args, ws, rank, local):
