@@ -66,6 +66,7 @@ extern "C" {
 #define GEON_FLAG_NO_GHOSTS   (1u << 2)  /* periodic BH without image ghosts (min-image only) */
 #define GEON_FLAG_SIMPLE_WALK (1u << 3)  /* one node per warp iteration (cross-check of the batched walk) */
 #define GEON_FLAG_LEARN       (1u << 4)  /* cell moments + learned far-field correction (when weights are set) */
+#define GEON_FLAG_BOSONS      (1u << 5)  /* Physics.bosonInterEnabled: boson gravity on particles in every force pass */
 
 /* Physics parameters.  Mirrors the Physics fields that Physics.update reads
  * (src/integrator.js:65-107, :726-736) plus theta/softening, which the

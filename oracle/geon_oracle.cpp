@@ -57,6 +57,7 @@ constexpr double INERTIA_K = 0.4;            // config.js:52
 constexpr double MAG_MOMENT_K = 0.2;         // config.js:53
 constexpr double TIDAL_STRENGTH = 64;        // config.js:54
 constexpr double BOSON_CHARGE = 0.1;         // config.js:75
+constexpr double BOSON_SOFTENING_SQ = 4;     // config.js:48
 constexpr double YUKAWA_COUPLING = 14;       // config.js:80
 constexpr int    QT_CAPACITY = 4;            // config.js:59
 constexpr int    HISTORY_SIZE = 256;         // config.js:120
@@ -303,6 +304,12 @@ struct Sim {
     // collision results of the last update (collisions.js:24-107)
     std::vector<std::array<double, 6>> events; // type (1 annihilation, 2 merge), x, y, energy, px, py
     int nMerges = 0, nAnnihilations = 0, nSpawned = 0, nRemovedCol = 0;
+    // boson pool (photons, pions, leptons as the Simulation holds them): the
+    // fields the boson tree and its walks read
+    struct Boson { double x, y, srcMass, srcCharge, vSq; int kind; };   // kind 0 photon, 1 massive
+    std::vector<Boson> bosons;
+    QuadTree btree;
+    int broot = -1;
     std::string err;
 
     bool on(uint32_t bit) const { return (prm.toggles & bit) != 0; }
@@ -1322,11 +1329,150 @@ struct Sim {
     }
 
     // One force pass at the current state (integrator.js:754-780 without fields/bosons).
+    // ---- boson tree (integrator.js:263-277, quadtree.js:316-368) ----
+    void buildBosonTree() {
+        broot = -1;
+        if (bosons.empty()) return;
+        const double bxr = prm.off_x + prm.domain_w / 2, byr = prm.off_y + prm.domain_h / 2;
+        const double bwr = prm.domain_w * 2, bhr = prm.domain_h * 2;
+        const int nb = (int)bosons.size();
+        btree.count = 0;
+        btree.overflow = false;
+        btree.nodeLimit = (size_t)64 * (nb + 16);
+        if (btree.bx.size() < (size_t)2 * nb + 16) btree.grow((size_t)2 * nb + 16);
+        const int r = btree.alloc(bxr, byr, bwr, bhr, 0);
+        std::vector<std::pair<int, int>> work;
+        auto pos = [this](int i, double& x, double& y) { x = bosons[i].x; y = bosons[i].y; };
+        for (int i = 0; i < nb; i++) btree.insert(r, i, pos, work);
+        // calculateBosonDistribution: post-order sums of _srcMass, _srcCharge, COM by _srcMass
+        QuadTree& t = btree;
+        std::vector<int> stack, order;
+        stack.push_back(r);
+        while (!stack.empty()) {
+            const int idx = stack.back(); stack.pop_back();
+            order.push_back(idx);
+            if (t.divided[idx]) { stack.push_back(t.nw[idx]); stack.push_back(t.ne[idx]); stack.push_back(t.sw[idx]); stack.push_back(t.se[idx]); }
+        }
+        for (int k = (int)order.size() - 1; k >= 0; k--) {
+            const int idx = order[k];
+            if (!t.divided[idx]) {
+                const int cnt = t.pointCount[idx];
+                if (cnt == 0) continue;
+                double mass = 0, charge = 0, cx = 0, cy = 0;
+                for (int i = 0; i < cnt; i++) {
+                    const Boson& b = bosons[t.points[idx * QT_CAPACITY + i]];
+                    mass += b.srcMass; charge += b.srcCharge;
+                    cx += b.x * b.srcMass; cy += b.y * b.srcMass;
+                }
+                t.totalMass[idx] = mass; t.totalCharge[idx] = charge;
+                if (mass > 0) { t.comX[idx] = cx / mass; t.comY[idx] = cy / mass; }
+            } else {
+                const int c0 = t.nw[idx], c1 = t.ne[idx], c2 = t.sw[idx], c3 = t.se[idx];
+                const double m0 = t.totalMass[c0], m1 = t.totalMass[c1], m2 = t.totalMass[c2], m3 = t.totalMass[c3];
+                const double mass = m0 + m1 + m2 + m3;
+                t.totalMass[idx] = mass;
+                t.totalCharge[idx] = t.totalCharge[c0] + t.totalCharge[c1] + t.totalCharge[c2] + t.totalCharge[c3];
+                if (mass > 0) {
+                    t.comX[idx] = (t.comX[c0] * m0 + t.comX[c1] * m1 + t.comX[c2] * m2 + t.comX[c3] * m3) / mass;
+                    t.comY[idx] = (t.comY[c0] * m0 + t.comY[c1] * m1 + t.comY[c2] * m2 + t.comY[c3] * m3) / mass;
+                }
+            }
+        }
+        broot = r;
+    }
+
+    // _walkBosonTreeCore (forces.js:713-770): softened monopole sum of the
+    // boson pool's mass (or charge) at (px, py), times `scale`.
+    Vec walkBosonTree(double px, double py, double scale, double softSq, bool byCharge) const {
+        const QuadTree& t = btree;
+        double kx = 0, ky = 0;
+        if (broot < 0) return { 0, 0 };
+        const bool per = periodic();
+        const double W = prm.domain_w, H = prm.domain_h;
+        const double thetaSq = prm.theta * prm.theta;
+        std::vector<int> stack;
+        stack.push_back(broot);
+        while (!stack.empty()) {
+            const int idx = stack.back(); stack.pop_back();
+            if (byCharge ? t.totalCharge[idx] == 0 : t.totalMass[idx] < EPS) continue;
+            double dx, dy;
+            if (per) { Vec d = minImage(px, py, t.comX[idx], t.comY[idx], prm.topology, W, H, W * 0.5, H * 0.5); dx = d.x; dy = d.y; }
+            else { dx = t.comX[idx] - px; dy = t.comY[idx] - py; }
+            const double dSq = dx * dx + dy * dy;
+            const double size = t.bw[idx] * 2;
+            const int cnt = t.pointCount[idx];
+            if (!t.divided[idx] && cnt > 0) {
+                for (int k = 0; k < cnt; k++) {
+                    const Boson& b = bosons[t.points[idx * QT_CAPACITY + k]];
+                    const double val = byCharge ? b.srcCharge : b.srcMass;
+                    if (byCharge && val == 0) continue;
+                    double bdx, bdy;
+                    if (per) { Vec d = minImage(px, py, b.x, b.y, prm.topology, W, H, W * 0.5, H * 0.5); bdx = d.x; bdy = d.y; }
+                    else { bdx = b.x - px; bdy = b.y - py; }
+                    const double rSq = bdx * bdx + bdy * bdy + softSq;
+                    const double invRSq = 1 / rSq;
+                    const double f = scale * val * std::sqrt(invRSq) * invRSq;
+                    kx += bdx * f; ky += bdy * f;
+                }
+            } else if (t.divided[idx] && size * size < thetaSq * dSq) {
+                const double rSq = dSq + softSq;
+                const double invRSq = 1 / rSq;
+                const double f = scale * (byCharge ? t.totalCharge[idx] : t.totalMass[idx]) * std::sqrt(invRSq) * invRSq;
+                kx += dx * f; ky += dy * f;
+            } else if (t.divided[idx]) {
+                stack.push_back(t.nw[idx]); stack.push_back(t.ne[idx]);
+                stack.push_back(t.sw[idx]); stack.push_back(t.se[idx]);
+            }
+        }
+        return { kx, ky };
+    }
+
+    bool bosonsOn() const { return (prm.flags & GEON_FLAG_BOSONS) && !bosons.empty(); }
+
+    // computeBosonGravity (forces.js:788-804): boson mass acting on the particles.
+    void bosonGravity() {
+        if (!bosonsOn() || !on(GEON_GRAVITY)) return;
+        buildBosonTree();
+        if (broot < 0 || btree.totalMass[broot] < EPS) return;
+        const double softSq = prm.softening * prm.softening;
+#pragma omp parallel for num_threads(nThreads) schedule(dynamic, 64)
+        for (int i = 0; i < nReal(); i++) {
+            Particle& p = ps[i];
+            if (p.dead) continue;
+            const Vec k = walkBosonTree(p.x, p.y, p.mass, softSq, false);
+            p.fx += k.x; p.fy += k.y;
+            p.comp[C_GRAV][0] += k.x; p.comp[C_GRAV][1] += k.y;
+        }
+    }
+
+    // The kicks of applyBosonBosonGravity (forces.js:812-856; photons 2 dt,
+    // massive bosons (1 + v^2) dt, before the photons' renormalisation) and
+    // applyPionPionCoulomb (forces.js:878-901; -q dt for charged massive bosons).
+    void bosonKicks(double dt, unsigned what, double* out) {
+        buildBosonTree();
+        const int nb = (int)bosons.size();
+        for (int i = 0; i < nb; i++) {
+            const Boson& b = bosons[i];
+            double kx = 0, ky = 0;
+            if ((what & 1) && broot >= 0 && btree.totalMass[broot] >= EPS && nb >= 2) {
+                const double scale = b.kind == 0 ? 2 * dt : (1 + b.vSq) * dt;
+                const Vec k = walkBosonTree(b.x, b.y, scale, BOSON_SOFTENING_SQ, false);
+                kx += k.x; ky += k.y;
+            }
+            if ((what & 2) && broot >= 0 && b.kind != 0 && b.srcCharge != 0 && nb >= 2) {
+                const Vec k = walkBosonTree(b.x, b.y, -b.srcCharge * dt, BOSON_SOFTENING_SQ, true);
+                kx += k.x; ky += k.y;
+            }
+            out[2 * i] = kx; out[2 * i + 1] = ky;
+        }
+    }
+
     void forcePass(bool rebuild) {
         resetForces();
         if (rebuild) buildTree();
         computeAllForces();
         applyExternalFields();
+        bosonGravity();                                          // integrator.js:773-777
         if (prm.boundary_mode == GEON_BOUND_BOUNCE) applyBoundaryForces();
     }
 
@@ -1482,6 +1628,7 @@ struct Sim {
             resetForces();                                           // integrator.js:1490-1493
             computeAllForces();
             applyExternalFields();
+            bosonGravity();                                          // integrator.js:1508-1513
             if (prm.boundary_mode == GEON_BOUND_BOUNCE) applyBoundaryForces();
             if (merge) { compactDead(); n = nReal(); }
         }
@@ -1579,6 +1726,19 @@ int oracle_add_particles(void* h, int n, const double* x, const double* y, const
 }
 
 int oracle_count(void* h) { return (int)static_cast<Sim*>(h)->ps.size(); }
+
+// Boson pool: n rows of 6 doubles (x, y, src_mass, src_charge, kind, vSq);
+// kind 0 = photon, 1 = pion or lepton.
+void oracle_set_bosons(void* h, int n, const double* rows) {
+    Sim* s = static_cast<Sim*>(h);
+    s->bosons.resize(n);
+    for (int i = 0; i < n; i++) {
+        const double* r = rows + (size_t)i * 6;
+        s->bosons[i] = { r[0], r[1], r[2], r[3], r[5], (int)r[4] };
+    }
+}
+// Kicks of the boson pool on itself (what: 1 gravity, 2 Coulomb), 2 doubles per boson.
+void oracle_boson_kicks(void* h, double dt, unsigned what, double* out) { static_cast<Sim*>(h)->bosonKicks(dt, what, out); }
 
 // Antimatter flags and base masses of the first n particles (null: unchanged).
 void oracle_set_matter(void* h, int n, const int* antimatter, const double* base_mass) {

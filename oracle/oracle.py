@@ -80,6 +80,8 @@ def load() -> C.CDLL:
         "oracle_heatmap": ([v, d, d, d, d, i, C.c_uint, i, P(d), P(d), P(d)], None),
         "oracle_set_matter": ([v, i, P(C.c_int), P(d)], None),
         "oracle_tree_leaf_slots": ([v, P(C.c_int), i], None),
+        "oracle_set_bosons": ([v, i, P(d)], None),
+        "oracle_boson_kicks": ([v, d, C.c_uint, P(d)], None),
         "oracle_get_matter": ([v, P(C.c_int), P(d), i], i),
         "oracle_collision_events": ([v, P(d), i], i),
         "oracle_collision_counts": ([v, P(C.c_int)], None),
@@ -279,6 +281,18 @@ class OracleSim:
         out = np.zeros(4, dtype=np.int32)
         self.lib.oracle_collision_counts(self._h, _ip(out))
         return dict(zip(("merges", "annihilations", "spawned", "removed"), out.tolist()))
+
+    def set_bosons(self, rows):
+        """Boson pool: rows (x, y, src_mass, src_charge, kind, vSq); kind 0 photon, 1 massive."""
+        rows = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1, 6)
+        self._bosons = len(rows)
+        self.lib.oracle_set_bosons(self._h, len(rows), _dp(rows))
+
+    def boson_kicks(self, dt: float, what: int = 3) -> np.ndarray:
+        n = getattr(self, "_bosons", 0)
+        out = np.zeros((max(n, 1), 2))
+        self.lib.oracle_boson_kicks(self._h, dt, what, _dp(out))
+        return out[:n]
 
     def set_forces_init(self, v: bool):
         self.lib.oracle_set_forces_init(self._h, 1 if v else 0)

@@ -46,6 +46,7 @@ FLAG_BREAKDOWN = 1 << 1
 FLAG_NO_GHOSTS = 1 << 2
 FLAG_SIMPLE_WALK = 1 << 3
 FLAG_LEARN = 1 << 4
+FLAG_BOSONS = 1 << 5
 MLP_NPARAM = 4930
 DIRECT_NOALLOC_MAX_K = 16384
 BATCH_MAX_SYSTEMS = 512
