@@ -377,6 +377,27 @@ int geon_heatmap(GeonHandle* h, double left, double top, double cell_w, double c
 int geon_set_matter(GeonHandle* h, int32_t first, int32_t count, const int32_t* antimatter, const float* base_mass);
 int geon_get_matter(GeonHandle* h, int32_t* antimatter, float* base_mass, int32_t capacity, int32_t* n);
 
+/* ---- boson pool (src/forces.js:697-901) ---------------------------------
+ * The photons, pions and leptons of the Simulation, as the boson tree reads
+ * them: n rows of 6 doubles (x, y, _srcMass, _srcCharge, kind, v^2), kind 0
+ * for photons and 1 for pions and leptons (only alive ones).  The pool's
+ * quadtree is built at once (Physics._buildBosonTree, integrator.js:263-277)
+ * and kept until the next call; n = 0 clears the pool.  With the
+ * GEON_FLAG_BOSONS flag and gravity on, every force pass of geon_update adds
+ * computeBosonGravity (forces.js:788-804) for this pool, which stays where it
+ * was uploaded for the whole frame (the reference moves bosons every
+ * substep).  No reference counterpart as an entry point: the reference keeps
+ * the pool in its Simulation object. */
+int geon_set_bosons(GeonHandle* h, int32_t n, const double* rows);
+
+/* The kicks the pool's bosons get from one another: what & 1 gravity
+ * (applyBosonBosonGravity, forces.js:812-856: 2 dt for photons, (1 + v^2) dt
+ * for pions and leptons, before the photons' speed renormalisation), what & 2
+ * Coulomb between charged pions and leptons (applyPionPionCoulomb,
+ * forces.js:878-901: -q dt).  kicks[2n] receives (dx, dy) per boson in
+ * upload order: photons add it to their velocity, pions and leptons to w. */
+int geon_boson_kicks(GeonHandle* h, double dt, uint32_t what, float* kicks);
+
 /* Collision counts of the last geon_update. */
 typedef struct GeonCollisionInfo {
     int32_t merges;          /* merged pairs (each appends one particle)                 */

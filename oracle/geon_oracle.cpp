@@ -1451,6 +1451,8 @@ struct Sim {
     void bosonKicks(double dt, unsigned what, double* out) {
         buildBosonTree();
         const int nb = (int)bosons.size();
+        int massive = 0;
+        for (const Boson& b : bosons) massive += b.kind != 0;
         for (int i = 0; i < nb; i++) {
             const Boson& b = bosons[i];
             double kx = 0, ky = 0;
@@ -1459,7 +1461,7 @@ struct Sim {
                 const Vec k = walkBosonTree(b.x, b.y, scale, BOSON_SOFTENING_SQ, false);
                 kx += k.x; ky += k.y;
             }
-            if ((what & 2) && broot >= 0 && b.kind != 0 && b.srcCharge != 0 && nb >= 2) {
+            if ((what & 2) && broot >= 0 && b.kind != 0 && b.srcCharge != 0 && massive >= 2) {   // nPi + nLe >= 2
                 const Vec k = walkBosonTree(b.x, b.y, -b.srcCharge * dt, BOSON_SOFTENING_SQ, true);
                 kx += k.x; ky += k.y;
             }

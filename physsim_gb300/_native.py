@@ -183,6 +183,8 @@ SIGNATURES = {
                      _P(C.c_float), _P(C.c_float), _P(C.c_float)],
     "geon_set_matter": [_handle_t, C.c_int32, C.c_int32, _P(C.c_int32), _P(C.c_float)],
     "geon_get_matter": [_handle_t, _P(C.c_int32), _P(C.c_float), C.c_int32, _P(C.c_int32)],
+    "geon_set_bosons": [_handle_t, C.c_int32, _P(C.c_double)],
+    "geon_boson_kicks": [_handle_t, C.c_double, C.c_uint32, _P(C.c_float)],
     "geon_collision_info": [_handle_t, _P(GeonCollisionInfo)],
     "geon_collision_events": [_handle_t, _P(C.c_double), C.c_int32, _P(C.c_int32)],
     "geon_download_forces": [_handle_t, C.c_int32, C.c_int32, _P(C.c_float), C.c_int32],

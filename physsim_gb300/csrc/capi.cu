@@ -18,6 +18,7 @@
 #include "mlp.cuh"
 #include "batch.cuh"
 #include "collide.cuh"
+#include "boson.cuh"
 
 using namespace geon;
 
@@ -129,6 +130,15 @@ struct GeonHandle {
     bool col_tgt_active = false;    // the next force pass walks col.tgt2
     int col_tgt_count = 0;
     GeonCollisionInfo col_info{};
+    // boson pool: a second handle holds it as particles (its tree is the boson tree)
+    GeonHandle* bos = nullptr;
+    int nb = 0;                     // bosons of the current pool
+    int nb_massive = 0;             // pions and leptons among them
+    DevArena boson_arena;
+    float2* bkind = nullptr;        // [bos->n_cap] kind, v^2
+    float2* bkick = nullptr;        // [bos->n_cap] kicks
+    double* biq = nullptr;          // exact node charges of the pool's tree
+    double* blq = nullptr;
     // batched systems (nsys > 0)
     int nsys = 0;
     Batch* batch = nullptr;
@@ -620,15 +630,41 @@ static int learned_force_pass(GeonHandle* h) {
     return GEON_OK;
 }
 
+static BosonTree boson_tree(GeonHandle* h) {
+    BosonTree B{};
+    B.T = h->bos->T;
+    B.ctl = h->bos->ctl;
+    B.d_root = h->bos->d_root;
+    B.S = h->bos->S;
+    B.kind = h->bkind;
+    B.iq = h->biq;
+    B.lq = h->blq;
+    B.n = h->nb;
+    return B;
+}
+
+static bool bosons_act(const GeonHandle* h) {
+    return (h->prm.flags & GEON_FLAG_BOSONS) && h->nb > 0 && h->bos && (h->prm.toggles & GEON_GRAVITY);
+}
+
 static int run_force_pass(GeonHandle* h, bool rebuild) {
     const bool bh = bh_on(h);
     if (bh && rebuild) { int r = build_tree(h); if (r) return r; }
     if (h->P.rel) { launch_hist_tables(h->hist_t, h->simTime, h->hist_age, h->hist_segdt, h->st, h->lc); CKL(); }
-    if (bh && learn_active(h)) return learned_force_pass(h);
-    const int ps = prof_begin(h, PH_FORCE);
-    force_pass(h->P, h->S, h->T, h->d_root, h->ctl, make_ctx(h), bh, h->n_cap, h->st, h->lc);
-    prof_end(h, ps);
-    CKL();
+    if (bh && learn_active(h)) {
+        int r = learned_force_pass(h);
+        if (r || !bosons_act(h)) return r;
+    } else {
+        const int ps = prof_begin(h, PH_FORCE);
+        force_pass(h->P, h->S, h->T, h->d_root, h->ctl, make_ctx(h), bh, h->n_cap, h->st, h->lc);
+        prof_end(h, ps);
+        CKL();
+    }
+    if (bosons_act(h)) {                      // computeBosonGravity (integrator.js:773-777, 1508-1513)
+        boson_gravity(h->P, h->S, h->ctl, boson_tree(h), h->col_tgt_active ? h->col.tgt2 : nullptr, h->col_tgt_count,
+                      (h->prm.flags & GEON_FLAG_BREAKDOWN) != 0, h->n_cap, h->st, h->lc);
+        CKL();
+    }
     return GEON_OK;
 }
 
@@ -838,6 +874,8 @@ int geon_destroy(GeonHandle* h) {
     h->learn_arena.free_all();
     h->state_arena.free_all();
     h->col_arena.free_all();
+    h->boson_arena.free_all();
+    if (h->bos) { geon_destroy(h->bos); h->bos = nullptr; }
     if (h->col_h) cudaFreeHost(h->col_h);
     if (h->pairs) cudaFree(h->pairs);
     if (h->batch) {
@@ -1310,6 +1348,70 @@ int geon_collision_events(GeonHandle* h, double* events, int32_t capacity, int32
     return GEON_OK;
 }
 
+int geon_set_bosons(GeonHandle* h, int32_t n, const double* rows) {
+    if (!h || n < 0 || (n > 0 && !rows)) return GEON_ERR_ARG;
+    if (h->batch) return set_err(h, GEON_ERR_UNSUPPORTED, "batched handles have no boson pool");
+    h->nb = 0;
+    h->nb_massive = 0;
+    if (n == 0) return GEON_OK;
+    GeonParams bp = h->prm;                   // the pool's tree: same root box, no ghosts (integrator.js:263-277)
+    bp.flags = GEON_FLAG_NO_GHOSTS;
+    bp.collision_mode = GEON_COL_PASS;
+    int r;
+    if (!h->bos || h->bos->n_cap < n) {
+        if (h->bos) { geon_destroy(h->bos); h->bos = nullptr; }
+        h->boson_arena.free_all();
+        h->boson_arena.failed = false;
+        int cap = 1024;
+        while (cap < n) cap *= 2;
+        r = geon_create(&bp, cap, &h->bos);
+        if (r) { h->bos = nullptr; return set_err(h, r, std::string("boson pool: ") + g_err); }
+        h->bkind = h->boson_arena.alloc<float2>(cap);
+        h->bkick = h->boson_arena.alloc<float2>(cap);
+        h->biq = h->boson_arena.alloc<double>(h->bos->T.cap_int);
+        h->blq = h->boson_arena.alloc<double>(h->bos->T.cap_pts);
+        if (h->boson_arena.failed) return set_err(h, GEON_ERR_NOMEM, "boson pool allocation failed");
+    } else {
+        r = geon_set_params(h->bos, &bp);
+        if (r) return set_err(h, r, std::string("boson pool: ") + h->bos->err);
+    }
+    std::vector<double> soa((size_t)GEON_ST_ROWS_IN * n, 0.0);
+    std::vector<float2> kind(n);
+    int massive = 0;
+    for (int i = 0; i < n; i++) {
+        const double* q = rows + (size_t)i * 6;
+        soa[i] = q[0];                        // x, y, (w = 0), mass = _srcMass, charge = _srcCharge, (angw = 0)
+        soa[(size_t)n + i] = q[1];
+        soa[(size_t)4 * n + i] = q[2];
+        soa[(size_t)5 * n + i] = q[3];
+        kind[i] = make_float2(q[4] != 0 ? 1.f : 0.f, (float)q[5]);
+        massive += q[4] != 0;
+    }
+    r = geon_upload_state_f64(h->bos, n, soa.data(), 0.0);
+    if (r) return set_err(h, r, std::string("boson pool: ") + h->bos->err);
+    r = build_tree(h->bos);
+    if (r) return set_err(h, r, std::string("boson pool: ") + h->bos->err);
+    r = read_ctl(h->bos);
+    if (r) return set_err(h, r, std::string("boson pool: ") + h->bos->err);
+    CK(cudaMemcpyAsync(h->bkind, kind.data(), n * sizeof(float2), cudaMemcpyHostToDevice, h->st));
+    h->nb = n;
+    boson_charges(boson_tree(h), h->biq, h->blq, h->st, h->lc);
+    CKL();
+    CK(cudaStreamSynchronize(h->st));
+    h->nb_massive = massive;
+    return GEON_OK;
+}
+
+int geon_boson_kicks(GeonHandle* h, double dt, uint32_t what, float* kicks) {
+    if (!h || (h->nb > 0 && !kicks)) return GEON_ERR_ARG;
+    if (h->nb == 0) return GEON_OK;
+    boson_kicks(h->P, boson_tree(h), (float)dt, what, h->nb_massive, h->bkick, h->st, h->lc);
+    CKL();
+    CK(cudaMemcpyAsync(kicks, h->bkick, (size_t)h->nb * sizeof(float2), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return GEON_OK;
+}
+
 int geon_heatmap(GeonHandle* h, double left, double top, double cell_w, double cell_h, int32_t grid, uint32_t fields,
                  int32_t blur, float* grav, float* elec, float* yuk) {
     if (!h || grid < 1 || grid > 4096 || !grav || !elec || !yuk) return GEON_ERR_ARG;
@@ -1768,6 +1870,8 @@ static int validate_batch_params(GeonHandle* h, const GeonParams& p) {
         return set_err(h, GEON_ERR_UNSUPPORTED, "batched systems run without the learned correction");
     if (p.collision_mode != GEON_COL_PASS)
         return set_err(h, GEON_ERR_UNSUPPORTED, "batched systems run without merge collisions (spawns would reorder systems)");
+    if (p.flags & GEON_FLAG_BOSONS)
+        return set_err(h, GEON_ERR_UNSUPPORTED, "batched systems run without a boson pool");
     return GEON_OK;
 }
 

@@ -213,6 +213,18 @@ class GeonSystem:
         self._ck(self.lib.geon_get_matter(self._h, N.iptr(am), N.fptr(bm), max(n, 1), C.byref(cnt)))
         return {"antimatter": am[:n].astype(bool), "base_mass": bm[:n]}
 
+    def set_bosons(self, rows):
+        """Boson pool: rows (x, y, src_mass, src_charge, kind, v^2); kind 0 photon, 1 pion or lepton."""
+        rows = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1, 6)
+        self._nb = len(rows)
+        self._ck(self.lib.geon_set_bosons(self._h, len(rows), N.dptr(rows) if len(rows) else None))
+
+    def boson_kicks(self, dt: float, what: int = 3) -> np.ndarray:
+        n = getattr(self, "_nb", 0)
+        out = np.zeros((max(n, 1), 2), dtype=np.float32)
+        self._ck(self.lib.geon_boson_kicks(self._h, float(dt), int(what), N.fptr(out)))
+        return out[:n]
+
     def collision_info(self) -> dict:
         info = N.GeonCollisionInfo()
         self._ck(self.lib.geon_collision_info(self._h, C.byref(info)))
