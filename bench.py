@@ -503,7 +503,54 @@ def run_configs(args, g_big, wl_big, idx, fx, fy, fp32_peak):
                           "walk_frac_of_fp32_peak": tf / fp32_peak if fp32_peak else None}
     out["plummer_disk_n1048576_theta_sweep"] = sweep
     out["sparse_field_merge"] = run_merge()
+    out["boson_pool"] = run_bosons()
     return out
+
+
+def run_bosons():
+    """The boson-tree walks at N = 1,048,576 (sparse field, gravity + Coulomb,
+    BH theta 0.5) with a pool of 16,384 bosons (60 % photons, 40 % charged
+    pions) uniform over the box: the boson gravity added to a force pass
+    (forces.js:788-804) and the pool's own kicks (forces.js:812-901)."""
+    import torch
+    from physsim_gb300 import _native as N, workloads as W
+    from physsim_gb300.system import GeonSystem
+    wl = W.sparse_field(1 << 20)
+    p = wl.params
+    p.collision_mode = N.COL_PASS
+    g = GeonSystem(p, wl.n)
+    g.upload(*[wl.state[k] for k in STATE_KEYS])
+    rng = np.random.default_rng(17)
+    nb = 16384
+    L = wl.info["box"]
+    kind = (rng.random(nb) < 0.4).astype(float)
+    rows = np.stack([rng.uniform(0, L, nb), rng.uniform(0, L, nb), rng.uniform(0.05, 1.0, nb),
+                     np.where(kind > 0, rng.choice([-0.1, 0.1], nb), 0.0), kind, 0.1 * kind], 1)
+    st = torch.cuda.ExternalStream(g.stream_ptr())
+
+    def timed(fn, reps=5):
+        fn()
+        g.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            fn()
+        e1.record(st)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    t0 = time.perf_counter()
+    g.set_bosons(rows)
+    upload_ms = 1e3 * (time.perf_counter() - t0)
+    plain = timed(g.compute_forces)
+    p.flags |= N.FLAG_BOSONS
+    g.set_params(p)
+    with_bosons = timed(g.compute_forces)
+    kicks = timed(lambda: g.boson_kicks(1 / 60, 3))
+    g.close()
+    return {"n": wl.n, "bosons": nb, "force_pass_ms": plain, "force_pass_with_boson_gravity_ms": with_bosons,
+            "boson_gravity_ms": with_bosons - plain, "kicks_ms_incl_copy": kicks,
+            "set_bosons_ms_incl_tree": upload_ms}
 
 
 def run_merge():

@@ -26,11 +26,12 @@ struct BosonTree {
 void boson_charges(const BosonTree& B, double* iq, double* lq, cudaStream_t st, LaunchCounter& lc);
 
 // computeBosonGravity (src/forces.js:788-804) on every particle of the force
-// pass just run (targets from `tgt_list` when not null, else slots < ctl->n),
+// pass just run (targets from `tgt_list` when not null, else the particle
+// tree's order TP.tgt, whose tree must be current),
 // added to force and the gravity breakdown rows; then the planner maxima of
 // that pass are recomputed from the updated forces.
-void boson_gravity(const DevParams& P, const DevState& S, FrameCtl* ctl, const BosonTree& B, const int* tgt_list,
-                   int tgt_count, bool brk, int n_cap, cudaStream_t st, LaunchCounter& lc);
+void boson_gravity(const DevParams& P, const DevState& S, const TreeBufs& TP, FrameCtl* ctl, const BosonTree& B,
+                   const int* tgt_list, int tgt_count, bool brk, int n_cap, cudaStream_t st, LaunchCounter& lc);
 
 // The kicks of applyBosonBosonGravity (what & 1; src/forces.js:812-856) and
 // applyPionPionCoulomb (what & 2; src/forces.js:878-901) on every boson of

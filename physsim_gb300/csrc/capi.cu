@@ -661,7 +661,9 @@ static int run_force_pass(GeonHandle* h, bool rebuild) {
         CKL();
     }
     if (bosons_act(h)) {                      // computeBosonGravity (integrator.js:773-777, 1508-1513)
-        boson_gravity(h->P, h->S, h->ctl, boson_tree(h), h->col_tgt_active ? h->col.tgt2 : nullptr, h->col_tgt_count,
+        TreeBufs order = h->T;
+        if (!bh) order.tgt = nullptr;         // pairwise sum: no tree of this state
+        boson_gravity(h->P, h->S, order, h->ctl, boson_tree(h), h->col_tgt_active ? h->col.tgt2 : nullptr, h->col_tgt_count,
                       (h->prm.flags & GEON_FLAG_BREAKDOWN) != 0, h->n_cap, h->st, h->lc);
         CKL();
     }

@@ -142,6 +142,9 @@ class GeonGPUPhysics:
             v = _get(physics, name, None)
             if v is not None:
                 self._ext[key] = float(v)
+        bi = _get(physics, "bosonInterEnabled", None)       # integrator.js:66 (a flag here, not a toggle bit)
+        if bi is not None:
+            self._flags = (self._flags | N.FLAG_BOSONS) if bi else (self._flags & ~N.FLAG_BOSONS)
         cm = _get(physics, "collisionMode", None)
         if cm is not None:          # COL_* number or the settings string (config.js:10-14)
             self._collisionMode = self.COL_NAMES.index(cm) if cm in self.COL_NAMES else int(cm) if isinstance(cm, int) else 0
@@ -236,6 +239,7 @@ class GeonGPUPhysics:
                           "wy": float(st["wy"][i]), "mass": float(st["mass"][i]), "baseMass": float(base),
                           "charge": float(st["charge"][i]), "angw": float(st["angw"][i]), "antimatter": bool(anti)})
         toggles = {name: bool(bit and (self._toggles & bit)) for name, bit in self._SAVE_TOGGLES}
+        toggles["bosonInterEnabled"] = bool(self._flags & N.FLAG_BOSONS)
         settings = {"collision": self.COL_NAMES[int(self._collisionMode) % 3] if isinstance(self._collisionMode, int)
                     else str(self._collisionMode),
                     "boundary": BOUND_NAMES[self.boundaryMode], "topology": TOPO_NAMES[self.topologyMode],
@@ -265,6 +269,10 @@ class GeonGPUPhysics:
                 if bit and tg.get(name, False):
                     t |= bit
             self._toggles = t
+            if tg.get("bosonInterEnabled", False):
+                self._flags |= N.FLAG_BOSONS
+            else:
+                self._flags &= ~N.FLAG_BOSONS
         for key, name in (("ext_gravity", "extGravity"), ("ext_gravity_angle", "extGravityAngle"),
                           ("ext_electric", "extElectric"), ("ext_electric_angle", "extElectricAngle"),
                           ("ext_bz", "extBz")):
@@ -296,6 +304,33 @@ class GeonGPUPhysics:
     def reset(self):
         self._sys.reset()
         self._stats = None
+
+    def setBosonPool(self, photons=(), pions=(), leptons=()):
+        """The Simulation's alive bosons for the boson tree (integrator.js:263-277):
+        objects with pos {x, y} (or x, y), _srcMass and, for pions and
+        leptons, charge and vSq.  With bosonInterEnabled, every force pass of
+        update() adds their gravity on the particles (forces.js:788-804)."""
+        rows = []
+        for kind, group in ((0, photons), (1, pions), (1, leptons)):
+            for b in group:
+                if not _get(b, "alive", True):
+                    continue
+                pos = _get(b, "pos", None)
+                x = float(_get(pos, "x") if pos is not None else _get(b, "x"))
+                y = float(_get(pos, "y") if pos is not None else _get(b, "y"))
+                q = 0.0 if kind == 0 else float(_get(b, "charge", 0.0))
+                rows.append((x, y, float(_get(b, "_srcMass", 0.0)), q, kind,
+                             0.0 if kind == 0 else float(_get(b, "vSq", 0.0))))
+        self._sys.set_bosons(np.array(rows, dtype=np.float64).reshape(-1, 6))
+
+    def bosonKicks(self, dt: float) -> np.ndarray:
+        """Kicks of the pool on itself, in setBosonPool order (photons, pions,
+        leptons): gravity (forces.js:812-856, before the photons' speed
+        renormalisation) plus, with Coulomb on, Coulomb between pions and
+        leptons (forces.js:878-901).  Photons add the kick to their velocity,
+        pions and leptons to w."""
+        what = (1 if self._toggles & N.GRAVITY else 0) | (2 if self._toggles & N.COULOMB else 0)
+        return self._sys.boson_kicks(dt, what)
 
     def collisionEvents(self) -> np.ndarray:
         """Events of the last update (rows type, x, y, energy, px, py; type 1

@@ -45,12 +45,12 @@ def both(p, st, rows):
     return g, o
 
 
-@pytest.mark.parametrize("boundary", [N.BOUND_DESPAWN, N.BOUND_LOOP])
-def test_boson_gravity_on_particles(gpu_lib, oracle_mod, boundary):
+@pytest.mark.parametrize("boundary,bh", [(N.BOUND_DESPAWN, True), (N.BOUND_LOOP, True), (N.BOUND_DESPAWN, False)])
+def test_boson_gravity_on_particles(gpu_lib, oracle_mod, boundary, bh):
     rng = np.random.default_rng(1)
     st = particles(rng, 3000)
     rows = pool(rng, 800)
-    p = N.make_params(toggles=N.GRAVITY | N.BARNES_HUT, flags=N.FLAG_BOSONS | N.FLAG_BREAKDOWN,
+    p = N.make_params(toggles=N.GRAVITY | (N.BARNES_HUT if bh else 0), flags=N.FLAG_BOSONS | N.FLAG_BREAKDOWN,
                       boundary_mode=boundary, softening=2.0)
     g, o = both(p, st, rows)
     g.compute_forces()
@@ -60,7 +60,7 @@ def test_boson_gravity_on_particles(gpu_lib, oracle_mod, boundary):
         e = vec_err(fg[kx], fg[ky], fo[kx], fo[ky])
         assert e["norm"] <= 1e-5, (kx, e)
     # the bosons' share alone: against the same pass without the flag
-    p2 = N.make_params(toggles=N.GRAVITY | N.BARNES_HUT, boundary_mode=boundary, softening=2.0)
+    p2 = N.make_params(toggles=N.GRAVITY | (N.BARNES_HUT if bh else 0), boundary_mode=boundary, softening=2.0)
     g.set_params(p2)
     g.compute_forces()
     f0 = g.forces()
@@ -121,3 +121,33 @@ def test_no_effect_without_flag_or_pool(gpu_lib):
     f = g.forces()
     assert np.array_equal(f["fx"], ref["fx"])
     g.close()
+
+
+def test_gpu_physics_mirror_boson_pool(gpu_lib, oracle_mod):
+    """The GPUPhysics mirror: bosonInterEnabled from setToggles, the pool from
+    Simulation-style objects, kicks in pool order, the saved toggle."""
+    from physsim_gb300.gpu_physics import GeonGPUPhysics
+
+    class Phys:
+        gravityEnabled = True
+        coulombEnabled = True
+        barnesHutEnabled = True
+        bosonInterEnabled = True
+
+    b = GeonGPUPhysics(domainW=100.0, domainH=100.0, maxParticles=16).init()
+    b.setToggles(Phys())
+    b.addParticle({"x": 40.0, "y": 50.0, "mass": 2.0})
+    photons = [{"pos": {"x": 45.0, "y": 50.0}, "_srcMass": 1.0}]
+    pions = [{"pos": {"x": 60.0, "y": 50.0}, "_srcMass": 0.5, "charge": 0.1, "vSq": 0.2},
+             {"pos": {"x": 62.0, "y": 50.0}, "_srcMass": 0.5, "charge": 0.1, "vSq": 0.2},
+             {"pos": {"x": 80.0, "y": 50.0}, "_srcMass": 0.5, "charge": 0.1, "vSq": 0.2, "alive": False}]
+    b.setBosonPool(photons, pions)
+    k = b.bosonKicks(0.01)
+    assert k.shape == (3, 2)                      # the dead pion is left out
+    assert k[0, 0] > 0 and k[1, 0] > 0 > k[2, 0]  # gravity pulls the three together
+    assert np.array_equal(k, b._sys.boson_kicks(0.01, 3))
+    b._sys.compute_forces()
+    f = b._sys.forces()
+    assert f["fx"][0] > 0                         # pulled towards the photon at x = 45
+    assert b.serialize()["toggles"]["bosonInterEnabled"]
+    b.destroy()
