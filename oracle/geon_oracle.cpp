@@ -1809,7 +1809,28 @@ long long oracle_compute_forces_subset(void* h, const int* idx, int k) {
             const int i = idx[t];
             Sim::resetOne(s->ps[i]);
             s->ps[i].pe = 0;
-            s->calculateForce(i, tg, s->relOn(), cutSq, stack, inter);
+            if (s->on(GEON_BARNES_HUT)) {
+                if (s->root >= 0) s->calculateForce(i, tg, s->relOn(), cutSq, stack, inter);
+                continue;
+            }
+            Particle& p = s->ps[i];                                  // the pairwise branch (forces.js:94-125)
+            for (int j = 0; j < s->nReal(); j++) {
+                if (j == i) continue;
+                const Particle& o = s->ps[j];
+                if (s->relOn()) {
+                    if (o.h.count < 2) continue;
+                    Sim::Delayed ret;
+                    if (!s->getDelayedState(o, p.x, p.y, ret)) continue;
+                    const double rr = o.bodyRadiusSq;
+                    const double av = ret.angw / std::sqrt(1 + ret.angw * ret.angw * rr);
+                    s->pairForce(p, ret.x, ret.y, ret.vx, ret.vy, o.mass, o.charge, av, MAG_MOMENT_K * o.charge * av * rr,
+                                 INERTIA_K * o.mass * av * rr, tg, o.axMod, o.yukMod, true, o.higgsMod, cutSq);
+                } else {
+                    s->pairForce(p, o.x, o.y, o.vx, o.vy, o.mass, o.charge, o.angVel, o.magMoment, o.angMomentum, tg,
+                                 o.axMod, o.yukMod, false, o.higgsMod, cutSq);
+                }
+                inter++;
+            }
         }
     }
     return inter;
