@@ -146,6 +146,17 @@ def test_forces_full_set_torus_no_relativity(gpu_lib, oracle_mod):
     check_forces(wl, FULL_KEYS)
 
 
+@pytest.mark.parametrize("topology", [N.KLEIN, N.RP2])
+@pytest.mark.parametrize("bh", [True, False])
+def test_forces_full_set_nonorientable(gpu_lib, oracle_mod, topology, bh):
+    """Klein bottle and RP^2: the 2- and 4-candidate minimum image
+    (topology.js:18-76) on every source, aggregate and retarded position."""
+    wl = _with(W.clusters_torus(4096, barnes_hut=bh), N.FLAG_PE | N.FLAG_BREAKDOWN)
+    wl.params.topology = topology
+    hist = W.straight_line_history(wl.state, 96, 120.0, 64 / 60)
+    check_forces(wl, FULL_KEYS, history=hist)
+
+
 @pytest.mark.parametrize("bh", [True, False])
 def test_onepn_pass(gpu_lib, oracle_mod, bh):
     wl = W.clusters_torus(2048, barnes_hut=bh)
@@ -207,6 +218,29 @@ def test_frame_full_set_torus(gpu_lib, oracle_mod):
     errs, _ = run_frames(wl, 1, history=hist)
     for k, e in errs.items():
         assert e["norm"] <= TRAJ_TOL, (k, e)
+
+
+@pytest.mark.parametrize("topology", [N.TORUS, N.KLEIN, N.RP2])
+def test_frames_edge_crossings(gpu_lib, oracle_mod, topology):
+    """Two frames in which particles cross every edge and corner of the
+    periodic domain: wrapPosition with the Klein / RP^2 flips of position and
+    velocity (topology.js:81-135, integrator.js:1798-1824)."""
+    wl = W.clusters_torus(2048)
+    wl.params.topology = topology
+    L = wl.info["box"]
+    e = 2e-4
+    st = wl.state
+    # (x, y, wx, wy): across the right, left, top and bottom edges and two corners
+    cross = [(L - e, 200.0, 0.05, 0.0), (e, 120.0, -0.05, 0.0), (150.0, e, 0.0, -0.05),
+             (260.0, L - e, 0.0, 0.05), (L - e, L - e, 0.05, 0.05), (e, e, -0.05, -0.05)]
+    for i, (x, y, wx, wy) in enumerate(cross):
+        st["x"][i], st["y"][i], st["wx"][i], st["wy"][i] = x, y, wx, wy
+    for k in ("x", "y", "wx", "wy"):
+        st[k] = np.asarray(st[k], dtype=np.float32).astype(np.float64)
+    hist = W.straight_line_history(st, 96, 120.0, 64 / 60)
+    errs, _ = run_frames(wl, 2, history=hist)
+    for k, err in errs.items():
+        assert err["norm"] <= TRAJ_TOL, (k, err)
 
 
 def test_despawn_compaction_matches(gpu_lib, oracle_mod):
