@@ -729,7 +729,15 @@ def run_native(args, ws, rank, local):
     inter = prof["interactions"] / max(prof["force_count"], 1)
     achieved = inter * FLOP_PER_INTERACTION_GCY / (walk_ms / 1e3) / 1e12
     tree_ms = prof["tree_ms"] / max(prof["tree_count"], 1)
+    tinfo = g.build_tree()
     g.close()
+    # algorithmic bytes of one tree build: keys (16 B read, 12 B written per
+    # point), eight 8-bit radix passes over (key, index) (24 B per point each),
+    # the gathered point records (48 B read, 48 B written per point), the
+    # aggregation (48 B per point) and node emission, linking and sums (80 B
+    # per node)
+    tree_nodes = tinfo["n_internal"] + tinfo["n_leaves"]
+    tree_bytes = tinfo["n_points"] * (28 + 8 * 24 + 96 + 48) + tree_nodes * 80
 
     if rank != 0:
         return
@@ -765,8 +773,14 @@ def run_native(args, ws, rank, local):
                      "flop_per_interaction": FLOP_PER_INTERACTION_GCY,
                      "interactions_per_launch": inter, "launch_ms": walk_ms,
                      "peak_source": "project FP32 FMA microbenchmark on this GPU (MEASURED_PEAKS.json has no FP32 figure)"},
-        "tree_build": {"ms": tree_ms, "bound": "hbm",
-                       "algorithmic_bytes": None, "peak_gbs": pk.get("hbm_gbs")},
+        "tree_build": {"ms": tree_ms, "bound": "hbm", "algorithmic_bytes": tree_bytes,
+                       "points": tinfo["n_points"], "nodes": tree_nodes,
+                       "achieved_gbs": tree_bytes / (tree_ms / 1e3) / 1e9 if tree_ms > 0 else None,
+                       "peak_gbs": pk.get("hbm_gbs"),
+                       "frac": (tree_bytes / (tree_ms / 1e3) / 1e9) / pk["hbm_gbs"]
+                       if tree_ms > 0 and pk.get("hbm_gbs") else None,
+                       "note": "62 dependent launches (eight radix passes of five) on an L2-resident working "
+                               "set: launch- and latency-bound, not HBM-bound"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 7 * 4 * n, "d2h_bytes_per_step": 7 * 4 * n,
                 "note": "per step: upload state (re-bootstraps forces), one frame, download state"},
         "clocks": clk,

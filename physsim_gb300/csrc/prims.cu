@@ -9,6 +9,11 @@
 // shared memory, then run-contiguous global writes.  Passes whose 8 bits are
 // the same in every key are turned into a plain copy by a pre-pass that
 // AND/OR-reduces the keys.
+//
+// Small inputs (at most 8192 pairs of capacity, e.g. a 2048-particle system)
+// take single-CTA forms instead: one launch sorts the whole tile through all
+// passes in shared memory, and one launch scans a tile.  Multi-kernel forms
+// there are bound by launch latency, not by work.
 #include "prims.cuh"
 
 namespace geon {
@@ -103,11 +108,40 @@ __global__ void scan_apply_kernel(const int* __restrict__ in, int* __restrict__ 
     }
 }
 
+// The whole scan in one CTA (len <= SCAN_TILE).
+__global__ void scan_single_kernel(const int* __restrict__ in, int* __restrict__ out, int len, const int* d_n,
+                                   int* __restrict__ total_out) {
+    __shared__ int sw[SCAN_THREADS / 32 + 1];
+    const int n = d_n ? min(len, *d_n) : len;
+    int v[SCAN_ITEMS];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        const int i = threadIdx.x * SCAN_ITEMS + k;
+        v[k] = i < n ? in[i] : 0;
+        s += v[k];
+    }
+    int tot;
+    int ex = block_excl_scan<SCAN_THREADS>(s, sw, &tot);
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        const int i = threadIdx.x * SCAN_ITEMS + k;
+        if (i < len) out[i] = (i < n) ? ex : 0;
+        ex += v[k];
+    }
+    if (threadIdx.x == 0 && total_out) *total_out = tot;
+}
+
 size_t scan_temp_ints(int len) { return (size_t)(len + SCAN_TILE - 1) / SCAN_TILE + 1; }
 
 void exclusive_scan(const int* d_in, int* d_out, int len, const int* d_n, int* d_total, int* d_temp,
                     cudaStream_t st, LaunchCounter* lc) {
     if (len <= 0) return;
+    if (len <= SCAN_TILE) {
+        scan_single_kernel<<<1, SCAN_THREADS, 0, st>>>(d_in, d_out, len, d_n, d_total);
+        if (lc) lc->add(1);
+        return;
+    }
     const int nb = (len + SCAN_TILE - 1) / SCAN_TILE;
     scan_reduce_kernel<<<nb, SCAN_THREADS, 0, st>>>(d_in, len, d_n, d_temp);
     scan_blocks_kernel<<<1, SCAN_THREADS, 0, st>>>(d_temp, nb, d_total);
@@ -256,6 +290,119 @@ radix_downsweep_kernel(const uint64_t* __restrict__ keys_in, const uint32_t* __r
 constexpr size_t RS_DOWN_SMEM = RS_TILE * (sizeof(uint64_t) + sizeof(uint32_t)) +
                                 (RS_WARPS + 2) * RS_RADIX * sizeof(unsigned) + (RS_THREADS / 32 + 1) * sizeof(int);
 
+// Single-CTA sort of at most THREADS * ITEMS pairs, in place: every pass of
+// the tile sort above (match_any ranking, per-warp running counts, digit
+// scan, stable scatter) with the keys kept in shared memory between passes;
+// passes whose 8 bits are the same in every key are skipped.
+template <int THREADS, int ITEMS>
+__global__ void __launch_bounds__(THREADS)
+radix_tile_sort_kernel(uint64_t* __restrict__ keys, uint32_t* __restrict__ vals, const int* d_n, int len,
+                       int end_bit) {
+    constexpr int WARPS = THREADS / 32, TILE = THREADS * ITEMS;
+    static_assert(THREADS >= RS_RADIX, "one thread per digit");
+    extern __shared__ __align__(16) unsigned char ts_smem[];
+    uint64_t* s_keys = reinterpret_cast<uint64_t*>(ts_smem);
+    uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + TILE);
+    unsigned (*s_warp)[RS_RADIX] = reinterpret_cast<unsigned (*)[RS_RADIX]>(s_vals + TILE);
+    unsigned* s_start = &s_warp[WARPS][0];
+    int* s_scan = reinterpret_cast<int*>(s_start + RS_RADIX);
+    __shared__ unsigned long long s_ao[2];
+    const int n = min(min(len, *d_n), TILE);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int base = warp * (32 * ITEMS);
+    uint64_t k[ITEMS];
+    uint32_t v[ITEMS];
+    uint64_t a = ~0ull, o = 0ull;
+#pragma unroll
+    for (int j = 0; j < ITEMS; j++) {
+        const int idx = base + j * 32 + lane;
+        const bool valid = idx < n;
+        k[j] = valid ? keys[idx] : 0ull;
+        v[j] = valid ? vals[idx] : 0u;
+        if (valid) { a &= k[j]; o |= k[j]; }
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+        a &= __shfl_xor_sync(0xffffffffu, a, s);
+        o |= __shfl_xor_sync(0xffffffffu, o, s);
+    }
+    if (threadIdx.x == 0) { s_ao[0] = ~0ull; s_ao[1] = 0ull; }
+    __syncthreads();
+    if (lane == 0) { atomicAnd(&s_ao[0], (unsigned long long)a); atomicOr(&s_ao[1], (unsigned long long)o); }
+    __syncthreads();
+    const uint64_t diff = s_ao[0] ^ s_ao[1];
+    const unsigned lt = lanemask_lt();
+    for (int shift = 0; shift < end_bit; shift += 8) {
+        if (((diff >> shift) & 0xffull) == 0) continue;                 // same for the whole CTA
+        for (int i = threadIdx.x; i < WARPS * RS_RADIX; i += THREADS) (&s_warp[0][0])[i] = 0;
+        __syncthreads();
+        unsigned rank[ITEMS];
+#pragma unroll
+        for (int j = 0; j < ITEMS; j++) {
+            const bool valid = base + j * 32 + lane < n;
+            const unsigned d = valid ? (unsigned)((k[j] >> shift) & 0xffu) : 0x100u;
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            const unsigned prior = valid ? s_warp[warp][d] : 0u;
+            rank[j] = prior + __popc(peers & lt);
+            __syncwarp();
+            if (valid && lane == (unsigned)(__ffs(peers) - 1)) s_warp[warp][d] = prior + __popc(peers);
+            __syncwarp();
+        }
+        __syncthreads();
+        int run = 0;
+        if (threadIdx.x < RS_RADIX) {                                 // per digit: exclusive over warps
+            const int d = threadIdx.x;
+            for (int w = 0; w < WARPS; w++) {
+                const unsigned c = s_warp[w][d];
+                s_warp[w][d] = (unsigned)run;
+                run += (int)c;
+            }
+        }
+        const int ex = block_excl_scan<THREADS>(run, s_scan, nullptr);  // then over digits
+        if (threadIdx.x < RS_RADIX) s_start[threadIdx.x] = (unsigned)ex;
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < ITEMS; j++) {
+            if (base + j * 32 + lane < n) {
+                const unsigned d = (unsigned)((k[j] >> shift) & 0xffu);
+                const unsigned pos = s_start[d] + s_warp[warp][d] + rank[j];
+                s_keys[pos] = k[j];
+                s_vals[pos] = v[j];
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < ITEMS; j++) {
+            const int idx = base + j * 32 + lane;
+            if (idx < n) { k[j] = s_keys[idx]; v[j] = s_vals[idx]; }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int j = 0; j < ITEMS; j++) {
+        const int idx = base + j * 32 + lane;
+        if (idx < n) { keys[idx] = k[j]; vals[idx] = v[j]; }
+    }
+}
+
+template <int THREADS, int ITEMS>
+constexpr size_t tile_sort_smem() {
+    return (size_t)THREADS * ITEMS * (sizeof(uint64_t) + sizeof(uint32_t)) +
+           (size_t)(THREADS / 32 + 1) * RS_RADIX * sizeof(unsigned) + (THREADS / 32 + 1) * sizeof(int);
+}
+
+template <int THREADS, int ITEMS>
+static void tile_sort(uint64_t* keys, uint32_t* vals, int len, const int* d_n, int end_bit, cudaStream_t st) {
+    constexpr size_t smem = tile_sort_smem<THREADS, ITEMS>();
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(radix_tile_sort_kernel<THREADS, ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        attr = true;
+    }
+    radix_tile_sort_kernel<THREADS, ITEMS><<<1, THREADS, smem, st>>>(keys, vals, d_n, len, end_bit);
+}
+
 __global__ void clear_and_or_kernel(unsigned long long* and_or) {
     and_or[0] = ~0ull;
     and_or[1] = 0ull;
@@ -273,6 +420,16 @@ size_t radix_temp_bytes(int len) {
 int radix_sort_pairs(uint64_t* keys, uint32_t* vals, uint64_t* keys_alt, uint32_t* vals_alt,
                      int len, const int* d_n, int end_bit, void* d_temp, cudaStream_t st, LaunchCounter* lc) {
     if (len <= 0) return 0;
+    if (len <= 256 * 16) {                          // one CTA, in place
+        tile_sort<256, 16>(keys, vals, len, d_n, end_bit, st);
+        if (lc) lc->add(1);
+        return 0;
+    }
+    if (len <= 1024 * 8) {
+        tile_sort<1024, 8>(keys, vals, len, d_n, end_bit, st);
+        if (lc) lc->add(1);
+        return 0;
+    }
     static bool attr_set = false;
     if (!attr_set) {
         cudaFuncSetAttribute(radix_downsweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RS_DOWN_SMEM);
