@@ -37,31 +37,44 @@ enum { Q_FX = 0, Q_FY, Q_TID, Q_PE, Q_NBASE };
 enum { M_BZ = 0, M_BGZ, M_DBZX, M_DBZY, M_DBGZX, M_DBGZY, M_FD, M_F1X, M_F1Y, M_N };
 enum { K_GX = 0, K_GY, K_CX, K_CY, K_MX, K_MY, K_GMX, K_GMY, K_YX, K_YY, K_N };
 
-template <bool MAGGM, bool BRK>
+// SH: the compensated (hi, lo) sums live in rows of shared memory at the
+// start of the dynamic buffer, [2 * NQ][ACC_SH_THREADS] with one column per
+// thread, instead of registers.  They are touched only every FLUSH_EVERY
+// terms; the registers they free let the open-box Barnes-Hut walk run six
+// CTAs per SM instead of five without spills.
+extern __shared__ __align__(16) unsigned char geon_dsmem[];
+constexpr int ACC_SH_THREADS = 128;
+template <bool MAGGM, bool BRK, bool SH = false>
 struct Acc {
     static constexpr int QM = Q_NBASE;
     static constexpr int QK = Q_NBASE + (MAGGM ? M_N : 0);
     static constexpr int NQ = QK + (BRK ? K_N : 0);
-    float part[NQ], hi[NQ], lo[NQ];
+    static constexpr size_t SH_BYTES = SH ? (size_t)2 * NQ * ACC_SH_THREADS * sizeof(float) : 0;
+    float part[NQ], hi_[SH ? 1 : NQ], lo_[SH ? 1 : NQ];
     int cnt;
+    __device__ __forceinline__ static float* row(int q) {
+        return reinterpret_cast<float*>(geon_dsmem) + q * ACC_SH_THREADS + threadIdx.x;
+    }
+    __device__ __forceinline__ float& hi(int q) { if constexpr (SH) return *row(q); else return hi_[q]; }
+    __device__ __forceinline__ float& lo(int q) { if constexpr (SH) return *row(NQ + q); else return lo_[q]; }
     __device__ __forceinline__ void init() {
 #pragma unroll
-        for (int q = 0; q < NQ; q++) { part[q] = 0.f; hi[q] = 0.f; lo[q] = 0.f; }
+        for (int q = 0; q < NQ; q++) { part[q] = 0.f; hi(q) = 0.f; lo(q) = 0.f; }
         cnt = 0;
     }
     __device__ __forceinline__ void flush() {
 #pragma unroll
         for (int q = 0; q < NQ; q++) {
-            df s = two_sum(hi[q], part[q]);
-            hi[q] = s.hi;
-            lo[q] = __fadd_rn(lo[q], s.lo);
+            df s = two_sum(hi(q), part[q]);
+            hi(q) = s.hi;
+            lo(q) = __fadd_rn(lo(q), s.lo);
             part[q] = 0.f;
         }
     }
     __device__ __forceinline__ void tick() {
         if (++cnt >= FLUSH_EVERY) { flush(); cnt = 0; }
     }
-    __device__ __forceinline__ float get(int q) const { return __fadd_rn(hi[q], lo[q]); }
+    __device__ __forceinline__ float get(int q) { return __fadd_rn(hi(q), lo(q)); }
     __device__ __forceinline__ void add(int q, float v) { part[q] = __fadd_rn(part[q], v); }
     __device__ __forceinline__ void addm(int q, float v) { if (MAGGM) add(QM + q, v); }
     __device__ __forceinline__ void addk(int q, float v) { if (BRK) add(QK + q, v); }
@@ -101,11 +114,11 @@ __device__ __forceinline__ void target_coupling(const DevParams& P, Tgt& t) {
 __device__ __forceinline__ bool on(const DevParams& P, uint32_t bit) { return (P.toggles & bit) != 0; }
 
 // ---- pairForce (forces.js:163-442) ----------------------------------------------------
-template <bool MAGGM, bool BRK>
+template <bool MAGGM, bool BRK, class ACC>
 __device__ __forceinline__ void pair_force(const DevParams& P, const Tgt& t, float rx, float ry,
                                            float svx, float svy, float sm, float sq, float sAngVel,
                                            float sMu, float sL, bool delayed, bool yukIn, bool pe,
-                                           Acc<MAGGM, BRK>& A) {
+                                           ACC& A) {
     const float rawRSq = __fmaf_rn(rx, rx, ry * ry);
     const float rSq = rawRSq + P.softSq;
     const float invR = rsqrtf(rSq);
@@ -425,9 +438,9 @@ __device__ __forceinline__ void delayed_disp(const DevParams& P, const Tgt& t, c
 }
 
 // ---- epilogue: outputs, external fields, walls, planner reductions -------------------------
-template <bool MAGGM, bool BRK>
+template <bool MAGGM, bool BRK, class ACC>
 __device__ __forceinline__ void finalize_target(const DevParams& P, const DevState& S, const ForceCtx& C,
-                                                FrameCtl* ctl, const Tgt& t, bool valid, Acc<MAGGM, BRK>& A,
+                                                FrameCtl* ctl, const Tgt& t, bool valid, ACC& A,
                                                 unsigned inter32, int sysId = -1) {
     unsigned long long inter = inter32;
     A.flush();
@@ -440,7 +453,7 @@ __device__ __forceinline__ void finalize_target(const DevParams& P, const DevSta
         if (P.extEx != 0.f || P.extEy != 0.f) { ex += t.q * P.extEx; ey += t.q * P.extEy; }
         if (P.extBz != 0.f) Bz += P.extBz;
         if (C.bounce) {                                              // integrator.js:607-668
-            const float r = t.r, fr = P.friction;
+            const float r = S.spin[t.idx].z, fr = P.friction;   // reloaded: not kept live through the walk
             const float left = (float)P.offXd, top = (float)P.offYd;
             const float right = (float)(P.offXd + P.Wd), bottom = (float)(P.offYd + P.Hd);
             auto clamp1 = [](float v) { return fminf(1.f, fmaxf(-1.f, v)); };
@@ -696,22 +709,31 @@ walk_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root,
 //    another lane's sources.
 constexpr int WC_THREADS = 128;
 constexpr int WC_WARPS = WC_THREADS / 32;
-constexpr int WC_STACK = 512;
+constexpr int WC_STACK = 448;
 constexpr int WC_RESERVE = 3 * KEY_LEVELS + 3 * 16 + 4;   // growth a depth-first tail can still need
-constexpr int WC_POOL = 96;
+constexpr int WC_POOL_SIX = 64;    // the six-CTA walk (below)
+constexpr int WC_POOL_WIDE = 96;   // the others: fewer, fuller flushes
 constexpr int WC_POP = 16;
+// one pop step stages at most WC_POP leaves of LEAF_CAP points (or one
+// aggregate per lane) and a bucket chunk 32 points, each after a flush
+static_assert(WC_POOL_SIX >= WC_POP * LEAF_CAP && WC_POOL_SIX >= 32, "source pool smaller than one step's staging");
+static_assert(WC_POOL_WIDE >= WC_POOL_SIX && WC_POOL_WIDE <= 255, "pool indices are bytes");
 constexpr uint32_t AGG_REF = 0xffffffffu;
 
-template <bool NEEDC>
+template <bool NEEDC, int POOL>
 struct WcSmem {
+    static constexpr int kPool = POOL;
     int stk_node[WC_STACK];
     unsigned stk_mask[WC_STACK];
-    float4 a[WC_POOL];                 // x (hi), y (hi), mass, charge
-    float4 b[WC_POOL];                 // x (lo), y (lo), vx, vy
-    float4 c[NEEDC ? WC_POOL : 1];     // angVel, magMoment, angMomentum, -
-    uint32_t ref[WC_POOL];             // particle ref, AGG_REF for aggregates
-    uint8_t full[WC_POOL];             // pool indices every lane evaluates
-    uint8_t lst[WC_POOL][32];          // per-lane lists (column = lane) of partial entries
+    float4 a[POOL];                    // x (hi), y (hi), mass, charge
+    float4 b[POOL];                    // x (lo), y (lo), vx, vy
+    float4 c[NEEDC ? POOL : 1];        // angVel, magMoment, angMomentum, -
+    uint32_t ref[POOL];                // particle ref, AGG_REF for aggregates
+    uint8_t full[POOL];                // pool indices every lane evaluates
+    uint8_t lst[POOL][32];             // per-lane lists (column = lane) of partial entries
+    // read at each node classification, kept here rather than in registers
+    float gbox[4];                     // the warp's target box: centre x, y, half-widths x, y
+    int counts[3];                     // internal nodes, leaves, valid points of the tree
 };
 
 __device__ __forceinline__ int warp_incl_scan_i(int v) {
@@ -739,10 +761,10 @@ __device__ __forceinline__ int warp_max_i(int v) {
     return v;
 }
 
-template <bool MAGGM, bool REL, bool BRK, bool PER>
+template <bool MAGGM, bool REL, bool BRK, bool PER, class ACC, class WS>
 __device__ __forceinline__ void eval_entry(const DevParams& P, const DevState& S, const ForceCtx& C,
-                                           const float* s_age, const float* s_segdt, const WcSmem<MAGGM || REL>& W,
-                                           int e, const Tgt& t, Acc<MAGGM, BRK>& A, unsigned& inter, bool pe) {
+                                           const float* s_age, const float* s_segdt, const WS& W,
+                                           int e, const Tgt& t, ACC& A, unsigned& inter, bool pe) {
     const float4 a = W.a[e];
     const float4 b = W.b[e];
     const uint32_t ref = W.ref[e];
@@ -781,10 +803,10 @@ __device__ __forceinline__ void eval_entry(const DevParams& P, const DevState& S
     inter++;
 }
 
-template <bool MAGGM, bool REL, bool BRK, bool PER>
+template <bool MAGGM, bool REL, bool BRK, bool PER, class ACC, class WS>
 __device__ __forceinline__ void flush_pool(const DevParams& P, const DevState& S, const ForceCtx& C,
-                                           const float* s_age, const float* s_segdt, WcSmem<MAGGM || REL>& W,
-                                           int& nfull, int& lcnt, int& npool, const Tgt& t, Acc<MAGGM, BRK>& A,
+                                           const float* s_age, const float* s_segdt, WS& W,
+                                           int& nfull, int& lcnt, int& npool, const Tgt& t, ACC& A,
                                            unsigned& inter, bool pe) {
     __syncwarp();
     const unsigned lane = threadIdx.x & 31;
@@ -803,8 +825,8 @@ __device__ __forceinline__ void flush_pool(const DevParams& P, const DevState& S
     nfull = 0; lcnt = 0; npool = 0;
 }
 
-template <bool NEEDC>
-__device__ __forceinline__ void stage_point(const TreeBufs& T, WcSmem<NEEDC>& W, int e, int q) {
+template <bool NEEDC, class WS>
+__device__ __forceinline__ void stage_point(const TreeBufs& T, WS& W, int e, int q) {
     W.a[e] = T.ps_a[q];
     W.b[e] = T.ps_b[q];
     if (NEEDC) {
@@ -825,8 +847,8 @@ __device__ __forceinline__ bool accept_exact(const DevParams& P, double tx, doub
 }
 
 // Adds entries [e0, e0+cnt) with lane mask m to the full list or the per-lane lists.
-template <bool NEEDC>
-__device__ __forceinline__ void list_entries(WcSmem<NEEDC>& W, unsigned m, unsigned active, int e0, int cnt,
+template <bool NEEDC, class WS>
+__device__ __forceinline__ void list_entries(WS& W, unsigned m, unsigned active, int e0, int cnt,
                                              int& nfull, int& lcnt) {
     const unsigned lane = threadIdx.x & 31;
     if (m == active) {
@@ -841,19 +863,27 @@ __device__ __forceinline__ void list_entries(WcSmem<NEEDC>& W, unsigned m, unsig
 // NOPE: the potential-energy sums are off at compile time (the common case
 // of a force pass that only integrates), which keeps their code out of the
 // evaluation loop.  EMIT: record the accepted (cell, particle) pairs for the
-// learned correction.
+// learned correction.  The plain open-box walk without energy sums keeps its
+// compensated sums, group box and node counts in shared memory and runs six
+// CTAs per SM (80 registers); the other forms keep them in registers.
+template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE>
+__host__ __device__ constexpr bool wc_six() { return !MAGGM && !REL && !BRK && !PER && NOPE; }
+
 template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE = false, bool EMIT = false>
-__global__ void __launch_bounds__(WC_THREADS, (MAGGM || REL || BRK) ? 3 : 5)
+__global__ void __launch_bounds__(WC_THREADS, (MAGGM || REL || BRK) ? 3 : (wc_six<MAGGM, REL, BRK, PER, NOPE>() ? 6 : 5))
 walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
     constexpr bool NEEDC = MAGGM || REL;
-    extern __shared__ __align__(16) unsigned char wc_smem[];
-    WcSmem<NEEDC>* Wall = reinterpret_cast<WcSmem<NEEDC>*>(wc_smem);
+    constexpr bool SIX = wc_six<MAGGM, REL, BRK, PER, NOPE>();
+    using AccT = Acc<MAGGM, BRK, SIX>;
+    using WS = WcSmem<NEEDC, SIX ? WC_POOL_SIX : WC_POOL_WIDE>;
+    unsigned char* wc_smem = geon_dsmem + AccT::SH_BYTES;
+    WS* Wall = reinterpret_cast<WS*>(wc_smem);
     float* s_age = reinterpret_cast<float*>(Wall + WC_WARPS);
     float* s_segdt = s_age + HIST_LEN;
     if (REL) load_hist_tables(C, s_age, s_segdt);
     const int warp = threadIdx.x >> 5;
     const unsigned lane = threadIdx.x & 31;
-    WcSmem<NEEDC>& W = Wall[warp];
+    WS& W = Wall[warp];
     const int k0 = (blockIdx.x * WC_WARPS + warp) * 32 + (int)lane;
     int sysId;
     const int ti = walk_target(S, T, ctl, C, k0, sysId);
@@ -864,21 +894,23 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
     Tgt t;
     if (valid) { t = load_target(S, ti); target_coupling(P, t); }
     else { t = Tgt{}; t.idx = -1; }
-    Acc<MAGGM, BRK> A;
+    AccT A;
     A.init();
     unsigned inter = 0;
     const bool pe = NOPE ? false : (C.pe != 0);
     // bounding box of the warp's particles (padded beyond the rounding of hi + lo)
     const float bx0 = warp_min_f(valid ? t.x : 3.0e38f), bx1 = warp_max_f(valid ? t.x : -3.0e38f);
     const float by0 = warp_min_f(valid ? t.y : 3.0e38f), by1 = warp_max_f(valid ? t.y : -3.0e38f);
-    const float gcx = 0.5f * (bx0 + bx1), gcy = 0.5f * (by0 + by1);
-    const float ghx = 0.5f * (bx1 - bx0) * (1.f + 1e-6f) + 1e-6f * fabsf(gcx) + 1e-30f;
-    const float ghy = 0.5f * (by1 - by0) * (1.f + 1e-6f) + 1e-6f * fabsf(gcy) + 1e-30f;
+    const float gcx0 = 0.5f * (bx0 + bx1), gcy0 = 0.5f * (by0 + by1);
+    const float ghx0 = 0.5f * (bx1 - bx0) * (1.f + 1e-6f) + 1e-6f * fabsf(gcx0) + 1e-30f;
+    const float ghy0 = 0.5f * (by1 - by0) * (1.f + 1e-6f) + 1e-6f * fabsf(gcy0) + 1e-30f;
+    if (SIX && lane == 0) { W.gbox[0] = gcx0; W.gbox[1] = gcy0; W.gbox[2] = ghx0; W.gbox[3] = ghy0; }
     const bool groupTests = !P.periodic || P.topology == GEON_TORUS;
 
     const int root = C.roots ? C.roots[sysId] : *d_root;
     const bool treeOk = (ctl->err & (ERR_NODE_OVERFLOW | ERR_BAD_INDEX)) == 0;
-    const int nIntW = ctl->nInternal, nLeafW = ctl->nLeaves, nValidW = ctl->nValid;
+    const int nInt0 = ctl->nInternal, nLeaf0 = ctl->nLeaves, nValid0 = ctl->nValid;
+    if (SIX && lane == 0) { W.counts[0] = nInt0; W.counts[1] = nLeaf0; W.counts[2] = nValid0; }
     int top = 0, npool = 0, nfull = 0, lcnt = 0;
     if (root != ROOT_NONE && treeOk) {
         if (lane == 0) { W.stk_node[0] = root; W.stk_mask[0] = active; }
@@ -902,17 +934,19 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
         if (node >= 0) {
             if (node & LEAF_REF) {
                 const int li = node & ~LEAF_REF;
-                if (li < nLeafW) {
+                if (li < (SIX ? W.counts[1] : nLeaf0)) {
                     lm = T.leaf_meta[li];
                     const float lmass = T.leaf_a[li].z;
-                    if (lmass >= EPS_F && lm.x >= 0 && lm.x + lm.y <= nValidW) kind = 1;   // forces.js:630,643
+                    if (lmass >= EPS_F && lm.x >= 0 && lm.x + lm.y <= (SIX ? W.counts[2] : nValid0)) kind = 1;   // forces.js:630,643
                 } else atomicOr(&ctl->err, ERR_BAD_INDEX);
-            } else if (node < nIntW) {
+            } else if (node < (SIX ? W.counts[0] : nInt0)) {
                 na = T.int_a[node];
                 nc = T.int_c[node];
                 if (na.z >= EPS_F) {
                     kind = 4;
                     if (groupTests) {
+                        const float gcx = SIX ? W.gbox[0] : gcx0, gcy = SIX ? W.gbox[1] : gcy0;
+                        const float ghx = SIX ? W.gbox[2] : ghx0, ghy = SIX ? W.gbox[3] : ghy0;
                         float dx, dy;
                         if (PER && P.periodic) {
                             dx = wrap_axis_comp(na.x, gcx, nc.x, P.W, P.W_lo, P.halfW);
@@ -981,7 +1015,7 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
         const int myEnt = (myAcc ? 1 : 0) + myPts;
         int incl = warp_incl_scan_i(myEnt);
         const int tot = __shfl_sync(0xffffffffu, incl, 31);
-        if (npool + tot > WC_POOL)
+        if (npool + tot > WS::kPool)
             flush_pool<MAGGM, REL, BRK, PER>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
         const int e0 = npool + incl - myEnt;
         if (myAcc) {                                                  // forces.js:682-685
@@ -1026,7 +1060,7 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
             const unsigned bmask = __shfl_sync(0xffffffffu, leafMask, jj);
             for (int b0 = 0; b0 < bcount; b0 += 32) {
                 const int chunk = min(32, bcount - b0);
-                if (npool + chunk > WC_POOL)
+                if (npool + chunk > WS::kPool)
                     flush_pool<MAGGM, REL, BRK, PER>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
                 if ((int)lane < chunk) stage_point<NEEDC>(T, W, npool + lane, bstart + b0 + lane);
                 __syncwarp();
@@ -1057,8 +1091,32 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
     finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter, sysId);
 }
 
-template <bool MAGGM, bool REL>
-constexpr size_t wc_smem_bytes() { return sizeof(WcSmem<MAGGM || REL>) * WC_WARPS + 2 * HIST_LEN * sizeof(float); }
+// Dynamic shared memory of one walk CTA: accumulator rows (six-CTA form),
+// the four warps' stacks and source pools, and the history tables when
+// relativity is on.
+template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE>
+constexpr size_t wc_smem_bytes() {
+    constexpr bool SIX = wc_six<MAGGM, REL, BRK, PER, NOPE>();
+    return Acc<MAGGM, BRK, SIX>::SH_BYTES + sizeof(WcSmem<MAGGM || REL, SIX ? WC_POOL_SIX : WC_POOL_WIDE>) * WC_WARPS +
+           (REL ? 2 * HIST_LEN * sizeof(float) : 0);
+}
+static_assert(6 * (wc_smem_bytes<false, false, false, false, true>() + 1024) <= 228 * 1024,
+              "six plain walk CTAs per SM must fit in shared memory");
+static_assert(5 * (wc_smem_bytes<false, false, false, true, false>() + 1024) <= 228 * 1024,
+              "five walk CTAs per SM must fit in shared memory");
+
+template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE = false, bool EMIT = false>
+static void launch_walkc(int blocks, const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root,
+                         FrameCtl* ctl, const ForceCtx& C, cudaStream_t st) {
+    constexpr size_t smem = wc_smem_bytes<MAGGM, REL, BRK, PER, NOPE>();
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK, PER, NOPE, EMIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        attr = true;
+    }
+    walkc_kernel<MAGGM, REL, BRK, PER, NOPE, EMIT><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+}
 
 // ---- pairwise O(N^2) sum (forces.js:94-125) -------------------------------------------------
 constexpr int DIRECT_THREADS = 256;
@@ -1572,40 +1630,23 @@ static void launch_force(bool bh, const DevParams& P, const DevState& S, const T
         const int blocks = std::max(1, (slots + WALK_THREADS - 1) / WALK_THREADS);
         walk_kernel<MAGGM, REL, BRK><<<blocks, WALK_THREADS, 0, st>>>(P, S, T, d_root, ctl, C);
     } else if (bh) {
-        constexpr size_t smem = wc_smem_bytes<MAGGM, REL>();
-        static bool attr = false;
         constexpr bool PLAIN = !MAGGM && !REL && !BRK;
-        if (!attr) {
-            cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK, false, PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK, true, PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            attr = true;
-        }
         const int blocks = std::max(1, (slots + WC_THREADS - 1) / WC_THREADS);
         const bool lean = PLAIN && !C.pe;
         if (PLAIN && C.pair_count) {               // learned correction (plain forces only)
-            static bool eattr = false;
-            if (!eattr) {
-                cudaFuncSetAttribute(walkc_kernel<false, false, false, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                cudaFuncSetAttribute(walkc_kernel<false, false, false, true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                cudaFuncSetAttribute(walkc_kernel<false, false, false, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                cudaFuncSetAttribute(walkc_kernel<false, false, false, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                eattr = true;
-            }
             if (P.periodic) {
-                if (lean) walkc_kernel<false, false, false, true, true, true><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
-                else walkc_kernel<false, false, false, true, false, true><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+                if (lean) launch_walkc<false, false, false, true, true, true>(blocks, P, S, T, d_root, ctl, C, st);
+                else launch_walkc<false, false, false, true, false, true>(blocks, P, S, T, d_root, ctl, C, st);
             } else {
-                if (lean) walkc_kernel<false, false, false, false, true, true><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
-                else walkc_kernel<false, false, false, false, false, true><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+                if (lean) launch_walkc<false, false, false, false, true, true>(blocks, P, S, T, d_root, ctl, C, st);
+                else launch_walkc<false, false, false, false, false, true>(blocks, P, S, T, d_root, ctl, C, st);
             }
         } else if (P.periodic) {
-            if (lean) walkc_kernel<MAGGM, REL, BRK, true, PLAIN><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
-            else walkc_kernel<MAGGM, REL, BRK, true><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+            if (lean) launch_walkc<MAGGM, REL, BRK, true, PLAIN>(blocks, P, S, T, d_root, ctl, C, st);
+            else launch_walkc<MAGGM, REL, BRK, true>(blocks, P, S, T, d_root, ctl, C, st);
         } else {
-            if (lean) walkc_kernel<MAGGM, REL, BRK, false, PLAIN><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
-            else walkc_kernel<MAGGM, REL, BRK, false><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+            if (lean) launch_walkc<MAGGM, REL, BRK, false, PLAIN>(blocks, P, S, T, d_root, ctl, C, st);
+            else launch_walkc<MAGGM, REL, BRK, false>(blocks, P, S, T, d_root, ctl, C, st);
         }
     } else {
         const int blocks = std::max(1, (n_cap + DIRECT_THREADS - 1) / DIRECT_THREADS);
