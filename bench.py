@@ -41,7 +41,7 @@ UNIT = "particle-substeps/s"
 # tidal torque 16, Yukawa 16.
 FLOP_PER_INTERACTION_GCY = 58
 # DRAM bytes of one walk launch at N = 1M, theta 0.0955 (ncu, read 576.0 MB + write 186.0 MB)
-WALK_TRAFFIC_BYTES = 762.0e6
+WALK_TRAFFIC_BYTES = 767.4e6
 STATE_KEYS = ("x", "y", "wx", "wy", "mass", "charge", "angw")
 
 
