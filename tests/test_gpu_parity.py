@@ -243,6 +243,26 @@ def test_frames_edge_crossings(gpu_lib, oracle_mod, topology):
         assert err["norm"] <= TRAJ_TOL, (k, err)
 
 
+@pytest.mark.parametrize("relativity", [False, True])
+def test_nan_velocity_is_zeroed(gpu_lib, oracle_mod, relativity):
+    """A particle loaded with a NaN proper velocity: the kick's NaN guard
+    zeroes its velocity (integrator.js:921-922), and the spin guard zeroes
+    every spin its NaN cell velocity reaches through the tidal torque; the
+    same particles on both sides, and no NaN left anywhere."""
+    wl = W.small_disk(256, relativity=relativity, softening=8.0)
+    wl.state["wx"][5] = np.nan
+    g, o = load_both(wl)
+    assert g.update(wl.dt) == o.update(wl.dt)
+    sg, so = g.state(f64=True), o.state()
+    g.close()
+    for k in ("x", "y", "wx", "wy", "angw"):
+        assert not np.isnan(sg[k]).any(), k
+    assert sg["wx"][5] == 0 and sg["wy"][5] == 0
+    assert np.array_equal(sg["angw"] == 0, so["angw"] == 0)
+    for k in ("x", "y", "wx", "wy"):
+        assert rel_err(sg[k], so[k])["norm"] <= TRAJ_TOL, k
+
+
 def test_despawn_compaction_matches(gpu_lib, oracle_mod):
     wl = W.small_disk(256, relativity=False, softening=8.0)
     wl.state["x"][[3, 100, 200]] = [170.0, -70.0, 180.0]
