@@ -118,6 +118,8 @@ struct GeonHandle {
     double* stats_h = nullptr;     // pinned
     double simTime = 0.0;
     bool forcesInit = false;
+    float* dpart = nullptr;          // pairwise-sum slice partials (direct_plan), grown on demand
+    size_t dpart_floats = 0;
     int histStride = 0;
     long long histTotal = 0;
     int lastSubsteps = 0;
@@ -647,6 +649,28 @@ static bool bosons_act(const GeonHandle* h) {
     return (h->prm.flags & GEON_FLAG_BOSONS) && h->nb > 0 && h->bos && (h->prm.toggles & GEON_GRAVITY);
 }
 
+// The pairwise sum over few targets runs split over source slices that fill
+// the GPU; their partial sums need scratch, allocated on first use.  Without
+// it the pass runs unsliced.
+static void direct_slices(GeonHandle* h, ForceCtx& C) {
+    const DirectPlan pl = direct_plan(h->P, C.brk != 0, h->n_cap);
+    if (pl.slices <= 1) return;
+    if (h->dpart_floats < pl.floats) {
+        cudaStreamSynchronize(h->st);
+        if (h->dpart) cudaFree(h->dpart);
+        h->dpart = nullptr;
+        h->dpart_floats = 0;
+        if (cudaMalloc(&h->dpart, pl.floats * sizeof(float)) != cudaSuccess) {
+            cudaGetLastError();
+            h->dpart = nullptr;
+            return;
+        }
+        h->dpart_floats = pl.floats;
+    }
+    C.dpart = h->dpart;
+    C.dslices = pl.slices;
+}
+
 static int run_force_pass(GeonHandle* h, bool rebuild) {
     const bool bh = bh_on(h);
     if (bh && rebuild) { int r = build_tree(h); if (r) return r; }
@@ -655,8 +679,10 @@ static int run_force_pass(GeonHandle* h, bool rebuild) {
         int r = learned_force_pass(h);
         if (r || !bosons_act(h)) return r;
     } else {
+        ForceCtx C = make_ctx(h);
+        if (!bh) direct_slices(h, C);
         const int ps = prof_begin(h, PH_FORCE);
-        force_pass(h->P, h->S, h->T, h->d_root, h->ctl, make_ctx(h), bh, h->n_cap, h->st, h->lc);
+        force_pass(h->P, h->S, h->T, h->d_root, h->ctl, C, bh, h->n_cap, h->st, h->lc);
         prof_end(h, ps);
         CKL();
     }
@@ -880,6 +906,7 @@ int geon_destroy(GeonHandle* h) {
     if (h->bos) { geon_destroy(h->bos); h->bos = nullptr; }
     if (h->col_h) cudaFreeHost(h->col_h);
     if (h->pairs) cudaFree(h->pairs);
+    if (h->dpart) cudaFree(h->dpart);
     if (h->batch) {
         Batch* B = h->batch;
         if (B->exec) cudaGraphExecDestroy(B->exec);

@@ -1124,8 +1124,16 @@ static void launch_walkc(int blocks, const DevParams& P, const DevState& S, cons
 // ---- pairwise O(N^2) sum (forces.js:94-125) -------------------------------------------------
 constexpr int DIRECT_THREADS = 256;
 
+// Partial sums of one source slice: hi and lo of every accumulated quantity,
+// then the interaction count, each a row of (gridDim.x * DIRECT_THREADS) floats.
+template <bool MAGGM, bool BRK>
+__host__ __device__ constexpr int direct_part_rows() { return 2 * Acc<MAGGM, BRK>::NQ + 1; }
+
+// blockIdx.y selects a slice of the source tiles (gridDim.y slices).  With
+// one slice the kernel finishes each target itself; with more it writes the
+// slice's partial sums to C.dpart and direct_combine_kernel finishes.
 template <bool MAGGM, bool REL, bool BRK>
-__global__ void __launch_bounds__(DIRECT_THREADS)
+__global__ void __launch_bounds__(DIRECT_THREADS, (MAGGM || REL || BRK) ? 2 : 3)
 direct_kernel(DevParams P, DevState S, FrameCtl* ctl, ForceCtx C) {
     __shared__ float4 s_pos[DIRECT_THREADS];
     __shared__ float4 s_vel[DIRECT_THREADS];   // vx, vy, angVel, radius^2
@@ -1142,7 +1150,10 @@ direct_kernel(DevParams P, DevState S, FrameCtl* ctl, ForceCtx C) {
     A.init();
     unsigned inter = 0;
     const bool pe = C.pe != 0;
-    for (int base = 0; base < n; base += DIRECT_THREADS) {
+    const int ntile = (n + DIRECT_THREADS - 1) / DIRECT_THREADS;
+    const int tile0 = (int)((long long)ntile * blockIdx.y / gridDim.y);
+    const int tile1 = (int)((long long)ntile * (blockIdx.y + 1) / gridDim.y);
+    for (int base = tile0 * DIRECT_THREADS; base < tile1 * DIRECT_THREADS; base += DIRECT_THREADS) {
         const int j = base + threadIdx.x;
         __syncthreads();
         if (j < n) {
@@ -1185,7 +1196,93 @@ direct_kernel(DevParams P, DevState S, FrameCtl* ctl, ForceCtx C) {
             inter++;
         }
     }
+    if (gridDim.y == 1) {
+        finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter);
+        return;
+    }
+    A.flush();
+    if (valid) {
+        constexpr int NQ = Acc<MAGGM, BRK>::NQ;
+        const size_t stride = (size_t)gridDim.x * DIRECT_THREADS;
+        float* part = C.dpart + (size_t)blockIdx.y * direct_part_rows<MAGGM, BRK>() * stride + i;
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+            part[(size_t)q * stride] = A.hi(q);
+            part[(size_t)(NQ + q) * stride] = A.lo(q);
+        }
+        part[(size_t)(2 * NQ) * stride] = __uint_as_float(inter);
+    }
+}
+
+// Adds the slices' partial sums in slice order through the same compensated
+// accumulator, then runs the per-particle epilogue of the pairwise sum.
+template <bool MAGGM, bool BRK>
+__global__ void __launch_bounds__(DIRECT_THREADS)
+direct_combine_kernel(DevParams P, DevState S, FrameCtl* ctl, ForceCtx C, int slices) {
+    const int n = ctl->n;
+    const int i = blockIdx.x * DIRECT_THREADS + threadIdx.x;
+    const bool valid = i < n;
+    Tgt t;
+    if (valid) { t = load_target(S, i); target_coupling(P, t); }
+    else { t = Tgt{}; t.idx = -1; }
+    Acc<MAGGM, BRK> A;
+    A.init();
+    unsigned inter = 0;
+    if (valid) {
+        constexpr int NQ = Acc<MAGGM, BRK>::NQ;
+        const size_t stride = (size_t)gridDim.x * DIRECT_THREADS;
+        for (int y = 0; y < slices; y++) {
+            const float* part = C.dpart + (size_t)y * direct_part_rows<MAGGM, BRK>() * stride + i;
+#pragma unroll
+            for (int q = 0; q < NQ; q++) A.part[q] = part[(size_t)q * stride];
+            A.flush();
+#pragma unroll
+            for (int q = 0; q < NQ; q++) A.part[q] = part[(size_t)(NQ + q) * stride];
+            A.flush();
+            inter += __float_as_uint(part[(size_t)(2 * NQ) * stride]);
+        }
+    }
     finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter);
+}
+
+// Source slices for the pairwise sum: the fewest that bring the CTAs' wave
+// efficiency within 2 % of the best, at most 16 slices and 8 waves.
+template <bool MAGGM, bool REL, bool BRK>
+static DirectPlan direct_plan_t(int n_cap) {
+    static int occ = 0, sms = 0;
+    if (!occ) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, direct_kernel<MAGGM, REL, BRK>, DIRECT_THREADS, 0);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (occ < 1) occ = 1;
+        if (sms < 1) sms = 1;
+    }
+    const long long blocks = std::max(1, (n_cap + DIRECT_THREADS - 1) / DIRECT_THREADS);
+    const long long slots = (long long)occ * sms;
+    auto eff = [&](int s) {
+        const long long c = blocks * s;
+        return (double)c / (double)(((c + slots - 1) / slots) * slots);
+    };
+    int best = 1;
+    double bestEff = eff(1);
+    for (int s = 2; s <= 16 && blocks * s <= 8 * slots; s++) {
+        const double e = eff(s);
+        if (e > bestEff + 0.02) { best = s; bestEff = e; }
+    }
+    const size_t floats = best > 1 ? (size_t)best * direct_part_rows<MAGGM, BRK>() * blocks * DIRECT_THREADS : 0;
+    return DirectPlan{ best, floats };
+}
+
+DirectPlan direct_plan(const DevParams& P, bool brk, int n_cap) {
+    const bool maggm = (P.toggles & (GEON_MAGNETIC | GEON_GRAVITOMAG | GEON_ONE_PN)) != 0;
+    const bool rel = P.rel != 0;
+    if (maggm) {
+        if (rel) return brk ? direct_plan_t<true, true, true>(n_cap) : direct_plan_t<true, true, false>(n_cap);
+        return brk ? direct_plan_t<true, false, true>(n_cap) : direct_plan_t<true, false, false>(n_cap);
+    }
+    if (rel) return brk ? direct_plan_t<false, true, true>(n_cap) : direct_plan_t<false, true, false>(n_cap);
+    return brk ? direct_plan_t<false, false, true>(n_cap) : direct_plan_t<false, false, false>(n_cap);
 }
 
 // ---- pairwise forces for a subset of targets (no state change) -----------------------------
@@ -1653,7 +1750,9 @@ static void launch_force(bool bh, const DevParams& P, const DevState& S, const T
         }
     } else {
         const int blocks = std::max(1, (n_cap + DIRECT_THREADS - 1) / DIRECT_THREADS);
-        direct_kernel<MAGGM, REL, BRK><<<blocks, DIRECT_THREADS, 0, st>>>(P, S, ctl, C);
+        const int slices = (C.dpart && C.dslices > 1) ? C.dslices : 1;
+        direct_kernel<MAGGM, REL, BRK><<<dim3(blocks, slices), DIRECT_THREADS, 0, st>>>(P, S, ctl, C);
+        if (slices > 1) direct_combine_kernel<MAGGM, BRK><<<blocks, DIRECT_THREADS, 0, st>>>(P, S, ctl, C, slices);
     }
 }
 
@@ -1670,7 +1769,7 @@ void force_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const 
         if (rel) { if (brk) launch_force<false, true, true>(bh, P, S, T, d_root, ctl, C, n_cap, st); else launch_force<false, true, false>(bh, P, S, T, d_root, ctl, C, n_cap, st); }
         else     { if (brk) launch_force<false, false, true>(bh, P, S, T, d_root, ctl, C, n_cap, st); else launch_force<false, false, false>(bh, P, S, T, d_root, ctl, C, n_cap, st); }
     }
-    lc.add(clear ? 2 : 1);
+    lc.add((clear ? 2 : 1) + ((!bh && C.dpart && C.dslices > 1) ? 1 : 0));
 }
 
 void onepn_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,

@@ -28,7 +28,17 @@ struct ForceCtx {
     int2* pairs;
     long long pair_cap;
     unsigned long long* pair_count;
+    // pairwise sum split over source slices (direct_plan): scratch of partial
+    // sums, null or dslices <= 1 for one pass over all sources
+    float* dpart;
+    int dslices;
 };
+
+// How the pairwise sum over n_cap targets is split: the number of source
+// slices that fills whole waves of the GPU (1 when the targets alone do) and
+// the scratch floats they need.
+struct DirectPlan { int slices; size_t floats; };
+DirectPlan direct_plan(const DevParams& P, bool brk, int n_cap);
 
 // Force pass: resetForces + computeAllForces (+ external fields, bounce
 // walls) for every particle, with the max-acceleration / cyclotron
