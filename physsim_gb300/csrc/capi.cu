@@ -652,8 +652,7 @@ static bool bosons_act(const GeonHandle* h) {
 // The pairwise sum over few targets runs split over source slices that fill
 // the GPU; their partial sums need scratch, allocated on first use.  Without
 // it the pass runs unsliced.
-static void direct_slices(GeonHandle* h, ForceCtx& C) {
-    const DirectPlan pl = direct_plan(h->P, C.brk != 0, h->n_cap);
+static void use_slices(GeonHandle* h, ForceCtx& C, const DirectPlan& pl) {
     if (pl.slices <= 1) return;
     if (h->dpart_floats < pl.floats) {
         cudaStreamSynchronize(h->st);
@@ -669,6 +668,14 @@ static void direct_slices(GeonHandle* h, ForceCtx& C) {
     }
     C.dpart = h->dpart;
     C.dslices = pl.slices;
+}
+
+static void direct_slices(GeonHandle* h, ForceCtx& C) { use_slices(h, C, direct_plan(h->P, C.brk != 0, h->n_cap)); }
+
+static ForceCtx onepn_ctx(GeonHandle* h, bool bh) {
+    ForceCtx C = make_ctx(h);
+    if (!bh) use_slices(h, C, direct1pn_plan(h->n_cap));
+    return C;
 }
 
 static int run_force_pass(GeonHandle* h, bool rebuild) {
@@ -1113,7 +1120,7 @@ int geon_compute_1pn(GeonHandle* h) {
     const bool bh = bh_on(h);
     if (bh) { int r = build_tree(h); if (r) return r; }
     launch_hist_tables(h->hist_t, h->simTime, h->hist_age, h->hist_segdt, h->st, h->lc);
-    onepn_pass(h->P, h->S, h->T, h->d_root, h->ctl, make_ctx(h), bh, h->n_cap, h->st, h->lc);
+    onepn_pass(h->P, h->S, h->T, h->d_root, h->ctl, onepn_ctx(h, bh), bh, h->n_cap, h->st, h->lc);
     CKL();
     return read_ctl(h);
 }
@@ -1627,7 +1634,7 @@ int geon_update(GeonHandle* h, double dt, int32_t* substeps) {
             if (bh) { r = build_tree(h); if (r) return r; haveTree = true; }
             launch_hist_tables(h->hist_t, h->simTime, h->hist_age, h->hist_segdt, h->st, h->lc);
             const int ps = prof_begin(h, PH_ONEPN);
-            onepn_pass(h->P, h->S, h->T, h->d_root, h->ctl, make_ctx(h), bh, h->n_cap, h->st, h->lc);
+            onepn_pass(h->P, h->S, h->T, h->d_root, h->ctl, onepn_ctx(h, bh), bh, h->n_cap, h->st, h->lc);
             prof_end(h, ps);
             launch_vv_kick(h->P, h->S, h->ctl, (float)(dtSub * 0.5), h->n_cap, h->st, h->lc);
             CKL();

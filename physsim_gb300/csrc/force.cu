@@ -1245,8 +1245,24 @@ direct_combine_kernel(DevParams P, DevState S, FrameCtl* ctl, ForceCtx C, int sl
     finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter);
 }
 
-// Source slices for the pairwise sum: the fewest that bring the CTAs' wave
-// efficiency within 2 % of the best, at most 16 slices and 8 waves.
+// Source slices for a pairwise sum over n_cap targets with `slots` resident
+// CTAs: each added slice must raise the CTAs' wave efficiency (CTAs over
+// whole waves of slots) by 2 %; at most 16 slices and 8 waves.
+static int direct_slice_count(int n_cap, long long slots) {
+    const long long blocks = std::max(1, (n_cap + DIRECT_THREADS - 1) / DIRECT_THREADS);
+    auto eff = [&](int s) {
+        const long long c = blocks * s;
+        return (double)c / (double)(((c + slots - 1) / slots) * slots);
+    };
+    int best = 1;
+    double bestEff = eff(1);
+    for (int s = 2; s <= 16 && blocks * s <= 8 * slots; s++) {
+        const double e = eff(s);
+        if (e > bestEff + 0.02) { best = s; bestEff = e; }
+    }
+    return best;
+}
+
 template <bool MAGGM, bool REL, bool BRK>
 static DirectPlan direct_plan_t(int n_cap) {
     static int occ = 0, sms = 0;
@@ -1258,18 +1274,8 @@ static DirectPlan direct_plan_t(int n_cap) {
         if (occ < 1) occ = 1;
         if (sms < 1) sms = 1;
     }
+    const int best = direct_slice_count(n_cap, (long long)occ * sms);
     const long long blocks = std::max(1, (n_cap + DIRECT_THREADS - 1) / DIRECT_THREADS);
-    const long long slots = (long long)occ * sms;
-    auto eff = [&](int s) {
-        const long long c = blocks * s;
-        return (double)c / (double)(((c + slots - 1) / slots) * slots);
-    };
-    int best = 1;
-    double bestEff = eff(1);
-    for (int s = 2; s <= 16 && blocks * s <= 8 * slots; s++) {
-        const double e = eff(s);
-        if (e > bestEff + 0.02) { best = s; bestEff = e; }
-    }
     const size_t floats = best > 1 ? (size_t)best * direct_part_rows<MAGGM, BRK>() * blocks * DIRECT_THREADS : 0;
     return DirectPlan{ best, floats };
 }
@@ -1681,6 +1687,9 @@ walk1pn_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_ro
     if (valid) S.f1pn[t.idx] = make_float2(A.x.value(), A.y.value());
 }
 
+// blockIdx.y selects a slice of the source tiles, as in direct_kernel; with
+// more than one slice the partial sums (x hi, x lo, y hi, y lo) go to C.dpart
+// and direct1pn_combine_kernel finishes.
 __global__ void __launch_bounds__(DIRECT_THREADS)
 direct1pn_kernel(DevParams P, DevState S, FrameCtl* ctl, ForceCtx C) {
     __shared__ float4 s_pos[DIRECT_THREADS];
@@ -1693,7 +1702,10 @@ direct1pn_kernel(DevParams P, DevState S, FrameCtl* ctl, ForceCtx C) {
     if (valid) t = load_target(S, i);
     else { t = Tgt{}; t.idx = -1; }
     Acc2 A; A.init();
-    for (int base = 0; base < n; base += DIRECT_THREADS) {
+    const int ntile = (n + DIRECT_THREADS - 1) / DIRECT_THREADS;
+    const int tile0 = (int)((long long)ntile * blockIdx.y / gridDim.y);
+    const int tile1 = (int)((long long)ntile * (blockIdx.y + 1) / gridDim.y);
+    for (int base = tile0 * DIRECT_THREADS; base < tile1 * DIRECT_THREADS; base += DIRECT_THREADS) {
         const int j = base + threadIdx.x;
         __syncthreads();
         if (j < n) s_pos[threadIdx.x] = S.pos[j];
@@ -1712,7 +1724,50 @@ direct1pn_kernel(DevParams P, DevState S, FrameCtl* ctl, ForceCtx C) {
         }
     }
     A.flush();
-    if (valid) S.f1pn[i] = make_float2(A.x.value(), A.y.value());
+    if (!valid) return;
+    if (gridDim.y == 1) {
+        S.f1pn[i] = make_float2(A.x.value(), A.y.value());
+        return;
+    }
+    const size_t stride = (size_t)gridDim.x * DIRECT_THREADS;
+    float* part = C.dpart + (size_t)blockIdx.y * 4 * stride + i;
+    part[0] = A.x.hi;
+    part[stride] = A.x.lo;
+    part[2 * stride] = A.y.hi;
+    part[3 * stride] = A.y.lo;
+}
+
+__global__ void __launch_bounds__(DIRECT_THREADS)
+direct1pn_combine_kernel(DevState S, const FrameCtl* ctl, ForceCtx C, int slices) {
+    const int i = blockIdx.x * DIRECT_THREADS + threadIdx.x;
+    if (i >= ctl->n) return;
+    const size_t stride = (size_t)gridDim.x * DIRECT_THREADS;
+    CAcc x, y;
+    x.init();
+    y.init();
+    for (int k = 0; k < slices; k++) {
+        const float* part = C.dpart + (size_t)k * 4 * stride + i;
+        x.add(part[0]);
+        x.add(part[stride]);
+        y.add(part[2 * stride]);
+        y.add(part[3 * stride]);
+    }
+    S.f1pn[i] = make_float2(x.value(), y.value());
+}
+
+DirectPlan direct1pn_plan(int n_cap) {
+    static int occ = 0, sms = 0;
+    if (!occ) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, direct1pn_kernel, DIRECT_THREADS, 0);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (occ < 1) occ = 1;
+        if (sms < 1) sms = 1;
+    }
+    const int best = direct_slice_count(n_cap, (long long)occ * sms);
+    const long long blocks = std::max(1, (n_cap + DIRECT_THREADS - 1) / DIRECT_THREADS);
+    return DirectPlan{ best, best > 1 ? (size_t)best * 4 * blocks * DIRECT_THREADS : 0 };
 }
 
 // ---- dispatch ---------------------------------------------------------------------------------
@@ -1779,7 +1834,9 @@ void onepn_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const 
         walk1pn_kernel<<<blocks, WALK_THREADS, 0, st>>>(P, S, T, d_root, ctl, C);
     } else {
         const int blocks = std::max(1, (n_cap + DIRECT_THREADS - 1) / DIRECT_THREADS);
-        direct1pn_kernel<<<blocks, DIRECT_THREADS, 0, st>>>(P, S, ctl, C);
+        const int slices = (C.dpart && C.dslices > 1) ? C.dslices : 1;
+        direct1pn_kernel<<<dim3(blocks, slices), DIRECT_THREADS, 0, st>>>(P, S, ctl, C);
+        if (slices > 1) { direct1pn_combine_kernel<<<blocks, DIRECT_THREADS, 0, st>>>(S, ctl, C, slices); lc.add(1); }
     }
     lc.add(1);
 }

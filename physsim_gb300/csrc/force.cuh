@@ -39,6 +39,7 @@ struct ForceCtx {
 // the scratch floats they need.
 struct DirectPlan { int slices; size_t floats; };
 DirectPlan direct_plan(const DevParams& P, bool brk, int n_cap);
+DirectPlan direct1pn_plan(int n_cap);   // the same for the 1PN-only pairwise pass
 
 // Force pass: resetForces + computeAllForces (+ external fields, bounce
 // walls) for every particle, with the max-acceleration / cyclotron
