@@ -41,7 +41,8 @@ enum { K_GX = 0, K_GY, K_CX, K_CY, K_MX, K_MY, K_GMX, K_GMY, K_YX, K_YY, K_N };
 // start of the dynamic buffer, [2 * NQ][ACC_SH_THREADS] with one column per
 // thread, instead of registers.  They are touched only every FLUSH_EVERY
 // terms; the registers they free let the open-box Barnes-Hut walk run six
-// CTAs per SM instead of five without spills.
+// CTAs per SM instead of five without spills (the dipole / 1PN walks: four
+// instead of three).
 extern __shared__ __align__(16) unsigned char geon_dsmem[];
 constexpr int ACC_SH_THREADS = 128;
 template <bool MAGGM, bool BRK, bool SH = false>
@@ -869,12 +870,25 @@ __device__ __forceinline__ void list_entries(WS& W, unsigned m, unsigned active,
 // still 2 % faster than at five); the other forms keep them in registers.
 template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE>
 __host__ __device__ constexpr bool wc_six() { return !MAGGM && !REL && !BRK && NOPE; }
+// The walks with dipole / 1PN terms and without breakdown rows take the same
+// shared-memory form and run four CTAs per SM instead of three (torus
+// N = 65,536 with the full force set: 12 % faster).  The relativistic walk
+// without them keeps the register form: on small systems, which a single
+// wave covers, the shared-memory form only adds work (N = 2,048: 6 % slower).
+template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE>
+__host__ __device__ constexpr bool wc_four() { return MAGGM && !BRK; }
+template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE>
+__host__ __device__ constexpr bool wc_sh() { return wc_six<MAGGM, REL, BRK, PER, NOPE>() || wc_four<MAGGM, REL, BRK, PER, NOPE>(); }
+template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE>
+__host__ __device__ constexpr int wc_min_blocks() {
+    return wc_six<MAGGM, REL, BRK, PER, NOPE>() ? 6 : wc_four<MAGGM, REL, BRK, PER, NOPE>() ? 4 : (MAGGM || REL || BRK) ? 3 : 5;
+}
 
 template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE = false, bool EMIT = false>
-__global__ void __launch_bounds__(WC_THREADS, (MAGGM || REL || BRK) ? 3 : (wc_six<MAGGM, REL, BRK, PER, NOPE>() ? 6 : 5))
+__global__ void __launch_bounds__(WC_THREADS, wc_min_blocks<MAGGM, REL, BRK, PER, NOPE>())
 walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
     constexpr bool NEEDC = MAGGM || REL;
-    constexpr bool SIX = wc_six<MAGGM, REL, BRK, PER, NOPE>();
+    constexpr bool SIX = wc_sh<MAGGM, REL, BRK, PER, NOPE>();   // shared-memory form
     using AccT = Acc<MAGGM, BRK, SIX>;
     using WS = WcSmem<NEEDC, SIX ? WC_POOL_SIX : WC_POOL_WIDE>;
     unsigned char* wc_smem = geon_dsmem + AccT::SH_BYTES;
@@ -1097,7 +1111,7 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
 // relativity is on.
 template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE>
 constexpr size_t wc_smem_bytes() {
-    constexpr bool SIX = wc_six<MAGGM, REL, BRK, PER, NOPE>();
+    constexpr bool SIX = wc_sh<MAGGM, REL, BRK, PER, NOPE>();
     return Acc<MAGGM, BRK, SIX>::SH_BYTES + sizeof(WcSmem<MAGGM || REL, SIX ? WC_POOL_SIX : WC_POOL_WIDE>) * WC_WARPS +
            (REL ? 2 * HIST_LEN * sizeof(float) : 0);
 }
@@ -1105,6 +1119,8 @@ static_assert(6 * (wc_smem_bytes<false, false, false, false, true>() + 1024) <= 
               "six plain walk CTAs per SM must fit in shared memory");
 static_assert(6 * (wc_smem_bytes<false, false, false, true, true>() + 1024) <= 228 * 1024,
               "six periodic plain walk CTAs per SM must fit in shared memory");
+static_assert(4 * (wc_smem_bytes<true, true, false, true, false>() + 1024) <= 228 * 1024,
+              "four dipole / 1PN walk CTAs per SM must fit in shared memory");
 static_assert(5 * (wc_smem_bytes<false, false, false, true, false>() + 1024) <= 228 * 1024,
               "five walk CTAs per SM must fit in shared memory");
 
