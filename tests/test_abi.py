@@ -32,6 +32,12 @@ def test_bindings_cover_header(gpu_lib):
     assert sorted(N.SIGNATURES) == declared_symbols()
 
 
+def test_integration_notes_name_every_entry_point():
+    notes = (ROOT / "INTEGRATION.md").read_text()
+    missing = [s for s in declared_symbols() if s not in notes]
+    assert not missing, f"entry points INTEGRATION.md does not name: {missing}"
+
+
 def test_version_and_error_strings(gpu_lib):
     assert gpu_lib.geon_version().startswith(b"geon-gb300")
     assert isinstance(gpu_lib.geon_last_error(None), bytes)
