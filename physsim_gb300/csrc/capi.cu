@@ -1647,6 +1647,10 @@ int geon_update(GeonHandle* h, double dt, int32_t* substeps) {
         }
         r = run_force_pass(h, !haveTree);                                  // integrator.js:1336-1348, 1489-1493
         if (r) { h->col_tgt_active = false; return r; }
+        // The planner maxima are read back only for a substep that follows;
+        // after the last one the boundary step's read reports any device flag.
+        const bool another = dtRemain > EPS && totalSteps < maxSub;
+        if (!another && !merge && !h->prof) continue;
         r = read_ctl(h);
         if (r) { h->col_tgt_active = false; return r; }
         if (colSpawned >= 0) { r = collide_finish(h, colSpawned, colRemoved); if (r) return r; }
