@@ -508,6 +508,7 @@ def run_configs(args, g_big, wl_big, idx, fx, fy, fp32_peak):
     out["plummer_disk_n1048576_theta_sweep"] = sweep
     out["sparse_field_merge"] = run_merge()
     out["boson_pool"] = run_bosons()
+    out["heatmap"] = run_heatmap()
     return out
 
 
@@ -555,6 +556,51 @@ def run_bosons():
     return {"n": wl.n, "bosons": nb, "force_pass_ms": plain, "force_pass_with_boson_gravity_ms": with_bosons,
             "boson_gravity_ms": with_bosons - plain, "kicks_ms_incl_copy": kicks,
             "set_bosons_ms_incl_tree": upload_ms}
+
+
+def run_heatmap():
+    """The potential heat map (heatmap.js:38-101, 133-206, 278-302): gravity,
+    electric and Yukawa grids with the 3 x 3 blur over the whole box, at the
+    reference's CPU grid (64 x 64) and its GPU overlay grid (128 x 128).  Tree
+    mode on the N = 1M Plummer disk (the tree of the current state is built
+    inside the call), pairwise mode on the N = 65,536 torus clusters; the FP64
+    oracle on all host threads times the 64 x 64 tree case."""
+    import torch
+    from physsim_gb300 import _native as N, workloads as W
+    from physsim_gb300.system import GeonSystem
+    from oracle import oracle
+    res = {}
+    for name, wl in (("plummer_disk_n1048576_tree", W.plummer_disk(1 << 20, theta=0.5)),
+                     ("clusters_torus_n65536_pairwise", W.clusters_torus(65536, barnes_hut=False, relativity=False))):
+        g = GeonSystem(wl.params, wl.n)
+        g.upload(*[wl.state[k] for k in STATE_KEYS])
+        st = torch.cuda.ExternalStream(g.stream_ptr())
+        L, H = wl.params.domain_w, wl.params.domain_h
+        entry = {"n": wl.n, "tree": bool(wl.params.toggles & N.BARNES_HUT)}
+        for grid in (64, 128):
+            call = lambda: g.heatmap(0.0, 0.0, L / grid, H / grid, grid, blur=True)
+            call()
+            g.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reps = 5
+            e0.record(st)
+            for _ in range(reps):
+                call()
+            e1.record(st)
+            e1.synchronize()
+            entry[f"grid{grid}_ms_incl_copy"] = e0.elapsed_time(e1) / reps
+        g.close()
+        res[name] = entry
+    wl = W.plummer_disk(1 << 20, theta=0.5)
+    o = oracle.OracleSim(wl.params, threads=oracle.max_threads())
+    o.add(*[wl.state[k] for k in STATE_KEYS])
+    t0 = time.perf_counter()
+    o.heatmap(0.0, 0.0, wl.params.domain_w / 64, wl.params.domain_h / 64, 64, blur=True)
+    res["plummer_disk_n1048576_tree"]["cpu_baseline"] = {
+        "grid64_ms": 1e3 * (time.perf_counter() - t0), "cores": oracle.max_threads(), "kind": "port",
+        "sample": "the same 64 x 64 tree heat map (tree build included) in the FP64 restatement"}
+    o.close()
+    return res
 
 
 def run_merge():
