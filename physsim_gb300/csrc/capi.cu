@@ -1464,12 +1464,14 @@ int geon_heatmap(GeonHandle* h, double left, double top, double cell_w, double c
     float* d_e = tmp.alloc<float>(gg);
     float* d_y = tmp.alloc<float>(gg);
     float* d_t = tmp.alloc<float>(gg);
+    const int slices = heatmap_slices(h->P, grid, tree);
+    float* d_part = slices > 1 ? tmp.alloc<float>((size_t)slices * 6 * gg) : nullptr;
     if (tmp.failed) { tmp.free_all(); return set_err(h, GEON_ERR_NOMEM, "heat map allocation failed"); }
     cudaError_t e = cudaSuccess;
     if (h->P.rel) { launch_hist_tables(h->hist_t, h->simTime, h->hist_age, h->hist_segdt, h->st, h->lc); e = cudaGetLastError(); }
     if (e == cudaSuccess) {
         heatmap_pass(h->P, h->S, h->T, h->d_root, h->ctl, make_ctx(h), left, top, cell_w, cell_h, grid, doG, doE, doY,
-                     tree, blur != 0, d_g, d_e, d_y, d_t, h->st, h->lc);
+                     tree, blur != 0, d_g, d_e, d_y, d_t, d_part, slices, h->st, h->lc);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(grav, d_g, gg * sizeof(float), cudaMemcpyDeviceToHost, h->st);

@@ -1264,8 +1264,7 @@ direct_combine_kernel(DevParams P, DevState S, FrameCtl* ctl, ForceCtx C, int sl
 // Source slices for a pairwise sum over n_cap targets with `slots` resident
 // CTAs: each added slice must raise the CTAs' wave efficiency (CTAs over
 // whole waves of slots) by 2 %; at most 16 slices and 8 waves.
-static int direct_slice_count(int n_cap, long long slots) {
-    const long long blocks = std::max(1, (n_cap + DIRECT_THREADS - 1) / DIRECT_THREADS);
+static int slice_count(long long blocks, long long slots) {
     auto eff = [&](int s) {
         const long long c = blocks * s;
         return (double)c / (double)(((c + slots - 1) / slots) * slots);
@@ -1277,6 +1276,10 @@ static int direct_slice_count(int n_cap, long long slots) {
         if (e > bestEff + 0.02) { best = s; bestEff = e; }
     }
     return best;
+}
+
+static int direct_slice_count(int n_cap, long long slots) {
+    return slice_count(std::max(1, (n_cap + DIRECT_THREADS - 1) / DIRECT_THREADS), slots);
 }
 
 template <bool MAGGM, bool REL, bool BRK>
@@ -1421,7 +1424,7 @@ template <bool REL>
 __global__ void __launch_bounds__(HM_THREADS)
 heatmap_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C,
                double left, double top, double cw, double chh, int G, int doG_, int doE_, int doY_, int useTree,
-               float* __restrict__ gOut, float* __restrict__ eOut, float* __restrict__ yOut) {
+               float* __restrict__ gOut, float* __restrict__ eOut, float* __restrict__ yOut, float* __restrict__ part) {
     __shared__ float s_age[REL ? HIST_LEN : 1], s_segdt[REL ? HIST_LEN : 1];
     if (REL) load_hist_tables(C, s_age, s_segdt);
     const bool doG = doG_ != 0, doE = doE_ != 0, doY = doY_ != 0;
@@ -1495,7 +1498,10 @@ heatmap_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_ro
             }
         }
     } else {
-        for (int i = 0; i < n; i++) {
+        // pairwise: blockIdx.y selects a slice of the sources (gridDim.y slices)
+        const int i0 = (int)((long long)n * blockIdx.y / gridDim.y);
+        const int i1 = (int)((long long)n * (blockIdx.y + 1) / gridDim.y);
+        for (int i = i0; i < i1; i++) {
             float rx, ry;
             const float4 p = S.pos[i];
             if (REL) {
@@ -1509,9 +1515,55 @@ heatmap_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_ro
             potential_terms(P, rx, ry, p.z, p.w, doG, doE, doY, true, g, e, y);
         }
     }
+    if (gridDim.y == 1) {
+        gOut[idx] = g.value();
+        eOut[idx] = e.value();
+        yOut[idx] = y.value();
+        return;
+    }
+    const size_t gg = (size_t)G * G;
+    float* q = part + (size_t)blockIdx.y * 6 * gg + idx;    // the slice's (hi, lo) per field
+    q[0] = g.hi; q[gg] = g.lo;
+    q[2 * gg] = e.hi; q[3 * gg] = e.lo;
+    q[4 * gg] = y.hi; q[5 * gg] = y.lo;
+}
+
+// Adds the pairwise heat map's slices in slice order (compensated).
+__global__ void __launch_bounds__(HM_THREADS)
+heatmap_combine_kernel(const float* __restrict__ part, int slices, int G, float* __restrict__ gOut,
+                       float* __restrict__ eOut, float* __restrict__ yOut) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t gg = (size_t)G * G;
+    if (idx >= (int)gg) return;
+    CAcc g, e, y;
+    g.init(); e.init(); y.init();
+    for (int k = 0; k < slices; k++) {
+        const float* q = part + (size_t)k * 6 * gg + idx;
+        g.add(q[0]); g.add(q[gg]);
+        e.add(q[2 * gg]); e.add(q[3 * gg]);
+        y.add(q[4 * gg]); y.add(q[5 * gg]);
+    }
     gOut[idx] = g.value();
     eOut[idx] = e.value();
     yOut[idx] = y.value();
+}
+
+int heatmap_slices(const DevParams& P, int G, bool useTree) {
+    if (useTree) return 1;
+    static int occ[2] = { 0, 0 }, sms = 0;
+    const int r = P.rel ? 1 : 0;
+    if (!occ[r]) {
+        if (r) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[r], heatmap_kernel<true>, HM_THREADS, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[r], heatmap_kernel<false>, HM_THREADS, 0);
+        if (occ[r] < 1) occ[r] = 1;
+    }
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms < 1) sms = 1;
+    }
+    return slice_count(((long long)G * G + HM_THREADS - 1) / HM_THREADS, (long long)occ[r] * sms);
 }
 
 // Heatmap._blur (heatmap.js:278-302): 3 x 3 box blur, clamp to edge, as two passes.
@@ -1530,11 +1582,18 @@ __global__ void blur_kernel(const float* __restrict__ in, float* __restrict__ ou
 
 void heatmap_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
                   const ForceCtx& C, double left, double top, double cw, double ch, int G, bool doG, bool doE, bool doY,
-                  bool useTree, bool blur, float* g, float* e, float* y, float* tmp, cudaStream_t st, LaunchCounter& lc) {
+                  bool useTree, bool blur, float* g, float* e, float* y, float* tmp, float* part, int slices,
+                  cudaStream_t st, LaunchCounter& lc) {
     const int blocks = (G * G + HM_THREADS - 1) / HM_THREADS;
-    if (P.rel) heatmap_kernel<true><<<blocks, HM_THREADS, 0, st>>>(P, S, T, d_root, ctl, C, left, top, cw, ch, G, doG, doE, doY, useTree, g, e, y);
-    else heatmap_kernel<false><<<blocks, HM_THREADS, 0, st>>>(P, S, T, d_root, ctl, C, left, top, cw, ch, G, doG, doE, doY, useTree, g, e, y);
+    if (useTree || !part) slices = 1;
+    const dim3 grid(blocks, std::max(slices, 1));
+    if (P.rel) heatmap_kernel<true><<<grid, HM_THREADS, 0, st>>>(P, S, T, d_root, ctl, C, left, top, cw, ch, G, doG, doE, doY, useTree, g, e, y, part);
+    else heatmap_kernel<false><<<grid, HM_THREADS, 0, st>>>(P, S, T, d_root, ctl, C, left, top, cw, ch, G, doG, doE, doY, useTree, g, e, y, part);
     lc.add(1);
+    if (slices > 1) {
+        heatmap_combine_kernel<<<blocks, HM_THREADS, 0, st>>>(part, slices, G, g, e, y);
+        lc.add(1);
+    }
     if (blur) {
         float* fields[3] = { g, e, y };
         const bool on3[3] = { doG, doE, doY };

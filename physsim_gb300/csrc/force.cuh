@@ -48,9 +48,14 @@ DirectPlan direct1pn_plan(int n_cap);   // the same for the 1PN-only pairwise pa
 // Potential heat map on a G x G grid of cell centres (heatmap.js:152-206):
 // tree walk (useTree, tree built) or pairwise sum; optional 3 x 3 box blur
 // of each computed field (tmp: G*G floats).  Device outputs of G*G floats.
+// The pairwise sum runs split over source slices (part: their partial sums).
 void heatmap_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
                   const ForceCtx& C, double left, double top, double cw, double ch, int G, bool doG, bool doE, bool doY,
-                  bool useTree, bool blur, float* g, float* e, float* y, float* tmp, cudaStream_t st, LaunchCounter& lc);
+                  bool useTree, bool blur, float* g, float* e, float* y, float* tmp, float* part, int slices,
+                  cudaStream_t st, LaunchCounter& lc);
+// Source slices of the pairwise heat map (1 in tree mode); `part` for
+// heatmap_pass then holds slices * 6 * G * G floats.
+int heatmap_slices(const DevParams& P, int G, bool useTree);
 
 // clear = false keeps the planner reductions and the interaction counter of
 // earlier passes (a force pass split over target chunks).
