@@ -1135,11 +1135,16 @@ int geon_direct_forces(GeonHandle* h, const int32_t* idx, int32_t k, float* fx, 
     int* d_idx = tmp.alloc<int>(k);
     float* d_fx = tmp.alloc<float>(k);
     float* d_fy = tmp.alloc<float>(k);
+    const DirectPlan pl = direct_subset_plan(h->P, k);           // source slices that fill the GPU
+    float* d_part = pl.slices > 1 ? tmp.alloc<float>(pl.floats) : nullptr;
     if (tmp.failed) { tmp.free_all(); return set_err(h, GEON_ERR_NOMEM, "direct-forces allocation failed"); }
+    ForceCtx C = make_ctx(h);
+    C.dpart = d_part;
+    C.dslices = pl.slices;
     cudaError_t e = cudaMemcpyAsync(d_idx, idx, k * sizeof(int), cudaMemcpyHostToDevice, h->st);
     if (e == cudaSuccess && h->P.rel) { launch_hist_tables(h->hist_t, h->simTime, h->hist_age, h->hist_segdt, h->st, h->lc); e = cudaGetLastError(); }
     if (e == cudaSuccess) {
-        direct_subset(h->P, h->S, h->ctl, make_ctx(h), d_idx, k, d_fx, d_fy, h->st, h->lc);
+        direct_subset(h->P, h->S, h->ctl, C, d_idx, k, d_fx, d_fy, h->st, h->lc);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(fx, d_fx, k * sizeof(float), cudaMemcpyDeviceToHost, h->st);
@@ -1820,9 +1825,11 @@ int geon_launch_count(GeonHandle* h, int64_t* count) {
 // nothing.
 //
 // Limits and rules:
-//   * at most GEON_DIRECT_NOALLOC_MAX_K targets per call (192 KiB of scratch:
+//   * at most GEON_DIRECT_NOALLOC_MAX_K targets per call (4.2 MiB of scratch:
 //     k indices, then k x forces, then k y forces, each row sized for the
-//     maximum); larger k is rejected with GEON_ERR_ARG;
+//     maximum, then the partial sums of up to 16 source slices, split as in
+//     geon_direct_forces so that both give identical bits); larger k is
+//     rejected with GEON_ERR_ARG;
 //   * the first call on a device does the setup (it looks up the array's
 //     device address with that device current and caches it per device), so
 //     make that first call before any stream capture begins;
@@ -1838,7 +1845,9 @@ int geon_launch_count(GeonHandle* h, int64_t* count) {
 
 static constexpr int NOALLOC_MAX_K = GEON_DIRECT_NOALLOC_MAX_K;
 static constexpr int NOALLOC_MAX_DEVICES = 64;
-static __device__ __align__(256) unsigned char g_direct_scratch[3 * NOALLOC_MAX_K * sizeof(float)];
+static constexpr size_t NOALLOC_PART_FLOATS = (size_t)16 * 4 * NOALLOC_MAX_K;   // slices x (fx, fy as hi, lo) x k
+static_assert(NOALLOC_MAX_K % 256 == 0, "slice rows are whole CTAs of targets");
+static __device__ __align__(256) unsigned char g_direct_scratch[(3 * NOALLOC_MAX_K + NOALLOC_PART_FLOATS) * sizeof(float)];
 static void* g_direct_scratch_addr[NOALLOC_MAX_DEVICES] = {};
 static std::mutex g_direct_scratch_mu;
 
@@ -1880,10 +1889,16 @@ extern "C" int geon_direct_forces_noalloc(GeonHandle* h, const int32_t* idx, int
     int* d_idx = static_cast<int*>(base);
     float* d_fx = reinterpret_cast<float*>(d_idx + NOALLOC_MAX_K);
     float* d_fy = d_fx + NOALLOC_MAX_K;
+    ForceCtx C = make_ctx(h);
+    const DirectPlan pl = direct_subset_plan(h->P, k);
+    if (pl.slices > 1 && pl.floats <= NOALLOC_PART_FLOATS) {
+        C.dpart = d_fy + NOALLOC_MAX_K;
+        C.dslices = pl.slices;
+    }
     cudaError_t e = cudaMemcpyAsync(d_idx, idx, k * sizeof(int), cudaMemcpyHostToDevice, h->st);
     if (e == cudaSuccess && h->P.rel) { launch_hist_tables(h->hist_t, h->simTime, h->hist_age, h->hist_segdt, h->st, h->lc); e = cudaGetLastError(); }
     if (e == cudaSuccess) {
-        direct_subset(h->P, h->S, h->ctl, make_ctx(h), d_idx, k, d_fx, d_fy, h->st, h->lc);
+        direct_subset(h->P, h->S, h->ctl, C, d_idx, k, d_fx, d_fy, h->st, h->lc);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(fx, d_fx, k * sizeof(float), cudaMemcpyDeviceToHost, h->st);

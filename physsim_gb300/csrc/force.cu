@@ -1332,7 +1332,10 @@ direct_subset_kernel(DevParams P, DevState S, const FrameCtl* ctl, ForceCtx C, c
     else { t = Tgt{}; t.idx = -1; }
     Acc<MAGGM, false> A;
     A.init();
-    for (int base = 0; base < n; base += DIRECT_THREADS) {
+    const int ntile = (n + DIRECT_THREADS - 1) / DIRECT_THREADS;       // blockIdx.y: a slice of the source tiles
+    const int tile0 = (int)((long long)ntile * blockIdx.y / gridDim.y);
+    const int tile1 = (int)((long long)ntile * (blockIdx.y + 1) / gridDim.y);
+    for (int base = tile0 * DIRECT_THREADS; base < tile1 * DIRECT_THREADS; base += DIRECT_THREADS) {
         const int j = base + threadIdx.x;
         __syncthreads();
         if (j < n) {
@@ -1373,21 +1376,76 @@ direct_subset_kernel(DevParams P, DevState S, const FrameCtl* ctl, ForceCtx C, c
         }
     }
     A.flush();
-    if (valid) { out_fx[ti] = A.get(Q_FX); out_fy[ti] = A.get(Q_FY); }
+    if (!valid) return;
+    if (gridDim.y == 1) { out_fx[ti] = A.get(Q_FX); out_fy[ti] = A.get(Q_FY); return; }
+    const size_t stride = (size_t)gridDim.x * DIRECT_THREADS;
+    float* q = C.dpart + (size_t)blockIdx.y * 4 * stride + ti;       // the slice's fx, fy as (hi, lo)
+    q[0] = A.hi(Q_FX); q[stride] = A.lo(Q_FX);
+    q[2 * stride] = A.hi(Q_FY); q[3 * stride] = A.lo(Q_FY);
 }
+
+__global__ void __launch_bounds__(DIRECT_THREADS)
+direct_subset_combine_kernel(ForceCtx C, const int* __restrict__ idx, int k, const FrameCtl* ctl, int slices,
+                             float* __restrict__ out_fx, float* __restrict__ out_fy) {
+    const int ti = blockIdx.x * DIRECT_THREADS + threadIdx.x;
+    if (ti >= k || idx[ti] < 0 || idx[ti] >= ctl->n) return;
+    const size_t stride = (size_t)gridDim.x * DIRECT_THREADS;
+    CAcc x, y;
+    x.init();
+    y.init();
+    for (int s = 0; s < slices; s++) {
+        const float* q = C.dpart + (size_t)s * 4 * stride + ti;
+        x.add(q[0]); x.add(q[stride]);
+        y.add(q[2 * stride]); y.add(q[3 * stride]);
+    }
+    out_fx[ti] = x.value();
+    out_fy[ti] = y.value();
+}
+
+DirectPlan direct_subset_plan(const DevParams& P, int k) {
+    static int occ[4] = { 0, 0, 0, 0 }, sms = 0;
+    const bool maggm = (P.toggles & (GEON_MAGNETIC | GEON_GRAVITOMAG | GEON_ONE_PN)) != 0;
+    const int v = (maggm ? 2 : 0) + (P.rel ? 1 : 0);
+    if (!occ[v]) {
+        switch (v) {
+            case 3: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[v], direct_subset_kernel<true, true>, DIRECT_THREADS, 0); break;
+            case 2: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[v], direct_subset_kernel<true, false>, DIRECT_THREADS, 0); break;
+            case 1: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[v], direct_subset_kernel<false, true>, DIRECT_THREADS, 0); break;
+            default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[v], direct_subset_kernel<false, false>, DIRECT_THREADS, 0); break;
+        }
+        if (occ[v] < 1) occ[v] = 1;
+    }
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms < 1) sms = 1;
+    }
+    const int best = direct_slice_count(k, (long long)occ[v] * sms);
+    const long long blocks = std::max(1, (k + DIRECT_THREADS - 1) / DIRECT_THREADS);
+    return DirectPlan{ best, best > 1 ? (size_t)best * 4 * blocks * DIRECT_THREADS : 0 };
+}
+
+
 
 void direct_subset(const DevParams& P, const DevState& S, const FrameCtl* ctl, const ForceCtx& C, const int* idx,
                    int k, float* fx, float* fy, cudaStream_t st, LaunchCounter& lc) {
     const bool maggm = (P.toggles & (GEON_MAGNETIC | GEON_GRAVITOMAG | GEON_ONE_PN)) != 0;
     const int blocks = std::max(1, (k + DIRECT_THREADS - 1) / DIRECT_THREADS);
+    const int slices = (C.dpart && C.dslices > 1) ? C.dslices : 1;
+    const dim3 grid(blocks, slices);
     if (maggm) {
-        if (P.rel) direct_subset_kernel<true, true><<<blocks, DIRECT_THREADS, 0, st>>>(P, S, ctl, C, idx, k, fx, fy);
-        else direct_subset_kernel<true, false><<<blocks, DIRECT_THREADS, 0, st>>>(P, S, ctl, C, idx, k, fx, fy);
+        if (P.rel) direct_subset_kernel<true, true><<<grid, DIRECT_THREADS, 0, st>>>(P, S, ctl, C, idx, k, fx, fy);
+        else direct_subset_kernel<true, false><<<grid, DIRECT_THREADS, 0, st>>>(P, S, ctl, C, idx, k, fx, fy);
     } else {
-        if (P.rel) direct_subset_kernel<false, true><<<blocks, DIRECT_THREADS, 0, st>>>(P, S, ctl, C, idx, k, fx, fy);
-        else direct_subset_kernel<false, false><<<blocks, DIRECT_THREADS, 0, st>>>(P, S, ctl, C, idx, k, fx, fy);
+        if (P.rel) direct_subset_kernel<false, true><<<grid, DIRECT_THREADS, 0, st>>>(P, S, ctl, C, idx, k, fx, fy);
+        else direct_subset_kernel<false, false><<<grid, DIRECT_THREADS, 0, st>>>(P, S, ctl, C, idx, k, fx, fy);
     }
     lc.add(1);
+    if (slices > 1) {
+        direct_subset_combine_kernel<<<blocks, DIRECT_THREADS, 0, st>>>(C, idx, k, ctl, slices, fx, fy);
+        lc.add(1);
+    }
 }
 
 // ---- potential heat map (heatmap.js:38-101, 152-206) ---------------------------------------------

@@ -40,6 +40,7 @@ struct ForceCtx {
 struct DirectPlan { int slices; size_t floats; };
 DirectPlan direct_plan(const DevParams& P, bool brk, int n_cap);
 DirectPlan direct1pn_plan(int n_cap);   // the same for the 1PN-only pairwise pass
+DirectPlan direct_subset_plan(const DevParams& P, int k);   // and for direct_subset over k targets
 
 // Force pass: resetForces + computeAllForces (+ external fields, bounce
 // walls) for every particle, with the max-acceleration / cyclotron
