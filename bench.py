@@ -64,7 +64,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=8192, help="targets per CPU sample step")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-correction arm")
-    ap.add_argument("--learn-thetas", default="0.9,0.3,0.2,0.15,0.12",
+    ap.add_argument("--learn-thetas", default="0.9,0.3,0.2,0.18,0.17,0.15,0.12",
                     help="opening angles at which the learned correction is trained and measured")
     ap.add_argument("--learn-steps", type=int, default=20000)
     ap.add_argument("--learn-batch", type=int, default=65536)
