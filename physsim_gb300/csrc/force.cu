@@ -712,13 +712,13 @@ constexpr int WC_THREADS = 128;
 constexpr int WC_WARPS = WC_THREADS / 32;
 constexpr int WC_STACK = 448;
 constexpr int WC_RESERVE = 3 * KEY_LEVELS + 3 * 16 + 4;   // growth a depth-first tail can still need
-constexpr int WC_POOL_SIX = 64;    // the six-CTA walk (below)
+constexpr int WC_POOL_SHF = 64;    // the walks in shared-memory form (below)
 constexpr int WC_POOL_WIDE = 96;   // the others: fewer, fuller flushes
 constexpr int WC_POP = 16;
 // one pop step stages at most WC_POP leaves of LEAF_CAP points (or one
 // aggregate per lane) and a bucket chunk 32 points, each after a flush
-static_assert(WC_POOL_SIX >= WC_POP * LEAF_CAP && WC_POOL_SIX >= 32, "source pool smaller than one step's staging");
-static_assert(WC_POOL_WIDE >= WC_POOL_SIX && WC_POOL_WIDE <= 255, "pool indices are bytes");
+static_assert(WC_POOL_SHF >= WC_POP * LEAF_CAP && WC_POOL_SHF >= 32, "source pool smaller than one step's staging");
+static_assert(WC_POOL_WIDE >= WC_POOL_SHF && WC_POOL_WIDE <= 255, "pool indices are bytes");
 constexpr uint32_t AGG_REF = 0xffffffffu;
 
 template <bool NEEDC, int POOL>
@@ -888,9 +888,9 @@ template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE = false, bool EMIT
 __global__ void __launch_bounds__(WC_THREADS, wc_min_blocks<MAGGM, REL, BRK, PER, NOPE>())
 walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
     constexpr bool NEEDC = MAGGM || REL;
-    constexpr bool SIX = wc_sh<MAGGM, REL, BRK, PER, NOPE>();   // shared-memory form
-    using AccT = Acc<MAGGM, BRK, SIX>;
-    using WS = WcSmem<NEEDC, SIX ? WC_POOL_SIX : WC_POOL_WIDE>;
+    constexpr bool SHF = wc_sh<MAGGM, REL, BRK, PER, NOPE>();   // shared-memory form (six or four CTAs per SM)
+    using AccT = Acc<MAGGM, BRK, SHF>;
+    using WS = WcSmem<NEEDC, SHF ? WC_POOL_SHF : WC_POOL_WIDE>;
     unsigned char* wc_smem = geon_dsmem + AccT::SH_BYTES;
     WS* Wall = reinterpret_cast<WS*>(wc_smem);
     float* s_age = reinterpret_cast<float*>(Wall + WC_WARPS);
@@ -919,13 +919,13 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
     const float gcx0 = 0.5f * (bx0 + bx1), gcy0 = 0.5f * (by0 + by1);
     const float ghx0 = 0.5f * (bx1 - bx0) * (1.f + 1e-6f) + 1e-6f * fabsf(gcx0) + 1e-30f;
     const float ghy0 = 0.5f * (by1 - by0) * (1.f + 1e-6f) + 1e-6f * fabsf(gcy0) + 1e-30f;
-    if (SIX && lane == 0) { W.gbox[0] = gcx0; W.gbox[1] = gcy0; W.gbox[2] = ghx0; W.gbox[3] = ghy0; }
+    if (SHF && lane == 0) { W.gbox[0] = gcx0; W.gbox[1] = gcy0; W.gbox[2] = ghx0; W.gbox[3] = ghy0; }
     const bool groupTests = !P.periodic || P.topology == GEON_TORUS;
 
     const int root = C.roots ? C.roots[sysId] : *d_root;
     const bool treeOk = (ctl->err & (ERR_NODE_OVERFLOW | ERR_BAD_INDEX)) == 0;
     const int nInt0 = ctl->nInternal, nLeaf0 = ctl->nLeaves, nValid0 = ctl->nValid;
-    if (SIX && lane == 0) { W.counts[0] = nInt0; W.counts[1] = nLeaf0; W.counts[2] = nValid0; }
+    if (SHF && lane == 0) { W.counts[0] = nInt0; W.counts[1] = nLeaf0; W.counts[2] = nValid0; }
     int top = 0, npool = 0, nfull = 0, lcnt = 0;
     if (root != ROOT_NONE && treeOk) {
         if (lane == 0) { W.stk_node[0] = root; W.stk_mask[0] = active; }
@@ -949,19 +949,19 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
         if (node >= 0) {
             if (node & LEAF_REF) {
                 const int li = node & ~LEAF_REF;
-                if (li < (SIX ? W.counts[1] : nLeaf0)) {
+                if (li < (SHF ? W.counts[1] : nLeaf0)) {
                     lm = T.leaf_meta[li];
                     const float lmass = T.leaf_a[li].z;
-                    if (lmass >= EPS_F && lm.x >= 0 && lm.x + lm.y <= (SIX ? W.counts[2] : nValid0)) kind = 1;   // forces.js:630,643
+                    if (lmass >= EPS_F && lm.x >= 0 && lm.x + lm.y <= (SHF ? W.counts[2] : nValid0)) kind = 1;   // forces.js:630,643
                 } else atomicOr(&ctl->err, ERR_BAD_INDEX);
-            } else if (node < (SIX ? W.counts[0] : nInt0)) {
+            } else if (node < (SHF ? W.counts[0] : nInt0)) {
                 na = T.int_a[node];
                 nc = T.int_c[node];
                 if (na.z >= EPS_F) {
                     kind = 4;
                     if (groupTests) {
-                        const float gcx = SIX ? W.gbox[0] : gcx0, gcy = SIX ? W.gbox[1] : gcy0;
-                        const float ghx = SIX ? W.gbox[2] : ghx0, ghy = SIX ? W.gbox[3] : ghy0;
+                        const float gcx = SHF ? W.gbox[0] : gcx0, gcy = SHF ? W.gbox[1] : gcy0;
+                        const float ghx = SHF ? W.gbox[2] : ghx0, ghy = SHF ? W.gbox[3] : ghy0;
                         float dx, dy;
                         if (PER && P.periodic) {
                             dx = wrap_axis_comp(na.x, gcx, nc.x, P.W, P.W_lo, P.halfW);
@@ -1111,8 +1111,8 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
 // relativity is on.
 template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE>
 constexpr size_t wc_smem_bytes() {
-    constexpr bool SIX = wc_sh<MAGGM, REL, BRK, PER, NOPE>();
-    return Acc<MAGGM, BRK, SIX>::SH_BYTES + sizeof(WcSmem<MAGGM || REL, SIX ? WC_POOL_SIX : WC_POOL_WIDE>) * WC_WARPS +
+    constexpr bool SHF = wc_sh<MAGGM, REL, BRK, PER, NOPE>();
+    return Acc<MAGGM, BRK, SHF>::SH_BYTES + sizeof(WcSmem<MAGGM || REL, SHF ? WC_POOL_SHF : WC_POOL_WIDE>) * WC_WARPS +
            (REL ? 2 * HIST_LEN * sizeof(float) : 0);
 }
 static_assert(6 * (wc_smem_bytes<false, false, false, false, true>() + 1024) <= 228 * 1024,
