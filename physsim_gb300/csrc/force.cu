@@ -40,9 +40,9 @@ enum { K_GX = 0, K_GY, K_CX, K_CY, K_MX, K_MY, K_GMX, K_GMY, K_YX, K_YY, K_N };
 // SH: the compensated (hi, lo) sums live in rows of shared memory at the
 // start of the dynamic buffer, [2 * NQ][ACC_SH_THREADS] with one column per
 // thread, instead of registers.  They are touched only every FLUSH_EVERY
-// terms; the registers they free let the open-box Barnes-Hut walk run six
-// CTAs per SM instead of five without spills (the dipole / 1PN walks: four
-// instead of three).
+// terms; the registers they free let the plain Barnes-Hut walk without
+// energy sums run six CTAs per SM instead of five (the dipole / 1PN walks:
+// four instead of three).
 extern __shared__ __align__(16) unsigned char geon_dsmem[];
 constexpr int ACC_SH_THREADS = 128;
 template <bool MAGGM, bool BRK, bool SH = false>
