@@ -269,45 +269,75 @@ int geon_direct_forces(GeonHandle* h, const int32_t* idx, int32_t k, float* fx, 
 #define GEON_DIRECT_NOALLOC_MAX_K 16384
 int geon_direct_forces_noalloc(GeonHandle* h, const int32_t* idx, int32_t k, float* fx, float* fy);
 
-/* Training data of the learned far-field correction (no reference
- * counterpart; the reference has plain monopole Barnes-Hut only).  Builds the
- * tree with cell moments, walks it for the k listed target particles at the
- * handle's theta, and for every (cell, target) aggregate interaction writes
- * 9 mass-net features, 9 charge-net features, the exact member-sum residual
- * (4: mass field x y, charge field x y, normalised) and the 2 scales
- * (M s^2 / r_e^4, sum|q| / r_e^2; s the cell size), and (when pair_target is not NULL) the
- * target particle of each pair.  Arrays hold `cap` records; *count receives
- * the number of pairs found (records beyond cap are dropped). */
-int geon_learn_dataset(GeonHandle* h, const int32_t* targets, int32_t k, int32_t cap, float* feat_mass,
-                       float* feat_charge, float* residual, float* scales, int32_t* pair_target, int32_t* count);
-
 /* ---- learned far-field correction (no reference counterpart) --------------
- * A 9 -> 64 -> 64 -> 2 GELU network (BF16 weights and activations, FP32
- * accumulation on the tensor cores) maps the mass-net features of an
- * accepted (cell, target) pair to the residual of its monopole term; the
- * force pass adds m_i * (M s^2 / r_e^4) * net(features) for every pair.  Weight
- * vector (FP32, GEON_MLP_NPARAM floats, nn.Linear layout W[out][in]):
- *     W1[64][9] b1[64] W2[64][64] b2[64] W3[2][64] b3[2] */
-#define GEON_MLP_NPARAM 4930
+ * The reference's far field is the plain monopole of an accepted cell
+ * (src/forces.js:680-685).  With GEON_FLAG_LEARN and weights set, a Barnes-Hut
+ * force pass keeps that monopole for every target and adds, once per pair of
+ * (accepted cell, group of 32 consecutive targets in walk order), a linear
+ * expansion about the group's centre of
+ *   - the cell's analytic second-order term (mass quadrupole through the
+ *     softened gravity + Yukawa kernel, charge dipole through the Coulomb
+ *     kernel), and
+ *   - the network's residual of the mass-sourced field: 14 features of the
+ *     cell seen from the group centre -> 64 -> 64 -> 6 (GELU; BF16 weights
+ *     and activations, FP32 accumulation on the tensor cores), the value and
+ *     gradient of the two field components in the frame of the cell's
+ *     direction, scaled by M / re^2 and M / (re^2 s).
+ * It applies to open boxes with gravity, Coulomb and Yukawa (no relativity,
+ * dipoles or 1PN).  Weight vector (FP32, GEON_MLP_NPARAM floats, nn.Linear
+ * layout W[out][in]):
+ *     mu[14] isd[14] W1[64][14] b1[64] W2[64][64] b2[64] W3[6][64] b3[6]
+ * where the features are first normalised in FP32, x' = (x - mu) * isd;
+ * training (geon_mlp_grad / geon_mlp_train) leaves mu and isd unchanged. */
+#define GEON_MLP_NPARAM 5538
+#define GEON_LEARN_FEATURES 14
+#define GEON_LEARN_OUTPUTS 6
+#define GEON_LEARN_TARGETS 18   /* per training record: y*[6], then A[6] of each of the 2 components */
+
+/* Training records.  Builds the tree with cell moments at the handle's
+ * theta, runs the Barnes-Hut force pass recording the (cell, group) pairs,
+ * and for the groups 0, stride, 2 stride, ... writes per record
+ *   feat[14]      the network's inputs,
+ *   target[18]    the least-squares outputs y*[6] that fit the exact residual
+ *                 at the record's accepting targets (the cell's member sum,
+ *                 src/forces.js:94-125 restricted to the cell, minus the
+ *                 monopole and the analytic term), then for each of the two
+ *                 components the quadratic form (A00 A11 A22 A01 A02 A12)
+ *                 with which an output error adds to the sum over those
+ *                 targets of the squared force error relative to |F|
+ *                 (weights m^2 / max(|F|^2, (m gfloor)^2), |F| from this pass),
+ *   rec_group     the group (may be NULL).
+ * Arrays hold `cap` records; *count receives the records of the selected
+ * groups (those beyond cap are dropped).  Forces are left as the plain pass
+ * computed them. */
+int geon_learn_dataset(GeonHandle* h, int32_t group_stride, int64_t cap, float gfloor, float* feat, float* target,
+                       int32_t* rec_group, int64_t* count);
+
+/* Test aid: the Barnes-Hut force pass at the handle's theta plus the
+ * correction with the network outputs taken from y[n][6] instead of the
+ * network, for the records of all groups in the order geon_learn_dataset
+ * lists them with stride 1 (n must equal that count). */
+int geon_learn_apply(GeonHandle* h, const float* y, int64_t n);
 
 /* Sets the correction's weights (copied); NULL clears them.  The correction
  * runs in Barnes-Hut force passes while GEON_FLAG_LEARN is set and weights
  * are present.  n_param must be GEON_MLP_NPARAM. */
 int geon_learn_set_weights(GeonHandle* h, const float* weights, int32_t n_param);
 
-/* y[n][2] = net(x[n][9]) on the device (host arrays). */
+/* y[n][6] = net(x[n][14]) on the device (host arrays). */
 int geon_mlp_forward(GeonHandle* h, const float* weights, const float* x, int32_t n, float* y);
 
-/* Gradient of L = (1/n) sum_s wt_s |net(x_s) - t_s|^2 over all n samples
- * (wt may be NULL: all 1), computed by the tensor-core backward pass:
- * grad[GEON_MLP_NPARAM], *loss = L. */
+/* Gradient of L = (1/n) sum_s wt_s sum_c (y_sc - y*_sc)^T A_sc (y_sc - y*_sc)
+ * over all n samples, y_sc = outputs 3c..3c+2 of net(x_s), t_s[18] = y*_s[6]
+ * then A_s0[6], A_s1[6] (A00 A11 A22 A01 A02 A12); wt may be NULL (all 1).
+ * Computed by the tensor-core backward pass: grad[GEON_MLP_NPARAM], *loss = L. */
 int geon_mlp_grad(GeonHandle* h, const float* weights, const float* x, const float* t, const float* wt, int32_t n,
                   float* grad, double* loss);
 
-/* Trains the network in place with Adam (beta 0.9 / 0.999, eps 1e-8) for
- * `steps` steps of `batch` samples drawn uniformly (seeded counter hash) from
- * the n samples, with a cosine learning-rate schedule from lr to 0.
- * loss_history[steps] (may be NULL) receives each step's batch loss. */
+/* Trains the network in place with Adam (beta 0.9 / 0.999, eps 1e-8) on that
+ * loss for `steps` steps of `batch` samples drawn uniformly (seeded counter
+ * hash) from the n samples, with a cosine learning-rate schedule from lr to
+ * 0.  loss_history[steps] (may be NULL) receives each step's batch loss. */
 int geon_mlp_train(GeonHandle* h, float* weights, const float* x, const float* t, const float* wt, int32_t n,
                    int32_t steps, int32_t batch, float lr, uint64_t seed, double* loss_history);
 
@@ -468,9 +498,9 @@ typedef struct GeonProfile {
     int64_t tree_count, force_count, onepn_count, push_count;
     int64_t interactions;    /* pair evaluations summed over the profiled force passes */
     int64_t particle_substeps;
-    double learn_ms;         /* learned correction: pair collection + network        */
+    double learn_ms;         /* learned correction: network and expansions            */
     int64_t learn_count;
-    int64_t learn_pairs;     /* (cell, target) pairs corrected                        */
+    int64_t learn_pairs;     /* (cell, group) records corrected                       */
     double collide_ms;       /* merge collisions: detection, resolution, target list  */
     int64_t collide_count;
 } GeonProfile;

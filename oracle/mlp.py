@@ -4,8 +4,11 @@ product path imports it).
 
 The reference has no learned correction (its far field is the plain monopole
 of src/forces.js:680-685), so this file restates the network the C ABI
-documents for geon_mlp_forward / geon_mlp_grad: 9 -> 64 -> 64 -> 2, GELU in
-its tanh form after both hidden layers, loss (1/B) sum_s wt_s |y_s - t_s|^2.
+documents for geon_mlp_forward / geon_mlp_grad: 14 -> 64 -> 64 -> 6, GELU in
+its tanh form after both hidden layers, and the loss
+    (1/B) sum_s wt_s sum_c (y_sc - y*_sc)^T A_sc (y_sc - y*_sc)
+with y_sc the outputs 3c .. 3c+2 and the target row t_s = y*_s[6], then the
+two symmetric 3 x 3 forms A_s0, A_s1 as (A00 A11 A22 A01 A02 A12).
 
 With ``bf16=True`` the operands are rounded to BF16 (round to nearest even)
 at the points where the device kernels round them — inputs, weights, hidden
@@ -19,8 +22,9 @@ from __future__ import annotations
 
 import numpy as np
 
-LF, LH, LO = 9, 64, 2
-NPARAM = LH * LF + LH + LH * LH + LH + LO * LH + LO
+LF, LH, LO = 14, 64, 6
+LT = LO + 12
+NPARAM = 2 * LF + LH * LF + LH + LH * LH + LH + LO * LH + LO
 GELU_C = np.sqrt(2.0 / np.pi)
 GELU_A = 0.044715
 
@@ -42,7 +46,8 @@ def unpack(w) -> dict:
     assert w.size == NPARAM
     o = 0
     out = {}
-    for name, shape in (("W1", (LH, LF)), ("b1", (LH,)), ("W2", (LH, LH)), ("b2", (LH,)), ("W3", (LO, LH)), ("b3", (LO,))):
+    for name, shape in (("mu", (LF,)), ("isd", (LF,)), ("W1", (LH, LF)), ("b1", (LH,)), ("W2", (LH, LH)), ("b2", (LH,)),
+                        ("W3", (LO, LH)), ("b3", (LO,))):
         k = int(np.prod(shape))
         out[name] = w[o:o + k].reshape(shape)
         o += k
@@ -50,13 +55,15 @@ def unpack(w) -> dict:
 
 
 def pack(d: dict) -> np.ndarray:
-    return np.concatenate([np.asarray(d[k], dtype=np.float64).ravel() for k in ("W1", "b1", "W2", "b2", "W3", "b3")])
+    return np.concatenate([np.asarray(d[k], dtype=np.float64).ravel()
+                           for k in ("mu", "isd", "W1", "b1", "W2", "b2", "W3", "b3")])
 
 
 def init_weights(seed: int = 0) -> np.ndarray:
-    """nn.Linear's default initialisation: U(-1/sqrt(fan_in), 1/sqrt(fan_in))."""
+    """nn.Linear's default initialisation: U(-1/sqrt(fan_in), 1/sqrt(fan_in));
+    identity normalisation."""
     rng = np.random.default_rng(seed)
-    d = {}
+    d = {"mu": np.zeros(LF), "isd": np.ones(LF)}
     for (wn, bn), (o, i) in zip((("W1", "b1"), ("W2", "b2"), ("W3", "b3")), ((LH, LF), (LH, LH), (LO, LH))):
         k = 1.0 / np.sqrt(i)
         d[wn] = rng.uniform(-k, k, (o, i))
@@ -79,7 +86,8 @@ def _r(a, on):
 
 def forward(w, x, bf16_ops: bool = True, keep: bool = False):
     p = unpack(w)
-    x = _r(np.asarray(x, dtype=np.float64).reshape(-1, LF), bf16_ops)
+    x = np.asarray(x, dtype=np.float64).reshape(-1, LF)
+    x = _r((x - p["mu"]) * p["isd"], bf16_ops)
     W1, W2, W3 = (_r(p[k], bf16_ops) for k in ("W1", "W2", "W3"))
     z1 = x @ W1.T + p["b1"]
     h1 = _r(gelu(z1), bf16_ops)
@@ -91,18 +99,43 @@ def forward(w, x, bf16_ops: bool = True, keep: bool = False):
     return y
 
 
+def quad_forms(t):
+    """The target rows [B, 18] as (y* [B, 6], A [B, 2, 3, 3])."""
+    t = np.asarray(t, dtype=np.float64).reshape(-1, LT)
+    A = np.zeros((len(t), 2, 3, 3))
+    for c in range(2):
+        a = t[:, LO + 6 * c:LO + 6 * c + 6]
+        A[:, c] = np.stack([np.stack([a[:, 0], a[:, 3], a[:, 4]], -1), np.stack([a[:, 3], a[:, 1], a[:, 5]], -1),
+                            np.stack([a[:, 4], a[:, 5], a[:, 2]], -1)], -2)
+    return t[:, :LO], A
+
+
 def loss_grad(w, x, t, wt=None, bf16_ops: bool = True):
-    """(gradient vector, loss) of (1/B) sum_s wt_s |net(x_s) - t_s|^2."""
+    """(gradient vector, loss) of (1/B) sum_s wt_s sum_c e_sc^T A_sc e_sc,
+    e_sc = y_sc - y*_sc."""
     y, c = forward(w, x, bf16_ops, keep=True)
-    t = np.asarray(t, dtype=np.float64).reshape(-1, LO)
+    ys, A = quad_forms(t)
     B = len(y)
     wt = np.ones(B) if wt is None else np.asarray(wt, dtype=np.float64)
-    e = y - t
-    loss = float(np.sum(wt[:, None] * e * e) / B)
-    dy = _r(2.0 * wt[:, None] * e / B, bf16_ops)
+    e = (y - ys).reshape(B, 2, 3)
+    Ae = np.einsum("bcij,bcj->bci", A, e)
+    loss = float(np.sum(wt * np.einsum("bci,bci->b", e, Ae)) / B)
+    dy = _r((2.0 * wt[:, None] * Ae.reshape(B, LO)) / B, bf16_ops)
     dh2 = dy @ c["W3"]
     dz2 = _r(dh2 * gelu_grad(c["z2"]), bf16_ops)
     dh1 = dz2 @ c["W2"]
     dz1 = _r(dh1 * gelu_grad(c["z1"]), bf16_ops)
-    g = dict(W3=dy.T @ c["h2"], b3=dy.sum(0), W2=dz2.T @ c["h1"], b2=dz2.sum(0), W1=dz1.T @ c["x"], b1=dz1.sum(0))
+    g = dict(mu=np.zeros(LF), isd=np.zeros(LF), W3=dy.T @ c["h2"], b3=dy.sum(0), W2=dz2.T @ c["h1"], b2=dz2.sum(0),
+             W1=dz1.T @ c["x"], b1=dz1.sum(0))
     return pack(g), loss
+
+
+def random_targets(rng, n, scale=0.1):
+    """Target rows with positive definite forms, for tests."""
+    t = np.zeros((n, LT))
+    t[:, :LO] = rng.normal(size=(n, LO)) * scale
+    for c in range(2):
+        L = rng.normal(size=(n, 3, 3)) * 0.5 + np.eye(3)
+        A = L @ np.transpose(L, (0, 2, 1))
+        t[:, LO + 6 * c:LO + 6 * c + 6] = np.stack([A[:, 0, 0], A[:, 1, 1], A[:, 2, 2], A[:, 0, 1], A[:, 0, 2], A[:, 1, 2]], 1)
+    return t

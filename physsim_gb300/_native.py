@@ -47,7 +47,10 @@ FLAG_NO_GHOSTS = 1 << 2
 FLAG_SIMPLE_WALK = 1 << 3
 FLAG_LEARN = 1 << 4
 FLAG_BOSONS = 1 << 5
-MLP_NPARAM = 4930
+MLP_NPARAM = 5538
+LEARN_FEATURES = 14
+LEARN_OUTPUTS = 6
+LEARN_TARGETS = 18
 DIRECT_NOALLOC_MAX_K = 16384
 BATCH_MAX_SYSTEMS = 512
 
@@ -167,8 +170,9 @@ SIGNATURES = {
     "geon_compute_1pn": [_handle_t],
     "geon_direct_forces": [_handle_t, _P(C.c_int32), C.c_int32, _P(C.c_float), _P(C.c_float)],
     "geon_direct_forces_noalloc": [_handle_t, _P(C.c_int32), C.c_int32, _P(C.c_float), _P(C.c_float)],
-    "geon_learn_dataset": [_handle_t, _P(C.c_int32), C.c_int32, C.c_int32, _P(C.c_float), _P(C.c_float),
-                           _P(C.c_float), _P(C.c_float), _P(C.c_int32), _P(C.c_int32)],
+    "geon_learn_dataset": [_handle_t, C.c_int32, C.c_int64, C.c_float, _P(C.c_float), _P(C.c_float),
+                           _P(C.c_int32), _P(C.c_int64)],
+    "geon_learn_apply": [_handle_t, _P(C.c_float), C.c_int64],
     "geon_learn_set_weights": [_handle_t, _P(C.c_float), C.c_int32],
     "geon_mlp_forward": [_handle_t, _P(C.c_float), _P(C.c_float), C.c_int32, _P(C.c_float)],
     "geon_mlp_grad": [_handle_t, _P(C.c_float), _P(C.c_float), _P(C.c_float), _P(C.c_float), C.c_int32,

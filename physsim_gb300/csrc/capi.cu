@@ -97,7 +97,7 @@ struct GeonHandle {
     DevArena col_arena;     // merge-collision buffers (allocated when the merge mode is first used)
     DevArena tree_arena;    // tree buffers (reallocated when ghost capacity changes)
     DevArena hist_arena;    // history rings (allocated when relativity is first enabled)
-    DevArena learn_arena;   // learned-correction weights and pair buffer
+    DevArena learn_arena;   // learned-correction weights and record counters
     DevState S{}, S2{};
     TreeBufs T{};
     bool tree_periodic = false;
@@ -146,10 +146,20 @@ struct GeonHandle {
     Batch* batch = nullptr;
     // learned correction
     float* learn_w = nullptr;       // [GEON_MLP_NPARAM] device weights (null: correction off)
-    LearnPair* pairs = nullptr;     // (cell, target) pairs of one chunk of targets
-    unsigned long long* pair_cnt = nullptr;
-    long long pair_cap = 0;
-    double pairs_per_target = 0.0;  // largest ratio seen, sizes the target chunks
+    float* learn_w_buf = nullptr;   // their buffer, kept when the weights are cleared
+    uint2* recs = nullptr;          // (cell, group) records: rec_cap per group of 32 walk slots
+    int* rec_cnt = nullptr;         // [rec_groups] records of each group in the last walk
+    unsigned* rec_max = nullptr;    // largest count of the last walk (counters: learn_arena)
+    unsigned long long* rec_total = nullptr;
+    long long rec_total_h = 0;      // records of the last walk
+    int rec_cap = 0;
+    int rec_groups = 0;
+    float4* gcen = nullptr;         // [rec_groups] group centres and radius bounds
+    int* rec_off = nullptr;         // [rec_groups + 1] exclusive prefix of the counts
+    void* rec_scan = nullptr;       // scan scratch of learn_record_offsets
+    float4* rec_exp = nullptr;      // per record expansions (3 float4) of the correction's phase A
+    uint32_t* rec_flags = nullptr;
+    long long rec_exp_cap = 0;
     LaunchCounter lc;
     std::string err;
     // profiling
@@ -225,6 +235,8 @@ static int validate_params(GeonHandle* h, const GeonParams& p) {
     if (p.collision_mode == GEON_COL_BOUNCE) return set_err(h, GEON_ERR_UNSUPPORTED, "the bounce collision mode (contact forces) is not part of this library");
     if (p.collision_mode == GEON_COL_MERGE && (p.flags & GEON_FLAG_LEARN))
         return set_err(h, GEON_ERR_UNSUPPORTED, "merge collisions and the learned correction cannot be combined");
+    if ((p.flags & GEON_FLAG_LEARN) && p.boundary_mode == GEON_BOUND_LOOP)
+        return set_err(h, GEON_ERR_UNSUPPORTED, "the learned correction covers open boxes (no periodic images)");
     return GEON_OK;
 }
 
@@ -553,82 +565,134 @@ static int build_tree(GeonHandle* h) {
     return GEON_OK;
 }
 
-static bool learn_active(const GeonHandle* h) {
-    return h->learn_w && (h->prm.flags & GEON_FLAG_LEARN) && h->T.mom_on && h->n > 0;
+// The force set the learned correction covers: gravity, Coulomb and Yukawa
+// without relativity, dipoles, 1PN or per-type breakdown rows, in an open box.
+static bool learn_supported(const GeonHandle* h) {
+    return !h->P.rel && !(h->prm.toggles & (GEON_MAGNETIC | GEON_GRAVITOMAG | GEON_ONE_PN)) &&
+           !(h->prm.flags & (GEON_FLAG_BREAKDOWN | GEON_FLAG_SIMPLE_WALK)) && !h->P.periodic && !h->batch;
 }
 
-// Largest pair buffer of the learned correction (pairs; 8 bytes each).  The
-// targets are processed in chunks that fit it.
-constexpr long long PAIR_CAP_MAX = 1ll << 28;
+static bool learn_active(const GeonHandle* h) {
+    return h->learn_w && (h->prm.flags & GEON_FLAG_LEARN) && h->T.mom_on && h->n > 0 && learn_supported(h);
+}
 
-// Grows the pair buffer to hold at least `need` (<= PAIR_CAP_MAX) pairs
-// (contents discarded).
-static int ensure_pairs(GeonHandle* h, long long need) {
-    if (need <= h->pair_cap) return GEON_OK;
-    const long long cap = std::min<long long>(PAIR_CAP_MAX, need + need / 4 + 4096);
-    if (h->pairs) { cudaStreamSynchronize(h->st); cudaFree(h->pairs); h->pairs = nullptr; h->pair_cap = 0; }
-    if (cudaMalloc(&h->pairs, (size_t)cap * sizeof(LearnPair)) != cudaSuccess) {
-        cudaGetLastError();
-        h->pairs = nullptr;
-        return set_err(h, GEON_ERR_NOMEM, "learned-correction pair buffer allocation failed");
+// Record buffers for `cap` records per group (contents discarded when they grow).
+static int ensure_recs(GeonHandle* h, int cap) {
+    const int groups = (h->n_cap + 31) / 32;
+    if (!h->rec_max) {
+        unsigned* m = h->learn_arena.alloc<unsigned>(1);
+        unsigned long long* t = h->learn_arena.alloc<unsigned long long>(1);
+        if (h->learn_arena.failed) return set_err(h, GEON_ERR_NOMEM, "record counter allocation failed");
+        h->rec_max = m;
+        h->rec_total = t;
     }
-    h->pair_cap = cap;
+    if (groups > h->rec_groups) {
+        cudaStreamSynchronize(h->st);
+        void** bufs[4] = { (void**)&h->rec_cnt, (void**)&h->gcen, (void**)&h->rec_off, &h->rec_scan };
+        const size_t bytes[4] = { (size_t)groups * sizeof(int), (size_t)groups * sizeof(float4),
+                                  (size_t)(groups + 1) * sizeof(int), learn_offsets_scratch_bytes(groups) };
+        for (int b = 0; b < 4; b++) {
+            if (*bufs[b]) { cudaFree(*bufs[b]); *bufs[b] = nullptr; }
+            if (cudaMalloc(bufs[b], bytes[b]) != cudaSuccess) {
+                cudaGetLastError();
+                h->rec_groups = 0;
+                return set_err(h, GEON_ERR_NOMEM, "record group buffer allocation failed");
+            }
+        }
+        h->rec_groups = groups;
+        h->rec_cap = 0;                       // the record buffer is sized per group: regrow it
+    }
+    if (cap <= h->rec_cap && h->recs) return GEON_OK;
+    cap = std::max(cap, 256);
+    if (h->recs) { cudaStreamSynchronize(h->st); cudaFree(h->recs); h->recs = nullptr; }
+    if (cudaMalloc(&h->recs, (size_t)h->rec_groups * cap * sizeof(uint2)) != cudaSuccess) {
+        cudaGetLastError();
+        h->rec_cap = 0;
+        return set_err(h, GEON_ERR_NOMEM, "learned-correction record buffer allocation failed");
+    }
+    h->rec_cap = cap;
     return GEON_OK;
 }
 
-// Barnes-Hut force pass with the learned far-field correction.  The targets
-// are processed in chunks (in walk order) whose pairs fit the pair buffer:
-// the walk of a chunk computes its forces and records every accepted
-// (cell, particle) pair, then the network adds its correction to those
-// particles.  The planner reductions are redone from the corrected forces.
-static int learned_force_pass(GeonHandle* h) {
-    const int n = h->n;
-    long long total = 0;
-    int k0 = 0;
-    bool first = true;
-    while (k0 < n) {
-        long long chunk = n - k0;
-        const double est = h->pairs_per_target > 0 ? h->pairs_per_target * 1.1 : 4096.0;
-        chunk = std::min<long long>(chunk, std::max<long long>(1024, (long long)(PAIR_CAP_MAX / est) / 32 * 32));
-        unsigned long long found = 0, inter0 = 0;
-        CK(cudaMemcpyAsync(&inter0, &h->ctl->interactions, sizeof(inter0), cudaMemcpyDeviceToHost, h->st));
-        for (;;) {
-            CK(cudaMemsetAsync(h->pair_cnt, 0, sizeof(unsigned long long), h->st));
-            ForceCtx C = make_ctx(h);
-            C.tgt_list = h->T.tgt + k0;
-            C.tgt_count = (int)chunk;
-            C.pairs = reinterpret_cast<int2*>(h->pairs);
-            C.pair_cap = h->pair_cap;
-            C.pair_count = h->pair_cnt;
-            const int ps = prof_begin(h, PH_FORCE);
-            force_pass(h->P, h->S, h->T, h->d_root, h->ctl, C, true, h->n_cap, h->st, h->lc, first);
-            prof_end(h, ps);
-            CKL();
-            CK(cudaMemcpyAsync(&found, h->pair_cnt, sizeof(found), cudaMemcpyDeviceToHost, h->st));
-            CK(cudaStreamSynchronize(h->st));
-            h->pairs_per_target = std::max(h->pairs_per_target, (double)found / (double)chunk);
-            if ((long long)found <= h->pair_cap) break;
-            // redo the chunk with room for its pairs (its forces are simply rewritten)
-            if (!first) CK(cudaMemcpyAsync(&h->ctl->interactions, &inter0, sizeof(inter0), cudaMemcpyHostToDevice, h->st));
-            if ((long long)found > PAIR_CAP_MAX) {
-                if (chunk <= 32) return set_err(h, GEON_ERR_OVERFLOW, "learned-correction pairs of one warp exceed the buffer");
-                chunk = std::max<long long>(32, chunk * PAIR_CAP_MAX / (long long)found / 2 / 32 * 32);
-                continue;
-            }
-            int r = ensure_pairs(h, (long long)found);
-            if (r) return r;
-        }
-        const int pl = prof_begin(h, PH_LEARN);
-        mlp_correct(h->P, h->S, h->T, h->learn_w, h->pairs, (int)found, &h->ctl->err, h->st, h->lc);
-        prof_end(h, pl);
+// Barnes-Hut walk with record emission: the plain monopole forces of every
+// particle, and the (cell, group) records.  A walk whose largest group
+// overflowed the per-group capacity is redone with room for it.
+static int learn_walk(GeonHandle* h) {
+    int r = ensure_recs(h, std::max(h->rec_cap, 2048));
+    if (r) return r;
+    for (int attempt = 0; attempt < 3; attempt++) {
+        CK(cudaMemsetAsync(h->rec_max, 0, sizeof(unsigned), h->st));
+        CK(cudaMemsetAsync(h->rec_total, 0, sizeof(unsigned long long), h->st));
+        ForceCtx C = make_ctx(h);
+        C.recs = h->recs;
+        C.rec_cap = h->rec_cap;
+        C.rec_cnt = h->rec_cnt;
+        C.rec_max = h->rec_max;
+        C.rec_total = h->rec_total;
+        C.gcen = h->gcen;
+        const int ps = prof_begin(h, PH_FORCE);
+        force_pass(h->P, h->S, h->T, h->d_root, h->ctl, C, true, h->n_cap, h->st, h->lc);
+        prof_end(h, ps);
         CKL();
-        total += (long long)found;
-        k0 += (int)chunk;
-        first = false;
+        unsigned mx = 0;
+        unsigned long long tot = 0;
+        CK(cudaMemcpyAsync(&mx, h->rec_max, sizeof(mx), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaMemcpyAsync(&tot, h->rec_total, sizeof(tot), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        if ((int)mx <= h->rec_cap) {
+            h->rec_total_h = (long long)tot;
+            if (h->prof) h->prof_acc.learn_pairs += (long long)tot;
+            return GEON_OK;
+        }
+        r = ensure_recs(h, (int)std::min<unsigned>(mx + mx / 4 + 64, 1u << 24));
+        if (r) return r;
     }
+    return set_err(h, GEON_ERR_OVERFLOW, "learned-correction records of one group exceed the buffer");
+}
+
+// Scratch of the correction's phase A for `total` records.
+static int ensure_rec_exp(GeonHandle* h, long long total) {
+    if (total > INT_MAX) return set_err(h, GEON_ERR_OVERFLOW, "more than 2^31 learned-correction records");
+    if (total <= h->rec_exp_cap) return GEON_OK;
+    const long long cap = total + total / 8 + 1024;
+    cudaStreamSynchronize(h->st);
+    if (h->rec_exp) { cudaFree(h->rec_exp); h->rec_exp = nullptr; }
+    if (h->rec_flags) { cudaFree(h->rec_flags); h->rec_flags = nullptr; }
+    h->rec_exp_cap = 0;
+    if (cudaMalloc(&h->rec_exp, (size_t)cap * 3 * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&h->rec_flags, (size_t)cap * sizeof(uint32_t)) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(h, GEON_ERR_NOMEM, "learned-correction scratch allocation failed");
+    }
+    h->rec_exp_cap = cap;
+    return GEON_OK;
+}
+
+// The correction of the last walk's records: network outputs from the
+// weights, or from yext (device, records in group order) when given.
+static int learn_correct_records(GeonHandle* h, const float* yext) {
+    const int ngroups = (h->n + 31) / 32;
+    int r = ensure_rec_exp(h, h->rec_total_h);
+    if (r) return r;
+    learn_record_offsets(h->rec_cnt, h->rec_cap, ngroups, 1, h->rec_off, h->rec_off + ngroups, h->rec_scan, h->st, h->lc);
+    learn_correct(h->P, h->S, h->T, h->ctl, h->learn_w, h->recs, h->rec_cnt, h->gcen, h->rec_cap, ngroups, h->rec_off,
+                  (int)h->rec_total_h, yext, h->rec_exp, h->rec_flags, &h->ctl->err, h->st, h->lc);
+    return GEON_OK;
+}
+
+// Barnes-Hut force pass with the learned far-field correction: the walk's
+// monopole forces, then the network and expansions of learn_correct; the
+// planner reductions are redone from the corrected forces.
+static int learned_force_pass(GeonHandle* h) {
+    int r = learn_walk(h);
+    if (r) return r;
+    const int pl = prof_begin(h, PH_LEARN);
+    r = learn_correct_records(h, nullptr);
+    prof_end(h, pl);
+    if (r) return r;
+    CKL();
     launch_frame_scan(h->P, h->S, h->ctl, h->n_cap, h->st, h->lc);
     CKL();
-    if (h->prof) h->prof_acc.learn_pairs += total;
     return GEON_OK;
 }
 
@@ -912,7 +976,14 @@ int geon_destroy(GeonHandle* h) {
     h->boson_arena.free_all();
     if (h->bos) { geon_destroy(h->bos); h->bos = nullptr; }
     if (h->col_h) cudaFreeHost(h->col_h);
-    if (h->pairs) cudaFree(h->pairs);
+    if (h->recs) cudaFree(h->recs);
+    if (h->learn_w_buf) cudaFree(h->learn_w_buf);
+    if (h->gcen) cudaFree(h->gcen);
+    if (h->rec_off) cudaFree(h->rec_off);
+    if (h->rec_scan) cudaFree(h->rec_scan);
+    if (h->rec_exp) cudaFree(h->rec_exp);
+    if (h->rec_flags) cudaFree(h->rec_flags);
+    if (h->rec_cnt) cudaFree(h->rec_cnt);
     if (h->dpart) cudaFree(h->dpart);
     if (h->batch) {
         Batch* B = h->batch;
@@ -1154,64 +1225,81 @@ int geon_direct_forces(GeonHandle* h, const int32_t* idx, int32_t k, float* fx, 
     return cuda_check(h, e, "direct forces");
 }
 
-int geon_learn_dataset(GeonHandle* h, const int32_t* targets, int32_t k, int32_t cap, float* feat_mass,
-                       float* feat_charge, float* residual, float* scales, int32_t* pair_target, int32_t* count) {
-    if (!h || k < 0 || cap < 0 || (k > 0 && !targets) || (cap > 0 && (!feat_mass || !feat_charge || !residual || !scales)))
-        return GEON_ERR_ARG;
+// Checks and tree of the learned-correction entry points: the force set the
+// correction covers, a tree with cell moments at the handle's theta, and the
+// Barnes-Hut walk with record emission (plain forces in S.force).
+static int learn_prepare(GeonHandle* h) {
     if (!(h->prm.toggles & GEON_BARNES_HUT)) return set_err(h, GEON_ERR_ARG, "the learned correction needs Barnes-Hut");
-    if (h->batch) return set_err(h, GEON_ERR_UNSUPPORTED, "batched handles run without the learned correction");
-    if (h->P.rel || (h->prm.toggles & (GEON_MAGNETIC | GEON_GRAVITOMAG | GEON_ONE_PN)))
-        return set_err(h, GEON_ERR_UNSUPPORTED, "the learned correction covers gravity, Coulomb and Yukawa without relativity");
-    if (count) *count = 0;
-    if (k == 0 || h->n == 0) return GEON_OK;
+    if (!learn_supported(h))
+        return set_err(h, GEON_ERR_UNSUPPORTED, "the learned correction covers gravity, Coulomb and Yukawa without "
+                                                "relativity, dipoles, 1PN or breakdown rows, in an open box, one system per handle");
     const uint32_t saved = h->prm.flags;
     h->prm.flags |= GEON_FLAG_LEARN;
     int r = build_tree(h);
     h->prm.flags = saved;
     if (r) return r;
+    return learn_walk(h);
+}
+
+int geon_learn_dataset(GeonHandle* h, int32_t group_stride, int64_t cap, float gfloor, float* feat, float* target,
+                       int32_t* rec_group, int64_t* count) {
+    if (!h || group_stride < 1 || cap < 0 || (cap > 0 && (!feat || !target)) || !(gfloor >= 0.f)) return GEON_ERR_ARG;
+    if (count) *count = 0;
+    if (h->n == 0) return GEON_OK;
+    int r = learn_prepare(h);
+    if (r) return r;
+    const int ngroups = (h->n + 31) / 32;
+    const int nsel = (ngroups + group_stride - 1) / group_stride;
     DevArena tmp;
-    int* d_t = tmp.alloc<int>(k);
-    unsigned long long* d_cnt = tmp.alloc<unsigned long long>(1);
-    const int capd = std::max(cap, 1);
-    LearnPair* d_pairs = tmp.alloc<LearnPair>(capd);
-    float* d_fm = tmp.alloc<float>((size_t)capd * LF);
-    float* d_fc = tmp.alloc<float>((size_t)capd * LF);
-    float* d_res = tmp.alloc<float>((size_t)capd * 4);
-    float* d_sc = tmp.alloc<float>((size_t)capd * 2);
-    LearnPair* d_sorted = tmp.alloc<LearnPair>(capd);
-    int* d_nsorted = tmp.alloc<int>(1);
-    void* d_sort_tmp = tmp.alloc<char>(learn_sort_scratch_bytes(capd));
+    int* d_off = tmp.alloc<int>(nsel + 1);
+    int* d_total = tmp.alloc<int>(1);
+    void* d_scan = tmp.alloc<char>(learn_offsets_scratch_bytes(nsel));
     if (tmp.failed) { tmp.free_all(); return set_err(h, GEON_ERR_NOMEM, "dataset allocation failed"); }
-    cudaError_t e = cudaMemcpyAsync(d_t, targets, k * sizeof(int), cudaMemcpyHostToDevice, h->st);
-    if (e == cudaSuccess) {
-        learn_collect_pairs(h->P, h->S, h->T, h->d_root, h->ctl, d_t, k, d_pairs, cap, d_cnt, h->st, h->lc);
-        learn_sort_pairs(d_pairs, d_cnt, capd, d_sorted, d_nsorted, d_sort_tmp, h->st, h->lc);
-        d_pairs = d_sorted;
-        learn_residuals(h->P, h->S, h->T, d_pairs, d_cnt, cap, d_fm, d_fc, d_res, d_sc, h->st, h->lc);
-        e = cudaGetLastError();
-    }
-    unsigned long long found64 = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&found64, d_cnt, sizeof(found64), cudaMemcpyDeviceToHost, h->st);
+    learn_record_offsets(h->rec_cnt, h->rec_cap, ngroups, group_stride, d_off, d_total, d_scan, h->st, h->lc);
+    int total = 0;
+    cudaError_t e = cudaMemcpyAsync(&total, d_total, sizeof(int), cudaMemcpyDeviceToHost, h->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
-    const int found = (int)std::min<unsigned long long>(found64, (unsigned long long)INT_MAX);
-    const int m = std::min(found, cap);
-    if (e == cudaSuccess && m > 0) {
-        cudaMemcpyAsync(feat_mass, d_fm, (size_t)m * LF * sizeof(float), cudaMemcpyDeviceToHost, h->st);
-        cudaMemcpyAsync(feat_charge, d_fc, (size_t)m * LF * sizeof(float), cudaMemcpyDeviceToHost, h->st);
-        cudaMemcpyAsync(residual, d_res, (size_t)m * 4 * sizeof(float), cudaMemcpyDeviceToHost, h->st);
-        e = cudaMemcpyAsync(scales, d_sc, (size_t)m * 2 * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+    if (e != cudaSuccess) { tmp.free_all(); return cuda_check(h, e, "dataset offsets"); }
+    const long long m = std::min<long long>(total, cap);
+    if (m > 0) {
+        float* d_feat = tmp.alloc<float>((size_t)m * LF);
+        float* d_tg = tmp.alloc<float>((size_t)m * LT);
+        int* d_grp = rec_group ? tmp.alloc<int>((size_t)m) : nullptr;
+        if (tmp.failed) { tmp.free_all(); return set_err(h, GEON_ERR_NOMEM, "dataset allocation failed"); }
+        learn_records(h->P, h->S, h->T, h->recs, h->rec_cnt, h->gcen, h->rec_cap, ngroups, group_stride, d_off, (int)m,
+                      gfloor, d_feat, d_tg, d_grp, h->ctl, h->st, h->lc);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(feat, d_feat, (size_t)m * LF * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(target, d_tg, (size_t)m * LT * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+        if (e == cudaSuccess && d_grp) e = cudaMemcpyAsync(rec_group, d_grp, (size_t)m * sizeof(int), cudaMemcpyDeviceToHost, h->st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
-        if (e == cudaSuccess && pair_target) {
-            std::vector<LearnPair> hp(m);
-            e = cudaMemcpy(hp.data(), d_pairs, (size_t)m * sizeof(LearnPair), cudaMemcpyDeviceToHost);
-            for (int q = 0; q < m; q++) pair_target[q] = hp[q].target;
-        }
     }
     tmp.free_all();
-    if (count) *count = found;
+    if (count) *count = total;
     r = cuda_check(h, e, "learned-correction dataset");
     if (r) return r;
     return read_ctl(h);
+}
+
+int geon_learn_apply(GeonHandle* h, const float* y, int64_t n) {
+    if (!h || n < 0 || (n > 0 && !y)) return GEON_ERR_ARG;
+    if (h->n == 0) return n == 0 ? GEON_OK : set_err(h, GEON_ERR_ARG, "no particles");
+    int r = learn_prepare(h);
+    if (r) return r;
+    if (h->rec_total_h != n) return set_err(h, GEON_ERR_ARG, "n differs from the record count");
+    DevArena tmp;
+    float* d_y = tmp.alloc<float>((size_t)std::max<int64_t>(n, 1) * LO);
+    if (tmp.failed) { tmp.free_all(); return set_err(h, GEON_ERR_NOMEM, "allocation failed"); }
+    cudaError_t e = n > 0 ? cudaMemcpyAsync(d_y, y, (size_t)n * LO * sizeof(float), cudaMemcpyHostToDevice, h->st) : cudaSuccess;
+    if (e == cudaSuccess) {
+        r = learn_correct_records(h, d_y);
+        if (r) { cudaStreamSynchronize(h->st); tmp.free_all(); return r; }
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    tmp.free_all();
+    r = cuda_check(h, e, "learned-correction apply");
+    return r ? r : read_ctl(h);
 }
 
 int geon_learn_set_weights(GeonHandle* h, const float* weights, int32_t n_param) {
@@ -1219,17 +1307,18 @@ int geon_learn_set_weights(GeonHandle* h, const float* weights, int32_t n_param)
     if (!weights) { h->learn_w = nullptr; return GEON_OK; }       // the buffer stays for reuse
     if (n_param != MLP_NPARAM) return set_err(h, GEON_ERR_ARG, "n_param must be GEON_MLP_NPARAM");
     static_assert(MLP_NPARAM == GEON_MLP_NPARAM, "weight count");
-    if (h->learn_arena.ptrs.empty()) {
-        float* w = h->learn_arena.alloc<float>(MLP_NPARAM);
-        unsigned long long* c = h->learn_arena.alloc<unsigned long long>(1);
-        if (h->learn_arena.failed) { h->learn_arena.free_all(); return set_err(h, GEON_ERR_NOMEM, "weight allocation failed"); }
-        (void)w; (void)c;
+    static_assert(LF == GEON_LEARN_FEATURES && LO == GEON_LEARN_OUTPUTS && LT == GEON_LEARN_TARGETS, "record layout");
+    if (!h->learn_w_buf) {
+        float* w = nullptr;
+        if (cudaMalloc(&w, MLP_NPARAM * sizeof(float)) != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(h, GEON_ERR_NOMEM, "weight allocation failed");
+        }
+        h->learn_w_buf = w;
     }
-    float* dw = static_cast<float*>(h->learn_arena.ptrs[0]);
-    h->pair_cnt = static_cast<unsigned long long*>(h->learn_arena.ptrs[1]);
-    CK(cudaMemcpyAsync(dw, weights, MLP_NPARAM * sizeof(float), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->learn_w_buf, weights, MLP_NPARAM * sizeof(float), cudaMemcpyHostToDevice, h->st));
     CK(cudaStreamSynchronize(h->st));
-    h->learn_w = dw;
+    h->learn_w = h->learn_w_buf;
     return GEON_OK;
 }
 
@@ -1244,7 +1333,7 @@ static int mlp_upload(GeonHandle* h, MlpData& D, const float* weights, const flo
                       int n, int nloss) {
     D.w = D.A.alloc<float>(MLP_NPARAM);
     D.x = D.A.alloc<float>((size_t)n * LF);
-    if (t) D.t = D.A.alloc<float>((size_t)n * 2);
+    if (t) D.t = D.A.alloc<float>((size_t)n * LT);
     if (wt) D.wt = D.A.alloc<float>(n);
     D.grad = D.A.alloc<float>(MLP_NPARAM);
     D.loss = D.A.alloc<double>(std::max(nloss, 1));
@@ -1253,7 +1342,7 @@ static int mlp_upload(GeonHandle* h, MlpData& D, const float* weights, const flo
     if (D.A.failed) { D.A.free_all(); return set_err(h, GEON_ERR_NOMEM, "network buffer allocation failed"); }
     cudaError_t e = cudaMemcpyAsync(D.w, weights, MLP_NPARAM * sizeof(float), cudaMemcpyHostToDevice, h->st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(D.x, x, (size_t)n * LF * sizeof(float), cudaMemcpyHostToDevice, h->st);
-    if (e == cudaSuccess && t) e = cudaMemcpyAsync(D.t, t, (size_t)n * 2 * sizeof(float), cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess && t) e = cudaMemcpyAsync(D.t, t, (size_t)n * LT * sizeof(float), cudaMemcpyHostToDevice, h->st);
     if (e == cudaSuccess && wt) e = cudaMemcpyAsync(D.wt, wt, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, h->st);
     if (e == cudaSuccess) e = cudaMemsetAsync(D.grad, 0, MLP_NPARAM * sizeof(float), h->st);
     if (e == cudaSuccess) e = cudaMemsetAsync(D.loss, 0, std::max(nloss, 1) * sizeof(double), h->st);
@@ -1267,13 +1356,13 @@ int geon_mlp_forward(GeonHandle* h, const float* weights, const float* x, int32_
     MlpData D;
     int r = mlp_upload(h, D, weights, x, nullptr, nullptr, n, 0);
     if (r) return r;
-    float* dy = D.A.alloc<float>((size_t)n * 2);
+    float* dy = D.A.alloc<float>((size_t)n * LO);
     cudaError_t e = D.A.failed ? cudaErrorMemoryAllocation : cudaSuccess;
     if (e == cudaSuccess) {
         mlp_forward(D.w, D.x, n, dy, &h->ctl->err, h->st, h->lc);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(y, dy, (size_t)n * 2 * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(y, dy, (size_t)n * LO * sizeof(float), cudaMemcpyDeviceToHost, h->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
     D.A.free_all();
     r = cuda_check(h, e, "network forward");

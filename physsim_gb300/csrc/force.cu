@@ -878,7 +878,7 @@ __device__ __forceinline__ void list_entries(WS& W, unsigned m, unsigned active,
 
 // NOPE: the potential-energy sums are off at compile time (the common case
 // of a force pass that only integrates), which keeps their code out of the
-// evaluation loop.  EMIT: record the accepted (cell, particle) pairs for the
+// evaluation loop.  EMIT: record the accepted (cell, group) pairs for the
 // learned correction.  The plain walk without energy sums keeps its
 // compensated sums, group box and node counts in shared memory and runs six
 // CTAs per SM (80 registers; the periodic form spills 32 bytes there and is
@@ -942,6 +942,8 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
     const int nInt0 = ctl->nInternal, nLeaf0 = ctl->nLeaves, nValid0 = ctl->nValid;
     if (SHF && lane == 0) { W.counts[0] = nInt0; W.counts[1] = nLeaf0; W.counts[2] = nValid0; }
     int top = 0, npool = 0, nfull = 0, lcnt = 0;
+    int rcnt = 0;                                                     // EMIT: records of this warp
+    const int grp = blockIdx.x * WC_WARPS + warp;
     if (root != ROOT_NONE && treeOk) {
         if (lane == 0) { W.stk_node[0] = root; W.stk_mask[0] = active; }
         top = 1;
@@ -1017,27 +1019,16 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
             const unsigned acc = __ballot_sync(0xffffffffu, accept);
             if ((int)lane == jj) { myAcc = acc & msk; myOpen = msk & ~acc; }
         }
-        if (EMIT) {                                                   // learned correction: (cell, particle) pairs
-            const int myCnt = __popc(myAcc);
-            const int pincl = warp_incl_scan_i(myCnt);
-            const int ptot = __shfl_sync(0xffffffffu, pincl, 31);
-            if (ptot) {
-                unsigned long long base = 0;
-                if (lane == 31) base = atomicAdd(C.pair_count, (unsigned long long)ptot);
-                base = __shfl_sync(0xffffffffu, base, 31);
-                // one accepted cell at a time, each accepting particle writes its
-                // own pair: the pairs of a cell are one contiguous write
-                for (unsigned om = __ballot_sync(0xffffffffu, myAcc != 0); om; om &= om - 1) {
-                    const int jj = __ffs(om) - 1;
-                    const unsigned m = __shfl_sync(0xffffffffu, myAcc, jj);
-                    const int nd = __shfl_sync(0xffffffffu, node, jj);
-                    const int off = __shfl_sync(0xffffffffu, pincl - myCnt, jj);
-                    if ((m >> lane) & 1u) {
-                        const unsigned long long pos = base + (unsigned long long)(off + __popc(m & lanemask_lt()));
-                        if (pos < (unsigned long long)C.pair_cap) C.pairs[pos] = make_int2(nd, ti);
-                    }
-                }
+        if (EMIT) {                                                   // learned correction: (cell, group) records
+            // one record per accepted cell: the node and the lanes that accept
+            // it, in this warp's own segment, in walk order
+            const bool mine = myAcc != 0;
+            const unsigned rb = __ballot_sync(0xffffffffu, mine);
+            if (mine) {
+                const int slot = rcnt + __popc(rb & lanemask_lt());
+                if (slot < C.rec_cap) C.recs[(size_t)grp * C.rec_cap + slot] = make_uint2((uint32_t)node, myAcc);
             }
+            rcnt += __popc(rb);
         }
         const unsigned leafMask = kind == 1 ? mask : 0u;
         const bool bucket = leafMask && lm.y > LEAF_CAP;
@@ -1118,6 +1109,14 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
         __syncwarp();
     }
     flush_pool<MAGGM, REL, BRK, PER>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
+    if (EMIT && lane == 0) {
+        const float cx = SHF ? W.gbox[0] : gcx0, cy = SHF ? W.gbox[1] : gcy0;
+        const float hx = SHF ? W.gbox[2] : ghx0, hy = SHF ? W.gbox[3] : ghy0;
+        C.gcen[grp] = make_float4(cx, cy, sqrtf(hx * hx + hy * hy) * (1.f + 1e-5f), 0.f);
+        C.rec_cnt[grp] = rcnt;
+        atomicMax(C.rec_max, (unsigned)rcnt);
+        atomicAdd(C.rec_total, (unsigned long long)rcnt);
+    }
     finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter, sysId);
 }
 
@@ -1936,7 +1935,7 @@ static void launch_force(bool bh, const DevParams& P, const DevState& S, const T
         constexpr bool PLAIN = !MAGGM && !REL && !BRK;
         const int blocks = std::max(1, (slots + WC_THREADS - 1) / WC_THREADS);
         const bool lean = PLAIN && !C.pe;
-        if (PLAIN && C.pair_count) {               // learned correction (plain forces only)
+        if (PLAIN && C.recs) {                     // learned correction (plain forces only)
             if (P.periodic) {
                 if (lean) launch_walkc<false, false, false, true, true, true>(blocks, P, S, T, d_root, ctl, C, st);
                 else launch_walkc<false, false, false, true, false, true>(blocks, P, S, T, d_root, ctl, C, st);

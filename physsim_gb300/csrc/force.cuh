@@ -23,11 +23,18 @@ struct ForceCtx {
     const double* sys_dt;     // substep of each system; systems with dt <= 0 sit this pass out
     unsigned long long* sys_accel;   // per-system planner maxima (double bits)
     unsigned long long* sys_cyc;
-    // learned correction: the walk records every accepted (cell, target)
-    // pair as (node, particle); pairs at positions >= pair_cap are counted only
-    int2* pairs;
-    long long pair_cap;
-    unsigned long long* pair_count;
+    // learned correction: each warp of the walk (a group of 32 consecutive
+    // targets in walk order) records every cell some of its targets accept as
+    // one aggregate, as (node, mask of accepting lanes), into its own segment
+    // recs[group * rec_cap ...]; rec_cnt[group] receives the count (records
+    // beyond rec_cap are counted, not stored), rec_max the largest count and
+    // rec_total their sum
+    uint2* recs;
+    int rec_cap;
+    int* rec_cnt;
+    unsigned* rec_max;
+    unsigned long long* rec_total;
+    float4* gcen;                // per group: centre of the targets' box (x, y), radius bound
     // pairwise sum split over source slices (direct_plan): scratch of partial
     // sums, null or dslices <= 1 for one pass over all sources
     float* dpart;

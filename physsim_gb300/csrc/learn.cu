@@ -1,212 +1,196 @@
-// learn.cu — training data of the learned far-field correction.
+// learn.cu — training records of the learned far-field correction.
 //
-// learn_collect_pairs walks the tree for a list of target particles with the
-// reference's opening rule (src/forces.js:622-694) and records every cell a
-// target accepts as an aggregate.  learn_residuals then evaluates, for each
-// pair, the exact sum over the cell's member particles (the pairwise sum of
-// src/forces.js:94-125 restricted to the cell, excluding the target itself)
-// minus the monopole term the walk uses, separately for the mass-sourced
-// field (gravity + Yukawa, per unit target mass) and the charge-sourced field
-// (Coulomb, per unit target charge), normalised by the scales of learn.cuh.
+// The walk with record emission (force.cu, walkc_kernel EMIT) leaves, for
+// each group of 32 consecutive targets in walk order, the cells some of its
+// targets accepted as one aggregate (src/forces.js:680-685) with the mask of
+// those targets.  For a record, learn_records_kernel evaluates at every
+// accepting target the exact field of the cell's member particles (the
+// pairwise sum of src/forces.js:94-125 restricted to the cell: gravity and
+// Yukawa per unit target mass with the per-pair cutoff of forces.js:387,
+// Coulomb per unit target charge), subtracts what the correction already has
+// without the network (the monopole with the group's Yukawa decision and the
+// analytic expansion of learn.cuh), and fits the mass-field residual with the
+// network's output form by weighted least squares.
 #include "learn.cuh"
 
 namespace geon {
 
-constexpr int LC_THREADS = 128;
-constexpr int LC_WARPS = LC_THREADS / 32;
+constexpr int LR_THREADS = 128;
+constexpr int LR_WARPS = LR_THREADS / 32;
 
-__global__ void __launch_bounds__(LC_THREADS)
-collect_pairs_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl,
-                     const int* __restrict__ targets, int k, LearnPair* pairs, long long cap,
-                     unsigned long long* d_count) {
-    __shared__ int s_node[LC_WARPS][WALK_STACK];
-    __shared__ unsigned s_mask[LC_WARPS][WALK_STACK];
-    const int warp = threadIdx.x >> 5;
-    const unsigned lane = threadIdx.x & 31;
-    const int ti = (blockIdx.x * LC_WARPS + warp) * 32 + (int)lane;
-    const int n = ctl->n;
-    const bool valid = ti < k && targets[ti] >= 0 && targets[ti] < n;
-    const unsigned active = __ballot_sync(0xffffffffu, valid);
-    if (!active) return;
-    const int i = valid ? targets[ti] : 0;
-    const float4 p = S.pos[i];
-    const float2 pl = S.pos_lo[i];
-    const int root = *d_root;
-    const int nInt = ctl->nInternal, nLeaf = ctl->nLeaves;
-    if ((ctl->err & (ERR_NODE_OVERFLOW | ERR_BAD_INDEX)) || root == ROOT_NONE || (root & LEAF_REF)) return;
-    int top = 0;
-    if (lane == 0) { s_node[warp][0] = root; s_mask[warp][0] = active; }
-    top = 1;
-    __syncwarp();
-    while (top > 0) {
-        top--;
-        const int node = s_node[warp][top];
-        const unsigned mask = s_mask[warp][top];
-        __syncwarp();
-        if (node & LEAF_REF) continue;                   // leaves are evaluated point by point
-        if (node < 0 || node >= nInt) { if (lane == 0) atomicOr(&ctl->err, ERR_BAD_INDEX); continue; }
-        const float4 a = T.int_a[node];
-        if (a.z < EPS_F) continue;
-        const float4 c = T.int_c[node];
-        bool accept = false;
-        if ((mask >> lane) & 1u) {
-            float rx, ry;
-            displacement(P, p.x, p.y, a.x, c.x - pl.x, a.y, c.y - pl.y, rx, ry);
-            const float rhs = P.thetaSq * __fmaf_rn(rx, rx, ry * ry);
-            accept = c.z < rhs;
-            if (fabsf(rhs - c.z) <= 1e-6f * c.z) {
-                double dx, dy;
-                const double ox = (double)p.x + (double)pl.x, oy = (double)p.y + (double)pl.y;
-                const double sx = (double)a.x + (double)c.x, sy = (double)a.y + (double)c.y;
-                if (P.periodic) min_image_d(ox, oy, sx, sy, P.topology, P.Wd, P.Hd, dx, dy);
-                else { dx = sx - ox; dy = sy - oy; }
-                const double size = 2.0 * ldexp(P.rootW, -(int)c.w);
-                accept = size * size < P.thetaSqD * (dx * dx + dy * dy);
-            }
-        }
-        const unsigned acc = __ballot_sync(0xffffffffu, accept);
-        if (acc) {
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(d_count, (unsigned long long)__popc(acc));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (accept) {
-                const unsigned long long pos = base + (unsigned long long)__popc(acc & lanemask_lt());
-                if (pos < (unsigned long long)cap) pairs[pos] = LearnPair{ node, i };
-            }
-        }
-        const unsigned open = mask & ~acc;
-        if (open) {
-            const int4 ch = T.int_child[node];
-            const int np = (ch.x >= 0) + (ch.y >= 0) + (ch.z >= 0) + (ch.w >= 0);
-            if (top + np > WALK_STACK) { if (lane == 0) atomicOr(&ctl->err, ERR_STACK_OVERFLOW); break; }
-            if (lane == 0) {
-                int tp = top;
-                if (ch.x >= 0) { s_node[warp][tp] = ch.x; s_mask[warp][tp++] = open; }
-                if (ch.y >= 0) { s_node[warp][tp] = ch.y; s_mask[warp][tp++] = open; }
-                if (ch.z >= 0) { s_node[warp][tp] = ch.z; s_mask[warp][tp++] = open; }
-                if (ch.w >= 0) { s_node[warp][tp] = ch.w; s_mask[warp][tp++] = open; }
-            }
-            top += np;
-            __syncwarp();
-        }
-    }
-    (void)nLeaf;
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
 }
 
-// Field of one source (mass m, charge q) at displacement (rx, ry) from the
-// target: mass-sourced (gravity + Yukawa) per unit target mass, and
-// charge-sourced (Coulomb) per unit target charge (src/forces.js:205-240, 387-399).
-__device__ __forceinline__ void source_fields(const DevParams& P, float rx, float ry, float m, float q,
-                                              float& gx, float& gy, float& ex, float& ey) {
-    const float rawRSq = rx * rx + ry * ry;
-    const float rSq = rawRSq + P.softSq;
+// Mass-sourced (gravity + Yukawa) field of a unit-mass-weighted source at
+// displacement (rx, ry), with the Yukawa cutoff decided by `yk`.
+__device__ __forceinline__ void mass_field(const DevParams& P, float rx, float ry, bool yk, float& gx, float& gy) {
+    const float rSq = __fmaf_rn(rx, rx, ry * ry) + P.softSq;
     const float invR = rsqrtf(rSq);
-    const float invRSq = invR * invR;
-    const float invR3 = invR * invRSq;
-    float fm = (P.toggles & GEON_GRAVITY) ? m * invR3 : 0.f;
-    if (P.yukOn && rawRSq < P.yukCutSq) {
+    const float invR3 = invR * invR * invR;
+    float f = (P.toggles & GEON_GRAVITY) ? invR3 : 0.f;
+    if (yk) {
         const float r = rSq * invR;
-        fm += YUKAWA_COUPLING * m * __expf(-P.yukMu * r) * (invRSq + P.yukMu * invR) * invR;
+        f += YUKAWA_COUPLING * __expf(-P.yukMu * r) * (invR * invR + P.yukMu * invR) * invR;
     }
-    const float fc = (P.toggles & GEON_COULOMB) ? -q * invR3 : 0.f;
-    gx += rx * fm; gy += ry * fm;
-    ex += rx * fc; ey += ry * fc;
+    gx = rx * f;
+    gy = ry * f;
 }
 
-__global__ void residual_kernel(DevParams P, DevState S, TreeBufs T, const LearnPair* __restrict__ pairs,
-                                const unsigned long long* d_count, int cap, float* feat_m, float* feat_c, float* target,
-                                float* scales) {
-    const int np = (int)min(*d_count, (unsigned long long)cap);
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < np; e += gridDim.x * blockDim.x) {
-        const LearnPair pr = pairs[e];
-        const int node = pr.node, i = pr.target;
-        const float4 p = S.pos[i];
-        const float2 pl = S.pos_lo[i];
-        const float4 a = T.int_a[node], c = T.int_c[node];
-        const int4 mm = T.int_meta[node];
-        float dx, dy;
-        displacement(P, p.x, p.y, a.x, c.x - pl.x, a.y, c.y - pl.y, dx, dy);
-        // monopole (forces.js:680-685)
-        float mgx = 0.f, mgy = 0.f, mex = 0.f, mey = 0.f;
-        source_fields(P, dx, dy, a.z, a.w, mgx, mgy, mex, mey);
-        // exact sum over the cell's members
-        float gx = 0.f, gy = 0.f, ex = 0.f, ey = 0.f;
-        for (int s = mm.y; s < mm.z; s++) {
-            const float4 pa = T.ps_a[s];
-            const float4 pb = T.ps_b[s];
-            if ((int)ref_index(__float_as_uint(T.ps_c[s].w)) == i) continue;
-            float rx, ry;
-            displacement(P, p.x, p.y, pa.x, pb.x - pl.x, pa.y, pb.y - pl.y, rx, ry);
-            source_fields(P, rx, ry, pa.z, pa.w, gx, gy, ex, ey);
+__global__ void sel_counts_kernel(const int* __restrict__ rec_cnt, int rec_cap, int nsel, int stride, int* out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nsel; i += gridDim.x * blockDim.x)
+        out[i] = min(rec_cnt[(size_t)i * stride], rec_cap);
+}
+
+__global__ void __launch_bounds__(LR_THREADS)
+learn_records_kernel(DevParams P, DevState S, TreeBufs T, const FrameCtl* __restrict__ ctl, const uint2* __restrict__ recs,
+                     const int* __restrict__ rec_cnt, const float4* __restrict__ gcen, int rec_cap, int nsel, int stride,
+                     const int* __restrict__ off,
+                     int cap, float gfloor, float* __restrict__ feat, float* __restrict__ target, int* __restrict__ rec_group) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = ctl->n;
+    for (int gi = blockIdx.x; gi < nsel; gi += gridDim.x) {
+        const int grp = gi * stride;
+        const int kk = grp * 32 + lane;
+        int ti = kk < n ? T.tgt[kk] : -1;
+        if (ti >= n) ti = -1;
+        const float4 gc = gcen[grp];
+        const float gx = gc.x, gy = gc.y;
+        float tx = 0.f, ty = 0.f, txl = 0.f, tyl = 0.f, w = 0.f;
+        if (ti >= 0) {
+            const float4 p = S.pos[ti];
+            const float2 pl = S.pos_lo[ti];
+            const float4 F = S.force[ti];
+            tx = p.x; ty = p.y; txl = pl.x; tyl = pl.y;
+            const float m2 = p.z * p.z, f2 = F.x * F.x + F.y * F.y;
+            w = m2 / fmaxf(fmaxf(f2, m2 * gfloor * gfloor), 1e-30f);
         }
-        float fm[LF], fc[LF], sm, sc;
-        const float size = sqrtf(c.z);
-        pair_features(P, dx, dy, size, a.z, a.w, T.int_m1[node], T.int_m2[node], T.int_m3[node], fm, fc, sm, sc);
-        for (int f = 0; f < LF; f++) { feat_m[(size_t)e * LF + f] = fm[f]; feat_c[(size_t)e * LF + f] = fc[f]; }
-        const float ism = sm > 0.f ? 1.f / sm : 0.f, isc = sc > 0.f ? 1.f / sc : 0.f;
-        target[(size_t)e * 4 + 0] = (gx - mgx) * ism;
-        target[(size_t)e * 4 + 1] = (gy - mgy) * ism;
-        target[(size_t)e * 4 + 2] = (ex - mex) * isc;
-        target[(size_t)e * 4 + 3] = (ey - mey) * isc;
-        scales[(size_t)e * 2 + 0] = sm;
-        scales[(size_t)e * 2 + 1] = sc;
+        // offset of this target from the group centre
+        const float ox = __fadd_rn(__fsub_rn(tx, gx), txl), oy = __fadd_rn(__fsub_rn(ty, gy), tyl);
+        const int cnt = min(rec_cnt[grp], rec_cap);
+        const int base = off[gi];
+        for (int r = warp; r < cnt; r += LR_WARPS) {
+            const int e = base + r;
+            if (e >= cap) break;
+            const uint2 rc = recs[(size_t)grp * rec_cap + r];
+            const int node = (int)rc.x;
+            const bool mine = ti >= 0 && ((rc.y >> lane) & 1u);
+            RecGeo R;
+            float f[LF];
+            record_geo(P, T, node, gx, gy, R, f);
+            const bool exact = (record_flags(P, R, gc.z) & REC_EXACT) != 0;
+            Lin Gm, Ec;
+            record_expansion(P, R, nullptr, exact, Gm, Ec);
+            if (exact) {
+                // no member sums for a record without weight (lane 0 still writes it)
+                if (lane == 0) {
+                    float* o = target + (size_t)e * LT;
+#pragma unroll
+                    for (int c = 0; c < LT; c++) o[c] = 0.f;
+                    float* fo = feat + (size_t)e * LF;
+#pragma unroll
+                    for (int c = 0; c < LF; c++) fo[c] = f[c];
+                    if (rec_group) rec_group[e] = grp;
+                }
+                continue;
+            }
+            // exact member sum at this target (two-sum compensated)
+            const int4 meta = T.int_meta[node];
+            float sx = 0.f, sxl = 0.f, sy = 0.f, syl = 0.f;
+            for (int q = meta.y; q < meta.z; q++) {
+                const float4 pa = T.ps_a[q];
+                const float4 pb = T.ps_b[q];
+                const int j = (int)ref_index(__float_as_uint(reinterpret_cast<const float*>(T.ps_c + q)[3]));
+                if (!mine || j == ti) continue;
+                float rx, ry;
+                displacement(P, tx, ty, pa.x, pb.x - txl, pa.y, pb.y - tyl, rx, ry);
+                float gxv, gyv;
+                mass_field(P, rx, ry, P.yukOn && __fmaf_rn(rx, rx, ry * ry) < P.yukCutSq, gxv, gyv);
+                const df a1 = two_sum(sx, pa.z * gxv); sx = a1.hi; sxl += a1.lo;
+                const df a2 = two_sum(sy, pa.z * gyv); sy = a2.hi; syl += a2.lo;
+            }
+            float resx = 0.f, resy = 0.f;
+            if (mine) {
+                // monopole with the group's Yukawa decision and the analytic expansion at this target
+                const float dx = R.dx - ox, dy = R.dy - oy;
+                float mgx, mgy;
+                mass_field(P, dx, dy, R.yg, mgx, mgy);
+                const float ax = Gm.v[0] + Gm.j[0] * ox + Gm.j[1] * oy, ay = Gm.v[1] + Gm.j[2] * ox + Gm.j[3] * oy;
+                resx = (sx + sxl) - R.M * mgx - ax;
+                resy = (sy + syl) - R.M * mgy - ay;
+            }
+            // weighted least squares in the frame (u, u_perp), basis (s0, s1 e_u, s1 e_v)
+            float s0, s1;
+            out_scales(R, s0, s1);
+            const float eu = ox * R.ux + oy * R.uy, ev = -ox * R.uy + oy * R.ux;
+            const float b0 = s0, b1 = s1 * eu, b2 = s1 * ev;
+            // wide groups do not use the network: their records carry no weight
+            const float wm = (mine && !exact) ? w : 0.f;
+            const float rp = resx * R.ux + resy * R.uy, rq = -resx * R.uy + resy * R.ux;
+            const float A00 = warp_sum(wm * b0 * b0), A11 = warp_sum(wm * b1 * b1), A22 = warp_sum(wm * b2 * b2);
+            const float A01 = warp_sum(wm * b0 * b1), A02 = warp_sum(wm * b0 * b2), A12 = warp_sum(wm * b1 * b2);
+            const float p0 = warp_sum(wm * b0 * rp), p1 = warp_sum(wm * b1 * rp), p2 = warp_sum(wm * b2 * rp);
+            const float q0 = warp_sum(wm * b0 * rq), q1 = warp_sum(wm * b1 * rq), q2 = warp_sum(wm * b2 * rq);
+            if (lane == 0) {
+                // (A + ridge) y = b by Cramer's rule in FP64 (3 x 3)
+                const double tr = (double)A00 + A11 + A22, rg = 1e-6 * tr + 1e-30;
+                const double m00 = A00 + rg, m11 = A11 + rg, m22 = A22 + rg, m01 = A01, m02 = A02, m12 = A12;
+                const double det = m00 * (m11 * m22 - m12 * m12) - m01 * (m01 * m22 - m12 * m02) + m02 * (m01 * m12 - m11 * m02);
+                double yp[3] = { 0, 0, 0 }, yq[3] = { 0, 0, 0 };
+                if (det != 0.0 && isfinite(det)) {
+                    const double id = 1.0 / det;
+                    const double c00 = m11 * m22 - m12 * m12, c01 = m02 * m12 - m01 * m22, c02 = m01 * m12 - m02 * m11;
+                    const double c11 = m00 * m22 - m02 * m02, c12 = m01 * m02 - m00 * m12, c22 = m00 * m11 - m01 * m01;
+                    yp[0] = id * (c00 * p0 + c01 * p1 + c02 * p2);
+                    yp[1] = id * (c01 * p0 + c11 * p1 + c12 * p2);
+                    yp[2] = id * (c02 * p0 + c12 * p1 + c22 * p2);
+                    yq[0] = id * (c00 * q0 + c01 * q1 + c02 * q2);
+                    yq[1] = id * (c01 * q0 + c11 * q1 + c12 * q2);
+                    yq[2] = id * (c02 * q0 + c12 * q1 + c22 * q2);
+                }
+                float* o = target + (size_t)e * LT;
+                o[0] = (float)yp[0]; o[1] = (float)yp[1]; o[2] = (float)yp[2];
+                o[3] = (float)yq[0]; o[4] = (float)yq[1]; o[5] = (float)yq[2];
+                // the same quadratic form for both components (the weights do not depend on the component)
+                const float Aq[6] = { A00, A11, A22, A01, A02, A12 };
+#pragma unroll
+                for (int c = 0; c < 6; c++) { o[LO + c] = Aq[c]; o[LO + 6 + c] = Aq[c]; }
+                float* fo = feat + (size_t)e * LF;
+#pragma unroll
+                for (int c = 0; c < LF; c++) fo[c] = f[c];
+                if (rec_group) rec_group[e] = grp;
+            }
+        }
     }
 }
 
-// Deterministic order of the collected pairs: (target, node) keys sorted
-// with the stable radix sort, then the records permuted.
-__global__ void pair_keys_kernel(const LearnPair* __restrict__ pairs, const unsigned long long* d_count, int cap,
-                                 int* d_n, uint64_t* keys, uint32_t* vals) {
-    const int n = (int)min(*d_count, (unsigned long long)cap);
-    if (blockIdx.x == 0 && threadIdx.x == 0) *d_n = n;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-        const LearnPair p = pairs[e];
-        keys[e] = ((uint64_t)(uint32_t)p.target << 32) | (uint64_t)(uint32_t)p.node;
-        vals[e] = (uint32_t)e;
-    }
-}
-__global__ void pair_permute_kernel(const LearnPair* __restrict__ in, const uint32_t* __restrict__ order,
-                                    const int* d_n, LearnPair* __restrict__ out) {
-    const int n = *d_n;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) out[e] = in[order[e]];
+size_t learn_offsets_scratch_bytes(int ngroups) {
+    return (size_t)(ngroups + 1) * sizeof(int) + scan_temp_ints(std::max(ngroups, 1)) * sizeof(int) + 256;
 }
 
-size_t learn_sort_scratch_bytes(int cap) {
-    const size_t c = (size_t)std::max(cap, 1);
-    return c * (2 * sizeof(uint64_t) + 2 * sizeof(uint32_t)) + radix_temp_bytes(std::max(cap, 1)) + 256;
-}
-
-void learn_sort_pairs(const LearnPair* pairs, const unsigned long long* d_count, int cap, LearnPair* out, int* d_n,
-                      void* scratch, cudaStream_t st, LaunchCounter& lc) {
-    const size_t c = (size_t)std::max(cap, 1);
-    char* p = static_cast<char*>(scratch);
-    uint64_t* keys = reinterpret_cast<uint64_t*>(p); p += c * sizeof(uint64_t);
-    uint64_t* keys_alt = reinterpret_cast<uint64_t*>(p); p += c * sizeof(uint64_t);
-    uint32_t* vals = reinterpret_cast<uint32_t*>(p); p += c * sizeof(uint32_t);
-    uint32_t* vals_alt = reinterpret_cast<uint32_t*>(p); p += c * sizeof(uint32_t);
-    p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(p) + 255) & ~(uintptr_t)255);
-    const int blocks = 152 * 8;
-    pair_keys_kernel<<<blocks, 256, 0, st>>>(pairs, d_count, cap, d_n, keys, vals);
+void learn_record_offsets(const int* rec_cnt, int rec_cap, int ngroups, int stride, int* off, int* total,
+                          void* scan_tmp, cudaStream_t st, LaunchCounter& lc) {
+    const int nsel = (ngroups + stride - 1) / stride;
+    int* sel = static_cast<int*>(scan_tmp);
+    int* tmp = reinterpret_cast<int*>(reinterpret_cast<char*>(scan_tmp) + (((size_t)(nsel + 1) * sizeof(int) + 255) & ~(size_t)255));
+    sel_counts_kernel<<<std::max(1, std::min((nsel + 255) / 256, 1024)), 256, 0, st>>>(rec_cnt, rec_cap, nsel, stride, sel);
     lc.add(1);
-    const int which = radix_sort_pairs(keys, vals, keys_alt, vals_alt, (int)c, d_n, 64, p, st, &lc);
-    pair_permute_kernel<<<blocks, 256, 0, st>>>(pairs, which ? vals_alt : vals, d_n, out);
-    lc.add(1);
+    exclusive_scan(sel, off, nsel, nullptr, total, tmp, st, &lc);
 }
 
-void learn_collect_pairs(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
-                         const int* d_targets, int k, LearnPair* pairs, long long cap, unsigned long long* d_count,
-                         cudaStream_t st, LaunchCounter& lc) {
-    cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), st);
-    const int blocks = std::max(1, (k + LC_THREADS - 1) / LC_THREADS);
-    collect_pairs_kernel<<<blocks, LC_THREADS, 0, st>>>(P, S, T, d_root, ctl, d_targets, k, pairs, cap, d_count);
-    lc.add(1);
-}
-
-void learn_residuals(const DevParams& P, const DevState& S, const TreeBufs& T, const LearnPair* pairs,
-                     const unsigned long long* d_count,
-                     int cap, float* feat_m, float* feat_c, float* target, float* scales, cudaStream_t st,
-                     LaunchCounter& lc) {
-    residual_kernel<<<152 * 8, 128, 0, st>>>(P, S, T, pairs, d_count, cap, feat_m, feat_c, target, scales);
+void learn_records(const DevParams& P, const DevState& S, const TreeBufs& T, const uint2* recs, const int* rec_cnt,
+                   const float4* gcen, int rec_cap, int ngroups, int stride, const int* off, int cap, float gfloor,
+                   float* feat, float* target, int* rec_group, const FrameCtl* ctl, cudaStream_t st, LaunchCounter& lc) {
+    const int nsel = (ngroups + stride - 1) / stride;
+    if (nsel <= 0) return;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = std::max(1, std::min(nsel, std::max(sms, 1) * 8));
+    learn_records_kernel<<<blocks, LR_THREADS, 0, st>>>(P, S, T, ctl, recs, rec_cnt, gcen, rec_cap, nsel, stride, off, cap,
+                                                        gfloor, feat, target, rec_group);
     lc.add(1);
 }
 

@@ -1,7 +1,8 @@
 // mlp.cu — the learned-correction network on fifth-generation tensor cores.
 //
-// Network (learn.cuh): 9 -> 64 -> 64 -> 2 with GELU (tanh form) after the two
-// hidden layers; BF16 weights and activations, FP32 accumulation in TMEM.
+// Network (learn.cuh): 14 -> 64 -> 64 -> 6 with GELU (tanh form) after the two
+// hidden layers; BF16 weights and activations, FP32 accumulation in TMEM, the
+// same roundings in inference and in training.
 // A CTA of 128 threads (one warpgroup) processes tiles of 128 samples: thread
 // t owns sample row t, which is TMEM lane t.  Per layer the epilogue of the
 // previous layer writes BF16 activations to shared memory in the canonical
@@ -16,10 +17,17 @@
 // (K = samples), accumulated in TMEM across every tile a CTA processes:
 //     GA = [dZ2^T ; dZ1^T] [H1^T ; X'^T]^T     (128 x 80)
 //     GB = [H2^T ; 1]      [dY^T]^T            (128 x 16)
-// X' is the feature row with a constant 1 in column 9, so GA column 64+9
+// X' is the feature row with a constant 1 in column 14, so GA column 64+14
 // holds the bias gradients db2 (rows 0..63) and db1 (rows 64..127); the ones
 // row of GB gives db3.  The epilogues write the transposed operands with
 // scattered 2-byte stores.
+//
+// Loss of a training sample: its 6 outputs y against the least-squares
+// targets y* of its record and the record's quadratic form, per component c
+// (the parallel and the perpendicular one),
+//     L_s = wt_s sum_c (y_c - y*_c)^T A_c (y_c - y*_c),   y_c = y[3c .. 3c+2],
+// the squared relative force error its output error causes at the targets
+// of the record (learn.cuh).
 #include "mlp.cuh"
 #include "tc.cuh"
 
@@ -33,13 +41,16 @@ namespace geon {
 using namespace tc;
 
 constexpr int MT = 128;          // samples per tile = threads per CTA = TMEM lanes
-constexpr int K1 = 16;           // layer-1 K: 9 features, a constant 1, zeros
-constexpr int N3 = 16;           // layer-3 N: 2 outputs, zeros
+constexpr int K1 = 16;           // layer-1 K: 14 features, a constant 1, zeros
+constexpr int N3 = 16;           // layer-3 N: 6 outputs, zeros
+static_assert(LF + 1 <= K1 && LO <= N3, "layer shapes");
 constexpr int NGA = LH + K1;     // N of the GA gradient GEMM
 constexpr float GELU_C = 0.7978845608028654f;   // sqrt(2/pi)
 constexpr float GELU_A = 0.044715f;
 
-constexpr int OFF_W1 = 0;
+constexpr int OFF_MU = 0;                 // input normalisation x' = (x - mu) * isd (FP32, not trained)
+constexpr int OFF_ISD = OFF_MU + LF;
+constexpr int OFF_W1 = OFF_ISD + LF;
 constexpr int OFF_B1 = OFF_W1 + LH * LF;
 constexpr int OFF_W2 = OFF_B1 + LH;
 constexpr int OFF_B2 = OFF_W2 + LH * LH;
@@ -60,22 +71,6 @@ __device__ __forceinline__ float gelu(float x) {
     const float u = GELU_C * fmaf(GELU_A * x, x * x, x);
     return 0.5f * x * (1.f + tanh_approx(u));
 }
-// Two GELUs in packed FP16 arithmetic (inference): 0.5 x (1 + tanh(x (c + c a x^2))),
-// returning the FP16 pair that the next layer reads.  The packed math halves
-// the CUDA-core instructions of the epilogue, which bound the inference
-// kernel; FP16 keeps 11 significant bits, more than the BF16 of training.
-__device__ __forceinline__ uint32_t gelu2_f16(float x0, float x1) {
-    const __half2 x = __floats2half2_rn(x0, x1);
-    const __half2 x2 = __hmul2(x, x);
-    const __half2 p = __hfma2(x2, __float2half2_rn(GELU_C * GELU_A), __float2half2_rn(GELU_C));
-    const __half2 u = __hmul2(p, x);
-    uint32_t ui = *reinterpret_cast<const uint32_t*>(&u), ti;
-    asm("tanh.approx.f16x2 %0, %1;" : "=r"(ti) : "r"(ui));
-    const __half2 t = *reinterpret_cast<const __half2*>(&ti);
-    const __half2 hx = __hmul2(x, __float2half2_rn(0.5f));
-    const __half2 g = __hfma2(t, hx, hx);
-    return *reinterpret_cast<const uint32_t*>(&g);
-}
 __device__ __forceinline__ float gelu_grad(float x) {
     const float x2 = x * x;
     const float t = tanh_approx(GELU_C * fmaf(GELU_A * x, x2, x));
@@ -91,14 +86,15 @@ struct NetSmem {
     __align__(128) uint8_t h1[MT * LH * 2];     // A of Z2
     __align__(128) uint8_t h2[MT * LH * 2];     // A of Y
     float b1[LH], b2[LH], b3[LO];
+    float nmu[LF], nisd[LF];
     float red[MT / 32];
     uint64_t bar;
     uint32_t tmem;
 };
 // Inference CTA: the second hidden layer reuses the first layer's activation
 // buffer and accumulator columns (GEMM 2 has consumed layer 1 before the
-// epilogue overwrites it), so a CTA needs 33 KB of shared memory and 64 TMEM
-// columns and six CTAs share an SM.
+// epilogue overwrites it), so the network needs 33 KB of shared memory and 64
+// TMEM columns per CTA.
 struct InfSmem {
     __align__(128) uint8_t w1[LH * K1 * 2];
     __align__(128) uint8_t w2[LH * LH * 2];
@@ -106,6 +102,7 @@ struct InfSmem {
     __align__(128) uint8_t x[MT * K1 * 2];
     __align__(128) uint8_t h[MT * LH * 2];      // A of Z2, then A of Y
     float b1[LH], b2[LH], b3[LO];
+    float nmu[LF], nisd[LF];
     uint64_t bar;
     uint32_t tmem;
 };
@@ -152,6 +149,14 @@ __device__ void stage_forward(SM& s, const float* __restrict__ W) {
     }
     for (int i = threadIdx.x; i < LH; i += blockDim.x) { s.b1[i] = W[OFF_B1 + i]; s.b2[i] = W[OFF_B2 + i]; }
     if (threadIdx.x < LO) s.b3[threadIdx.x] = W[OFF_B3 + threadIdx.x];
+    if (threadIdx.x < LF) { s.nmu[threadIdx.x] = W[OFF_MU + threadIdx.x]; s.nisd[threadIdx.x] = W[OFF_ISD + threadIdx.x]; }
+}
+
+// Input normalisation in FP32, before the features are rounded to BF16.
+template <class SM>
+__device__ __forceinline__ void normalise(const SM& s, float* x) {
+#pragma unroll
+    for (int k = 0; k < LF; k++) x[k] = (x[k] - s.nmu[k]) * s.nisd[k];
 }
 
 __device__ void stage_backward(TrainSmem& s, const float* __restrict__ W) {
@@ -246,38 +251,28 @@ __device__ __forceinline__ void stage_x(SM& s, const float* f) {
     put8(s.x, threadIdx.x, 8, K1, f + 8);
 }
 
-// ---- inference in FP16 operands ----------------------------------------------------
-__device__ __forceinline__ void put_f16(uint8_t* buf, int r, int k, int K, float v) {
-    *reinterpret_cast<__half*>(buf + kmajor_offset(r, k, K)) = __float2half_rn(v);
+// ---- inference ---------------------------------------------------------------------
+// Two GELUs (tanh form) in packed FP16 arithmetic, returned as the BF16 pair
+// of the next layer's operand.  FP16 keeps 11 significant bits against the
+// 8 of the BF16 result, so the result is the FP32 GELU's rounding to BF16
+// up to an occasional last-place difference, at half the instructions.
+__device__ __forceinline__ uint32_t gelu2_bf16(float x0, float x1) {
+    const __half2 x = __floats2half2_rn(x0, x1);
+    const __half2 x2 = __hmul2(x, x);
+    const __half2 pq = __hfma2(x2, __float2half2_rn(GELU_C * GELU_A), __float2half2_rn(GELU_C));
+    const __half2 u = __hmul2(pq, x);
+    uint32_t ui = *reinterpret_cast<const uint32_t*>(&u), ti;
+    asm("tanh.approx.f16x2 %0, %1;" : "=r"(ti) : "r"(ui));
+    const __half2 t = *reinterpret_cast<const __half2*>(&ti);
+    const __half2 hx = __hmul2(x, __float2half2_rn(0.5f));
+    const float2 g = __half22float2(__hfma2(t, hx, hx));
+    const __nv_bfloat162 b = __floats2bfloat162_rn(g.x, g.y);
+    return *reinterpret_cast<const uint32_t*>(&b);
 }
-__device__ __forceinline__ void put8_f16(uint8_t* buf, int r, int k0, int K, const float* v) {
-    uint4 u;
-    __half2 p;
-    p = __floats2half2_rn(v[0], v[1]); u.x = *reinterpret_cast<uint32_t*>(&p);
-    p = __floats2half2_rn(v[2], v[3]); u.y = *reinterpret_cast<uint32_t*>(&p);
-    p = __floats2half2_rn(v[4], v[5]); u.z = *reinterpret_cast<uint32_t*>(&p);
-    p = __floats2half2_rn(v[6], v[7]); u.w = *reinterpret_cast<uint32_t*>(&p);
-    *reinterpret_cast<uint4*>(buf + kmajor_offset(r, k0, K)) = u;
-}
-__device__ void stage_forward_f16(InfSmem& s, const float* __restrict__ W) {
-    for (int i = threadIdx.x; i < LH * K1; i += blockDim.x) {
-        const int r = i / K1, k = i % K1;
-        put_f16(s.w1, r, k, K1, k < LF ? W[OFF_W1 + r * LF + k] : 0.f);
-    }
-    for (int i = threadIdx.x; i < LH * LH; i += blockDim.x) put_f16(s.w2, i / LH, i % LH, LH, W[OFF_W2 + i]);
-    for (int i = threadIdx.x; i < N3 * LH; i += blockDim.x) {
-        const int r = i / LH, k = i % LH;
-        put_f16(s.w3, r, k, LH, r < LO ? W[OFF_W3 + r * LH + k] : 0.f);
-    }
-    for (int i = threadIdx.x; i < LH; i += blockDim.x) { s.b1[i] = W[OFF_B1 + i]; s.b2[i] = W[OFF_B2 + i]; }
-    if (threadIdx.x < LO) s.b3[threadIdx.x] = W[OFF_B3 + threadIdx.x];
-}
-__device__ __forceinline__ void stage_x_f16(InfSmem& s, const float* f) {
-    put8_f16(s.x, threadIdx.x, 0, K1, f);
-    put8_f16(s.x, threadIdx.x, 8, K1, f + 8);
-}
-// GELU epilogue of a 64-column accumulator into the next layer's FP16 operand.
-__device__ __forceinline__ void hidden_epilogue_f16(uint32_t tmem, const float* bias, uint8_t* out) {
+
+// GELU epilogue of a 64-column accumulator at column 0 into the next layer's
+// A operand (BF16, as in training).
+__device__ __forceinline__ void hidden_epilogue_inf(uint32_t tmem, const float* bias, uint8_t* out) {
     const int warp = threadIdx.x >> 5;
     const int row = threadIdx.x;
 #pragma unroll
@@ -286,25 +281,25 @@ __device__ __forceinline__ void hidden_epilogue_f16(uint32_t tmem, const float* 
         tmem_ld16(tmem_addr(tmem, warp, c0), v);
         uint32_t g[8];
 #pragma unroll
-        for (int i = 0; i < 8; i++) g[i] = gelu2_f16(v[2 * i] + bias[c0 + 2 * i], v[2 * i + 1] + bias[c0 + 2 * i + 1]);
+        for (int i = 0; i < 8; i++) g[i] = gelu2_bf16(v[2 * i] + bias[c0 + 2 * i], v[2 * i + 1] + bias[c0 + 2 * i + 1]);
         *reinterpret_cast<uint4*>(out + kmajor_offset(row, c0, LH)) = make_uint4(g[0], g[1], g[2], g[3]);
         *reinterpret_cast<uint4*>(out + kmajor_offset(row, c0 + 8, LH)) = make_uint4(g[4], g[5], g[6], g[7]);
     }
 }
 
-// Forward pass of the tile staged in s.x (FP16 operands; 64 TMEM columns,
-// reused by every layer); y0, y1 are this thread's outputs.
-__device__ __forceinline__ bool tile_forward(InfSmem& s, uint32_t& phase, bool ok, float& y0, float& y1) {
+// Forward pass of the tile staged in s.x (64 TMEM columns, reused by every
+// layer); y[LO] receives this thread's outputs.
+__device__ __forceinline__ bool tile_forward(InfSmem& s, uint32_t& phase, bool ok, float* y) {
     const int warp = threadIdx.x >> 5;
-    ok = mma_step(s, phase, ok, [&] { gemm(s.tmem + 0, s.x, s.w1, LH, K1, false, true); });
-    hidden_epilogue_f16(s.tmem, s.b1, s.h);
-    ok = mma_step(s, phase, ok, [&] { gemm(s.tmem + 0, s.h, s.w2, LH, LH, false, true); });
-    hidden_epilogue_f16(s.tmem, s.b2, s.h);
-    ok = mma_step(s, phase, ok, [&] { gemm(s.tmem + 0, s.h, s.w3, N3, LH, false, true); });
+    ok = mma_step(s, phase, ok, [&] { gemm(s.tmem + 0, s.x, s.w1, LH, K1, false); });
+    hidden_epilogue_inf(s.tmem, s.b1, s.h);
+    ok = mma_step(s, phase, ok, [&] { gemm(s.tmem + 0, s.h, s.w2, LH, LH, false); });
+    hidden_epilogue_inf(s.tmem, s.b2, s.h);
+    ok = mma_step(s, phase, ok, [&] { gemm(s.tmem + 0, s.h, s.w3, N3, LH, false); });
     float v[16];
     tmem_ld16(tmem_addr(s.tmem, warp, 0), v);
-    y0 = v[0] + s.b3[0];
-    y1 = v[1] + s.b3[1];
+#pragma unroll
+    for (int o = 0; o < LO; o++) y[o] = v[o] + s.b3[o];
     return ok;
 }
 
@@ -312,7 +307,7 @@ __global__ void __launch_bounds__(MT)
 mlp_forward_kernel(const float* __restrict__ W, const float* __restrict__ X, int n, float* __restrict__ Y, int* err) {
     extern __shared__ __align__(1024) uint8_t fwd_smem_raw[];
     InfSmem& s = *reinterpret_cast<InfSmem*>(fwd_smem_raw);
-    stage_forward_f16(s, W);
+    stage_forward(s, W);
     net_setup(s, INF_COLS);
     uint32_t phase = 0;
     bool ok = true;
@@ -322,56 +317,202 @@ mlp_forward_kernel(const float* __restrict__ W, const float* __restrict__ X, int
         float f[16];
 #pragma unroll
         for (int k = 0; k < 16; k++) f[k] = (i < n && k < LF) ? X[(size_t)i * LF + k] : 0.f;
+        normalise(s, f);
         f[LF] = 1.f;
-        stage_x_f16(s, f);
-        float y0, y1;
-        ok = tile_forward(s, phase, ok, y0, y1);
-        if (ok && i < n) { Y[(size_t)i * 2] = y0; Y[(size_t)i * 2 + 1] = y1; }
+        stage_x(s, f);
+        float y[LO];
+        ok = tile_forward(s, phase, ok, y);
+        if (ok && i < n)
+#pragma unroll
+            for (int o = 0; o < LO; o++) Y[(size_t)i * LO + o] = y[o];
     }
     net_teardown(s, ok, phase, err, INF_COLS);
 }
 
+// ---- the correction inside the force pass -------------------------------------------
+// Phase A (learn_expand_kernel) streams over the records of all groups in
+// group order: thread t of a tile forms the features of record t, the tensor
+// cores run the network on the tile, and thread t writes the record's
+// expansions (the analytic term unless the record takes it per target, plus
+// the network residual; learn.cuh) and its flags.  Several CTAs per SM hide
+// the MMA waits of one another.  Phase B (learn_apply_kernel) gives each
+// group to one warp, lane l its target l: the warp runs through the group's
+// records in order, and every accepting lane adds V + J (x - g), the exact
+// analytic term for wide groups, and the Yukawa swap near the cutoff.  A warp
+// owns its targets' forces, so the result does not depend on timing.
+constexpr int EXP_FLOATS = 12;     // Gm.v, Gm.j, Ec.v, Ec.j
+
+// Largest g with off[g] <= e (off: exclusive prefix of the groups' counts).
+__device__ __forceinline__ int group_of(const int* __restrict__ off, int ngroups, int e) {
+    int lo = 0, hi = ngroups - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= e) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <bool EXT>
 __global__ void __launch_bounds__(MT)
-mlp_correct_kernel(DevParams P, DevState S, TreeBufs T, const float* __restrict__ W, const LearnPair* __restrict__ pairs,
-                   int np, int* err) {
-    extern __shared__ __align__(1024) uint8_t cor_smem_raw[];
-    InfSmem& s = *reinterpret_cast<InfSmem*>(cor_smem_raw);
-    stage_forward_f16(s, W);
+learn_expand_kernel(DevParams P, TreeBufs T, const float* __restrict__ W, const uint2* __restrict__ recs,
+                    const float4* __restrict__ gcen, int rec_cap, const int* __restrict__ off, int ngroups, int total,
+                    const float* __restrict__ yext, float4* __restrict__ expo, uint32_t* __restrict__ flags, int* err) {
+    extern __shared__ __align__(1024) uint8_t le_smem_raw[];
+    InfSmem& s = *reinterpret_cast<InfSmem*>(le_smem_raw);
+    if (!EXT) stage_forward(s, W);
     net_setup(s, INF_COLS);
     uint32_t phase = 0;
     bool ok = true;
-    const int ntiles = (np + MT - 1) / MT;
+    const int tid = threadIdx.x;
+    const int ntiles = (total + MT - 1) / MT;
     for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int e = tile * MT + threadIdx.x;
+        const int e = tile * MT + tid;
+        const bool live = e < total;
+        RecGeo R;
         float f[16];
 #pragma unroll
-        for (int k = 0; k < 16; k++) f[k] = 0.f;
-        float scale = 0.f;
-        int target = -1;
-        if (e < np) {
-            const LearnPair pr = pairs[e];
-            target = pr.target;
-            const float4 p = S.pos[pr.target];
-            const float2 pl = S.pos_lo[pr.target];
-            const float4 a = T.int_a[pr.node], c = T.int_c[pr.node];
-            float dx, dy;
-            displacement(P, p.x, p.y, a.x, c.x - pl.x, a.y, c.y - pl.y, dx, dy);
-            float fc[LF], sc;
-            pair_features(P, dx, dy, sqrtf(c.z), a.z, a.w, T.int_m1[pr.node], T.int_m2[pr.node], T.int_m3[pr.node],
-                          f, fc, scale, sc);
-            scale *= p.z;                                     // target mass
+        for (int c = 0; c < 16; c++) f[c] = 0.f;
+        uint32_t fl = 0;
+        if (live) {
+            const int g = group_of(off, ngroups, e);
+            const uint2 rc = recs[(size_t)g * rec_cap + (e - off[g])];
+            const float4 gc = gcen[g];
+            record_geo(P, T, (int)rc.x, gc.x, gc.y, R, f);
+            fl = record_flags(P, R, gc.z);
         }
-        f[LF] = 1.f;
-        stage_x_f16(s, f);
-        float y0, y1;
-        ok = tile_forward(s, phase, ok, y0, y1);
-        if (ok && target >= 0) {
-            float* fp = reinterpret_cast<float*>(&S.force[target]);
-            atomicAdd(fp, scale * y0);
-            atomicAdd(fp + 1, scale * y1);
+        float y[LO];
+        if (EXT) {
+#pragma unroll
+            for (int o = 0; o < LO; o++) y[o] = live ? yext[(size_t)e * LO + o] : 0.f;
+        } else {
+            normalise(s, f);
+            f[LF] = 1.f;
+            stage_x(s, f);
+            ok = tile_forward(s, phase, ok, y);
+        }
+        if (live && ok) {
+            // wide groups: no expansion at all (phase B takes the analytic term per target)
+            const bool wide = (fl & REC_EXACT) != 0;
+            Lin Gm, Ec;
+            record_expansion(P, R, wide ? nullptr : y, wide, Gm, Ec);
+            float4* o = expo + (size_t)e * (EXP_FLOATS / 4);
+            o[0] = make_float4(Gm.v[0], Gm.v[1], Gm.j[0], Gm.j[1]);
+            o[1] = make_float4(Gm.j[2], Gm.j[3], Ec.v[0], Ec.v[1]);
+            o[2] = make_float4(Ec.j[0], Ec.j[1], Ec.j[2], Ec.j[3]);
+            flags[e] = fl;
         }
     }
     net_teardown(s, ok, phase, err, INF_COLS);
+}
+
+__device__ __forceinline__ void yuk_unit_field(const DevParams& P, float rx, float ry, float& gx, float& gy) {
+    const float rSq = __fmaf_rn(rx, rx, ry * ry) + P.softSq;
+    const float invR = rsqrtf(rSq);
+    const float r = rSq * invR;
+    const float f = YUKAWA_COUPLING * __expf(-P.yukMu * r) * (invR * invR + P.yukMu * invR) * invR;
+    gx = rx * f;
+    gy = ry * f;
+}
+
+// The walk's own Yukawa decision for an aggregate source (force.cu
+// yukawa_in): FP32 test, re-done in FP64 inside the guard band.
+__device__ __forceinline__ bool walk_yukawa_in(const DevParams& P, float rx, float ry, float sx, float sxl, float sy,
+                                               float syl, double tx, double ty) {
+    const float rr = __fmaf_rn(rx, rx, ry * ry);
+    const float cut = P.yukCutSq;
+    if (fabsf(rr - cut) > 1e-6f * cut) return rr < cut;
+    const double dx = ((double)sx + (double)sxl) - tx, dy = ((double)sy + (double)syl) - ty;
+    return dx * dx + dy * dy < P.yukCutSqD;
+}
+
+constexpr int LA_THREADS = 256;
+constexpr int LA_WARPS = LA_THREADS / 32;
+
+// Phase B.  A warp stages 32 of its group's records at a time in shared
+// memory (record r by lane r: coalesced loads, all in flight together), then
+// every lane reads them back in order as broadcasts.
+__global__ void __launch_bounds__(LA_THREADS)
+learn_apply_kernel(DevParams P, DevState S, TreeBufs T, const FrameCtl* __restrict__ ctl, const uint2* __restrict__ recs,
+                   const int* __restrict__ rec_cnt, const float4* __restrict__ gcen, int rec_cap, const int* __restrict__ off,
+                   const float4* __restrict__ expo, const uint32_t* __restrict__ flags) {
+    __shared__ float4 st[LA_WARPS][32][4];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int n = ctl->n;
+    const int ngroups = (n + 31) / 32;
+    for (int g = blockIdx.x * LA_WARPS + w; g < ngroups; g += gridDim.x * LA_WARPS) {
+        const int k = g * 32 + lane;
+        int ti = k < n ? T.tgt[k] : -1;
+        if (ti >= n) ti = -1;
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 pl = make_float2(0.f, 0.f);
+        if (ti >= 0) { p = S.pos[ti]; pl = S.pos_lo[ti]; }
+        const float4 gc = gcen[g];
+        const float ox = __fadd_rn(__fsub_rn(p.x, gc.x), pl.x), oy = __fadd_rn(__fsub_rn(p.y, gc.y), pl.y);
+        const double txd = (double)p.x + (double)pl.x, tyd = (double)p.y + (double)pl.y;
+        const unsigned bit = ti >= 0 ? (1u << lane) : 0u;
+        float G0 = 0.f, G1 = 0.f, E0 = 0.f, E1 = 0.f;
+        const int cnt = min(rec_cnt[g], rec_cap);
+        const int base = off[g];
+        for (int c0 = 0; c0 < cnt; c0 += 32) {
+            const int r = c0 + lane;
+            if (r < cnt) {
+                const uint2 rc = recs[(size_t)g * rec_cap + r];
+                const float4* o = expo + (size_t)(base + r) * (EXP_FLOATS / 4);
+                st[w][lane][0] = o[0];
+                st[w][lane][1] = o[1];
+                st[w][lane][2] = o[2];
+                st[w][lane][3] = make_float4(__uint_as_float(rc.y), __uint_as_float(flags[base + r]), __int_as_float((int)rc.x), 0.f);
+            }
+            __syncwarp();
+            const int m = min(32, cnt - c0);
+            for (int j = 0; j < m; j++) {
+                const float4 meta = st[w][j][3];
+                if (!(__float_as_uint(meta.x) & bit)) continue;
+                const float4 a0 = st[w][j][0], a1 = st[w][j][1], a2 = st[w][j][2];
+                G0 += a0.x + a0.z * ox + a0.w * oy;
+                G1 += a0.y + a1.x * ox + a1.y * oy;
+                E0 += a1.z + a2.x * ox + a2.y * oy;
+                E1 += a1.w + a2.z * ox + a2.w * oy;
+                const uint32_t fl = __float_as_uint(meta.y);
+                if (fl) {
+                    const int node = __float_as_int(meta.z);
+                    const float4 na = T.int_a[node], nc = T.int_c[node];
+                    const float rx = __fadd_rn(__fsub_rn(na.x, p.x), nc.x - pl.x);
+                    const float ry = __fadd_rn(__fsub_rn(na.y, p.y), nc.y - pl.y);
+                    if (fl & REC_EXACT) {
+                        // wide group: the analytic term at this target with its own
+                        // Yukawa decision (the one its monopole took), no network
+                        const float4 m1 = T.int_m1[node], m2 = T.int_m2[node];
+                        RecGeo R;
+                        R.ixx = m1.x; R.ixy = m1.y; R.iyy = m1.z; R.Dx = m2.x; R.Dy = m2.y;
+                        R.yg = P.yukOn && walk_yukawa_in(P, rx, ry, na.x, nc.x, na.y, nc.y, txd, tyd);
+                        float gx, gy, ex, ey;
+                        analytic_at(P, R, rx, ry, gx, gy, ex, ey);
+                        G0 += gx; G1 += gy; E0 += ex; E1 += ey;
+                    } else if (fl & REC_NEAR_CUT) {
+                        // the group's Yukawa decision, formed as record_geo forms it
+                        const float gdx = __fadd_rn(__fsub_rn(na.x, gc.x), nc.x), gdy = __fadd_rn(__fsub_rn(na.y, gc.y), nc.y);
+                        const bool yg = P.yukOn && gdx * gdx + gdy * gdy < P.yukCutSq;
+                        const bool own = walk_yukawa_in(P, rx, ry, na.x, nc.x, na.y, nc.y, txd, tyd);
+                        if (own != yg) {
+                            float yx, yy;
+                            yuk_unit_field(P, rx, ry, yx, yy);
+                            const float sg = own ? -na.z : na.z;
+                            G0 += sg * yx;
+                            G1 += sg * yy;
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        if (ti >= 0) {
+            float4 F = S.force[ti];
+            F.x += p.z * G0 + p.w * E0;
+            F.y += p.z * G1 + p.w * E1;
+            S.force[ti] = F;
+        }
+    }
 }
 
 // SplitMix64 finaliser (Steele, Lea, Flood 2014) of a (seed, step, j) counter,
@@ -411,14 +552,17 @@ mlp_train_kernel(const float* __restrict__ W, const float* __restrict__ X, const
         float x[16];
 #pragma unroll
         for (int k = 0; k < 16; k++) x[k] = 0.f;
-        float t0 = 0.f, t1 = 0.f, w = 0.f;
+        float tg[LT], w = 0.f;
+#pragma unroll
+        for (int k = 0; k < LT; k++) tg[k] = 0.f;
         if (smp >= 0) {
 #pragma unroll
             for (int k = 0; k < LF; k++) x[k] = X[(size_t)smp * LF + k];
-            t0 = Tg[(size_t)smp * 2];
-            t1 = Tg[(size_t)smp * 2 + 1];
+#pragma unroll
+            for (int k = 0; k < LT; k++) tg[k] = Tg[(size_t)smp * LT + k];
             w = wt ? wt[smp] : 1.f;
         }
+        normalise(f, x);
         x[LF] = 1.f;
         stage_x(f, x);
 #pragma unroll
@@ -432,18 +576,29 @@ mlp_train_kernel(const float* __restrict__ W, const float* __restrict__ X, const
         {
             float v[16];
             tmem_ld16(tmem_addr(f.tmem, warp, TC_Y), v);
-            const float e0 = v[0] + f.b3[0] - t0, e1 = v[1] + f.b3[1] - t1;
-            lsum += w * (e0 * e0 + e1 * e1);
+            // per component c: e = y_c - y*_c, loss e^T A_c e, gradient 2 A_c e
             const float g = 2.f * w * invB;
             float d[16];
 #pragma unroll
             for (int k = 0; k < 16; k++) d[k] = 0.f;
-            d[0] = g * e0;
-            d[1] = g * e1;
+#pragma unroll
+            for (int c = 0; c < 2; c++) {
+                const float e0 = v[3 * c] + f.b3[3 * c] - tg[3 * c];
+                const float e1 = v[3 * c + 1] + f.b3[3 * c + 1] - tg[3 * c + 1];
+                const float e2 = v[3 * c + 2] + f.b3[3 * c + 2] - tg[3 * c + 2];
+                const float* A = tg + LO + 6 * c;           // A00 A11 A22 A01 A02 A12
+                const float a0 = A[0] * e0 + A[3] * e1 + A[4] * e2;
+                const float a1 = A[3] * e0 + A[1] * e1 + A[5] * e2;
+                const float a2 = A[4] * e0 + A[5] * e1 + A[2] * e2;
+                lsum += w * (e0 * a0 + e1 * a1 + e2 * a2);
+                d[3 * c] = g * a0;
+                d[3 * c + 1] = g * a1;
+                d[3 * c + 2] = g * a2;
+            }
             put8(s.dy, row, 0, N3, d);
             put8(s.dy, row, 8, N3, d + 8);
-            put_bf16(s.bgb, 0, row, MT, d[0]);
-            put_bf16(s.bgb, 1, row, MT, d[1]);
+#pragma unroll
+            for (int o = 0; o < LO; o++) put_bf16(s.bgb, o, row, MT, d[o]);
         }
         // backward through layer 3 and the second GELU
         ok = mma_step(f, phase, ok, [&] { gemm(f.tmem + TC_DH2, s.dy, s.w3t, LH, N3, false); });
@@ -484,6 +639,7 @@ mlp_train_kernel(const float* __restrict__ W, const float* __restrict__ X, const
     __syncthreads();
     if (row == 0) loss_part[blockIdx.x] = ok ? (double)(f.red[0] + f.red[1] + f.red[2] + f.red[3]) * (double)invB : 0.0;
     // gradients: TMEM lane r holds row r of GA and of GB
+    for (int i = row; i < OFF_W1; i += MT) grad[i] = 0.f;      // the normalisation is not trained
     if (!ok || first) {
         for (int i = row; i < MLP_NPARAM; i += MT) grad[i] = 0.f;
     } else {
@@ -513,11 +669,11 @@ mlp_train_kernel(const float* __restrict__ W, const float* __restrict__ X, const
             float v[16];
             tmem_ld16(tmem_addr(f.tmem, warp, TC_GB), v);
             if (top) {
-                grad[OFF_W3 + row] = v[0];
-                grad[OFF_W3 + LH + row] = v[1];
+#pragma unroll
+                for (int o = 0; o < LO; o++) grad[OFF_W3 + o * LH + row] = v[o];
             } else if (row == LH) {
-                grad[OFF_B3] = v[0];
-                grad[OFF_B3 + 1] = v[1];
+#pragma unroll
+                for (int o = 0; o < LO; o++) grad[OFF_B3 + o] = v[o];
             }
         }
     }
@@ -591,14 +747,25 @@ void mlp_forward(const float* W, const float* X, int n, float* Y, int* err, cuda
     lc.add(1);
 }
 
-void mlp_correct(const DevParams& P, const DevState& S, const TreeBufs& T, const float* W, const LearnPair* pairs,
-                 int npairs, int* err, cudaStream_t st, LaunchCounter& lc) {
-    static bool attr = false;
-    allow_smem(mlp_correct_kernel, NET_SMEM, attr);
-    if (npairs <= 0) return;
-    const int tiles = (npairs + MT - 1) / MT;
-    const int blocks = std::max(1, std::min(tiles, sm_count() * 6));
-    mlp_correct_kernel<<<blocks, MT, NET_SMEM, st>>>(P, S, T, W, pairs, npairs, err);
+void learn_correct(const DevParams& P, const DevState& S, const TreeBufs& T, const FrameCtl* ctl, const float* W,
+                   const uint2* recs, const int* rec_cnt, const float4* gcen, int rec_cap, int ngroups, const int* off,
+                   int total, const float* yext, float4* expo, uint32_t* flags, int* err, cudaStream_t st,
+                   LaunchCounter& lc) {
+    static bool a0 = false, a1 = false;
+    allow_smem(learn_expand_kernel<false>, NET_SMEM, a0);
+    allow_smem(learn_expand_kernel<true>, NET_SMEM, a1);
+    if (ngroups <= 0) return;
+    if (total > 0) {
+        const int tiles = (total + MT - 1) / MT;
+        const int blocks = std::max(1, std::min(tiles, sm_count() * 6));
+        if (yext) learn_expand_kernel<true><<<blocks, MT, NET_SMEM, st>>>(P, T, W, recs, gcen, rec_cap, off, ngroups, total,
+                                                                          yext, expo, flags, err);
+        else learn_expand_kernel<false><<<blocks, MT, NET_SMEM, st>>>(P, T, W, recs, gcen, rec_cap, off, ngroups, total,
+                                                                       nullptr, expo, flags, err);
+        lc.add(1);
+    }
+    const int blocks = std::max(1, std::min((ngroups + LA_WARPS - 1) / LA_WARPS, sm_count() * 8));
+    learn_apply_kernel<<<blocks, LA_THREADS, 0, st>>>(P, S, T, ctl, recs, rec_cnt, gcen, rec_cap, off, expo, flags);
     lc.add(1);
 }
 

@@ -1,9 +1,10 @@
-"""Training helpers of the learned far-field correction (host side).
+"""Training of the learned far-field correction (host side).
 
-The network, its features and its training run in libgeon_cuda.so
-(geon_learn_dataset, geon_mlp_train); this module only draws the initial
-weights and strings the calls together.  The reference has no counterpart:
-its far field is the plain monopole of src/forces.js:680-685.
+The records, the network, its gradients and Adam run in libgeon_cuda.so
+(geon_learn_dataset, geon_mlp_train); this module draws the initial weights,
+resamples the records and sets the network's input normalisation from them.
+The reference has no counterpart: its far field is the plain monopole of
+src/forces.js:680-685.
 """
 from __future__ import annotations
 
@@ -11,49 +12,73 @@ import numpy as np
 
 from . import _native as N
 
-LF, LH, LO = 9, 64, 2
+LF, LH, LO = N.LEARN_FEATURES, 64, N.LEARN_OUTPUTS
 
 
 def init_weights(seed: int = 0) -> np.ndarray:
-    """FP32 weight vector (W1 b1 W2 b2 W3 b3, W[out][in]) drawn like
-    nn.Linear's default: U(-1/sqrt(fan_in), 1/sqrt(fan_in))."""
+    """FP32 weight vector (mu isd W1 b1 W2 b2 W3 b3, W[out][in]) drawn like
+    nn.Linear's default, U(-1/sqrt(fan_in), 1/sqrt(fan_in)), with the output
+    layer scaled down so that an untrained network corrects little."""
     rng = np.random.default_rng(seed)
-    parts = []
-    for o, i in ((LH, LF), (LH, LH), (LO, LH)):
+    parts = [np.zeros(LF), np.ones(LF)]                      # identity input normalisation
+    for o, i, sc in ((LH, LF, 1.0), (LH, LH, 1.0), (LO, LH, 0.1)):
         k = 1.0 / np.sqrt(i)
-        parts.append(rng.uniform(-k, k, o * i))
-        parts.append(rng.uniform(-k, k, o))
+        parts.append(rng.uniform(-k, k, o * i) * sc)
+        parts.append(rng.uniform(-k, k, o) * sc)
     w = np.concatenate(parts).astype(np.float32)
     assert w.size == N.MLP_NPARAM
     return w
 
 
-def pair_weights(system, ds, mass) -> np.ndarray:
-    """Loss weight of each pair: its share of its particle's relative force
-    error per unit network error, (m_i * scale / |F_i|)^2, normalised to mean
-    1 (|F_i| from a Barnes-Hut force pass at the same theta).  This makes the
-    loss the mean squared relative force error the correction is judged by."""
-    system.compute_forces()
-    f = system.forces()
-    fmag = np.hypot(f["fx"], f["fy"]).astype(np.float64)
-    t = ds["target"]
-    w = (mass[t] * ds["scales"][:, 0].astype(np.float64) / np.maximum(fmag[t], 1e-30)) ** 2
-    return (w / max(w.mean(), 1e-300)).astype(np.float32)
+def form_trace(target: np.ndarray) -> np.ndarray:
+    """Trace of a record's two quadratic forms: its weight in the loss."""
+    t = np.asarray(target, dtype=np.float64)
+    return t[:, LO + 0] + t[:, LO + 1] + t[:, LO + 2] + t[:, LO + 6] + t[:, LO + 7] + t[:, LO + 8]
 
 
-def train_correction(system, targets, steps: int = 20000, batch: int = 65536, lr: float = 2e-3, seed: int = 3,
-                     cap: int = 60_000_000, init_seed: int = 1, mass=None) -> dict:
-    """Builds the residual dataset of `targets` on `system` at its current
-    theta and trains the network on the device.  With `mass` (the system's
-    particle masses) the pairs are weighted by pair_weights.  Returns the
-    weights, the per-step losses and the dataset size."""
-    targets = np.asarray(targets, dtype=np.int32)
-    ds = system.learn_dataset(targets, cap)
-    while ds["count"] > cap:                 # small theta: fewer targets so that the pairs fit
-        keep = max(1, int(len(targets) * cap / ds["count"] * 0.9))
-        targets = targets[np.linspace(0, len(targets) - 1, keep).astype(np.int64)]
-        ds = system.learn_dataset(targets, cap)
-    wt = pair_weights(system, ds, np.asarray(mass, dtype=np.float64)) if mass is not None else None
-    w, hist = system.mlp_train(init_weights(init_seed), ds["feat_mass"], ds["residual"][:, 0:2], steps=steps,
-                               batch=batch, lr=lr, seed=seed, wt=wt)
-    return {"weights": w, "loss": hist, "pairs": int(ds["count"]), "targets": int(len(targets))}
+def resample(feat, target, size: int, seed: int = 0, alpha: float = 0.5):
+    """Records drawn with probability proportional to their loss weight
+    raised to alpha, each quadratic form scaled by weight^(1 - alpha) / weight
+    (normalised to mean 1): the same expected loss.  alpha = 1 gives the
+    lowest variance per sample but, because a few records near the disk
+    centre (where the net field nearly cancels) carry most of the weight,
+    draws only a few hundred distinct records; alpha < 1 keeps the data
+    diverse."""
+    tr = form_trace(target)
+    keep = tr > 0
+    feat, target, tr = feat[keep], target[keep], tr[keep]
+    pw = tr ** alpha
+    rng = np.random.default_rng(seed)
+    idx = np.sort(rng.choice(len(tr), size=int(size), p=pw / pw.sum()))
+    x = np.ascontiguousarray(feat[idx], dtype=np.float32)
+    t = np.array(target[idx], dtype=np.float64)
+    scale = tr[idx] ** (1.0 - alpha) / tr[idx]
+    scale /= np.mean(tr[idx] ** (1.0 - alpha))
+    t[:, LO:] *= scale[:, None]
+    return x, np.ascontiguousarray(t, dtype=np.float32)
+
+
+def set_normalisation(w: np.ndarray, mu: np.ndarray, sd: np.ndarray) -> np.ndarray:
+    """The weight vector with the input normalisation x' = (x - mu) / sd."""
+    w = np.array(w, dtype=np.float32, copy=True)
+    w[:LF] = mu
+    w[LF:2 * LF] = 1.0 / sd
+    return w
+
+
+def train_correction(system, steps: int = 20000, batch: int = 65536, lr: float = 2e-3, seed: int = 3,
+                     init_seed: int = 1, group_stride: int = 1, samples: int = 4_000_000, gfloor: float = 0.0,
+                     alpha: float = 0.5) -> dict:
+    """Builds the training records of `system` at its current theta, resamples
+    them and trains the network on the device.  Returns the weights (taking
+    raw features), the per-step losses and the dataset size."""
+    ds = system.learn_dataset(group_stride=group_stride, gfloor=gfloor)
+    feat, tg = ds["feat"], ds["target"]
+    x, t = resample(feat, tg, min(samples, max(len(feat), 1) * 4), seed=seed, alpha=alpha)
+    mu = x.astype(np.float64).mean(0)
+    sd = x.astype(np.float64).std(0)
+    sd = np.where(sd > 1e-6, sd, 1.0)
+    w0 = set_normalisation(init_weights(init_seed), mu, sd)
+    w, hist = system.mlp_train(w0, x, t, steps=steps, batch=batch, lr=lr, seed=seed)
+    return {"weights": w, "loss": hist, "records": int(ds["count"]),
+            "samples": int(len(x)), "groups": int((system.count() + 31) // 32 // group_stride)}

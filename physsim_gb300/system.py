@@ -126,22 +126,31 @@ class GeonSystem:
         self._ck(self.lib.geon_direct_forces(self._h, N.iptr(idx), idx.size, N.fptr(fx), N.fptr(fy)))
         return fx[:idx.size], fy[:idx.size]
 
-    def learn_dataset(self, targets, cap: int) -> dict:
-        """(cell, target) aggregate interactions of the listed targets with
-        features, exact residuals and scales (learned correction training data)."""
-        t = np.ascontiguousarray(targets, dtype=np.int32)
+    def learn_dataset(self, group_stride: int = 1, cap: int | None = None, gfloor: float = 0.0) -> dict:
+        """Training records of the learned correction at the current theta for
+        the groups 0, stride, 2 stride, ... (geon_learn_dataset): features
+        [m, 14], targets [m, 18] (y*[6], A[12]) and the group of each record.
+        With cap None the records are counted first and all returned."""
+        if cap is None:
+            cnt = C.c_int64()
+            self._ck(self.lib.geon_learn_dataset(self._h, int(group_stride), 0, float(gfloor), None, None, None,
+                                                 C.byref(cnt)))
+            cap = cnt.value
         cap = int(cap)
-        fm = np.zeros((max(cap, 1), 9), dtype=np.float32)
-        fc = np.zeros((max(cap, 1), 9), dtype=np.float32)
-        res = np.zeros((max(cap, 1), 4), dtype=np.float32)
-        sc = np.zeros((max(cap, 1), 2), dtype=np.float32)
-        pt = np.zeros(max(cap, 1), dtype=np.int32)
-        cnt = C.c_int32()
-        self._ck(self.lib.geon_learn_dataset(self._h, N.iptr(t), t.size, cap, N.fptr(fm), N.fptr(fc), N.fptr(res),
-                                             N.fptr(sc), N.iptr(pt), C.byref(cnt)))
+        feat = np.zeros((max(cap, 1), N.LEARN_FEATURES), dtype=np.float32)
+        tg = np.zeros((max(cap, 1), N.LEARN_TARGETS), dtype=np.float32)
+        grp = np.zeros(max(cap, 1), dtype=np.int32)
+        cnt = C.c_int64()
+        self._ck(self.lib.geon_learn_dataset(self._h, int(group_stride), cap, float(gfloor), N.fptr(feat), N.fptr(tg),
+                                             N.iptr(grp), C.byref(cnt)))
         m = min(cnt.value, cap)
-        return {"count": cnt.value, "feat_mass": fm[:m], "feat_charge": fc[:m], "residual": res[:m], "scales": sc[:m],
-                "target": pt[:m]}
+        return {"count": cnt.value, "feat": feat[:m], "target": tg[:m], "group": grp[:m]}
+
+    def learn_apply(self, y):
+        """Barnes-Hut force pass plus the correction with the given network
+        outputs y[m, 6] for the records of all groups (geon_learn_apply)."""
+        y = np.ascontiguousarray(y, dtype=np.float32).reshape(-1, N.LEARN_OUTPUTS)
+        self._ck(self.lib.geon_learn_apply(self._h, N.fptr(y), len(y)))
 
     def learn_set_weights(self, weights):
         """Weights of the learned correction (None clears them)."""
@@ -153,15 +162,15 @@ class GeonSystem:
 
     def mlp_forward(self, weights, x) -> np.ndarray:
         w = np.ascontiguousarray(weights, dtype=np.float32)
-        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 9)
-        y = np.zeros((max(len(x), 1), 2), dtype=np.float32)
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, N.LEARN_FEATURES)
+        y = np.zeros((max(len(x), 1), N.LEARN_OUTPUTS), dtype=np.float32)
         self._ck(self.lib.geon_mlp_forward(self._h, N.fptr(w), N.fptr(x), len(x), N.fptr(y)))
         return y[:len(x)]
 
     def mlp_grad(self, weights, x, t, wt=None) -> tuple:
         w = np.ascontiguousarray(weights, dtype=np.float32)
-        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 9)
-        t = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, 2)
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, N.LEARN_FEATURES)
+        t = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, N.LEARN_TARGETS)
         wp = None
         if wt is not None:
             wt = np.ascontiguousarray(wt, dtype=np.float32)
@@ -175,8 +184,8 @@ class GeonSystem:
     def mlp_train(self, weights, x, t, steps: int, batch: int, lr: float, seed: int = 1, wt=None) -> tuple:
         """Adam training on the device; returns (trained weights, per-step loss)."""
         w = np.array(weights, dtype=np.float32, copy=True)
-        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 9)
-        t = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, 2)
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, N.LEARN_FEATURES)
+        t = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, N.LEARN_TARGETS)
         wp = None
         if wt is not None:
             wt = np.ascontiguousarray(wt, dtype=np.float32)

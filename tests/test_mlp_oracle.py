@@ -23,13 +23,15 @@ def test_bf16_rounding_known_answers():
 def test_exact_gradient_matches_finite_differences():
     rng = np.random.default_rng(5)
     w = M.init_weights(3).astype(np.float64)
+    w[:M.LF] = rng.normal(size=M.LF) * 0.1                 # a normalisation that is not the identity
+    w[M.LF:2 * M.LF] = rng.uniform(0.5, 2.0, M.LF)
     x = rng.normal(size=(48, M.LF))
-    t = rng.normal(size=(48, M.LO)) * 0.1
+    t = M.random_targets(rng, 48)
     wt = rng.uniform(0.5, 2.0, size=48)
     g, loss = M.loss_grad(w, x, t, wt, bf16_ops=False)
     assert np.isfinite(loss) and loss > 0
-    idx = rng.choice(M.NPARAM, 60, replace=False)
-    idx = np.concatenate([idx, [M.NPARAM - 1, M.NPARAM - 2, M.LH * M.LF]])   # b3 and b1[0]
+    idx = rng.choice(np.arange(2 * M.LF, M.NPARAM), 60, replace=False)
+    idx = np.concatenate([idx, [M.NPARAM - 1, M.NPARAM - 2, 2 * M.LF + M.LH * M.LF]])   # b3 and b1[0]
     h = 1e-6
     for i in idx:
         wp, wm = w.copy(), w.copy()
@@ -45,7 +47,7 @@ def test_bf16_gradient_close_to_exact():
     rng = np.random.default_rng(6)
     w = M.init_weights(4)
     x = rng.normal(size=(512, M.LF))
-    t = rng.normal(size=(512, M.LO)) * 0.1
+    t = M.random_targets(rng, 512)
     g64, _ = M.loss_grad(w, x, t, bf16_ops=False)
     g16, _ = M.loss_grad(w, x, t, bf16_ops=True)
     cos = g64 @ g16 / np.linalg.norm(g64) / np.linalg.norm(g16)
