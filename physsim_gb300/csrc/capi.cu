@@ -157,8 +157,9 @@ struct GeonHandle {
     float4* gcen = nullptr;         // [rec_groups] group centres and radius bounds
     int* rec_off = nullptr;         // [rec_groups + 1] exclusive prefix of the counts
     void* rec_scan = nullptr;       // scan scratch of learn_record_offsets
-    float4* rec_exp = nullptr;      // per record expansions (3 float4) of the correction's phase A
-    uint32_t* rec_flags = nullptr;
+    float4* rec_exp = nullptr;      // per record output (4 float4) of the correction's phase A
+    uint2* rec_flags = nullptr;     // per record flags and cell mass
+    int* rec_net = nullptr;         // records the network applies to (+ 1 count at the end)
     long long rec_exp_cap = 0;
     LaunchCounter lc;
     std::string err;
@@ -658,9 +659,11 @@ static int ensure_rec_exp(GeonHandle* h, long long total) {
     cudaStreamSynchronize(h->st);
     if (h->rec_exp) { cudaFree(h->rec_exp); h->rec_exp = nullptr; }
     if (h->rec_flags) { cudaFree(h->rec_flags); h->rec_flags = nullptr; }
+    if (h->rec_net) { cudaFree(h->rec_net); h->rec_net = nullptr; }
     h->rec_exp_cap = 0;
-    if (cudaMalloc(&h->rec_exp, (size_t)cap * 3 * sizeof(float4)) != cudaSuccess ||
-        cudaMalloc(&h->rec_flags, (size_t)cap * sizeof(uint32_t)) != cudaSuccess) {
+    if (cudaMalloc(&h->rec_exp, (size_t)cap * 4 * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&h->rec_flags, (size_t)cap * sizeof(uint2)) != cudaSuccess ||
+        cudaMalloc(&h->rec_net, (size_t)(cap + 1) * sizeof(int)) != cudaSuccess) {
         cudaGetLastError();
         return set_err(h, GEON_ERR_NOMEM, "learned-correction scratch allocation failed");
     }
@@ -676,7 +679,8 @@ static int learn_correct_records(GeonHandle* h, const float* yext) {
     if (r) return r;
     learn_record_offsets(h->rec_cnt, h->rec_cap, ngroups, 1, h->rec_off, h->rec_off + ngroups, h->rec_scan, h->st, h->lc);
     learn_correct(h->P, h->S, h->T, h->ctl, h->learn_w, h->recs, h->rec_cnt, h->gcen, h->rec_cap, ngroups, h->rec_off,
-                  (int)h->rec_total_h, yext, h->rec_exp, h->rec_flags, &h->ctl->err, h->st, h->lc);
+                  (int)h->rec_total_h, yext, h->rec_exp, h->rec_flags, h->rec_net, h->rec_net + h->rec_exp_cap,
+                  &h->ctl->err, h->st, h->lc);
     return GEON_OK;
 }
 
@@ -983,6 +987,7 @@ int geon_destroy(GeonHandle* h) {
     if (h->rec_scan) cudaFree(h->rec_scan);
     if (h->rec_exp) cudaFree(h->rec_exp);
     if (h->rec_flags) cudaFree(h->rec_flags);
+    if (h->rec_net) cudaFree(h->rec_net);
     if (h->rec_cnt) cudaFree(h->rec_cnt);
     if (h->dpart) cudaFree(h->dpart);
     if (h->batch) {

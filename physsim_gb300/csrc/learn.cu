@@ -80,11 +80,12 @@ learn_records_kernel(DevParams P, DevState S, TreeBufs T, const FrameCtl* __rest
             RecGeo R;
             float f[LF];
             record_geo(P, T, node, gx, gy, R, f);
-            const bool exact = (record_flags(P, R, gc.z) & REC_EXACT) != 0;
+            const uint32_t rflags = record_flags(P, R, gc.z);
+            const bool exact = (rflags & REC_EXACT) != 0;
             Lin Gm, Ec;
             record_expansion(P, R, nullptr, exact, Gm, Ec);
-            if (exact) {
-                // no member sums for a record without weight (lane 0 still writes it)
+            if (!(rflags & REC_NET)) {
+                // no member sums for a record the network does not see (lane 0 still writes it, without weight)
                 if (lane == 0) {
                     float* o = target + (size_t)e * LT;
 #pragma unroll
@@ -126,8 +127,7 @@ learn_records_kernel(DevParams P, DevState S, TreeBufs T, const FrameCtl* __rest
             out_scales(R, s0, s1);
             const float eu = ox * R.ux + oy * R.uy, ev = -ox * R.uy + oy * R.ux;
             const float b0 = s0, b1 = s1 * eu, b2 = s1 * ev;
-            // wide groups do not use the network: their records carry no weight
-            const float wm = (mine && !exact) ? w : 0.f;
+            const float wm = mine ? w : 0.f;
             const float rp = resx * R.ux + resy * R.uy, rq = -resx * R.uy + resy * R.ux;
             const float A00 = warp_sum(wm * b0 * b0), A11 = warp_sum(wm * b1 * b1), A22 = warp_sum(wm * b2 * b2);
             const float A01 = warp_sum(wm * b0 * b1), A02 = warp_sum(wm * b0 * b2), A12 = warp_sum(wm * b1 * b2);

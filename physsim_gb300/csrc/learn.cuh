@@ -213,11 +213,18 @@ __device__ __forceinline__ void record_geo(const DevParams& P, const TreeBufs& T
 // tens of units), so the record takes the analytic term exactly at each
 // target, with each target's own Yukawa decision, and no network.
 constexpr float EXPAND_MAX = 0.1f;
-enum { REC_EXACT = 1u, REC_NEAR_CUT = 2u };
+enum { REC_EXACT = 1u, REC_NEAR_CUT = 2u, REC_NET = 4u };
 
 // How the correction treats a record of a group of radius bound `grad`:
-// REC_EXACT (analytic term per target) and REC_NEAR_CUT (targets may decide
-// the Yukawa range unlike the centre: |d| - grad <= r_Y <= |d| + grad).
+//   REC_EXACT     wide group: the analytic term per target, no network;
+//   REC_NEAR_CUT  targets may decide the Yukawa range unlike the centre
+//                 (|d| - grad <= r_Y <= |d| + grad): the monopole's Yukawa
+//                 term is swapped to the group's decision;
+//   REC_NET       the Yukawa cutoff can separate a member of the cell from a
+//                 target (| |d| - r_Y | <= s sqrt 2 + grad: members lie
+//                 within s sqrt 2 of the COM): the network applies.  Away
+//                 from the cutoff the analytic expansion is accurate and the
+//                 network would only add its output noise.
 __device__ __forceinline__ uint32_t record_flags(const DevParams& P, const RecGeo& R, float grad) {
     const float dn = sqrtf(R.dx * R.dx + R.dy * R.dy);
     uint32_t f = 0;
@@ -227,6 +234,7 @@ __device__ __forceinline__ uint32_t record_flags(const DevParams& P, const RecGe
     if (P.yukOn) {
         const float cut = sqrtf(P.yukCutSq);
         if ((dn - grad) <= cut * (1.f + 1e-5f) && (dn + grad) >= cut * (1.f - 1e-5f)) f |= REC_NEAR_CUT;
+        if (!(f & REC_EXACT) && fabsf(dn - cut) <= 1.4143f * R.s + grad) f |= REC_NET;
     }
     return f;
 }
@@ -260,6 +268,22 @@ __device__ __forceinline__ void out_scales(const RecGeo& R, float& s0, float& s1
     s1 = R.s > 0.f ? s0 / R.s : 0.f;
 }
 
+// Adds the network residual y[6] to the mass-field expansion about g.
+__device__ __forceinline__ void add_net_expansion(const RecGeo& R, const float* y, Lin& Gm) {
+    float s0, s1;
+    out_scales(R, s0, s1);
+    const float ux = R.ux, uy = R.uy;
+    // value s0 (y0 u + y3 u_perp); gradient s1 [(y1 u + y4 u_perp) u^T + (y2 u + y5 u_perp) u_perp^T]
+    Gm.v[0] += s0 * (y[0] * ux - y[3] * uy);
+    Gm.v[1] += s0 * (y[0] * uy + y[3] * ux);
+    const float ax = y[1] * ux - y[4] * uy, ay = y[1] * uy + y[4] * ux;   // column along u
+    const float bx = y[2] * ux - y[5] * uy, by = y[2] * uy + y[5] * ux;   // column along u_perp
+    Gm.j[0] += s1 * (ax * ux - bx * uy);
+    Gm.j[1] += s1 * (ax * uy + bx * ux);
+    Gm.j[2] += s1 * (ay * ux - by * uy);
+    Gm.j[3] += s1 * (ay * uy + by * ux);
+}
+
 // The record's mass- and charge-field expansions about g: the analytic
 // second-order term (unless `exact`: then it is added per target) plus
 // (y != null) the network residual y[6].
@@ -275,20 +299,7 @@ __device__ __forceinline__ void record_expansion(const DevParams& P, const RecGe
         if (P.toggles & GEON_COULOMB) dipole_term(R.re2, R.dx, R.dy, R.Dx, R.Dy, Ec);
         else { Ec.v[0] = Ec.v[1] = 0.f; Ec.j[0] = Ec.j[1] = Ec.j[2] = Ec.j[3] = 0.f; }
     }
-    if (y) {
-        float s0, s1;
-        out_scales(R, s0, s1);
-        const float ux = R.ux, uy = R.uy;
-        // value s0 (y0 u + y3 u_perp); gradient s1 [(y1 u + y4 u_perp) u^T + (y2 u + y5 u_perp) u_perp^T]
-        Gm.v[0] += s0 * (y[0] * ux - y[3] * uy);
-        Gm.v[1] += s0 * (y[0] * uy + y[3] * ux);
-        const float ax = y[1] * ux - y[4] * uy, ay = y[1] * uy + y[4] * ux;   // column along u
-        const float bx = y[2] * ux - y[5] * uy, by = y[2] * uy + y[5] * ux;   // column along u_perp
-        Gm.j[0] += s1 * (ax * ux - bx * uy);
-        Gm.j[1] += s1 * (ax * uy + bx * ux);
-        Gm.j[2] += s1 * (ay * ux - by * uy);
-        Gm.j[3] += s1 * (ay * uy + by * ux);
-    }
+    if (y) add_net_expansion(R, y, Gm);
 }
 
 // learn.cu

@@ -330,17 +330,24 @@ mlp_forward_kernel(const float* __restrict__ W, const float* __restrict__ X, int
 }
 
 // ---- the correction inside the force pass -------------------------------------------
-// Phase A (learn_expand_kernel) streams over the records of all groups in
-// group order: thread t of a tile forms the features of record t, the tensor
-// cores run the network on the tile, and thread t writes the record's
-// expansions (the analytic term unless the record takes it per target, plus
-// the network residual; learn.cuh) and its flags.  Several CTAs per SM hide
-// the MMA waits of one another.  Phase B (learn_apply_kernel) gives each
-// group to one warp, lane l its target l: the warp runs through the group's
-// records in order, and every accepting lane adds V + J (x - g), the exact
-// analytic term for wide groups, and the Yukawa swap near the cutoff.  A warp
-// owns its targets' forces, so the result does not depend on timing.
-constexpr int EXP_FLOATS = 12;     // Gm.v, Gm.j, Ec.v, Ec.j
+// Phase A1 (learn_geo_kernel) streams over the records of all groups in
+// group order and writes each record's flags and analytic expansion
+// (learn.cuh), listing the records near the Yukawa cutoff that the network
+// applies to.  Phase A2 (learn_net_kernel) runs the network on that list in
+// tiles of 128 on the tensor cores (several CTAs per SM hide one another's
+// MMA waits) and adds its residual to the records' expansions.  Phase B
+// (learn_apply_kernel) gives each group to one warp, lane l its target l:
+// the warp runs through the group's records in order, and every accepting
+// lane adds V + J (x - g), the exact analytic term for wide groups, and the
+// Yukawa swap near the cutoff.  A warp owns its targets' forces, so the
+// result does not depend on timing.
+// Record layout of phase A's output, 4 float4:
+//   compact group: Gm.v, Gm.j, Ec.v, Ec.j (12 floats), then the COM as
+//                  (hi x, hi y, lo x, lo y);
+//   wide group:    (M, Ixx, Ixy, Iyy), (Dx, Dy, -, -), -, then the COM;
+// plus the cell mass for the Yukawa swap and the flags (uint32, mass as a
+// float in the upper word of a uint2).
+constexpr int EXP_FLOATS = 16;
 
 // Largest g with off[g] <= e (off: exclusive prefix of the groups' counts).
 __device__ __forceinline__ int group_of(const int* __restrict__ off, int ngroups, int e) {
@@ -352,33 +359,91 @@ __device__ __forceinline__ int group_of(const int* __restrict__ off, int ngroups
     return lo;
 }
 
-template <bool EXT>
-__global__ void __launch_bounds__(MT)
-learn_expand_kernel(DevParams P, TreeBufs T, const float* __restrict__ W, const uint2* __restrict__ recs,
-                    const float4* __restrict__ gcen, int rec_cap, const int* __restrict__ off, int ngroups, int total,
-                    const float* __restrict__ yext, float4* __restrict__ expo, uint32_t* __restrict__ flags, int* err) {
-    extern __shared__ __align__(1024) uint8_t le_smem_raw[];
-    InfSmem& s = *reinterpret_cast<InfSmem*>(le_smem_raw);
-    if (!EXT) stage_forward(s, W);
-    net_setup(s, INF_COLS);
-    uint32_t phase = 0;
-    bool ok = true;
-    const int tid = threadIdx.x;
-    const int ntiles = (total + MT - 1) / MT;
-    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int e = tile * MT + tid;
+// Phase A1: every record's geometry, flags and analytic expansion; the
+// records the network applies to (REC_NET) are listed in net_list (in no
+// fixed order: each list entry only adds to its own record, so the result
+// does not depend on it).
+constexpr int LG_THREADS = 256;
+__global__ void __launch_bounds__(LG_THREADS)
+learn_geo_kernel(DevParams P, TreeBufs T, const uint2* __restrict__ recs, const float4* __restrict__ gcen, int rec_cap,
+                 const int* __restrict__ off, int ngroups, int total, float4* __restrict__ expo, uint2* __restrict__ flags,
+                 int* __restrict__ net_list, int* __restrict__ net_count) {
+    const int lane = threadIdx.x & 31;
+    const int nround = (total + LG_THREADS - 1) / LG_THREADS * LG_THREADS;
+    for (int e = blockIdx.x * LG_THREADS + threadIdx.x; e < nround; e += gridDim.x * LG_THREADS) {
         const bool live = e < total;
-        RecGeo R;
-        float f[16];
-#pragma unroll
-        for (int c = 0; c < 16; c++) f[c] = 0.f;
         uint32_t fl = 0;
         if (live) {
             const int g = group_of(off, ngroups, e);
             const uint2 rc = recs[(size_t)g * rec_cap + (e - off[g])];
             const float4 gc = gcen[g];
+            RecGeo R;
+            float f[LF];
             record_geo(P, T, (int)rc.x, gc.x, gc.y, R, f);
             fl = record_flags(P, R, gc.z);
+            float4* o = expo + (size_t)e * (EXP_FLOATS / 4);
+            if (fl & REC_EXACT) {
+                // wide groups: no expansion (phase B takes the analytic term per target)
+                o[0] = make_float4(R.M, R.ixx, R.ixy, R.iyy);
+                o[1] = make_float4(R.Dx, R.Dy, 0.f, 0.f);
+            } else {
+                Lin Gm, Ec;
+                record_expansion(P, R, nullptr, false, Gm, Ec);
+                o[0] = make_float4(Gm.v[0], Gm.v[1], Gm.j[0], Gm.j[1]);
+                o[1] = make_float4(Gm.j[2], Gm.j[3], Ec.v[0], Ec.v[1]);
+                o[2] = make_float4(Ec.j[0], Ec.j[1], Ec.j[2], Ec.j[3]);
+            }
+            if (fl & (REC_EXACT | REC_NEAR_CUT)) {
+                const float4 na = T.int_a[rc.x], nc = T.int_c[rc.x];
+                o[3] = make_float4(na.x, na.y, nc.x, nc.y);
+            }
+            flags[e] = make_uint2(fl, __float_as_uint(R.M));
+        }
+        const bool net = live && (fl & REC_NET);
+        const unsigned bal = __ballot_sync(0xffffffffu, net);
+        if (bal) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(net_count, __popc(bal));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (net) net_list[base + __popc(bal & lanemask_lt())] = e;
+        }
+    }
+}
+
+// Phase A2: the network on the listed records, in tiles of 128 (thread t of
+// a tile forms the features of its record, the tensor cores run the tile),
+// its residual added to the record's mass-field expansion.  With EXT the
+// outputs come from yext[e * 6 ...] instead.
+template <bool EXT>
+__global__ void __launch_bounds__(MT)
+learn_net_kernel(DevParams P, TreeBufs T, const float* __restrict__ W, const uint2* __restrict__ recs,
+                 const float4* __restrict__ gcen, int rec_cap, const int* __restrict__ off, int ngroups,
+                 const int* __restrict__ net_list, const int* __restrict__ net_count, const float* __restrict__ yext,
+                 float4* __restrict__ expo, int* err) {
+    extern __shared__ __align__(1024) uint8_t ln_smem_raw[];
+    InfSmem& s = *reinterpret_cast<InfSmem*>(ln_smem_raw);
+    const int cnt = *net_count;
+    const int ntiles = (cnt + MT - 1) / MT;
+    if ((int)blockIdx.x >= ntiles) return;                 // uniform: no TMEM taken
+    if (!EXT) stage_forward(s, W);
+    net_setup(s, INF_COLS);
+    uint32_t phase = 0;
+    bool ok = true;
+    const int tid = threadIdx.x;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int i = tile * MT + tid;
+        const bool live = i < cnt;
+        RecGeo R;
+        float f[16];
+#pragma unroll
+        for (int c = 0; c < 16; c++) f[c] = 0.f;
+        int e = 0;
+        if (live) {
+            e = net_list[i];
+            const int g = group_of(off, ngroups, e);
+            const uint2 rc = recs[(size_t)g * rec_cap + (e - off[g])];
+            const float4 gc = gcen[g];
+            record_geo(P, T, (int)rc.x, gc.x, gc.y, R, f);
         }
         float y[LO];
         if (EXT) {
@@ -391,15 +456,12 @@ learn_expand_kernel(DevParams P, TreeBufs T, const float* __restrict__ W, const 
             ok = tile_forward(s, phase, ok, y);
         }
         if (live && ok) {
-            // wide groups: no expansion at all (phase B takes the analytic term per target)
-            const bool wide = (fl & REC_EXACT) != 0;
-            Lin Gm, Ec;
-            record_expansion(P, R, wide ? nullptr : y, wide, Gm, Ec);
             float4* o = expo + (size_t)e * (EXP_FLOATS / 4);
+            const float4 a0 = o[0], a1 = o[1];
+            Lin Gm{ { a0.x, a0.y }, { a0.z, a0.w, a1.x, a1.y } };
+            add_net_expansion(R, y, Gm);
             o[0] = make_float4(Gm.v[0], Gm.v[1], Gm.j[0], Gm.j[1]);
-            o[1] = make_float4(Gm.j[2], Gm.j[3], Ec.v[0], Ec.v[1]);
-            o[2] = make_float4(Ec.j[0], Ec.j[1], Ec.j[2], Ec.j[3]);
-            flags[e] = fl;
+            o[1] = make_float4(Gm.j[2], Gm.j[3], a1.z, a1.w);
         }
     }
     net_teardown(s, ok, phase, err, INF_COLS);
@@ -430,12 +492,13 @@ constexpr int LA_WARPS = LA_THREADS / 32;
 
 // Phase B.  A warp stages 32 of its group's records at a time in shared
 // memory (record r by lane r: coalesced loads, all in flight together), then
-// every lane reads them back in order as broadcasts.
+// every lane reads them back in order as broadcasts.  Everything a record
+// needs is in its phase-A output: no tree node is read here.
 __global__ void __launch_bounds__(LA_THREADS)
 learn_apply_kernel(DevParams P, DevState S, TreeBufs T, const FrameCtl* __restrict__ ctl, const uint2* __restrict__ recs,
                    const int* __restrict__ rec_cnt, const float4* __restrict__ gcen, int rec_cap, const int* __restrict__ off,
-                   const float4* __restrict__ expo, const uint32_t* __restrict__ flags) {
-    __shared__ float4 st[LA_WARPS][32][4];
+                   const float4* __restrict__ expo, const uint2* __restrict__ flags) {
+    __shared__ float4 st[LA_WARPS][32][5];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int n = ctl->n;
     const int ngroups = (n + 31) / 32;
@@ -456,48 +519,51 @@ learn_apply_kernel(DevParams P, DevState S, TreeBufs T, const FrameCtl* __restri
         for (int c0 = 0; c0 < cnt; c0 += 32) {
             const int r = c0 + lane;
             if (r < cnt) {
-                const uint2 rc = recs[(size_t)g * rec_cap + r];
+                const uint32_t mask = recs[(size_t)g * rec_cap + r].y;
+                const uint2 fm = flags[base + r];
                 const float4* o = expo + (size_t)(base + r) * (EXP_FLOATS / 4);
                 st[w][lane][0] = o[0];
                 st[w][lane][1] = o[1];
                 st[w][lane][2] = o[2];
-                st[w][lane][3] = make_float4(__uint_as_float(rc.y), __uint_as_float(flags[base + r]), __int_as_float((int)rc.x), 0.f);
+                if (fm.x & (REC_EXACT | REC_NEAR_CUT)) st[w][lane][3] = o[3];
+                st[w][lane][4] = make_float4(__uint_as_float(mask), __uint_as_float(fm.x), __uint_as_float(fm.y), 0.f);
             }
             __syncwarp();
             const int m = min(32, cnt - c0);
             for (int j = 0; j < m; j++) {
-                const float4 meta = st[w][j][3];
+                const float4 meta = st[w][j][4];
                 if (!(__float_as_uint(meta.x) & bit)) continue;
-                const float4 a0 = st[w][j][0], a1 = st[w][j][1], a2 = st[w][j][2];
-                G0 += a0.x + a0.z * ox + a0.w * oy;
-                G1 += a0.y + a1.x * ox + a1.y * oy;
-                E0 += a1.z + a2.x * ox + a2.y * oy;
-                E1 += a1.w + a2.z * ox + a2.w * oy;
                 const uint32_t fl = __float_as_uint(meta.y);
-                if (fl) {
-                    const int node = __float_as_int(meta.z);
-                    const float4 na = T.int_a[node], nc = T.int_c[node];
-                    const float rx = __fadd_rn(__fsub_rn(na.x, p.x), nc.x - pl.x);
-                    const float ry = __fadd_rn(__fsub_rn(na.y, p.y), nc.y - pl.y);
+                const float4 a0 = st[w][j][0], a1 = st[w][j][1];
+                if (!(fl & REC_EXACT)) {
+                    const float4 a2 = st[w][j][2];
+                    G0 += a0.x + a0.z * ox + a0.w * oy;
+                    G1 += a0.y + a1.x * ox + a1.y * oy;
+                    E0 += a1.z + a2.x * ox + a2.y * oy;
+                    E1 += a1.w + a2.z * ox + a2.w * oy;
+                }
+                if (fl & (REC_EXACT | REC_NEAR_CUT)) {
+                    const float4 cm = st[w][j][3];
+                    const float rx = __fadd_rn(__fsub_rn(cm.x, p.x), cm.z - pl.x);
+                    const float ry = __fadd_rn(__fsub_rn(cm.y, p.y), cm.w - pl.y);
+                    const bool own = P.yukOn && walk_yukawa_in(P, rx, ry, cm.x, cm.z, cm.y, cm.w, txd, tyd);
                     if (fl & REC_EXACT) {
                         // wide group: the analytic term at this target with its own
                         // Yukawa decision (the one its monopole took), no network
-                        const float4 m1 = T.int_m1[node], m2 = T.int_m2[node];
                         RecGeo R;
-                        R.ixx = m1.x; R.ixy = m1.y; R.iyy = m1.z; R.Dx = m2.x; R.Dy = m2.y;
-                        R.yg = P.yukOn && walk_yukawa_in(P, rx, ry, na.x, nc.x, na.y, nc.y, txd, tyd);
+                        R.ixx = a0.y; R.ixy = a0.z; R.iyy = a0.w; R.Dx = a1.x; R.Dy = a1.y; R.yg = own;
                         float gx, gy, ex, ey;
                         analytic_at(P, R, rx, ry, gx, gy, ex, ey);
                         G0 += gx; G1 += gy; E0 += ex; E1 += ey;
-                    } else if (fl & REC_NEAR_CUT) {
-                        // the group's Yukawa decision, formed as record_geo forms it
-                        const float gdx = __fadd_rn(__fsub_rn(na.x, gc.x), nc.x), gdy = __fadd_rn(__fsub_rn(na.y, gc.y), nc.y);
+                    } else {
+                        // near the cutoff: the group's Yukawa decision, formed as record_geo forms it
+                        const float gdx = __fadd_rn(__fsub_rn(cm.x, gc.x), cm.z), gdy = __fadd_rn(__fsub_rn(cm.y, gc.y), cm.w);
                         const bool yg = P.yukOn && gdx * gdx + gdy * gdy < P.yukCutSq;
-                        const bool own = walk_yukawa_in(P, rx, ry, na.x, nc.x, na.y, nc.y, txd, tyd);
                         if (own != yg) {
                             float yx, yy;
                             yuk_unit_field(P, rx, ry, yx, yy);
-                            const float sg = own ? -na.z : na.z;
+                            const float M = meta.z;
+                            const float sg = own ? -M : M;
                             G0 += sg * yx;
                             G1 += sg * yy;
                         }
@@ -749,20 +815,25 @@ void mlp_forward(const float* W, const float* X, int n, float* Y, int* err, cuda
 
 void learn_correct(const DevParams& P, const DevState& S, const TreeBufs& T, const FrameCtl* ctl, const float* W,
                    const uint2* recs, const int* rec_cnt, const float4* gcen, int rec_cap, int ngroups, const int* off,
-                   int total, const float* yext, float4* expo, uint32_t* flags, int* err, cudaStream_t st,
-                   LaunchCounter& lc) {
+                   int total, const float* yext, float4* expo, uint2* flags, int* net_list, int* net_count, int* err,
+                   cudaStream_t st, LaunchCounter& lc) {
     static bool a0 = false, a1 = false;
-    allow_smem(learn_expand_kernel<false>, NET_SMEM, a0);
-    allow_smem(learn_expand_kernel<true>, NET_SMEM, a1);
+    allow_smem(learn_net_kernel<false>, NET_SMEM, a0);
+    allow_smem(learn_net_kernel<true>, NET_SMEM, a1);
     if (ngroups <= 0) return;
     if (total > 0) {
+        cudaMemsetAsync(net_count, 0, sizeof(int), st);
+        const int gblocks = std::max(1, std::min((total + LG_THREADS - 1) / LG_THREADS, sm_count() * 8));
+        learn_geo_kernel<<<gblocks, LG_THREADS, 0, st>>>(P, T, recs, gcen, rec_cap, off, ngroups, total, expo, flags,
+                                                         net_list, net_count);
+        // the network's CTAs: enough for every listed record (the count is read on the device)
         const int tiles = (total + MT - 1) / MT;
         const int blocks = std::max(1, std::min(tiles, sm_count() * 6));
-        if (yext) learn_expand_kernel<true><<<blocks, MT, NET_SMEM, st>>>(P, T, W, recs, gcen, rec_cap, off, ngroups, total,
-                                                                          yext, expo, flags, err);
-        else learn_expand_kernel<false><<<blocks, MT, NET_SMEM, st>>>(P, T, W, recs, gcen, rec_cap, off, ngroups, total,
-                                                                       nullptr, expo, flags, err);
-        lc.add(1);
+        if (yext) learn_net_kernel<true><<<blocks, MT, NET_SMEM, st>>>(P, T, W, recs, gcen, rec_cap, off, ngroups,
+                                                                       net_list, net_count, yext, expo, err);
+        else learn_net_kernel<false><<<blocks, MT, NET_SMEM, st>>>(P, T, W, recs, gcen, rec_cap, off, ngroups, net_list,
+                                                                    net_count, nullptr, expo, err);
+        lc.add(2);
     }
     const int blocks = std::max(1, std::min((ngroups + LA_WARPS - 1) / LA_WARPS, sm_count() * 8));
     learn_apply_kernel<<<blocks, LA_THREADS, 0, st>>>(P, S, T, ctl, recs, rec_cnt, gcen, rec_cap, off, expo, flags);

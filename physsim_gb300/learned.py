@@ -69,11 +69,16 @@ def set_normalisation(w: np.ndarray, mu: np.ndarray, sd: np.ndarray) -> np.ndarr
 def train_correction(system, steps: int = 20000, batch: int = 65536, lr: float = 2e-3, seed: int = 3,
                      init_seed: int = 1, group_stride: int = 1, samples: int = 4_000_000, gfloor: float = 0.0,
                      alpha: float = 0.5) -> dict:
-    """Builds the training records of `system` at its current theta, resamples
-    them and trains the network on the device.  Returns the weights (taking
-    raw features), the per-step losses and the dataset size."""
-    ds = system.learn_dataset(group_stride=group_stride, gfloor=gfloor)
-    feat, tg = ds["feat"], ds["target"]
+    """Builds the training records of `system` (one GeonSystem, or a list of
+    snapshots of the same distribution) at its current theta, resamples them
+    and trains the network on the device.  Returns the weights (taking raw
+    features), the per-step losses and the dataset size."""
+    systems = list(system) if isinstance(system, (list, tuple)) else [system]
+    parts = [s.learn_dataset(group_stride=group_stride, gfloor=gfloor) for s in systems]
+    feat = np.concatenate([d["feat"] for d in parts])
+    tg = np.concatenate([d["target"] for d in parts])
+    ds = {"count": sum(int(d["count"]) for d in parts)}
+    system = systems[0]
     x, t = resample(feat, tg, min(samples, max(len(feat), 1) * 4), seed=seed, alpha=alpha)
     mu = x.astype(np.float64).mean(0)
     sd = x.astype(np.float64).std(0)
@@ -81,4 +86,4 @@ def train_correction(system, steps: int = 20000, batch: int = 65536, lr: float =
     w0 = set_normalisation(init_weights(init_seed), mu, sd)
     w, hist = system.mlp_train(w0, x, t, steps=steps, batch=batch, lr=lr, seed=seed)
     return {"weights": w, "loss": hist, "records": int(ds["count"]),
-            "samples": int(len(x)), "groups": int((system.count() + 31) // 32 // group_stride)}
+            "samples": int(len(x)), "snapshots": len(systems)}
