@@ -298,9 +298,13 @@ def run_learned(args, g, wl, idx, fx, fy, stream):
     from physsim_gb300.learned import train_correction
     from physsim_gb300.system import GeonSystem
 
+    # training snapshots: the seeded N = learn_train_n disk, and the same disk
+    # after as many frames as the timed run covers (the state the error is
+    # checked on at the end has evolved that far)
     wt = W.plummer_disk(args.learn_train_n, seed=5)
     gt = GeonSystem(wt.params, wt.n)
-    gt.upload(*[wt.state[k] for k in STATE_KEYS])
+    gt2 = GeonSystem(wt.params, wt.n)
+    evolve = max(3, args.warmup) + max(1, args.steps)
     host = {k: np.ascontiguousarray(wl.state[k], dtype=np.float32) for k in STATE_KEYS}
     g.upload(*[host[k] for k in STATE_KEYS])
     sweep = {}
@@ -308,13 +312,16 @@ def run_learned(args, g, wl, idx, fx, fy, stream):
     p0 = g.params()
     zero = np.zeros(N.MLP_NPARAM, np.float32)
     for th in [float(t) for t in args.learn_thetas.split(",") if t]:
-        q = gt.params()
-        q.theta = th
-        gt.set_params(q)
-        gt.upload(*[wt.state[k] for k in STATE_KEYS])
+        for s_ in (gt, gt2):
+            q = s_.params()
+            q.theta = th
+            s_.set_params(q)
+            s_.upload(*[wt.state[k] for k in STATE_KEYS])
+        for _ in range(evolve):
+            gt2.update(wl.dt)
         t0 = time.perf_counter()
-        tr = train_correction(gt, steps=args.learn_steps, batch=args.learn_batch, group_stride=args.learn_stride,
-                              samples=args.learn_samples)
+        tr = train_correction([gt, gt2], steps=args.learn_steps, batch=args.learn_batch,
+                              group_stride=args.learn_stride, samples=args.learn_samples)
         train_s = time.perf_counter() - t0
         p = g.params()
         p.theta = th
@@ -340,6 +347,7 @@ def run_learned(args, g, wl, idx, fx, fy, stream):
                      "final_loss": float(np.mean(tr["loss"][-100:]))}
         sweep[th]["weights"] = tr["weights"]
     gt.close()
+    gt2.close()
     # candidates: the angles meeting the target with a 5 % margin on the initial
     # state, largest first (then the most accurate angle if none does); each is
     # timed over the frames and kept if the last frame's state meets the target too
@@ -390,7 +398,9 @@ def run_learned(args, g, wl, idx, fx, fy, stream):
             "profile_per_pass_ms": {"tree": pr["tree_ms"] / max(pr["tree_count"], 1),
                                     "walk": pr["force_ms"] / max(pr["force_count"], 1),
                                     "correction": pr["learn_ms"] / max(pr["learn_count"], 1)},
-            "train": {"snapshot_n": args.learn_train_n, "steps": args.learn_steps, "batch": args.learn_batch,
+            "train": {"snapshot_n": args.learn_train_n, "snapshots": "the seeded disk and the same disk after "
+                      f"{max(3, args.warmup) + max(1, args.steps)} frames", "steps": args.learn_steps,
+                      "batch": args.learn_batch,
                       "group_stride": args.learn_stride, "samples": args.learn_samples,
                       "optimizer": "Adam, cosine lr 2e-3 -> 0",
                       "kernels": "geon_learn_dataset (exact member sums) + geon_mlp_train (tcgen05 forward + backward)"},

@@ -364,48 +364,54 @@ __device__ __forceinline__ int group_of(const int* __restrict__ off, int ngroups
 // fixed order: each list entry only adds to its own record, so the result
 // does not depend on it).
 constexpr int LG_THREADS = 256;
+constexpr int LG_WARPS = LG_THREADS / 32;
 __global__ void __launch_bounds__(LG_THREADS)
-learn_geo_kernel(DevParams P, TreeBufs T, const uint2* __restrict__ recs, const float4* __restrict__ gcen, int rec_cap,
-                 const int* __restrict__ off, int ngroups, int total, float4* __restrict__ expo, uint2* __restrict__ flags,
-                 int* __restrict__ net_list, int* __restrict__ net_count) {
+learn_geo_kernel(DevParams P, TreeBufs T, const uint2* __restrict__ recs, const int* __restrict__ rec_cnt,
+                 const float4* __restrict__ gcen, int rec_cap, const int* __restrict__ off, int ngroups,
+                 float4* __restrict__ expo, uint2* __restrict__ flags, int* __restrict__ net_list, int* __restrict__ net_count) {
     const int lane = threadIdx.x & 31;
-    const int nround = (total + LG_THREADS - 1) / LG_THREADS * LG_THREADS;
-    for (int e = blockIdx.x * LG_THREADS + threadIdx.x; e < nround; e += gridDim.x * LG_THREADS) {
-        const bool live = e < total;
-        uint32_t fl = 0;
-        if (live) {
-            const int g = group_of(off, ngroups, e);
-            const uint2 rc = recs[(size_t)g * rec_cap + (e - off[g])];
-            const float4 gc = gcen[g];
-            RecGeo R;
-            float f[LF];
-            record_geo(P, T, (int)rc.x, gc.x, gc.y, R, f);
-            fl = record_flags(P, R, gc.z);
-            float4* o = expo + (size_t)e * (EXP_FLOATS / 4);
-            if (fl & REC_EXACT) {
-                // wide groups: no expansion (phase B takes the analytic term per target)
-                o[0] = make_float4(R.M, R.ixx, R.ixy, R.iyy);
-                o[1] = make_float4(R.Dx, R.Dy, 0.f, 0.f);
-            } else {
-                Lin Gm, Ec;
-                record_expansion(P, R, nullptr, false, Gm, Ec);
-                o[0] = make_float4(Gm.v[0], Gm.v[1], Gm.j[0], Gm.j[1]);
-                o[1] = make_float4(Gm.j[2], Gm.j[3], Ec.v[0], Ec.v[1]);
-                o[2] = make_float4(Ec.j[0], Ec.j[1], Ec.j[2], Ec.j[3]);
+    // one warp per group: its records r = lane, lane + 32, ...
+    for (int g = blockIdx.x * LG_WARPS + (threadIdx.x >> 5); g < ngroups; g += gridDim.x * LG_WARPS) {
+        const int cnt = min(rec_cnt[g], rec_cap);
+        const int base = off[g];
+        const float4 gc = gcen[g];
+        const int nround = (cnt + 31) & ~31;
+        for (int r = lane; r < nround; r += 32) {
+            const bool live = r < cnt;
+            const int e = base + r;
+            uint32_t fl = 0;
+            if (live) {
+                const uint2 rc = recs[(size_t)g * rec_cap + r];
+                RecGeo R;
+                float f[LF];
+                record_geo(P, T, (int)rc.x, gc.x, gc.y, R, f);
+                fl = record_flags(P, R, gc.z);
+                float4* o = expo + (size_t)e * (EXP_FLOATS / 4);
+                if (fl & REC_EXACT) {
+                    // wide groups: no expansion (phase B takes the analytic term per target)
+                    o[0] = make_float4(R.M, R.ixx, R.ixy, R.iyy);
+                    o[1] = make_float4(R.Dx, R.Dy, 0.f, 0.f);
+                } else {
+                    Lin Gm, Ec;
+                    record_expansion(P, R, nullptr, false, Gm, Ec);
+                    o[0] = make_float4(Gm.v[0], Gm.v[1], Gm.j[0], Gm.j[1]);
+                    o[1] = make_float4(Gm.j[2], Gm.j[3], Ec.v[0], Ec.v[1]);
+                    o[2] = make_float4(Ec.j[0], Ec.j[1], Ec.j[2], Ec.j[3]);
+                }
+                if (fl & (REC_EXACT | REC_NEAR_CUT)) {
+                    const float4 na = T.int_a[rc.x], nc = T.int_c[rc.x];
+                    o[3] = make_float4(na.x, na.y, nc.x, nc.y);
+                }
+                flags[e] = make_uint2(fl, __float_as_uint(R.M));
             }
-            if (fl & (REC_EXACT | REC_NEAR_CUT)) {
-                const float4 na = T.int_a[rc.x], nc = T.int_c[rc.x];
-                o[3] = make_float4(na.x, na.y, nc.x, nc.y);
+            const bool net = live && (fl & REC_NET);
+            const unsigned bal = __ballot_sync(0xffffffffu, net);
+            if (bal) {
+                int b0 = 0;
+                if (lane == 0) b0 = atomicAdd(net_count, __popc(bal));
+                b0 = __shfl_sync(0xffffffffu, b0, 0);
+                if (net) net_list[b0 + __popc(bal & lanemask_lt())] = e;
             }
-            flags[e] = make_uint2(fl, __float_as_uint(R.M));
-        }
-        const bool net = live && (fl & REC_NET);
-        const unsigned bal = __ballot_sync(0xffffffffu, net);
-        if (bal) {
-            int base = 0;
-            if (lane == 0) base = atomicAdd(net_count, __popc(bal));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (net) net_list[base + __popc(bal & lanemask_lt())] = e;
         }
     }
 }
@@ -490,10 +496,15 @@ __device__ __forceinline__ bool walk_yukawa_in(const DevParams& P, float rx, flo
 constexpr int LA_THREADS = 256;
 constexpr int LA_WARPS = LA_THREADS / 32;
 
-// Phase B.  A warp stages 32 of its group's records at a time in shared
-// memory (record r by lane r: coalesced loads, all in flight together), then
-// every lane reads them back in order as broadcasts.  Everything a record
-// needs is in its phase-A output: no tree node is read here.
+// Phase B.  One warp per group, lane l its target l.  Records every target
+// of the group accepts, and that need nothing per target, add the same
+// expansion to all of them: the lanes sum those records (lane l takes
+// records l, l + 32, ...) and a butterfly gives every lane the sums, so each
+// target adds sum V + (sum J)(x - g).  The other records (some targets only,
+// wide groups, near the cutoff) are staged 32 at a time in shared memory
+// (coalesced loads, all in flight together) and read back in order as
+// broadcasts by every lane.  Everything a record needs is in its phase-A
+// output: no tree node is read here.  The summation order is fixed.
 __global__ void __launch_bounds__(LA_THREADS)
 learn_apply_kernel(DevParams P, DevState S, TreeBufs T, const FrameCtl* __restrict__ ctl, const uint2* __restrict__ recs,
                    const int* __restrict__ rec_cnt, const float4* __restrict__ gcen, int rec_cap, const int* __restrict__ off,
@@ -513,23 +524,44 @@ learn_apply_kernel(DevParams P, DevState S, TreeBufs T, const FrameCtl* __restri
         const float ox = __fadd_rn(__fsub_rn(p.x, gc.x), pl.x), oy = __fadd_rn(__fsub_rn(p.y, gc.y), pl.y);
         const double txd = (double)p.x + (double)pl.x, tyd = (double)p.y + (double)pl.y;
         const unsigned bit = ti >= 0 ? (1u << lane) : 0u;
-        float G0 = 0.f, G1 = 0.f, E0 = 0.f, E1 = 0.f;
+        const unsigned active = __ballot_sync(0xffffffffu, ti >= 0);
         const int cnt = min(rec_cnt[g], rec_cap);
         const int base = off[g];
-        for (int c0 = 0; c0 < cnt; c0 += 32) {
+        // records shared by the whole group: lane sums, then a butterfly
+        float sv[12];
+#pragma unroll
+        for (int c = 0; c < 12; c++) sv[c] = 0.f;
+        const int nround = (cnt + 31) & ~31;
+        float G0 = 0.f, G1 = 0.f, E0 = 0.f, E1 = 0.f;
+        for (int c0 = 0; c0 < nround; c0 += 32) {
             const int r = c0 + lane;
+            uint32_t mask = 0u;
+            uint2 fm = make_uint2(0u, 0u);
+            const float4* o = expo + (size_t)(base + r) * (EXP_FLOATS / 4);
             if (r < cnt) {
-                const uint32_t mask = recs[(size_t)g * rec_cap + r].y;
-                const uint2 fm = flags[base + r];
-                const float4* o = expo + (size_t)(base + r) * (EXP_FLOATS / 4);
-                st[w][lane][0] = o[0];
-                st[w][lane][1] = o[1];
-                st[w][lane][2] = o[2];
-                if (fm.x & (REC_EXACT | REC_NEAR_CUT)) st[w][lane][3] = o[3];
-                st[w][lane][4] = make_float4(__uint_as_float(mask), __uint_as_float(fm.x), __uint_as_float(fm.y), 0.f);
+                mask = recs[(size_t)g * rec_cap + r].y;
+                fm = flags[base + r];
+            }
+            const bool shared = r < cnt && mask == active && !(fm.x & (REC_EXACT | REC_NEAR_CUT));
+            if (shared) {
+                const float4 a0 = o[0], a1 = o[1], a2 = o[2];
+                sv[0] += a0.x; sv[1] += a0.y; sv[2] += a0.z; sv[3] += a0.w;
+                sv[4] += a1.x; sv[5] += a1.y; sv[6] += a1.z; sv[7] += a1.w;
+                sv[8] += a2.x; sv[9] += a2.y; sv[10] += a2.z; sv[11] += a2.w;
+            }
+            // the rest, compacted into shared memory in record order
+            const bool own = r < cnt && !shared && mask != 0u;
+            const unsigned ob = __ballot_sync(0xffffffffu, own);
+            if (own) {
+                const int q = __popc(ob & lanemask_lt());
+                st[w][q][0] = o[0];
+                st[w][q][1] = o[1];
+                st[w][q][2] = o[2];
+                if (fm.x & (REC_EXACT | REC_NEAR_CUT)) st[w][q][3] = o[3];
+                st[w][q][4] = make_float4(__uint_as_float(mask), __uint_as_float(fm.x), __uint_as_float(fm.y), 0.f);
             }
             __syncwarp();
-            const int m = min(32, cnt - c0);
+            const int m = __popc(ob);
             for (int j = 0; j < m; j++) {
                 const float4 meta = st[w][j][4];
                 if (!(__float_as_uint(meta.x) & bit)) continue;
@@ -546,12 +578,12 @@ learn_apply_kernel(DevParams P, DevState S, TreeBufs T, const FrameCtl* __restri
                     const float4 cm = st[w][j][3];
                     const float rx = __fadd_rn(__fsub_rn(cm.x, p.x), cm.z - pl.x);
                     const float ry = __fadd_rn(__fsub_rn(cm.y, p.y), cm.w - pl.y);
-                    const bool own = P.yukOn && walk_yukawa_in(P, rx, ry, cm.x, cm.z, cm.y, cm.w, txd, tyd);
+                    const bool ownY = P.yukOn && walk_yukawa_in(P, rx, ry, cm.x, cm.z, cm.y, cm.w, txd, tyd);
                     if (fl & REC_EXACT) {
                         // wide group: the analytic term at this target with its own
                         // Yukawa decision (the one its monopole took), no network
                         RecGeo R;
-                        R.ixx = a0.y; R.ixy = a0.z; R.iyy = a0.w; R.Dx = a1.x; R.Dy = a1.y; R.yg = own;
+                        R.ixx = a0.y; R.ixy = a0.z; R.iyy = a0.w; R.Dx = a1.x; R.Dy = a1.y; R.yg = ownY;
                         float gx, gy, ex, ey;
                         analytic_at(P, R, rx, ry, gx, gy, ex, ey);
                         G0 += gx; G1 += gy; E0 += ex; E1 += ey;
@@ -559,11 +591,11 @@ learn_apply_kernel(DevParams P, DevState S, TreeBufs T, const FrameCtl* __restri
                         // near the cutoff: the group's Yukawa decision, formed as record_geo forms it
                         const float gdx = __fadd_rn(__fsub_rn(cm.x, gc.x), cm.z), gdy = __fadd_rn(__fsub_rn(cm.y, gc.y), cm.w);
                         const bool yg = P.yukOn && gdx * gdx + gdy * gdy < P.yukCutSq;
-                        if (own != yg) {
+                        if (ownY != yg) {
                             float yx, yy;
                             yuk_unit_field(P, rx, ry, yx, yy);
                             const float M = meta.z;
-                            const float sg = own ? -M : M;
+                            const float sg = ownY ? -M : M;
                             G0 += sg * yx;
                             G1 += sg * yy;
                         }
@@ -572,6 +604,14 @@ learn_apply_kernel(DevParams P, DevState S, TreeBufs T, const FrameCtl* __restri
             }
             __syncwarp();
         }
+#pragma unroll
+        for (int c = 0; c < 12; c++)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) sv[c] += __shfl_xor_sync(0xffffffffu, sv[c], o);
+        G0 += sv[0] + sv[2] * ox + sv[3] * oy;
+        G1 += sv[1] + sv[4] * ox + sv[5] * oy;
+        E0 += sv[6] + sv[8] * ox + sv[9] * oy;
+        E1 += sv[7] + sv[10] * ox + sv[11] * oy;
         if (ti >= 0) {
             float4 F = S.force[ti];
             F.x += p.z * G0 + p.w * E0;
@@ -823,8 +863,8 @@ void learn_correct(const DevParams& P, const DevState& S, const TreeBufs& T, con
     if (ngroups <= 0) return;
     if (total > 0) {
         cudaMemsetAsync(net_count, 0, sizeof(int), st);
-        const int gblocks = std::max(1, std::min((total + LG_THREADS - 1) / LG_THREADS, sm_count() * 8));
-        learn_geo_kernel<<<gblocks, LG_THREADS, 0, st>>>(P, T, recs, gcen, rec_cap, off, ngroups, total, expo, flags,
+        const int gblocks = std::max(1, std::min((ngroups + LG_WARPS - 1) / LG_WARPS, sm_count() * 8));
+        learn_geo_kernel<<<gblocks, LG_THREADS, 0, st>>>(P, T, recs, rec_cnt, gcen, rec_cap, off, ngroups, expo, flags,
                                                          net_list, net_count);
         // the network's CTAs: enough for every listed record (the count is read on the device)
         const int tiles = (total + MT - 1) / MT;
