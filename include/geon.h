@@ -15,7 +15,7 @@
  *
  * The reference (a9lim/physsim, "Geon") has no native interface; each entry
  * point below names the JavaScript method whose contract it carries.  The
- * JS-side binding a maintainer would add (N-API) is shown in INTEGRATION.md.
+ * JS side binds these entry points through a thin N-API addon.
  */
 #ifndef GEON_H
 #define GEON_H
@@ -259,13 +259,18 @@ int geon_direct_forces(GeonHandle* h, const int32_t* idx, int32_t k, float* fx, 
  * allocation (no reference counterpart: the reference's JS path has no
  * device memory to allocate).  For callers that must not call cudaMalloc /
  * cudaFree during a run: the indices and outputs are staged in a fixed
- * device array reserved when the library loads, one per device, so
+ * device array, one per device, which the device holds from the first load
+ * of the library's device code on it (its first upload or call) until the
+ * process exits, so
  *   - k is at most GEON_DIRECT_NOALLOC_MAX_K (larger k: GEON_ERR_ARG);
  *   - the first call on a device sets up the array's address; make it before
- *     any stream capture begins;
+ *     any stream capture begins; a device reset while the library is loaded
+ *     is not supported;
+ *   - the call makes the handle's device current while it runs;
  *   - no part of the array needs to start at zero;
  *   - calls that overlap in time on one device race on the array: serialise
- *     them (consecutive calls are safe; each waits for its stream). */
+ *     them (consecutive calls are safe; each waits for its stream, on error
+ *     paths too). */
 #define GEON_DIRECT_NOALLOC_MAX_K 16384
 int geon_direct_forces_noalloc(GeonHandle* h, const int32_t* idx, int32_t k, float* fx, float* fy);
 

@@ -5,7 +5,7 @@ namespace geon {
 
 static inline int grid_for(int n, int threads) {
     const int b = (n + threads - 1) / threads;
-    return b < 1 ? 1 : (b > 152 * 16 ? 152 * 16 : b);
+    return b < 1 ? 1 : (b > device_sms() * 16 ? device_sms() * 16 : b);
 }
 __device__ __forceinline__ bool on(const DevParams& P, uint32_t bit) { return (P.toggles & bit) != 0; }
 

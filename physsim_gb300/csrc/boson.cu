@@ -16,7 +16,7 @@ namespace geon {
 
 static inline int grid_for(int n, int threads) {
     const int b = (n + threads - 1) / threads;
-    return b < 1 ? 1 : (b > 152 * 16 ? 152 * 16 : b);
+    return b < 1 ? 1 : (b > device_sms() * 16 ? device_sms() * 16 : b);
 }
 
 constexpr int BOSON_STACK = 128;

@@ -497,7 +497,7 @@ __global__ void fma_peak_kernel(float* out, int iters, float a, float b) {
 
 static inline int grid_for(int n, int threads) {
     int b = (n + threads - 1) / threads;
-    return std::max(1, std::min(b, 152 * 16));
+    return std::max(1, std::min(b, device_sms() * 16));
 }
 
 static inline double bits_to_double(unsigned long long b) {
@@ -1915,8 +1915,9 @@ int geon_launch_count(GeonHandle* h, int64_t* count) {
 // them), and embeddings that fix their device-memory footprint at start-up
 // and must not meet an allocation failure in the middle of a run.  This
 // variant stages the indices and the two output rows in one fixed array in
-// device global memory, reserved when the library is loaded, and allocates
-// nothing.
+// device global memory, which the device holds from the time the library's
+// device code is first loaded on it (its first upload or call) until the
+// process exits, and allocates nothing.
 //
 // Limits and rules:
 //   * at most GEON_DIRECT_NOALLOC_MAX_K targets per call (4.2 MiB of scratch:
@@ -1926,7 +1927,11 @@ int geon_launch_count(GeonHandle* h, int64_t* count) {
 //     rejected with GEON_ERR_ARG;
 //   * the first call on a device does the setup (it looks up the array's
 //     device address with that device current and caches it per device), so
-//     make that first call before any stream capture begins;
+//     make that first call before any stream capture begins; a device reset
+//     (cudaDeviceReset) while the library is loaded is not supported, as the
+//     cached address would then be stale;
+//   * the call makes the handle's device current for its duration and
+//     restores the caller's device before it returns;
 //   * nothing in the scratch has to start at zero: each call copies its k
 //     indices in before the kernel reads them, and the kernel writes all k
 //     outputs before they are copied out;
@@ -1977,6 +1982,13 @@ extern "C" int geon_direct_forces_noalloc(GeonHandle* h, const int32_t* idx, int
     if (k == 0 || h->n == 0) return GEON_OK;
     for (int i = 0; i < k; i++)
         if (idx[i] < 0 || idx[i] >= h->n) return set_err(h, GEON_ERR_ARG, "index out of range");
+    // the handle's device current for the whole call (the plan queries it)
+    int dev = -1, cur = -1;
+    cudaError_t de = cudaStreamGetDevice(h->st, &dev);
+    if (de == cudaSuccess) de = cudaGetDevice(&cur);
+    if (de == cudaSuccess && cur != dev) de = cudaSetDevice(dev);
+    if (de != cudaSuccess) return cuda_check(h, de, "device of the handle");
+    struct Restore { int d; ~Restore() { if (d >= 0) cudaSetDevice(d); } } restore{ cur != dev ? cur : -1 };
     void* base = nullptr;
     int r = direct_scratch(h, &base);
     if (r) return r;
@@ -1997,7 +2009,11 @@ extern "C" int geon_direct_forces_noalloc(GeonHandle* h, const int32_t* idx, int
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(fx, d_fx, k * sizeof(float), cudaMemcpyDeviceToHost, h->st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(fy, d_fy, k * sizeof(float), cudaMemcpyDeviceToHost, h->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    // wait for the stream on every path once work may be queued on the shared
+    // array, so that the next call (from any handle) finds it free; report the
+    // first error
+    const cudaError_t ws = cudaStreamSynchronize(h->st);
+    if (e == cudaSuccess) e = ws;
     return cuda_check(h, e, "direct forces (no allocation)");
 }
 

@@ -816,16 +816,7 @@ __global__ void mlp_adam_kernel(float* W, float* g, float* m, float* v, float lr
 }
 
 // ---- launchers ------------------------------------------------------------------
-static int sm_count() {
-    static int n = 0;
-    if (!n) {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-        n = v > 0 ? v : 1;
-    }
-    return n;
-}
+static int sm_count() { return device_sms(); }
 
 template <class K>
 static void allow_smem(K kernel, size_t bytes, bool& done) {

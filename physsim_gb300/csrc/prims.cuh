@@ -10,6 +10,20 @@
 
 namespace geon {
 
+// Streaming multiprocessors of the current device (queried once per device).
+inline int device_sms() {
+    static int cache[64] = { 0 };
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) dev = 0;
+    if (!cache[dev]) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        cache[dev] = v > 0 ? v : 1;
+    }
+    return cache[dev];
+}
+
 // Counts kernel launches issued on behalf of a handle.
 struct LaunchCounter {
     long long n = 0;

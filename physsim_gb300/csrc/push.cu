@@ -16,7 +16,7 @@ namespace geon {
 
 static inline int grid_for(int n, int threads) {
     int b = (n + threads - 1) / threads;
-    return std::max(1, std::min(b, 152 * 16));
+    return std::max(1, std::min(b, device_sms() * 16));
 }
 
 __device__ __forceinline__ bool on(const DevParams& P, uint32_t bit) { return (P.toggles & bit) != 0; }

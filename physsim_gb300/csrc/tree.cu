@@ -550,7 +550,7 @@ __global__ void aggregate_kernel(DevParams P, DevState S, TreeBufs T, FrameCtl* 
 
 static inline int grid_for(int n, int threads) {
     int b = (n + threads - 1) / threads;
-    return std::max(1, std::min(b, 152 * 16));
+    return std::max(1, std::min(b, device_sms() * 16));
 }
 
 void tree_build(const DevParams& P, const DevState& S, TreeBufs& T, FrameCtl* ctl, int* d_root,
