@@ -69,6 +69,12 @@ def test_tree_plummer_65536(gpu_lib, oracle_mod):
     check_tree(W.plummer_disk(65536))
 
 
+def test_tree_plummer_1m(gpu_lib, oracle_mod):
+    """The benchmarked workload (config 3: N = 1,048,576 Plummer disk):
+    every point in the same leaf as the oracle's, bit for bit."""
+    check_tree(W.plummer_disk(1 << 20))
+
+
 def test_tree_edge_points(gpu_lib, oracle_mod):
     """Points on node boundaries (ties go NW), on the root box edge, and outside it."""
     p = N.make_params(domain_w=100, domain_h=100)
@@ -81,8 +87,11 @@ def test_tree_edge_points(gpu_lib, oracle_mod):
 
 
 def test_tree_coincident_points_bucket(gpu_lib, oracle_mod):
-    """Five coincident points: the reference never terminates there; the GPU
-    tree stops at level 31 with one bucket leaf and reports it."""
+    """Five exactly coincident points: the reference's insert restarts its
+    depth count with every re-inserted point (quadtree.js:211-233), so it
+    never terminates there and has no result to compare with (the oracle
+    stops at its node limit); the GPU tree stops at level 31, the depth its
+    keys resolve, with one bucket leaf and reports it."""
     from physsim_gb300.system import GeonSystem
     p = N.make_params(domain_w=100, domain_h=100)
     xs = np.array([10, 10, 10, 10, 10, 70.0])
@@ -95,6 +104,37 @@ def test_tree_coincident_points_bucket(gpu_lib, oracle_mod):
     lop, bx, by, bw, lv = g.leaves(info)
     assert len(set(lop[:5])) == 1
     g.close()
+
+
+def test_near_coincident_points_forces(gpu_lib, oracle_mod):
+    """Ten points within 2.7e-7 of one another in a 100 box: the reference
+    divides to about level 33 to separate them, the GPU keys resolve 31
+    levels and keep five or more of them in one level-31 bucket leaf, whose
+    points every target takes one by one.  The forces on all points agree
+    within the force bar."""
+    p = N.make_params(toggles=N.GRAVITY | N.COULOMB | N.BARNES_HUT, domain_w=100, domain_h=100, softening=1.0)
+    rng = np.random.default_rng(4)
+    # ten distinct FP32 values 2^-25 apart (the spacing of FP32 at 0.25): they
+    # span 2.7e-7, within two level-31 cells (1.86e-7 wide), so one of them
+    # holds at least five; the reference separates them near level 33
+    xs = np.concatenate([0.25 + np.arange(10) * 2.0 ** -25, rng.uniform(5, 95, 250)])
+    ys = np.concatenate([np.full(10, 20.0), rng.uniform(5, 95, 250)])
+    n = xs.size
+    assert np.unique(np.asarray(xs[:10], np.float32)).size == 10
+    xs, ys = (np.asarray(a, np.float32).astype(np.float64) for a in (xs, ys))
+    z = np.zeros(n)
+    q = np.asarray(rng.integers(-5, 6, n) * 0.1, np.float32).astype(np.float64)
+    wl = W.Workload("near_coincident", p, {"x": xs, "y": ys, "wx": z, "wy": z, "mass": np.ones(n), "charge": q,
+                                           "angw": z}, 1 / 60, 1)
+    g, o = load_both(wl)
+    info = g.build_tree()
+    assert info["n_bucket"] >= 1 and info["max_level"] == 31
+    g.compute_forces()
+    o.compute_forces()
+    fg, fo = g.forces(), o.forces()
+    e = vec_err(fg["fx"], fg["fy"], fo["fx"], fo["fy"])
+    g.close()
+    assert e["norm"] <= FORCE_TOL, e
 
 
 # ---- forces ---------------------------------------------------------------------------
@@ -144,6 +184,54 @@ def test_forces_full_set_torus(gpu_lib, oracle_mod, bh):
 def test_forces_full_set_torus_no_relativity(gpu_lib, oracle_mod):
     wl = _with(W.clusters_torus(4096, relativity=False), N.FLAG_PE | N.FLAG_BREAKDOWN)
     check_forces(wl, FULL_KEYS)
+
+
+def test_forces_config2_bh_65536(gpu_lib, oracle_mod):
+    """Config 2 as stated: N = 65,536 clusters in a 400 torus, gravity,
+    Coulomb, Yukawa, magnetic and gravitomagnetic dipoles, 1PN, relativity
+    with a warmed 96-sample history; Barnes-Hut theta 0.5 against the
+    oracle's full pass, every quantity within the force bar, equal
+    interaction counts."""
+    wl = _with(W.clusters_torus(65536), N.FLAG_PE | N.FLAG_BREAKDOWN)
+    hist = W.straight_line_history(wl.state, 96, 120.0, 64 / 60)
+    check_forces(wl, FULL_KEYS, history=hist)
+
+
+# velocity-dependent fields of the pairwise sum under signal delay (measured
+# at N = 65,536: Bz 3.0e-4, dBz 6e-5, Bgz 1.2e-5; forces 3.2e-7)
+DELAYED_FIELD_TOL = 1e-3
+
+
+@pytest.mark.parametrize("relativity", [True, False])
+def test_forces_config2_pairwise_65536(gpu_lib, oracle_mod, relativity):
+    """Config 2's pairwise sum at N = 65,536: the GPU's full pass against the
+    oracle's pairwise sum over all sources for 2,048 random targets.  Forces
+    and every field within the force bar without relativity.  With signal
+    delay every source is retarded, and for the far ones the light cone
+    meets the history near its ends, where the FP32 solve (segment choice,
+    extrapolation before the first sample) can land on the other side of a
+    decision than the FP64 one: forces stay within the force bar, the
+    velocity-dependent fields (Bz, Bgz and their gradients), which sum
+    large terms of both signs, within DELAYED_FIELD_TOL."""
+    wl = _with(W.clusters_torus(65536, barnes_hut=False, relativity=relativity), N.FLAG_PE | N.FLAG_BREAKDOWN)
+    hist = W.straight_line_history(wl.state, 96, 120.0, 64 / 60) if relativity else None
+    g, o = load_both(wl, history=hist)
+    g.compute_forces()
+    idx = np.sort(np.random.default_rng(8).choice(wl.n, 2048, replace=False)).astype(np.int32)
+    o.compute_forces_subset(idx)
+    fg, fo = g.forces(), o.forces()
+    e = vec_err(fg["fx"][idx], fg["fy"][idx], fo["fx"][idx], fo["fy"][idx])
+    assert e["norm"] <= FORCE_TOL, e
+    errs = {}
+    for k in FULL_KEYS:
+        if not np.any(fo[k][idx]):
+            continue
+        errs[k] = rel_err(fg[k][idx], fo[k][idx])["norm"]
+    print("config 2 pairwise (relativity %s) per-quantity errors:" % relativity, errs)
+    delayed = ("Bz", "Bgz", "dBzdx", "dBzdy", "dBgzdx", "dBgzdy")
+    for k, r in errs.items():
+        assert r <= (DELAYED_FIELD_TOL if relativity and k in delayed else FORCE_TOL), (k, r)
+    g.close()
 
 
 @pytest.mark.parametrize("topology", [N.KLEIN, N.RP2])
@@ -206,16 +294,25 @@ def test_frame_small_disk(gpu_lib, oracle_mod):
 def test_frames_small_disk_config(gpu_lib, oracle_mod):
     """The stated small config: relativity on, softening 0.1, 10 frames."""
     errs, _ = run_frames(W.small_disk(2048), 10)
-    for k in ("x", "y"):
+    print("small disk, 10 frames, per-quantity relative errors:", {k: e["norm"] for k, e in errs.items()})
+    for k in ("x", "y", "wx", "wy", "angw"):
         assert errs[k]["norm"] <= TRAJ_TOL, (k, errs[k])
-    for k in ("wx", "wy", "angw"):
-        assert errs[k]["norm"] <= 1e-4, (k, errs[k])
 
 
-def test_frame_full_set_torus(gpu_lib, oracle_mod):
-    wl = W.clusters_torus(2048)
+def test_frames_config2_16384(gpu_lib, oracle_mod):
+    """Config 2's full force set (torus, relativity with a warmed history,
+    1PN velocity-Verlet) for one frame at N = 16,384: the same substep
+    count, trajectories within the bar.  Longer runs of this configuration
+    measure its blow-up, not the arithmetic: the Yukawa coupling in clusters
+    of sigma 4 with softening 8 drives proper velocities to about 100 within
+    two frames and spins near the 0.999 clamp overflow (measured after two
+    frames: positions 2.6e-6, velocities 2e-3, spins NaN on both sides), and
+    even without relativity three frames of 4,096 particles part by 2.8e-2
+    at equal substep counts."""
+    wl = W.clusters_torus(16384)
     hist = W.straight_line_history(wl.state, 96, 120.0, 64 / 60)
     errs, _ = run_frames(wl, 1, history=hist)
+    print("config 2 (N = 16,384), 1 frame, per-quantity relative errors:", {k: e["norm"] for k, e in errs.items()})
     for k, e in errs.items():
         assert e["norm"] <= TRAJ_TOL, (k, e)
 
