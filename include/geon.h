@@ -67,6 +67,7 @@ extern "C" {
 #define GEON_FLAG_SIMPLE_WALK (1u << 3)  /* one node per warp iteration (cross-check of the batched walk) */
 #define GEON_FLAG_LEARN       (1u << 4)  /* cell moments + learned far-field correction (when weights are set) */
 #define GEON_FLAG_BOSONS      (1u << 5)  /* Physics.bosonInterEnabled: boson gravity on particles in every force pass */
+#define GEON_FLAG_SPLIT_FRAME (1u << 6)  /* geon_update launches every phase separately (cross-check of the one-launch frame) */
 
 /* Physics parameters.  Mirrors the Physics fields that Physics.update reads
  * (src/integrator.js:65-107, :726-736) plus theta/softening, which the
@@ -232,8 +233,22 @@ int geon_particle_count(GeonHandle* h, int32_t* n);
  * in-scope part: force bootstrap on the first call, adaptive Boris substeps
  * (<= max_substeps) with tree rebuild and force recompute, 1PN velocity-Verlet,
  * history sampling every 64 calls, boundary handling.  `substeps` (may be
- * NULL) receives the number of substeps taken. */
+ * NULL) receives the number of substeps taken.
+ *
+ * A single system in an open box with at most 4,096 particles, Barnes-Hut on
+ * and no dipole / 1PN terms, merge collisions, breakdown rows, energy sums,
+ * learned correction or bosons runs the whole frame (planner, substeps, tree
+ * builds, walks, history, boundary) as ONE kernel launch with a device-side
+ * planner, then reads the results back once; GEON_FLAG_SPLIT_FRAME selects
+ * the launch-per-phase path instead.  Same physics either way. */
 int geon_update(GeonHandle* h, double dt, int32_t* substeps);
+
+/* Waits of the one-launch frame: each grid-wide barrier gives up after
+ * wait_ns nanoseconds (default 1e9); the frame then returns GEON_ERR_TIMEOUT
+ * and the handle keeps the error.  extra_arrivals > 0 makes every barrier
+ * wait for that many blocks that do not exist, so the wait runs out (a test
+ * of the time-out path); 0 restores normal operation. */
+int geon_set_frame_wait(GeonHandle* h, int64_t wait_ns, int32_t extra_arrivals);
 
 /* Waits for all work enqueued on the handle's stream. */
 int geon_synchronize(GeonHandle* h);

@@ -47,6 +47,8 @@ FLAG_NO_GHOSTS = 1 << 2
 FLAG_SIMPLE_WALK = 1 << 3
 FLAG_LEARN = 1 << 4
 FLAG_BOSONS = 1 << 5
+FLAG_SPLIT_FRAME = 1 << 6
+FRAME_MAX_POINTS = 4096
 MLP_NPARAM = 5538
 LEARN_FEATURES = 14
 LEARN_OUTPUTS = 6
@@ -165,6 +167,7 @@ SIGNATURES = {
     "geon_upload_state_f64": [_handle_t, C.c_int32, _P(C.c_double), C.c_double],
     "geon_particle_count": [_handle_t, _P(C.c_int32)],
     "geon_update": [_handle_t, C.c_double, _P(C.c_int32)],
+    "geon_set_frame_wait": [_handle_t, C.c_int64, C.c_int32],
     "geon_synchronize": [_handle_t],
     "geon_compute_forces": [_handle_t],
     "geon_compute_1pn": [_handle_t],

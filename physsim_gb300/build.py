@@ -19,7 +19,7 @@ BUILD = PKG / "_build"
 LIB = LIBDIR / "libgeon_cuda.so"
 INCLUDE = PKG.parent / "include"
 
-SOURCES = ["prims.cu", "tree.cu", "force.cu", "push.cu", "learn.cu", "mlp.cu", "batch.cu", "collide.cu", "boson.cu", "capi.cu"]
+SOURCES = ["prims.cu", "tree.cu", "force.cu", "push.cu", "frame.cu", "learn.cu", "mlp.cu", "batch.cu", "collide.cu", "boson.cu", "capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

@@ -19,6 +19,7 @@
 #include "batch.cuh"
 #include "collide.cuh"
 #include "boson.cuh"
+#include "frame.cuh"
 
 using namespace geon;
 
@@ -105,6 +106,10 @@ struct GeonHandle {
     bool hist_alloc = false;
     FrameCtl* ctl = nullptr;
     FrameCtl* ctl_h = nullptr;     // pinned
+    FrameRun* frun = nullptr;      // one-launch frame: barrier state and results
+    FrameRun* frun_h = nullptr;    // pinned
+    long long frame_wait_ns = 1000000000LL;   // a frame barrier gives up after this long
+    int frame_extra = 0;           // barrier arrivals waited for beyond the grid (time-out test)
     int* d_root = nullptr;
     double* hist_t = nullptr;
     float* hist_age = nullptr;
@@ -530,7 +535,7 @@ static int read_ctl(GeonHandle* h) {
     CK(cudaStreamSynchronize(h->st));
     if (h->ctl_h->err) {
         const int e = h->ctl_h->err;
-        if (e & (ERR_MMA_TIMEOUT | ERR_AGG_TIMEOUT))
+        if (e & (ERR_MMA_TIMEOUT | ERR_AGG_TIMEOUT | ERR_FRAME_TIMEOUT))
             return set_err(h, GEON_ERR_TIMEOUT, std::string("device wait timed out, flag ") + std::to_string(e));
         return set_err(h, GEON_ERR_OVERFLOW, std::string("device overflow flag ") + std::to_string(e) +
                        ((e & ERR_NODE_OVERFLOW) ? " (node capacity)" : "") + ((e & ERR_STACK_OVERFLOW) ? " (walk stack)" : ""));
@@ -949,9 +954,14 @@ int geon_create(const GeonParams* params, int32_t max_particles, GeonHandle** ou
     h->staging = A.alloc<float>((size_t)GEON_ST_ROWS * h->n_cap);
     h->staging_d = A.alloc<double>((size_t)GEON_ST_ROWS * h->n_cap);
     h->stats_d = A.alloc<double>(16);
+    h->frun = A.alloc<FrameRun>(1);
     if (A.failed || cudaMallocHost(&h->ctl_h, sizeof(FrameCtl)) != cudaSuccess ||
-        cudaMallocHost(&h->stats_h, 16 * sizeof(double)) != cudaSuccess) {
+        cudaMallocHost(&h->stats_h, 16 * sizeof(double)) != cudaSuccess ||
+        cudaMallocHost(&h->frun_h, sizeof(FrameRun)) != cudaSuccess) {
         A.free_all();
+        if (h->ctl_h) cudaFreeHost(h->ctl_h);
+        if (h->stats_h) cudaFreeHost(h->stats_h);
+        if (h->frun_h) cudaFreeHost(h->frun_h);
         cudaStreamDestroy(h->st);
         g_err = "device allocation failed";
         delete h;
@@ -959,6 +969,7 @@ int geon_create(const GeonParams* params, int32_t max_particles, GeonHandle** ou
     }
     cudaMemsetAsync(h->ctl, 0, sizeof(FrameCtl), h->st);
     cudaMemsetAsync(h->hist_t, 0, HIST_LEN * sizeof(double), h->st);
+    cudaMemsetAsync(h->frun, 0, sizeof(FrameRun), h->st);
     r = alloc_state(h, slots_wanted(h));
     if (r) { g_err = h->err; geon_destroy(h); return r; }
     r = ensure_history(h);
@@ -1006,6 +1017,7 @@ int geon_destroy(GeonHandle* h) {
     for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
     if (h->ctl_h) cudaFreeHost(h->ctl_h);
     if (h->stats_h) cudaFreeHost(h->stats_h);
+    if (h->frun_h) cudaFreeHost(h->frun_h);
     if (h->st) cudaStreamDestroy(h->st);
     delete h;
     return GEON_OK;
@@ -1660,6 +1672,86 @@ int geon_interaction_count(GeonHandle* h, int64_t* count) {
 
 static int batch_update(GeonHandle* h, double dt, int32_t* substeps);
 
+// The whole frame in one launch (frame.cu): a single open system with forces
+// already bootstrapped, Barnes-Hut without dipole / 1PN terms, breakdown
+// rows, energy sums, merge collisions, learned correction, bosons or
+// profiling, and at most FRAME_MAX_POINTS particles.
+static bool frame_eligible(const GeonHandle* h) {
+    const uint32_t tg = h->prm.toggles, fl = h->prm.flags;
+    return !h->batch && h->forcesInit && frame_fits(h->n) && bh_on(h) && !h->P.periodic &&
+           !(tg & (GEON_MAGNETIC | GEON_GRAVITOMAG | GEON_ONE_PN)) &&
+           !(fl & (GEON_FLAG_PE | GEON_FLAG_BREAKDOWN | GEON_FLAG_SIMPLE_WALK | GEON_FLAG_LEARN | GEON_FLAG_BOSONS |
+                   GEON_FLAG_SPLIT_FRAME)) &&
+           !merge_on(h) && !h->prof;
+}
+
+// geon_update through the frame kernel: one launch, then one read of the
+// control block and the frame's results.
+static int frame_update(GeonHandle* h, double dt, int32_t* substeps) {
+    int r = ensure_tree(h);
+    if (r) return r;
+    const GeonParams& p = h->prm;
+    const uint32_t tg = p.toggles;
+    const bool rel = (tg & GEON_RELATIVITY) != 0;
+    const bool hasMag = tg & GEON_MAGNETIC, hasGM = tg & GEON_GRAVITOMAG;
+    const bool recordHist = rel && h->histStride + 1 >= HIST_STRIDE;    // integrator.js:1550-1565
+    if (rel) { r = ensure_history(h); if (r) return r; }
+    h->T.mom_on = 0;
+    h->T.skey = h->T.key_alt;                 // where the frame kernel's sort leaves the tree order
+    h->T.sidx = h->T.idx_alt;
+    FrameArgs A{};
+    A.dt = dt;
+    A.simTime = h->simTime;
+    A.softening = p.softening;
+    A.maxSub = p.max_substeps;
+    A.F.has1PN = 0;
+    A.F.needBoris = hasMag || hasGM || p.ext_bz != 0;
+    A.F.needSpinOrbit = (tg & GEON_SPIN_ORBIT) && (hasMag || hasGM);
+    A.F.needTorques = (hasGM && rel) || (tg & GEON_GRAVITY);
+    A.recordHist = recordHist ? 1 : 0;
+    A.histSlot = (int)(h->histTotal & HIST_MASK);
+    A.hist_t = h->hist_t;
+    A.hist_age = h->hist_age;
+    A.hist_segdt = h->hist_segdt;
+    A.keep = h->keep;
+    A.dst = h->dst;
+    A.slots = h->slots;
+    A.withHist = h->hist_alloc ? 1 : 0;
+    A.waitNs = h->frame_wait_ns;
+    A.extraArrivals = h->frame_extra;
+    const ForceCtx C = make_ctx(h);
+    const cudaError_t e = frame_launch(rel, h->P, h->S, h->S2, h->T, h->d_root, h->ctl, C, A, h->frun, h->n, h->st, h->lc);
+    if (e != cudaSuccess) return cuda_check(h, e, "frame kernel launch");
+    CK(cudaMemcpyAsync(h->frun_h, h->frun, sizeof(FrameRun), cudaMemcpyDeviceToHost, h->st));
+    r = read_ctl(h);
+    if (r) {
+        // a frame that gave up leaves the barrier mid-way: start the next one afresh
+        cudaMemsetAsync(h->frun, 0, sizeof(FrameRun), h->st);
+        cudaStreamSynchronize(h->st);
+        return r;
+    }
+    const FrameRun& R = *h->frun_h;
+    h->simTime = R.simTime;
+    h->lastSubsteps = R.substeps;
+    if (substeps) *substeps = R.substeps;
+    if (rel && ++h->histStride >= HIST_STRIDE) {
+        h->histStride -= HIST_STRIDE;
+        h->histTotal++;
+    }
+    if (R.removed > 0) {                      // compacted into S2 by the kernel
+        std::swap(h->S, h->S2);
+        h->n -= R.removed;
+    }
+    return GEON_OK;
+}
+
+int geon_set_frame_wait(GeonHandle* h, int64_t wait_ns, int32_t extra_arrivals) {
+    if (!h || wait_ns <= 0 || extra_arrivals < 0) return GEON_ERR_ARG;
+    h->frame_wait_ns = wait_ns;
+    h->frame_extra = extra_arrivals;
+    return GEON_OK;
+}
+
 int geon_update(GeonHandle* h, double dt, int32_t* substeps) {
     if (!h) return GEON_ERR_ARG;
     if (h->batch) return batch_update(h, dt, substeps);
@@ -1691,6 +1783,7 @@ int geon_update(GeonHandle* h, double dt, int32_t* substeps) {
         if (r) return r;
         h->forcesInit = true;
     }
+    if (frame_eligible(h)) return frame_update(h, dt, substeps);
     // frame-start planner scan (integrator.js:813-836)
     launch_frame_scan(h->P, h->S, h->ctl, h->n_cap, h->st, h->lc);
     CKL();

@@ -33,6 +33,7 @@ constexpr int ERR_NODE_OVERFLOW = 2;
 constexpr int ERR_AGG_TIMEOUT = 4;
 constexpr int ERR_BAD_INDEX = 8;        // an index failed its bounds check (access skipped)
 constexpr int ERR_MMA_TIMEOUT = 16;     // a tensor-core completion wait ran out (kernel returned early)
+constexpr int ERR_FRAME_TIMEOUT = 32;   // a grid-wide barrier of the frame kernel ran out (kernel returned early)
 
 // ---- point references: particle index + periodic image code ----------------
 // code bits: [0,1] sx+1, [2,3] sy+1, [4] mirror x (x -> W - x), [5] mirror y,

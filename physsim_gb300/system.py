@@ -109,6 +109,11 @@ class GeonSystem:
         self._ck(self.lib.geon_update(self._h, float(dt), C.byref(s)))
         return s.value
 
+    def set_frame_wait(self, wait_ns: int = 1_000_000_000, extra_arrivals: int = 0):
+        """Time limit of the one-launch frame's barriers; extra_arrivals > 0
+        makes them wait for blocks that do not exist (time-out test)."""
+        self._ck(self.lib.geon_set_frame_wait(self._h, int(wait_ns), int(extra_arrivals)))
+
     def synchronize(self):
         self._ck(self.lib.geon_synchronize(self._h))
 

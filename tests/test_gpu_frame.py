@@ -1,0 +1,139 @@
+"""The one-launch frame (frame.cu) against the launch-per-phase path and the
+oracle, through the C ABI.
+
+* small open systems run each frame as exactly one kernel launch;
+* the frame kernel and the split path (GEON_FLAG_SPLIT_FRAME) run the same
+  bodies on the same tree order: equal substep counts, ids and counts, and
+  states equal to 1e-6 relative after ten frames (relativity on and off,
+  despawn with compaction, bounce walls with external fields, the largest
+  system the kernel takes);
+* the split path itself stays within the trajectory bar of the oracle on the
+  small config, as the frame kernel does (test_gpu_parity.py);
+* a barrier that waits for a block that does not exist gives up after its
+  time limit: geon_update returns GEON_ERR_TIMEOUT, and the GPU stays usable.
+"""
+import numpy as np
+import pytest
+
+from physsim_gb300 import _native as N
+from physsim_gb300 import workloads as W
+from physsim_gb300.system import GeonSystem
+from tests.parity import STATE_KEYS, load_both, rel_err
+
+pytestmark = pytest.mark.gpu
+
+FRAME_TOL = 1e-6
+TRAJ_TOL = 1e-5          # the trajectory bar of the frame parity tests
+
+
+def make(wl, split=False):
+    g = GeonSystem(wl.params, wl.n)
+    g.upload(*[wl.state[k] for k in STATE_KEYS])
+    if split:
+        p = g.params()
+        p.flags |= N.FLAG_SPLIT_FRAME
+        g.set_params(p)
+    return g
+
+
+def run_pair(wl, frames):
+    a, b = make(wl), make(wl, split=True)
+    try:
+        for f in range(frames):
+            sa, sb = a.update(wl.dt), b.update(wl.dt)
+            assert sa == sb, ("substeps", f, sa, sb)
+        assert a.count() == b.count()
+        assert np.array_equal(a.ids(), b.ids())
+        return a.state(f64=True), b.state(f64=True), a.stats(), b.stats()
+    finally:
+        a.close()
+        b.close()
+
+
+def assert_close(sa, sb, keys=("x", "y", "wx", "wy", "angw")):
+    for k in keys:
+        e = rel_err(sa[k], sb[k])
+        assert e["norm"] <= FRAME_TOL, (k, e)
+
+
+def test_one_launch_per_frame(gpu_lib):
+    wl = W.small_disk(2048)
+    g = make(wl)
+    try:
+        g.update(wl.dt)                       # the first frame bootstraps forces on the split path
+        c0 = g.launch_count()
+        for _ in range(5):
+            g.update(wl.dt)
+        per_frame = (g.launch_count() - c0) / 5
+    finally:
+        g.close()
+    assert per_frame == 1, per_frame
+
+
+@pytest.mark.parametrize("relativity", [True, False])
+def test_frame_kernel_matches_split_path(gpu_lib, relativity):
+    wl = W.small_disk(2048, relativity=relativity, softening=0.1 if relativity else 8.0)
+    sa, sb, ta, tb = run_pair(wl, 10)
+    assert_close(sa, sb)
+    assert ta["sim_time"] == tb["sim_time"]
+
+
+def test_frame_kernel_despawn_compaction(gpu_lib):
+    wl = W.small_disk(256, relativity=True, softening=8.0)
+    wl.state["x"][[3, 100, 200]] = [170.0, -70.0, 180.0]
+    sa, sb, ta, tb = run_pair(wl, 3)
+    assert ta["alive_count"] == tb["alive_count"] == 253
+    assert_close(sa, sb)
+
+
+def test_frame_kernel_bounce_and_external_fields(gpu_lib):
+    wl = W.small_disk(512, relativity=False, softening=8.0)
+    p = wl.params
+    p.boundary_mode = N.BOUND_BOUNCE
+    p.ext_gravity, p.ext_electric, p.ext_bz = 0.3, 0.2, 0.05
+    wl.state["x"][:8] = np.linspace(0.1, 0.8, 8)
+    sa, sb, _, _ = run_pair(wl, 5)
+    assert_close(sa, sb)
+
+
+def test_frame_kernel_largest_system(gpu_lib):
+    wl = W.small_disk(N.FRAME_MAX_POINTS, relativity=True, softening=0.1)
+    sa, sb, _, _ = run_pair(wl, 4)
+    assert_close(sa, sb)
+
+
+def test_split_path_small_config_against_oracle(gpu_lib, oracle_mod):
+    wl = W.small_disk(2048)
+    g, o = load_both(wl)
+    p = g.params()
+    p.flags |= N.FLAG_SPLIT_FRAME
+    g.set_params(p)
+    try:
+        for _ in range(10):
+            assert g.update(wl.dt) == o.update(wl.dt)
+        sg, so = g.state(f64=True), o.state()
+    finally:
+        g.close()
+    for k in ("x", "y", "wx", "wy", "angw"):
+        assert rel_err(sg[k], so[k])["norm"] <= TRAJ_TOL, k
+
+
+def test_barrier_timeout_is_reported(gpu_lib):
+    wl = W.small_disk(1024)
+    g = make(wl)
+    try:
+        g.update(wl.dt)
+        g.set_frame_wait(20_000_000, extra_arrivals=1)     # 20 ms, one block that never arrives
+        with pytest.raises(N.GeonError) as ei:
+            g.update(wl.dt)
+        assert ei.value.code == N.GEON_ERR_TIMEOUT, str(ei.value)
+    finally:
+        g.close()
+    # the context is still usable: a new system runs its frames
+    h = make(wl)
+    try:
+        for _ in range(2):
+            h.update(wl.dt)
+        assert h.count() == wl.n
+    finally:
+        h.close()
