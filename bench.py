@@ -514,17 +514,32 @@ def run_configs(args, g_big, wl_big, idx, fx, fy, fp32_peak):
     from physsim_gb300 import _native as N, workloads as W
     from physsim_gb300.system import GeonSystem
     out = {}
-    # small disk: N = 2048, gravity + Coulomb + relativity, softening 0.1, 10 frames
+    # small disk: N = 2048, gravity + Coulomb + relativity, softening 0.1; the
+    # one-launch frame kernel and, for comparison, the launch-per-phase path
     wl = W.small_disk(2048)
-    g = GeonSystem(wl.params, wl.n)
-    g.upload(*[wl.state[k] for k in STATE_KEYS])
-    st = torch.cuda.ExternalStream(g.stream_ptr())
-    secs, sub, lat = time_frames(g, wl.dt, 10, 3, st)
-    out["small_disk_n2048"] = {"value": wl.n * sub / secs, "unit": UNIT, "frames": 10, "substeps": sub,
-                               "frame_ms_p50": float(np.percentile(lat, 50)),
-                               "frame_ms_p99": float(np.percentile(lat, 99)),
-                               "note": "fresh particles: no history yet, so no near-field forces under signal delay"}
-    g.close()
+    small = {}
+    for split in (False, True):
+        g = GeonSystem(wl.params, wl.n)
+        g.upload(*[wl.state[k] for k in STATE_KEYS])
+        if split:
+            p = g.params()
+            p.flags |= N.FLAG_SPLIT_FRAME
+            g.set_params(p)
+        st = torch.cuda.ExternalStream(g.stream_ptr())
+        g.update(wl.dt)                              # first frame: force bootstrap
+        l0 = g.launch_count()
+        secs, sub, lat = time_frames(g, wl.dt, 30, 3, st)
+        launches = (g.launch_count() - l0) / 33
+        small["split" if split else "frame"] = {
+            "value": wl.n * sub / secs, "unit": UNIT, "frames": 30, "substeps": sub,
+            "frame_ms_p50": float(np.percentile(lat, 50)), "frame_ms_p99": float(np.percentile(lat, 99)),
+            "gpu_launches_per_frame": launches,
+            **({} if split else {"phases_us": g.frame_phases()})}
+        g.close()
+    out["small_disk_n2048"] = {**small["frame"], "launch_per_phase": small["split"],
+                               "note": "one cooperative launch per frame (planner, substeps, tree builds, walks, "
+                                       "history, boundary); fresh particles: no history yet, so no near-field "
+                                       "forces under signal delay"}
     # torus, full force set with relativity and a warmed history; BH theta 0.5 and the pairwise sum
     for bh in (True, False):
         wl = W.clusters_torus(65536, barnes_hut=bh)

@@ -250,6 +250,13 @@ int geon_update(GeonHandle* h, double dt, int32_t* substeps);
  * of the time-out path); 0 restores normal operation. */
 int geon_set_frame_wait(GeonHandle* h, int64_t wait_ns, int32_t extra_arrivals);
 
+/* Phase durations (microseconds, block 0's clock) of the last one-launch
+ * frame: frame-start scan, then the first substep's push + keys, sort,
+ * gather, scans, emit, link, aggregation and walk, then the rest of the
+ * frame (later substeps, history, boundary).  Writes min(n, 10) values, 0
+ * for phases the frame did not reach; returns 10. */
+int geon_frame_phases(GeonHandle* h, double* us, int32_t n);
+
 /* Waits for all work enqueued on the handle's stream. */
 int geon_synchronize(GeonHandle* h);
 

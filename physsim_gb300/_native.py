@@ -168,6 +168,7 @@ SIGNATURES = {
     "geon_particle_count": [_handle_t, _P(C.c_int32)],
     "geon_update": [_handle_t, C.c_double, _P(C.c_int32)],
     "geon_set_frame_wait": [_handle_t, C.c_int64, C.c_int32],
+    "geon_frame_phases": [_handle_t, _P(C.c_double), C.c_int32],
     "geon_synchronize": [_handle_t],
     "geon_compute_forces": [_handle_t],
     "geon_compute_1pn": [_handle_t],

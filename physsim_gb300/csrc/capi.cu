@@ -970,6 +970,7 @@ int geon_create(const GeonParams* params, int32_t max_particles, GeonHandle** ou
     cudaMemsetAsync(h->ctl, 0, sizeof(FrameCtl), h->st);
     cudaMemsetAsync(h->hist_t, 0, HIST_LEN * sizeof(double), h->st);
     cudaMemsetAsync(h->frun, 0, sizeof(FrameRun), h->st);
+    memset(h->frun_h, 0, sizeof(FrameRun));
     r = alloc_state(h, slots_wanted(h));
     if (r) { g_err = h->err; geon_destroy(h); return r; }
     r = ensure_history(h);
@@ -1719,7 +1720,12 @@ static int frame_update(GeonHandle* h, double dt, int32_t* substeps) {
     A.withHist = h->hist_alloc ? 1 : 0;
     A.waitNs = h->frame_wait_ns;
     A.extraArrivals = h->frame_extra;
-    const ForceCtx C = make_ctx(h);
+    ForceCtx C = make_ctx(h);
+    // the walk's four warps per group share the subtrees below level 8 (node
+    // size 2 rootW / 256); config 1 (N = 2,048): levels 5 / 6 / 7 / 8..10 give
+    // 112 / 112 / 101 / 100 us per walk, so 8 (and no deeper, where the
+    // duplicated top of the walk grows)
+    C.split_level = 8;
     const cudaError_t e = frame_launch(rel, h->P, h->S, h->S2, h->T, h->d_root, h->ctl, C, A, h->frun, h->n, h->st, h->lc);
     if (e != cudaSuccess) return cuda_check(h, e, "frame kernel launch");
     CK(cudaMemcpyAsync(h->frun_h, h->frun, sizeof(FrameRun), cudaMemcpyDeviceToHost, h->st));
@@ -1743,6 +1749,15 @@ static int frame_update(GeonHandle* h, double dt, int32_t* substeps) {
         h->n -= R.removed;
     }
     return GEON_OK;
+}
+
+int geon_frame_phases(GeonHandle* h, double* us, int32_t n) {
+    if (!h || n < 0 || (n > 0 && !us)) return GEON_ERR_ARG;
+    const FrameRun& R = *h->frun_h;
+    const int k = std::min(n, FRAME_STAMPS - 1);
+    for (int i = 0; i < k; i++)
+        us[i] = (R.stamp[i + 1] >= R.stamp[i] && R.stamp[i]) ? 1e-3 * (double)(R.stamp[i + 1] - R.stamp[i]) : 0.0;
+    return FRAME_STAMPS - 1;
 }
 
 int geon_set_frame_wait(GeonHandle* h, int64_t wait_ns, int32_t extra_arrivals) {

@@ -264,6 +264,21 @@ __device__ __forceinline__ unsigned lane_id() { unsigned r; asm volatile("mov.u3
 __device__ __forceinline__ unsigned lanemask_lt() { unsigned r; asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(r)); return r; }
 
 // Atomic max on non-negative doubles through their bit patterns.
+// Release + acquire fence at GPU scope.  Paired with a relaxed atomic it
+// forms the release (writes, fence, atomic) and acquire (atomic, fence,
+// reads) patterns of the PTX memory model, without the extra ordering of a
+// sequentially consistent fence (__threadfence).
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
+// atomicAdd with acquire-release semantics at GPU scope: the caller's earlier
+// writes are visible to whoever observes the new value, and the caller sees
+// the writes of everyone whose addition it observes.
+__device__ __forceinline__ int atomic_add_acq_rel_gpu(int* p, int v) {
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
 __device__ __forceinline__ void atomic_max_pos_double(unsigned long long* addr, double v) {
     if (!(v > 0.0)) return;   // skips NaN and zero
     atomicMax(addr, (unsigned long long)__double_as_longlong(v));

@@ -39,6 +39,10 @@ struct ForceCtx {
     // sums, null or dslices <= 1 for one pass over all sources
     float* dpart;
     int dslices;
+    // split walk (walkc_body with SPLIT warps per target group): nodes at
+    // levels up to split_level are evaluated by one warp each (node index
+    // modulo SPLIT), and a node at split_level is opened only by that warp
+    int split_level;
 };
 
 // How the pairwise sum over n_cap targets is split: the number of source

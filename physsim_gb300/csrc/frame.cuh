@@ -10,6 +10,11 @@ namespace geon {
 // all points held in shared memory.
 constexpr int FRAME_MAX_POINTS = 4096;
 
+// Phase boundaries recorded by block 0 (globaltimer ns): launch, then the end
+// of the frame-start scan, and of the first substep's push + keys, sort,
+// gather, scans, emit, link, aggregation and walk, then the end of the frame.
+constexpr int FRAME_STAMPS = 11;
+
 // Device-side state of one frame launch: the grid barrier, the frame-start
 // planner maxima and the frame's results.  count, abort and the maxima are
 // zero between launches; gen only grows.
@@ -23,6 +28,8 @@ struct FrameRun {
     double simTime;                  // simulation time at the end of the frame
     unsigned long long scanAccel;    // frame-start max |F|^2 / m^2 (double bits)
     unsigned long long scanCyc;      // frame-start max cyclotron frequency (double bits)
+    unsigned long long stamp[FRAME_STAMPS];   // phase boundaries of the last frame (block 0's clock)
+    int valid[2];                    // points inside the root box, by substep parity
 };
 
 struct FrameArgs {

@@ -468,12 +468,12 @@ __device__ __forceinline__ void aggregate_body(DevParams P, DevState S, TreeBufs
         int node = lm.w;
         int guard = 0;
         while (node >= 0 && node < nInt && guard++ <= KEY_LEVELS) {
-            __threadfence();
+            // the last child to arrive aggregates the node: the acquire-release
+            // count publishes this child and shows the others
             const int4 ch = T.int_child[node];
+            const int prev = atomic_add_acq_rel_gpu(&T.int_count[node], 1);
             const int nch = (ch.x >= 0) + (ch.y >= 0) + (ch.z >= 0) + (ch.w >= 0);
-            const int prev = atomicAdd(&T.int_count[node], 1);
             if (prev != nch - 1) break;
-            __threadfence();
             Agg h; agg_zero(h);
             const int cs[4] = { ch.x, ch.y, ch.z, ch.w };
 #pragma unroll

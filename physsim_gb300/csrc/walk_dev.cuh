@@ -895,9 +895,18 @@ __host__ __device__ constexpr int wc_min_blocks() {
 
 // One CTA of the walk: warps vb * WC_WARPS .. + WC_WARPS - 1 of the target
 // order, with WC_THREADS threads and wc_smem_bytes() of dynamic shared memory.
-template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE, bool EMIT>
+// SPLIT == WC_WARPS: the CTA's four warps walk the same group vb of 32
+// targets.  Every warp descends the levels above C.split_level; a node at
+// or above it is evaluated (aggregate or leaf points) only by warp
+// (index mod SPLIT), and a node at split_level is opened only by that warp,
+// so each subtree below it is walked once.  The warps' compensated partial
+// sums are then added in warp order by warp 0, which writes the target.
+// The interaction list of every target is the one of the plain walk; only
+// the order of the sums differs.
+template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE, bool EMIT, int SPLIT = 1>
 __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S, const TreeBufs& T,
                                            const int* d_root, FrameCtl* ctl, const ForceCtx& C, int vb) {
+    static_assert(SPLIT == 1 || (SPLIT == WC_WARPS && !EMIT), "split walk: one group per CTA, no records");
     constexpr bool NEEDC = MAGGM || REL;
     constexpr bool SHF = wc_sh<MAGGM, REL, BRK, PER, NOPE>();   // shared-memory form (six or four CTAs per SM)
     using AccT = Acc<MAGGM, BRK, SHF>;
@@ -910,7 +919,7 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
     const int warp = threadIdx.x >> 5;
     const unsigned lane = threadIdx.x & 31;
     WS& W = Wall[warp];
-    const int k0 = (vb * WC_WARPS + warp) * 32 + (int)lane;
+    const int k0 = (SPLIT > 1 ? vb * 32 : (vb * WC_WARPS + warp) * 32) + (int)lane;
     int sysId;
     const int ti = walk_target(S, T, ctl, C, k0, sysId);
     const bool valid = ti >= 0;
@@ -939,7 +948,7 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
     if (SHF && lane == 0) { W.counts[0] = nInt0; W.counts[1] = nLeaf0; W.counts[2] = nValid0; }
     int top = 0, npool = 0, nfull = 0, lcnt = 0;
     int rcnt = 0;                                                     // EMIT: records of this warp
-    const int grp = vb * WC_WARPS + warp;
+    const int grp = SPLIT > 1 ? vb : vb * WC_WARPS + warp;
     if (root != ROOT_NONE && treeOk) {
         if (lane == 0) { W.stk_node[0] = root; W.stk_mask[0] = active; }
         top = 1;
@@ -1014,6 +1023,18 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
             }
             const unsigned acc = __ballot_sync(0xffffffffu, accept);
             if ((int)lane == jj) { myAcc = acc & msk; myOpen = msk & ~acc; }
+        }
+        if (SPLIT > 1 && node >= 0 && kind != 0) {                   // split walk: this warp's share
+            const bool isLeaf = (node & LEAF_REF) != 0;
+            const int lvl = isLeaf ? lm.z : (int)nc.w;
+            if (lvl <= C.split_level) {
+                const unsigned id = isLeaf ? (unsigned)(node & ~LEAF_REF) : (unsigned)node;
+                if ((int)(id % (unsigned)SPLIT) != warp) {
+                    myAcc = 0u;
+                    if (lvl == C.split_level) myOpen = 0u;
+                    if (kind == 1) kind = 0;
+                }
+            }
         }
         if (EMIT) {                                                   // learned correction: (cell, group) records
             // one record per accepted cell: the node and the lanes that accept
@@ -1105,6 +1126,31 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
         __syncwarp();
     }
     flush_pool<MAGGM, REL, BRK, PER>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
+    if constexpr (SPLIT > 1) {
+        // partial sums of warps 1.. through their (now unused) stacks; warp 0 adds them in order
+        constexpr int NQ = AccT::NQ;
+        static_assert((2 * NQ + 1) * 32 * sizeof(float) <= sizeof(W.stk_node) + sizeof(W.stk_mask),
+                      "split walk exchange area");
+        A.flush();
+        if (warp > 0) {
+            float* xw = reinterpret_cast<float*>(W.stk_node);
+#pragma unroll
+            for (int q = 0; q < NQ; q++) { xw[q * 32 + lane] = A.hi(q); xw[(NQ + q) * 32 + lane] = A.lo(q); }
+            reinterpret_cast<unsigned*>(xw)[2 * NQ * 32 + lane] = inter;
+        }
+        __syncthreads();
+        if (warp > 0) return;
+        for (int k = 1; k < SPLIT; k++) {
+            const float* xk = reinterpret_cast<const float*>(Wall[k].stk_node);
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+                const df s2 = two_sum(A.hi(q), xk[q * 32 + lane]);
+                A.hi(q) = s2.hi;
+                A.lo(q) = __fadd_rn(__fadd_rn(A.lo(q), xk[(NQ + q) * 32 + lane]), s2.lo);
+            }
+            inter += reinterpret_cast<const unsigned*>(xk)[2 * NQ * 32 + lane];
+        }
+    }
     if (EMIT && lane == 0) {
         const float cx = SHF ? W.gbox[0] : gcx0, cy = SHF ? W.gbox[1] : gcy0;
         const float hx = SHF ? W.gbox[2] : ghx0, hy = SHF ? W.gbox[3] : ghy0;

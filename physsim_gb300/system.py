@@ -109,6 +109,14 @@ class GeonSystem:
         self._ck(self.lib.geon_update(self._h, float(dt), C.byref(s)))
         return s.value
 
+    FRAME_PHASES = ("scan", "push+keys", "sort", "gather", "scans", "emit", "link", "aggregate", "walk", "rest")
+
+    def frame_phases(self) -> dict:
+        """Phase durations (us) of the last one-launch frame."""
+        out = (C.c_double * 16)()
+        k = self._ck(self.lib.geon_frame_phases(self._h, out, 16))
+        return {name: float(out[i]) for i, name in enumerate(self.FRAME_PHASES[:k])}
+
     def set_frame_wait(self, wait_ns: int = 1_000_000_000, extra_arrivals: int = 0):
         """Time limit of the one-launch frame's barriers; extra_arrivals > 0
         makes them wait for blocks that do not exist (time-out test)."""

@@ -51,8 +51,9 @@ def run_pair(wl, frames):
 
 
 def assert_close(sa, sb, keys=("x", "y", "wx", "wy", "angw")):
-    for k in keys:
-        e = rel_err(sa[k], sb[k])
+    errs = {k: rel_err(sa[k], sb[k]) for k in keys}
+    print("frame kernel vs split path:", {k: e["norm"] for k, e in errs.items()})
+    for k, e in errs.items():
         assert e["norm"] <= FRAME_TOL, (k, e)
 
 
