@@ -71,6 +71,7 @@ struct Acc {
     }
     __device__ __forceinline__ float get(int q) { return __fadd_rn(hi(q), lo(q)); }
     __device__ __forceinline__ void add(int q, float v) { part[q] = __fadd_rn(part[q], v); }
+    __device__ __forceinline__ void fma(int q, float a, float b) { part[q] = __fmaf_rn(a, b, part[q]); }
     __device__ __forceinline__ void addm(int q, float v) { if (MAGGM) add(QM + q, v); }
     __device__ __forceinline__ void addk(int q, float v) { if (BRK) add(QK + q, v); }
 };
@@ -131,19 +132,24 @@ __device__ __forceinline__ void pair_force(const DevParams& P, const Tgt& t, flo
     const bool grav = on(P, GEON_GRAVITY), coul = on(P, GEON_COULOMB);
     float fr = 0.f;                                                  // sum of the radial (r-parallel) terms
 
-    if (grav) {                                                      // forces.js:205-220
-        const float k = t.m * sm;
-        const float fDir = k * invR3a;
-        fr += fDir;
-        A.addk(K_GX, rx * fDir); A.addk(K_GY, ry * fDir);
-        if (pe) A.add(Q_PE, -k * invR);
-    }
-    if (coul) {                                                      // forces.js:225-240
-        const float k = -(t.q * sq);
-        const float fDir = k * invR3a;
-        fr += fDir;
-        A.addk(K_CX, rx * fDir); A.addk(K_CY, ry * fDir);
-        if (pe) A.add(Q_PE, t.q * sq * invR);
+    if (!BRK && grav && coul) {                                      // forces.js:205-240, one radial coefficient
+        fr = __fmaf_rn(t.m, sm, -(t.q * sq)) * invR3a;
+        if (pe) { A.add(Q_PE, -(t.m * sm) * invR); A.add(Q_PE, t.q * sq * invR); }
+    } else {
+        if (grav) {                                                  // forces.js:205-220
+            const float k = t.m * sm;
+            const float fDir = k * invR3a;
+            fr += fDir;
+            A.addk(K_GX, rx * fDir); A.addk(K_GY, ry * fDir);
+            if (pe) A.add(Q_PE, -k * invR);
+        }
+        if (coul) {                                                  // forces.js:225-240
+            const float k = -(t.q * sq);
+            const float fDir = k * invR3a;
+            fr += fDir;
+            A.addk(K_CX, rx * fDir); A.addk(K_CY, ry * fDir);
+            if (pe) A.add(Q_PE, t.q * sq * invR);
+        }
     }
     if (MAGGM) {
         const bool mag = on(P, GEON_MAGNETIC), gm = on(P, GEON_GRAVITOMAG), pn = on(P, GEON_ONE_PN);
@@ -227,8 +233,8 @@ __device__ __forceinline__ void pair_force(const DevParams& P, const Tgt& t, flo
             if (pe) A.add(Q_PE, 0.5f * g * invR * (v1DotV2 + nDotV1 * nDotV2 * alpha));
         }
     }
-    A.add(Q_FX, rx * fr);
-    A.add(Q_FY, ry * fr);
+    A.fma(Q_FX, rx, fr);
+    A.fma(Q_FY, ry, fr);
     if (grav) {                                                      // forces.js:428-441
         const float crossRV = rx * (svy - t.vy) - ry * (svx - t.vx);
         const float dw = __fmaf_rn(-crossRV, invRSq, t.angVel);

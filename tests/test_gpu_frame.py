@@ -10,7 +10,10 @@ oracle, through the C ABI.
 * the split path itself stays within the trajectory bar of the oracle on the
   small config, as the frame kernel does (test_gpu_parity.py);
 * a barrier that waits for a block that does not exist gives up after its
-  time limit: geon_update returns GEON_ERR_TIMEOUT, and the GPU stays usable.
+  time limit: geon_update returns GEON_ERR_TIMEOUT, and the GPU stays usable;
+* the hand-traced cases of the oracle's known-answer tests: the substep
+  count when dtRemain is an exact multiple of dtSafe, and the Yukawa cutoff
+  at a separation of exactly 6 / mu.
 """
 import numpy as np
 import pytest
@@ -138,3 +141,45 @@ def test_barrier_timeout_is_reported(gpu_lib):
         assert h.count() == wl.n
     finally:
         h.close()
+
+
+# The hand-traced planner and cutoff cases of tests/test_oracle_kat.py on the
+# device: the substep count at an exact multiple dtRemain = 4 dtSafe (and one
+# part in 2^20 either side), through the one-launch frame, the split path and
+# the pairwise path.
+@pytest.mark.parametrize("g,expect", [(4096.0, 4), (4096.0 * (1 + 2.0 ** -20), 5), (4096.0 * (1 - 2.0 ** -20), 4)])
+@pytest.mark.parametrize("path", ["frame", "split", "pairwise"])
+def test_planner_ceil_at_exact_multiples(gpu_lib, g, expect, path):
+    tg = N.GRAVITY | (0 if path == "pairwise" else N.BARNES_HUT)
+    fl = N.FLAG_SPLIT_FRAME if path == "split" else 0
+    p = N.make_params(toggles=tg, flags=fl, softening=1.0, domain_w=1000, domain_h=1000, ext_gravity=g)
+    one = np.ones(1)
+    g_ = GeonSystem(p, 1)
+    try:
+        g_.upload_f64(np.array([100.0]), np.array([500.0]), 0 * one, 0 * one, one, 0 * one, 0 * one)
+        assert g_.update(1 / 16) == expect
+        assert g_.update(1 / 16) == expect
+    finally:
+        g_.close()
+
+
+@pytest.mark.parametrize("d,inside", [(8.0, False), (8.0 - 2.0 ** -40, True), (8.0 + 2.0 ** -40, False)])
+@pytest.mark.parametrize("bh", [True, False])
+def test_yukawa_cutoff_tie(gpu_lib, d, inside, bh):
+    mu, eps = 0.75, 1.0
+    p = N.make_params(toggles=N.YUKAWA | (N.BARNES_HUT if bh else 0), softening=eps, yukawa_mu=mu,
+                      domain_w=1000, domain_h=1000)
+    g_ = GeonSystem(p, 2)
+    z = np.zeros(2)
+    try:
+        g_.upload_f64(np.array([100.0, 100.0 + d]), np.array([500.0, 500.0]), z, z, np.array([2.0, 1.5]), z, z)
+        g_.compute_forces()
+        fx = float(g_.forces()["fx"][0])
+    finally:
+        g_.close()
+    if inside:
+        r = np.sqrt(d * d + eps * eps)
+        expect = 14 * 2.0 * 1.5 * np.exp(-mu * r) * (1 / r ** 2 + mu / r) / r * d
+        assert abs(fx - expect) <= 1e-5 * abs(expect), (fx, expect)
+    else:
+        assert fx == 0.0

@@ -228,3 +228,47 @@ def test_periodic_bh_counts_each_image(oracle_mod):
     ghosts = o.ghost_origins()
     copies_of_1 = 1 + int(np.sum(ghosts == 1))
     assert np.isclose(f_bh, copies_of_1 * f_direct, rtol=1e-12)
+
+
+# ---- hand-traced control flow of the reference ------------------------------------------
+# integrator.js:862-870: dtSafe = sqrt(softening / aMax), stepsNeeded =
+# min(ceil(dtRemain / dtSafe), budget), dtSub = dtRemain / stepsNeeded.  One
+# unit mass in a uniform field g = 4096 (angle 0: force (4096, 0) exactly),
+# softening 1, dt = 1/16: dtSafe = 1/64 exactly, dtRemain / dtSafe = 4 exactly,
+# so ceil gives 4 (not 5) and the later substeps (lagged aMax, the same field)
+# take 3, 2, 1 of the remaining quarters: 4 substeps.  With g = 4096 (1 + 2^-20)
+# the ratio is 4 (1 + 2^-21) and ceil gives 5; the next ratio is
+# (4/5) / (1 - 2^-21) * 4 = 3.2..., ceil 4, and so on: 5 substeps.
+PLANNER_CASES = ((4096.0, 4), (4096.0 * (1 + 2.0 ** -20), 5), (4096.0 * (1 - 2.0 ** -20), 4))
+
+
+@pytest.mark.parametrize("g,expect", PLANNER_CASES)
+def test_planner_ceil_at_exact_multiples(oracle_mod, g, expect):
+    p = N.make_params(toggles=N.GRAVITY, softening=1.0, domain_w=1000, domain_h=1000, ext_gravity=g)
+    o = sim(p, [100.0], [500.0])
+    assert o.update(1 / 16) == expect
+
+
+# forces.js:82-83, 387: the Yukawa term applies when the unsoftened r^2 is
+# strictly below (6 / mu)^2.  mu = 0.75 makes the cutoff 8 exactly: at a
+# separation of exactly 8 there is no Yukawa force, one ulp-scale step closer
+# (8 - 2^-40) there is the full term.
+YUKAWA_TIE_MU, YUKAWA_TIE_EPS = 0.75, 1.0
+
+
+def yukawa_expect(d, mu=YUKAWA_TIE_MU, eps=YUKAWA_TIE_EPS, m1=2.0, m2=1.5):
+    r = np.sqrt(d * d + eps * eps)
+    return 14 * m1 * m2 * np.exp(-mu * r) * (1 / r ** 2 + mu / r) / r * d
+
+
+@pytest.mark.parametrize("d,inside", [(8.0, False), (8.0 - 2.0 ** -40, True), (8.0 + 2.0 ** -40, False)])
+def test_yukawa_cutoff_tie(oracle_mod, d, inside):
+    p = N.make_params(toggles=N.YUKAWA, softening=YUKAWA_TIE_EPS, yukawa_mu=YUKAWA_TIE_MU,
+                      domain_w=1000, domain_h=1000)
+    o = sim(p, [100.0, 100.0 + d], [500.0, 500.0], m=[2.0, 1.5])
+    o.compute_forces()
+    fx = o.forces()["fx"][0]
+    if inside:
+        assert np.isclose(fx, yukawa_expect(d), rtol=1e-12, atol=0.0)
+    else:
+        assert fx == 0.0
