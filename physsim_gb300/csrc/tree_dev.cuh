@@ -428,20 +428,14 @@ __device__ __forceinline__ void aggregate_body(DevParams P, DevState S, TreeBufs
         const int4 lm = T.leaf_meta[leaf];
         Agg g; agg_zero(g);
         if (lm.x < 0 || lm.y < 1 || lm.x + lm.y > nValid || lm.w >= nInt) { atomicOr(&ctl->err, ERR_BAD_INDEX); continue; }
-        for (int k = 0; k < lm.y; k++) {                     // quadtree.js:276-287
-            const int s = lm.x + k;
-            const float4 pa = T.ps_a[s];
-            const float4 pb = T.ps_b[s];
-            const float4 pc = T.ps_c[s];
-            const uint32_t ref = __float_as_uint(pc.w);
-            const uint32_t j = ref_index(ref), code = ref_code(ref);
+        // one point of the leaf (quadtree.js:276-287); wx, wy and mom come from
+        // the particle the point refers to
+        auto add_point = [&](const float4& pa, const float4& pb, const float4& pc, const float4& vel, float2 mom) {
+            const uint32_t code = ref_code(__float_as_uint(pc.w));
             const float m = pa.z;
-            const float4 vel = S.vel[j];
             const float wx = code_fvx(code) ? -vel.x : vel.x;
             const float wy = code_fvy(code) ? -vel.y : vel.y;
-            float2 mom;
-            if (code == CODE_IDENTITY) mom = S.mom[j];       // cached by the previous force pass
-            else mom = make_float2(pc.y, pc.z);              // ghosts: formed at ghost creation (integrator.js:193-194)
+            if (code != CODE_IDENTITY) mom = make_float2(pc.y, pc.z);   // ghosts: formed at ghost creation (integrator.js:193-194)
             g.mass = df_add(g.mass, df{ m, 0.f });
             g.charge = df_add(g.charge, df{ pa.w, 0.f });
             g.mu = df_add(g.mu, df{ mom.x, 0.f });
@@ -449,6 +443,34 @@ __device__ __forceinline__ void aggregate_body(DevParams P, DevState S, TreeBufs
             g.px = df_add(g.px, two_prod(m, wx));
             g.py = df_add(g.py, two_prod(m, wy));
             agg_add_com(g, df{ pa.x, pb.x }, df{ pa.y, pb.y }, m);
+        };
+        if (lm.y <= LEAF_CAP) {
+            // all loads of the leaf first (two rounds: the point records, then
+            // the particles they refer to), then the sums in point order
+            float4 pa[LEAF_CAP], pb[LEAF_CAP], pc[LEAF_CAP], vel[LEAF_CAP];
+            float2 mom[LEAF_CAP];
+#pragma unroll
+            for (int k = 0; k < LEAF_CAP; k++) {
+                if (k < lm.y) { pa[k] = T.ps_a[lm.x + k]; pb[k] = T.ps_b[lm.x + k]; pc[k] = T.ps_c[lm.x + k]; }
+            }
+#pragma unroll
+            for (int k = 0; k < LEAF_CAP; k++) {
+                if (k < lm.y) {
+                    const uint32_t j = ref_index(__float_as_uint(pc[k].w));
+                    vel[k] = S.vel[j];
+                    mom[k] = S.mom[j];                         // cached by the previous force pass
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < LEAF_CAP; k++)
+                if (k < lm.y) add_point(pa[k], pb[k], pc[k], vel[k], mom[k]);
+        } else {
+            for (int k = 0; k < lm.y; k++) {                 // a level-31 bucket
+                const int s = lm.x + k;
+                const float4 pc = T.ps_c[s];
+                const uint32_t j = ref_index(__float_as_uint(pc.w));
+                add_point(T.ps_a[s], T.ps_b[s], pc, S.vel[j], S.mom[j]);
+            }
         }
         agg_write(T.leaf_a, T.leaf_b, T.leaf_c, leaf, g, node_size2(P, lm.z), lm.z);
         if (T.mom_on) {
@@ -471,24 +493,34 @@ __device__ __forceinline__ void aggregate_body(DevParams P, DevState S, TreeBufs
             // the last child to arrive aggregates the node: the acquire-release
             // count publishes this child and shows the others
             const int4 ch = T.int_child[node];
+            const int4 mm = T.int_meta[node];
             const int prev = atomic_add_acq_rel_gpu(&T.int_count[node], 1);
             const int nch = (ch.x >= 0) + (ch.y >= 0) + (ch.z >= 0) + (ch.w >= 0);
             if (prev != nch - 1) break;
             Agg h; agg_zero(h);
             const int cs[4] = { ch.x, ch.y, ch.z, ch.w };
+            // every child's record first (one round of loads), then the sums in child order
+            float4 ca[4], cb[4], cc[4];
+            bool have[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {                    // quadtree.js:297-309
                 const int c = cs[q];
+                have[q] = false;
                 if (c < 0) continue;
-                float4 a, b, cc;
                 if (c & LEAF_REF) {
                     const int li = c & ~LEAF_REF;
                     if (li >= nLeaves) { atomicOr(&ctl->err, ERR_BAD_INDEX); continue; }
-                    a = __ldcg(&T.leaf_a[li]); b = __ldcg(&T.leaf_b[li]); cc = __ldcg(&T.leaf_c[li]);
+                    ca[q] = __ldcg(&T.leaf_a[li]); cb[q] = __ldcg(&T.leaf_b[li]); cc[q] = __ldcg(&T.leaf_c[li]);
                 } else {
                     if (c >= nInt) { atomicOr(&ctl->err, ERR_BAD_INDEX); continue; }
-                    a = __ldcg(&T.int_a[c]); b = __ldcg(&T.int_b[c]); cc = __ldcg(&T.int_c[c]);
+                    ca[q] = __ldcg(&T.int_a[c]); cb[q] = __ldcg(&T.int_b[c]); cc[q] = __ldcg(&T.int_c[c]);
                 }
+                have[q] = true;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                if (!have[q]) continue;
+                const float4 a = ca[q], b = cb[q];
                 const float m = a.z;
                 h.mass = df_add(h.mass, df{ m, 0.f });
                 h.charge = df_add(h.charge, df{ a.w, 0.f });
@@ -496,9 +528,8 @@ __device__ __forceinline__ void aggregate_body(DevParams P, DevState S, TreeBufs
                 h.L = df_add(h.L, df{ b.w, 0.f });
                 h.px = df_add(h.px, two_prod(m, b.x));
                 h.py = df_add(h.py, two_prod(m, b.y));
-                if (m > 0.f) agg_add_com(h, df{ a.x, cc.x }, df{ a.y, cc.y }, m);
+                if (m > 0.f) agg_add_com(h, df{ a.x, cc[q].x }, df{ a.y, cc[q].y }, m);
             }
-            const int4 mm = T.int_meta[node];
             agg_write(T.int_a, T.int_b, T.int_c, node, h, node_size2(P, mm.x), mm.x);
             if (T.mom_on) {
                 df px, py;
