@@ -185,12 +185,22 @@ __device__ __forceinline__ float wrap_axis_comp(float a, float b, float a_lo, fl
 }
 
 // FP64 minimum image, used for Klein / RP^2 and for guard-band re-tests.
+__device__ __forceinline__ double torus_wrap_d(double d, double full, double half) {
+    if (d > half) d -= full; else if (d < -half) d += full;
+    return d;
+}
+// FP64 minimum image on the torus (the torus case of min_image_d).
+__device__ __forceinline__ void torus_image_d(double ox, double oy, double sx, double sy, double W, double H,
+                                              double& rx, double& ry) {
+    rx = torus_wrap_d(sx - ox, W, W * 0.5);
+    ry = torus_wrap_d(sy - oy, H, H * 0.5);
+}
 __device__ inline void min_image_d(double ox, double oy, double sx, double sy, int topology,
                                    double W, double H, double& rx, double& ry) {
-    const double halfW = W * 0.5, halfH = H * 0.5;
-    auto tw = [](double d, double full, double half) { if (d > half) d -= full; else if (d < -half) d += full; return d; };
+    if (topology == GEON_TORUS) { torus_image_d(ox, oy, sx, sy, W, H, rx, ry); return; }
+    const double halfW = W * 0.5;
+    auto tw = [](double d, double full, double half) { return torus_wrap_d(d, full, half); };
     double dx = sx - ox, dy = sy - oy;
-    if (topology == GEON_TORUS) { rx = tw(dx, W, halfW); ry = tw(dy, H, halfH); return; }
     const double doubleH = 2 * H;
     if (topology == GEON_KLEIN) {
         double bx = tw(dx, W, halfW), by = dy;

@@ -28,7 +28,7 @@
 
 namespace geon {
 
-template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE = false, bool EMIT = false>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE = false, bool EMIT = false>
 static void launch_walkc(int blocks, const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root,
                          FrameCtl* ctl, const ForceCtx& C, cudaStream_t st) {
     constexpr size_t smem = wc_smem_bytes<MAGGM, REL, BRK, PER, NOPE>();
@@ -827,18 +827,30 @@ static void launch_force(bool bh, const DevParams& P, const DevState& S, const T
         const bool lean = PLAIN && !C.pe;
         if (PLAIN && C.recs) {                     // learned correction (plain forces only)
             if (P.periodic) {
-                if (lean) launch_walkc<false, false, false, true, true, true>(blocks, P, S, T, d_root, ctl, C, st);
-                else launch_walkc<false, false, false, true, false, true>(blocks, P, S, T, d_root, ctl, C, st);
+                if (lean) launch_walkc<false, false, false, 1, true, true>(blocks, P, S, T, d_root, ctl, C, st);
+                else launch_walkc<false, false, false, 1, false, true>(blocks, P, S, T, d_root, ctl, C, st);
             } else {
-                if (lean) launch_walkc<false, false, false, false, true, true>(blocks, P, S, T, d_root, ctl, C, st);
-                else launch_walkc<false, false, false, false, false, true>(blocks, P, S, T, d_root, ctl, C, st);
+                if (lean) launch_walkc<false, false, false, 0, true, true>(blocks, P, S, T, d_root, ctl, C, st);
+                else launch_walkc<false, false, false, 0, false, true>(blocks, P, S, T, d_root, ctl, C, st);
             }
         } else if (P.periodic) {
-            if (lean) launch_walkc<MAGGM, REL, BRK, true, PLAIN>(blocks, P, S, T, d_root, ctl, C, st);
-            else launch_walkc<MAGGM, REL, BRK, true>(blocks, P, S, T, d_root, ctl, C, st);
+            // the torus walks of the ensemble (plain forces) and of the full
+            // force set with relativity carry the torus wrap alone
+            const bool torus = P.topology == GEON_TORUS;
+            if constexpr (PLAIN) {
+                if (lean) {
+                    if (torus) launch_walkc<false, false, false, 2, true>(blocks, P, S, T, d_root, ctl, C, st);
+                    else launch_walkc<false, false, false, 1, true>(blocks, P, S, T, d_root, ctl, C, st);
+                    return;
+                }
+            }
+            if constexpr (MAGGM && REL && !BRK) {
+                if (torus) { launch_walkc<MAGGM, REL, BRK, 2>(blocks, P, S, T, d_root, ctl, C, st); return; }
+            }
+            launch_walkc<MAGGM, REL, BRK, 1>(blocks, P, S, T, d_root, ctl, C, st);
         } else {
-            if (lean) launch_walkc<MAGGM, REL, BRK, false, PLAIN>(blocks, P, S, T, d_root, ctl, C, st);
-            else launch_walkc<MAGGM, REL, BRK, false>(blocks, P, S, T, d_root, ctl, C, st);
+            if (lean) launch_walkc<MAGGM, REL, BRK, 0, PLAIN>(blocks, P, S, T, d_root, ctl, C, st);
+            else launch_walkc<MAGGM, REL, BRK, 0>(blocks, P, S, T, d_root, ctl, C, st);
         }
     } else {
         const int blocks = std::max(1, (n_cap + DIRECT_THREADS - 1) / DIRECT_THREADS);

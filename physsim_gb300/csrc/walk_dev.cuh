@@ -247,9 +247,15 @@ __device__ __forceinline__ void pair_force(const DevParams& P, const Tgt& t, flo
 // ---- exact (FP64) displacement helpers for guard-band re-tests --------------------------
 // Every FP64 operation sits behind a guard that is taken only when an FP32
 // margin is within rounding: FP64 runs at a small fraction of the FP32 rate.
+// PER: the topology class of a walk fixed at compile time, 0 the open box,
+// 1 any topology (decided at run time), 2 the torus only.  The walks that
+// know their class carry no code for the others.
+template <int PER = 1>
 __device__ __forceinline__ void exact_disp(const DevParams& P, double ox, double oy, double sx, double sy,
                                            double& rx, double& ry) {
-    if (P.periodic) min_image_d(ox, oy, sx, sy, P.topology, P.Wd, P.Hd, rx, ry);
+    if (PER == 0) { rx = sx - ox; ry = sy - oy; }
+    else if (PER == 2) torus_image_d(ox, oy, sx, sy, P.Wd, P.Hd, rx, ry);
+    else if (P.periodic) min_image_d(ox, oy, sx, sy, P.topology, P.Wd, P.Hd, rx, ry);
     else { rx = sx - ox; ry = sy - oy; }
 }
 
@@ -257,28 +263,34 @@ __device__ __forceinline__ void exact_disp(const DevParams& P, double ox, double
 struct SPos { float x, xlo, y, ylo; };
 
 // FP64 re-test of the Yukawa cutoff inside the FP32 guard band (rarely taken).
+template <int PER = 1>
 __device__ __forceinline__ bool yukawa_in_exact(const DevParams& P, const SPos& sp, double tx, double ty) {
     double dx, dy;
-    exact_disp(P, tx, ty, (double)sp.x + (double)sp.xlo, (double)sp.y + (double)sp.ylo, dx, dy);
+    exact_disp<PER>(P, tx, ty, (double)sp.x + (double)sp.xlo, (double)sp.y + (double)sp.ylo, dx, dy);
     return dx * dx + dy * dy < P.yukCutSqD;
 }
 
+template <int PER = 1>
 __device__ __forceinline__ bool yukawa_in(const DevParams& P, float rx, float ry, const SPos& sp, const Tgt& t) {
     if (!P.yukOn) return false;
     const float rr = __fmaf_rn(rx, rx, ry * ry);
     const float cut = P.yukCutSq;
     if (fabsf(rr - cut) > 1e-6f * cut) return rr < cut;
-    return yukawa_in_exact(P, sp, t.xd(), t.yd());
+    return yukawa_in_exact<PER>(P, sp, t.xd(), t.yd());
 }
 
-// Displacement with the topology class fixed at compile time: PER false is
-// the open box (no wrap code at all), PER true the runtime periodic case.
-template <bool PER>
+// Displacement with the topology class fixed at compile time (PER as for
+// exact_disp): no wrap code for the open box, the torus wrap alone for the
+// torus, the run-time choice otherwise.
+template <int PER>
 __device__ __forceinline__ void displacement_p(const DevParams& P, float ox, float oy, float sx, float sx_lo,
                                                float sy, float sy_lo, float& rx, float& ry) {
-    if (!PER) {
+    if (PER == 0) {
         rx = __fadd_rn(__fsub_rn(sx, ox), sx_lo);
         ry = __fadd_rn(__fsub_rn(sy, oy), sy_lo);
+    } else if (PER == 2) {
+        rx = wrap_axis_comp(sx, ox, sx_lo, P.W, P.W_lo, P.halfW);
+        ry = wrap_axis_comp(sy, oy, sy_lo, P.H, P.H_lo, P.halfH);
     } else {
         displacement(P, ox, oy, sx, sx_lo, sy, sy_lo, rx, ry);
     }
@@ -762,7 +774,7 @@ __device__ __forceinline__ int warp_max_i(int v) {
     return v;
 }
 
-template <bool MAGGM, bool REL, bool BRK, bool PER, class ACC, class WS>
+template <bool MAGGM, bool REL, bool BRK, int PER, class ACC, class WS>
 __device__ __forceinline__ void eval_entry(const DevParams& P, const DevState& S, const ForceCtx& C,
                                            const float* s_age, const float* s_segdt, const WS& W,
                                            int e, const Tgt& t, ACC& A, unsigned& inter, bool pe) {
@@ -799,12 +811,12 @@ __device__ __forceinline__ void eval_entry(const DevParams& P, const DevState& S
     } else {
         displacement_p<PER>(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
     }
-    const bool yk = yukawa_in(P, rx, ry, sp, t);
+    const bool yk = yukawa_in<PER>(P, rx, ry, sp, t);
     pair_force<MAGGM, BRK>(P, t, rx, ry, svx, svy, a.z, a.w, sAng, sMu, sL, dl, yk, pe, A);
     inter++;
 }
 
-template <bool MAGGM, bool REL, bool BRK, bool PER, class ACC, class WS>
+template <bool MAGGM, bool REL, bool BRK, int PER, class ACC, class WS>
 __device__ __forceinline__ void flush_pool(const DevParams& P, const DevState& S, const ForceCtx& C,
                                            const float* s_age, const float* s_segdt, WS& W,
                                            int& nfull, int& lcnt, int& npool, const Tgt& t, ACC& A,
@@ -855,9 +867,10 @@ __device__ __forceinline__ void stage_point(const TreeBufs& T, WS& W, int e, int
 }
 
 // FP64 opening test (forces.js:680) inside the FP32 guard band (rarely taken).
+template <int PER = 1>
 __device__ __forceinline__ bool accept_exact(const DevParams& P, double tx, double ty, double sx, double sy, float lvl) {
     double dx, dy;
-    exact_disp(P, tx, ty, sx, sy, dx, dy);
+    exact_disp<PER>(P, tx, ty, sx, sy, dx, dy);
     const double size = 2.0 * ldexp(P.rootW, -(int)lvl);
     return size * size < P.thetaSqD * (dx * dx + dy * dy);
 }
@@ -883,18 +896,18 @@ __device__ __forceinline__ void list_entries(WS& W, unsigned m, unsigned active,
 // compensated sums, group box and node counts in shared memory and runs six
 // CTAs per SM (80 registers; the periodic form spills 32 bytes there and is
 // still 2 % faster than at five); the other forms keep them in registers.
-template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
 __host__ __device__ constexpr bool wc_six() { return !MAGGM && !REL && !BRK && NOPE; }
 // The walks with dipole / 1PN terms and without breakdown rows take the same
 // shared-memory form and run four CTAs per SM instead of three (torus
 // N = 65,536 with the full force set: 12 % faster).  The relativistic walk
 // without them keeps the register form: on small systems, which a single
 // wave covers, the shared-memory form only adds work (N = 2,048: 6 % slower).
-template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
 __host__ __device__ constexpr bool wc_four() { return MAGGM && !BRK; }
-template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
 __host__ __device__ constexpr bool wc_sh() { return wc_six<MAGGM, REL, BRK, PER, NOPE>() || wc_four<MAGGM, REL, BRK, PER, NOPE>(); }
-template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
 __host__ __device__ constexpr int wc_min_blocks() {
     return wc_six<MAGGM, REL, BRK, PER, NOPE>() ? 6 : wc_four<MAGGM, REL, BRK, PER, NOPE>() ? 4 : (MAGGM || REL || BRK) ? 3 : 5;
 }
@@ -909,7 +922,7 @@ __host__ __device__ constexpr int wc_min_blocks() {
 // sums are then added in warp order by warp 0, which writes the target.
 // The interaction list of every target is the one of the plain walk; only
 // the order of the sums differs.
-template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE, bool EMIT, int SPLIT = 1>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, bool EMIT, int SPLIT = 1>
 __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S, const TreeBufs& T,
                                            const int* d_root, FrameCtl* ctl, const ForceCtx& C, int vb) {
     static_assert(SPLIT == 1 || (SPLIT == WC_WARPS && !EMIT), "split walk: one group per CTA, no records");
@@ -1025,7 +1038,7 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
                 const float rhs = P.thetaSq * __fmaf_rn(rx, rx, ry * ry);
                 accept = s2 < rhs;
                 if (fabsf(rhs - s2) <= 1e-6f * s2)
-                    accept = accept_exact(P, t.xd(), t.yd(), (double)cx + (double)clx, (double)cy + (double)cly, lvl);
+                    accept = accept_exact<PER>(P, t.xd(), t.yd(), (double)cx + (double)clx, (double)cy + (double)cly, lvl);
             }
             const unsigned acc = __ballot_sync(0xffffffffu, accept);
             if ((int)lane == jj) { myAcc = acc & msk; myOpen = msk & ~acc; }
@@ -1168,7 +1181,7 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
     finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter, sysId);
 }
 
-template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE = false, bool EMIT = false>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE = false, bool EMIT = false>
 __global__ void __launch_bounds__(WC_THREADS, wc_min_blocks<MAGGM, REL, BRK, PER, NOPE>())
 walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
     walkc_body<MAGGM, REL, BRK, PER, NOPE, EMIT>(P, S, T, d_root, ctl, C, blockIdx.x);
@@ -1177,7 +1190,7 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
 // Dynamic shared memory of one walk CTA: accumulator rows (six-CTA form),
 // the four warps' stacks and source pools, and the history tables when
 // relativity is on.
-template <bool MAGGM, bool REL, bool BRK, bool PER, bool NOPE>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
 constexpr size_t wc_smem_bytes() {
     constexpr bool SHF = wc_sh<MAGGM, REL, BRK, PER, NOPE>();
     return Acc<MAGGM, BRK, SHF>::SH_BYTES + sizeof(WcSmem<MAGGM || REL, SHF ? WC_POOL_SHF : WC_POOL_WIDE>) * WC_WARPS +
