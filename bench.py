@@ -407,6 +407,14 @@ def run_learned(args, g, wl, idx, fx, fy, stream):
             "sweep": {str(k): v for k, v in sweep.items()}}
 
 
+def tune_name(m: dict) -> str:
+    """One autotuner candidate as text: execution, walk, warps per group, CTA cap."""
+    walk = "simple walk" if m["simple_walk"] else (
+        "grouped walk" if m["warps_per_group"] == 1 else f"split walk (4 warps per group, level {m['split_level']})")
+    cap = f", <= {m['ctas_per_sm']} CTAs/SM" if m["ctas_per_sm"] else ""
+    return ("graph" if m["use_graph"] else "launches") + ", " + walk + cap
+
+
 def run_ensemble(args):
     """Batched ensemble: 512 independent systems (N log-uniform in
     [256, 16384], one Gaussian cluster each, gravity + Coulomb, torus,
@@ -444,10 +452,9 @@ def run_ensemble(args):
     batched = {"value": nsys * args.ensemble_frames / total, "frames": args.ensemble_frames,
                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                "particle_substeps_per_s": prof["particle_substeps"] / total,
-               "mode": {0: "launches, grouped walk", 1: "graph, grouped walk", 2: "launches, simple walk",
-                        3: "graph, simple walk"}[choice],
-               "autotune_ms_per_frame": {"launches+grouped": tune_ms[0], "graph+grouped": tune_ms[1],
-                                         "launches+simple": tune_ms[2], "graph+simple": tune_ms[3]},
+               "mode": tune_name(BatchSystem.tune_mode(choice)),
+               "autotune_ms_per_frame": {tune_name(BatchSystem.tune_mode(m)): float(tune_ms[m])
+                                         for m in range(len(tune_ms))},
                "gpu_launches_per_frame": launches / args.ensemble_frames,
                "substeps_last_frame": {"min": int(steps.min()), "max": int(steps.max()),
                                        "mean": float(steps.mean())}}

@@ -79,6 +79,9 @@ struct Batch {
     double* dt_h = nullptr;         // pinned frame dt
     SysPlan* plan_h = nullptr;      // pinned copy of dev.plan
     int use_graph = 1;
+    int walk_split = 0;             // walk shape (geon_batch_set_shape): four warps per group
+    int split_level = 6;
+    int walk_ctas = 0;              // resident walk CTAs per SM (0: as many as fit)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     long long graph_head = 0, graph_body = 0, graph_tail = 0;   // kernels per part of the graph
@@ -2164,6 +2167,9 @@ static ForceCtx batch_ctx(GeonHandle* h, bool all) {
     C.sys_dt = all ? nullptr : B.dev.sys_dt;
     C.sys_accel = B.dev.sys_accel;
     C.sys_cyc = B.dev.sys_cyc;
+    C.walk_split = B.walk_split;
+    C.split_level = B.split_level;
+    C.walk_ctas = B.walk_ctas;
     return C;
 }
 
@@ -2439,6 +2445,43 @@ int geon_batch_set_mode(GeonHandle* h, int32_t use_graph, int32_t simple_walk) {
     return GEON_OK;
 }
 
+int geon_batch_set_shape(GeonHandle* h, int32_t warps_per_group, int32_t split_level, int32_t ctas_per_sm) {
+    if (!h) return GEON_ERR_ARG;
+    if (!h->batch) return set_err(h, GEON_ERR_ARG, "not a batched handle");
+    if ((warps_per_group != 1 && warps_per_group != 4) || split_level < 0 || split_level > KEY_LEVELS ||
+        ctas_per_sm < 0 || ctas_per_sm > 32)
+        return set_err(h, GEON_ERR_ARG, "walk shape: warps_per_group 1 or 4, split_level 0..31, ctas_per_sm 0..32");
+    Batch& B = *h->batch;
+    B.walk_split = warps_per_group == 4 ? 1 : 0;
+    B.split_level = split_level;
+    B.walk_ctas = ctas_per_sm;
+    batch_drop_graph(B);
+    return GEON_OK;
+}
+
+// The autotuner's candidates: use_graph, simple_walk, warps per group, split
+// level, walk CTAs per SM.  0-3 are the graph / launch and grouped / simple
+// modes; 4-6 cap the grouped walk's resident CTAs; 7-9 split each group's
+// walk over four warps at three depths.
+static const int32_t TUNE_MODES[GEON_BATCH_TUNE_MODES][5] = {
+    { 0, 0, 1, 6, 0 }, { 1, 0, 1, 6, 0 }, { 0, 1, 1, 6, 0 }, { 1, 1, 1, 6, 0 },
+    { 1, 0, 1, 6, 5 }, { 1, 0, 1, 6, 4 }, { 1, 0, 1, 6, 3 },
+    { 1, 0, 4, 4, 0 }, { 1, 0, 4, 6, 0 }, { 1, 0, 4, 8, 0 },
+};
+
+int geon_batch_tune_mode(int32_t mode, int32_t* desc) {
+    if (mode < 0 || mode >= GEON_BATCH_TUNE_MODES || !desc) return GEON_ERR_ARG;
+    for (int k = 0; k < 5; k++) desc[k] = TUNE_MODES[mode][k];
+    return GEON_OK;
+}
+
+static int batch_apply_mode(GeonHandle* h, int c) {
+    const int32_t* m = TUNE_MODES[c];
+    int r = geon_batch_set_mode(h, m[0], m[1]);
+    if (!r) r = geon_batch_set_shape(h, m[2], m[3], m[4]);
+    return r;
+}
+
 int geon_batch_autotune(GeonHandle* h, double dt, int32_t frames, int32_t* choice, double* ms_per_frame) {
     if (!h || frames < 1 || !(dt >= 0)) return GEON_ERR_ARG;
     if (!h->batch) return set_err(h, GEON_ERR_ARG, "not a batched handle");
@@ -2451,8 +2494,8 @@ int geon_batch_autotune(GeonHandle* h, double dt, int32_t frames, int32_t* choic
     cudaEvent_t a = get_event(h), b = get_event(h);
     double best = 1e300;
     int bestc = 0;
-    for (int c = 0; c < 4; c++) {
-        r = geon_batch_set_mode(h, c & 1, (c >> 1) & 1);
+    for (int c = 0; c < GEON_BATCH_TUNE_MODES; c++) {
+        r = batch_apply_mode(h, c);
         if (r) break;
         r = batch_snapshot(h, false);
         if (r) break;
@@ -2473,7 +2516,7 @@ int geon_batch_autotune(GeonHandle* h, double dt, int32_t frames, int32_t* choic
     }
     h->ev_pool.push_back(a);
     h->ev_pool.push_back(b);
-    const int r2 = geon_batch_set_mode(h, bestc & 1, (bestc >> 1) & 1);
+    const int r2 = batch_apply_mode(h, bestc);
     const int r3 = batch_snapshot(h, false);
     h->simTime = t0;
     h->forcesInit = init0;

@@ -28,6 +28,16 @@
 
 namespace geon {
 
+// Shared memory of a walk launch: the kernel's own, or padded so that at most
+// C.walk_ctas CTAs fit an SM (228 KB of shared memory, 1 KB reserved per CTA).
+constexpr size_t WC_SMEM_LIMIT = 227 * 1024;
+static size_t walk_dyn_smem(size_t smem, const ForceCtx& C) {
+    if (C.walk_ctas <= 0) return smem;
+    const size_t per = (size_t)228 * 1024 / (size_t)C.walk_ctas;
+    const size_t want = per > 1024 ? per - 1024 : smem;
+    return std::min(std::max(smem, want), WC_SMEM_LIMIT);
+}
+
 template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE = false, bool EMIT = false>
 static void launch_walkc(int blocks, const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root,
                          FrameCtl* ctl, const ForceCtx& C, cudaStream_t st) {
@@ -35,10 +45,34 @@ static void launch_walkc(int blocks, const DevParams& P, const DevState& S, cons
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK, PER, NOPE, EMIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
+                             (int)WC_SMEM_LIMIT);
         attr = true;
     }
-    walkc_kernel<MAGGM, REL, BRK, PER, NOPE, EMIT><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+    walkc_kernel<MAGGM, REL, BRK, PER, NOPE, EMIT><<<blocks, WC_THREADS, walk_dyn_smem(smem, C), st>>>(P, S, T, d_root,
+                                                                                                     ctl, C);
+}
+
+// The split walk: one CTA per group of 32 targets, its four warps sharing the
+// group's subtrees (walkc_body with SPLIT = WC_WARPS).
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+__global__ void __launch_bounds__(WC_THREADS, wc_min_blocks<MAGGM, REL, BRK, PER, NOPE>())
+walkc_split_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
+    walkc_body<MAGGM, REL, BRK, PER, NOPE, false, WC_WARPS>(P, S, T, d_root, ctl, C, blockIdx.x);
+}
+
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+static void launch_walkc_split(int slots, const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root,
+                               FrameCtl* ctl, const ForceCtx& C, cudaStream_t st) {
+    constexpr size_t smem = wc_smem_bytes<MAGGM, REL, BRK, PER, NOPE>();
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(walkc_split_kernel<MAGGM, REL, BRK, PER, NOPE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)WC_SMEM_LIMIT);
+        attr = true;
+    }
+    const int blocks = std::max(1, (slots + 31) / 32);
+    walkc_split_kernel<MAGGM, REL, BRK, PER, NOPE><<<blocks, WC_THREADS, walk_dyn_smem(smem, C), st>>>(P, S, T, d_root,
+                                                                                                     ctl, C);
 }
 
 // ---- pairwise O(N^2) sum (forces.js:94-125) -------------------------------------------------
@@ -838,6 +872,10 @@ static void launch_force(bool bh, const DevParams& P, const DevState& S, const T
             // force set with relativity carry the torus wrap alone
             const bool torus = P.topology == GEON_TORUS;
             if constexpr (PLAIN) {
+                if (lean && C.walk_split && torus) {
+                    launch_walkc_split<false, false, false, 2, true>(slots, P, S, T, d_root, ctl, C, st);
+                    return;
+                }
                 if (lean) {
                     if (torus) launch_walkc<false, false, false, 2, true>(blocks, P, S, T, d_root, ctl, C, st);
                     else launch_walkc<false, false, false, 1, true>(blocks, P, S, T, d_root, ctl, C, st);
@@ -849,6 +887,12 @@ static void launch_force(bool bh, const DevParams& P, const DevState& S, const T
             }
             launch_walkc<MAGGM, REL, BRK, 1>(blocks, P, S, T, d_root, ctl, C, st);
         } else {
+            if constexpr (PLAIN) {
+                if (lean && C.walk_split) {
+                    launch_walkc_split<false, false, false, 0, true>(slots, P, S, T, d_root, ctl, C, st);
+                    return;
+                }
+            }
             if (lean) launch_walkc<MAGGM, REL, BRK, 0, PLAIN>(blocks, P, S, T, d_root, ctl, C, st);
             else launch_walkc<MAGGM, REL, BRK, 0>(blocks, P, S, T, d_root, ctl, C, st);
         }

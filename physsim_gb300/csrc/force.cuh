@@ -43,6 +43,11 @@ struct ForceCtx {
     // levels up to split_level are evaluated by one warp each (node index
     // modulo SPLIT), and a node at split_level is opened only by that warp
     int split_level;
+    // walk shape of the launch-per-phase force pass (batched handles): walk_split
+    // selects four warps per group of 32 targets (plain forces only), walk_ctas
+    // > 0 caps the resident walk CTAs per SM by padding their shared memory
+    int walk_split;
+    int walk_ctas;
 };
 
 // How the pairwise sum over n_cap targets is split: the number of source

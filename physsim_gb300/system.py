@@ -351,10 +351,23 @@ class BatchSystem(GeonSystem):
     def set_mode(self, use_graph: bool = True, simple_walk: bool = False):
         self._ck(self.lib.geon_batch_set_mode(self._h, int(use_graph), int(simple_walk)))
 
+    def set_shape(self, warps_per_group: int = 1, split_level: int = 6, ctas_per_sm: int = 0):
+        self._ck(self.lib.geon_batch_set_shape(self._h, int(warps_per_group), int(split_level), int(ctas_per_sm)))
+
+    @staticmethod
+    def tune_mode(mode: int) -> dict:
+        """Candidate `mode` of autotune: graph, simple walk, warps per group, split level, CTAs per SM."""
+        d = (C.c_int32 * 5)()
+        lib = N.load()
+        N.check(lib, None, lib.geon_batch_tune_mode(int(mode), d))
+        return {"use_graph": bool(d[0]), "simple_walk": bool(d[1]), "warps_per_group": int(d[2]),
+                "split_level": int(d[3]), "ctas_per_sm": int(d[4])}
+
     def autotune(self, dt: float, frames: int = 2) -> tuple:
-        """Times the four modes, keeps the fastest; returns (choice, ms per frame of each)."""
+        """Times every candidate mode (tune_mode), keeps the fastest; returns
+        (choice, ms per frame of each)."""
         ch = C.c_int32()
-        ms = np.zeros(4, dtype=np.float64)
+        ms = np.zeros(N.BATCH_TUNE_MODES, dtype=np.float64)
         self._ck(self.lib.geon_batch_autotune(self._h, float(dt), int(frames), C.byref(ch),
                                               ms.ctypes.data_as(C.POINTER(C.c_double))))
         return ch.value, ms

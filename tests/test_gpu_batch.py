@@ -120,11 +120,12 @@ def test_autotune_restores_state_and_keeps_results(gpu_lib):
     ref.close()
     b = batch_of(wl)
     choice, ms = b.autotune(wl.dt, frames=1)
-    assert 0 <= choice < 4 and np.all(ms > 0)
+    assert 0 <= choice < N.BATCH_TUNE_MODES and np.all(ms > 0)
     st0 = b.state(f64=True)
     for k in ("x", "y", "wx", "wy"):
         np.testing.assert_array_equal(st0[k], wl.state[k].astype(np.float32).astype(np.float64))
-    b.set_mode(use_graph=bool(choice & 1), simple_walk=False)
+    b.set_mode(use_graph=BatchSystem.tune_mode(choice)["use_graph"], simple_walk=False)
+    b.set_shape(1, 6, 0)
     b.update(wl.dt)
     b.update(wl.dt)
     got = b.state(f64=True)
@@ -143,3 +144,27 @@ def test_batched_rejects_unsupported(gpu_lib):
     with pytest.raises(N.GeonError):
         b.set_params(p)
     b.close()
+
+
+@pytest.mark.parametrize("warps,ctas", [(1, 3), (4, 0)])
+def test_walk_shapes(gpu_lib, warps, ctas):
+    """The walk shapes the autotuner searches: a cap on resident walk CTAs runs
+    the same code (bit-identical frames); four warps per group of targets
+    change only the order of each target's sums (1e-6)."""
+    wl = small_ensemble(seed=46, n=10, lo=64, hi=3000)
+    ref = batch_of(wl)
+    b = batch_of(wl)
+    b.set_shape(warps, 6, ctas)
+    try:
+        for _ in range(2):
+            assert np.array_equal(ref.update(wl.dt), b.update(wl.dt))
+        sr, sb = ref.state(f64=True), b.state(f64=True)
+    finally:
+        ref.close()
+        b.close()
+    for k in ("x", "y", "wx", "wy"):
+        if warps == 1:
+            np.testing.assert_array_equal(sb[k], sr[k])
+        else:
+            d = np.linalg.norm(sb[k] - sr[k]) / max(np.linalg.norm(sr[k]), 1e-30)
+            assert d <= 1e-6, (k, d)
