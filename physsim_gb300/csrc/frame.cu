@@ -25,7 +25,7 @@
 
 namespace geon {
 
-constexpr int FR_THREADS = WC_THREADS;   // one walk CTA per block: four warps on one group of 32 targets
+constexpr int FR_THREADS = 2 * WC_THREADS;   // one block per group of 32 targets: its eight warps share the walk
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
@@ -133,8 +133,8 @@ __device__ __forceinline__ int count_below(const uint64_t* sk, int lo, int hi, u
 // Stable sort of the n keys by rank: point p goes to slot
 // #{q : key_q < key_p} + #{q < p : key_q == key_p}, the order of a stable
 // radix sort of (key, p) pairs.  Chunks of 32 keys go to the blocks in turn;
-// a block's four warps rank the chunk against a quarter of all keys each
-// (held in shared memory) and warp 0 adds the four counts.
+// a block's warps rank the chunk against an equal share of all keys each
+// (held in shared memory) and warp 0 adds their counts.
 __device__ __forceinline__ void rank_sort(const uint64_t* keys, uint64_t* okeys, uint32_t* ovals, int n, int b, int G,
                                           int (*s_part)[32]) {
     const int nch = (n + 31) / 32;
@@ -310,7 +310,7 @@ frame_kernel(DevParams P, DevState S, DevState S2, TreeBufs T, int* d_root, Fram
     }
 }
 
-// One block per group of 32 targets: the walk's four warps share a group.
+// One block per group of 32 targets: the walk's eight warps share a group.
 int frame_blocks(int n) {
     return std::max(1, std::min((n + 31) / 32, FRAME_MAX_POINTS / 32));
 }
@@ -319,7 +319,7 @@ template <bool REL>
 static cudaError_t launch_frame_t(const DevParams& P, const DevState& S, const DevState& S2, const TreeBufs& T,
                                   int* d_root, FrameCtl* ctl, const ForceCtx& C, const FrameArgs& A, FrameRun* run,
                                   int n, cudaStream_t st, LaunchCounter& lc) {
-    constexpr size_t walk_smem = wc_smem_bytes<false, REL, false, false, true>();
+    constexpr size_t walk_smem = wc_smem_bytes<false, REL, false, false, true, FR_THREADS / 32>();
     constexpr size_t sort_smem = (size_t)FRAME_MAX_POINTS * sizeof(uint64_t);
     constexpr size_t smem = walk_smem > sort_smem ? walk_smem : sort_smem;
     static_assert(smem <= 200 * 1024, "frame kernel shared memory");

@@ -914,8 +914,9 @@ __host__ __device__ constexpr int wc_min_blocks() {
 
 // One CTA of the walk: warps vb * WC_WARPS .. + WC_WARPS - 1 of the target
 // order, with WC_THREADS threads and wc_smem_bytes() of dynamic shared memory.
-// SPLIT == WC_WARPS: the CTA's four warps walk the same group vb of 32
-// targets.  Every warp descends the levels above C.split_level; a node at
+// SPLIT > 1 (WC_WARPS, or 2 WC_WARPS in a CTA of that many warps, whose
+// accumulators then stay in registers): the CTA's SPLIT warps walk the same
+// group vb of 32 targets.  Every warp descends the levels above C.split_level; a node at
 // or above it is evaluated (aggregate or leaf points) only by warp
 // (index mod SPLIT), and a node at split_level is opened only by that warp,
 // so each subtree below it is walked once.  The warps' compensated partial
@@ -925,14 +926,17 @@ __host__ __device__ constexpr int wc_min_blocks() {
 template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, bool EMIT, int SPLIT = 1>
 __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S, const TreeBufs& T,
                                            const int* d_root, FrameCtl* ctl, const ForceCtx& C, int vb) {
-    static_assert(SPLIT == 1 || (SPLIT == WC_WARPS && !EMIT), "split walk: one group per CTA, no records");
+    static_assert(SPLIT == 1 || ((SPLIT == WC_WARPS || SPLIT == 2 * WC_WARPS) && !EMIT),
+                  "split walk: one group per CTA of SPLIT warps, no records");
     constexpr bool NEEDC = MAGGM || REL;
-    constexpr bool SHF = wc_sh<MAGGM, REL, BRK, PER, NOPE>();   // shared-memory form (six or four CTAs per SM)
+    constexpr int NWARPS = SPLIT > WC_WARPS ? SPLIT : WC_WARPS;         // warps of the CTA
+    // shared-memory form (six or four CTAs per SM); its rows hold ACC_SH_THREADS columns
+    constexpr bool SHF = NWARPS == WC_WARPS && wc_sh<MAGGM, REL, BRK, PER, NOPE>();
     using AccT = Acc<MAGGM, BRK, SHF>;
     using WS = WcSmem<NEEDC, SHF ? WC_POOL_SHF : WC_POOL_WIDE>;
     unsigned char* wc_smem = geon_dsmem + AccT::SH_BYTES;
     WS* Wall = reinterpret_cast<WS*>(wc_smem);
-    float* s_age = reinterpret_cast<float*>(Wall + WC_WARPS);
+    float* s_age = reinterpret_cast<float*>(Wall + NWARPS);
     float* s_segdt = s_age + HIST_LEN;
     if (REL) load_hist_tables(C, s_age, s_segdt);
     const int warp = threadIdx.x >> 5;
@@ -1190,10 +1194,10 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
 // Dynamic shared memory of one walk CTA: accumulator rows (six-CTA form),
 // the four warps' stacks and source pools, and the history tables when
 // relativity is on.
-template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, int NWARPS = WC_WARPS>
 constexpr size_t wc_smem_bytes() {
-    constexpr bool SHF = wc_sh<MAGGM, REL, BRK, PER, NOPE>();
-    return Acc<MAGGM, BRK, SHF>::SH_BYTES + sizeof(WcSmem<MAGGM || REL, SHF ? WC_POOL_SHF : WC_POOL_WIDE>) * WC_WARPS +
+    constexpr bool SHF = NWARPS == WC_WARPS && wc_sh<MAGGM, REL, BRK, PER, NOPE>();
+    return Acc<MAGGM, BRK, SHF>::SH_BYTES + sizeof(WcSmem<MAGGM || REL, SHF ? WC_POOL_SHF : WC_POOL_WIDE>) * NWARPS +
            (REL ? 2 * HIST_LEN * sizeof(float) : 0);
 }
 static_assert(6 * (wc_smem_bytes<false, false, false, false, true>() + 1024) <= 228 * 1024,
