@@ -183,3 +183,32 @@ def test_yukawa_cutoff_tie(gpu_lib, d, inside, bh):
         assert abs(fx - expect) <= 1e-5 * abs(expect), (fx, expect)
     else:
         assert fx == 0.0
+
+
+@pytest.mark.parametrize("dt,max_sub", [(0.0, 32), (2.0, 2), (2.0, 32)])
+def test_frame_kernel_edge_frames(gpu_lib, dt, max_sub):
+    """A zero-length frame (no substep: history and boundary only), a frame
+    cut short by the substep cap, and a long frame of several substeps: the
+    one-launch frame takes the same substeps as the split path and ends in
+    the same state."""
+    wl = W.small_disk(1024, relativity=True, softening=0.1)
+    wl.params.max_substeps = max_sub
+    a, b = make(wl), make(wl, split=True)
+    try:
+        a.update(1 / 60)
+        b.update(1 / 60)                     # bootstrap forces and one ordinary frame first
+        for _ in range(3 if dt == 0.0 else 1):
+            sa, sb = a.update(dt), b.update(dt)
+            assert sa == sb, (sa, sb)
+            if dt == 0.0:
+                assert sa == 0
+            elif max_sub == 2:
+                assert sa == 2
+            else:
+                assert sa > 2
+        assert a.count() == b.count()
+        assert_close(a.state(f64=True), b.state(f64=True))
+        assert a.stats()["sim_time"] == b.stats()["sim_time"]
+    finally:
+        a.close()
+        b.close()
