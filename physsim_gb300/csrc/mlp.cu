@@ -341,13 +341,16 @@ mlp_forward_kernel(const float* __restrict__ W, const float* __restrict__ X, int
 // lane adds V + J (x - g), the exact analytic term for wide groups, and the
 // Yukawa swap near the cutoff.  A warp owns its targets' forces, so the
 // result does not depend on timing.
-// Record layout of phase A's output, 4 float4:
-//   compact group: Gm.v, Gm.j, Ec.v, Ec.j (12 floats), then the COM as
-//                  (hi x, hi y, lo x, lo y);
-//   wide group:    (M, Ixx, Ixy, Iyy), (Dx, Dy, -, -), -, then the COM;
+// Record layout of phase A's output: 3 float4 per record (48 bytes, so a
+// warp's records fill whole sectors),
+//   compact group: Gm.v, Gm.j, Ec.v, Ec.j (12 floats);
+//   wide group:    (M, Ixx, Ixy, Iyy), (Dx, Dy, -, -), -;
+// then, in a second region of one float4 per record written only for wide
+// groups and records near the cutoff, the COM as (hi x, hi y, lo x, lo y);
 // plus the cell mass for the Yukawa swap and the flags (uint32, mass as a
-// float in the upper word of a uint2).
-constexpr int EXP_FLOATS = 16;
+// float in the upper word of a uint2).  The buffer holds total x 16 floats:
+// the expansions at expo, the COMs at expo + 3 total.
+constexpr int EXP_F4 = 3;
 
 // Largest g with off[g] <= e (off: exclusive prefix of the groups' counts).
 __device__ __forceinline__ int group_of(const int* __restrict__ off, int ngroups, int e) {
@@ -368,7 +371,8 @@ constexpr int LG_WARPS = LG_THREADS / 32;
 __global__ void __launch_bounds__(LG_THREADS)
 learn_geo_kernel(DevParams P, TreeBufs T, const uint2* __restrict__ recs, const int* __restrict__ rec_cnt,
                  const float4* __restrict__ gcen, int rec_cap, const int* __restrict__ off, int ngroups,
-                 float4* __restrict__ expo, uint2* __restrict__ flags, int* __restrict__ net_list, int* __restrict__ net_count) {
+                 float4* __restrict__ expo, float4* __restrict__ cms, uint2* __restrict__ flags, int* __restrict__ net_list,
+                 int* __restrict__ net_count) {
     const int lane = threadIdx.x & 31;
     // one warp per group: its records r = lane, lane + 32, ...
     for (int g = blockIdx.x * LG_WARPS + (threadIdx.x >> 5); g < ngroups; g += gridDim.x * LG_WARPS) {
@@ -386,7 +390,7 @@ learn_geo_kernel(DevParams P, TreeBufs T, const uint2* __restrict__ recs, const 
                 float f[LF];
                 record_geo(P, T, (int)rc.x, gc.x, gc.y, R, f);
                 fl = record_flags(P, R, gc.z);
-                float4* o = expo + (size_t)e * (EXP_FLOATS / 4);
+                float4* o = expo + (size_t)e * EXP_F4;
                 if (fl & REC_EXACT) {
                     // wide groups: no expansion (phase B takes the analytic term per target)
                     o[0] = make_float4(R.M, R.ixx, R.ixy, R.iyy);
@@ -400,7 +404,7 @@ learn_geo_kernel(DevParams P, TreeBufs T, const uint2* __restrict__ recs, const 
                 }
                 if (fl & (REC_EXACT | REC_NEAR_CUT)) {
                     const float4 na = T.int_a[rc.x], nc = T.int_c[rc.x];
-                    o[3] = make_float4(na.x, na.y, nc.x, nc.y);
+                    cms[e] = make_float4(na.x, na.y, nc.x, nc.y);
                 }
                 flags[e] = make_uint2(fl, __float_as_uint(R.M));
             }
@@ -462,7 +466,7 @@ learn_net_kernel(DevParams P, TreeBufs T, const float* __restrict__ W, const uin
             ok = tile_forward(s, phase, ok, y);
         }
         if (live && ok) {
-            float4* o = expo + (size_t)e * (EXP_FLOATS / 4);
+            float4* o = expo + (size_t)e * EXP_F4;
             const float4 a0 = o[0], a1 = o[1];
             Lin Gm{ { a0.x, a0.y }, { a0.z, a0.w, a1.x, a1.y } };
             add_net_expansion(R, y, Gm);
@@ -508,7 +512,7 @@ constexpr int LA_WARPS = LA_THREADS / 32;
 __global__ void __launch_bounds__(LA_THREADS)
 learn_apply_kernel(DevParams P, DevState S, TreeBufs T, const FrameCtl* __restrict__ ctl, const uint2* __restrict__ recs,
                    const int* __restrict__ rec_cnt, const float4* __restrict__ gcen, int rec_cap, const int* __restrict__ off,
-                   const float4* __restrict__ expo, const uint2* __restrict__ flags) {
+                   const float4* __restrict__ expo, const float4* __restrict__ cms, const uint2* __restrict__ flags) {
     __shared__ float4 st[LA_WARPS][32][5];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int n = ctl->n;
@@ -537,7 +541,7 @@ learn_apply_kernel(DevParams P, DevState S, TreeBufs T, const FrameCtl* __restri
             const int r = c0 + lane;
             uint32_t mask = 0u;
             uint2 fm = make_uint2(0u, 0u);
-            const float4* o = expo + (size_t)(base + r) * (EXP_FLOATS / 4);
+            const float4* o = expo + (size_t)(base + r) * EXP_F4;
             if (r < cnt) {
                 mask = recs[(size_t)g * rec_cap + r].y;
                 fm = flags[base + r];
@@ -557,7 +561,7 @@ learn_apply_kernel(DevParams P, DevState S, TreeBufs T, const FrameCtl* __restri
                 st[w][q][0] = o[0];
                 st[w][q][1] = o[1];
                 st[w][q][2] = o[2];
-                if (fm.x & (REC_EXACT | REC_NEAR_CUT)) st[w][q][3] = o[3];
+                if (fm.x & (REC_EXACT | REC_NEAR_CUT)) st[w][q][3] = cms[base + r];
                 st[w][q][4] = make_float4(__uint_as_float(mask), __uint_as_float(fm.x), __uint_as_float(fm.y), 0.f);
             }
             __syncwarp();
@@ -855,8 +859,8 @@ void learn_correct(const DevParams& P, const DevState& S, const TreeBufs& T, con
     if (total > 0) {
         cudaMemsetAsync(net_count, 0, sizeof(int), st);
         const int gblocks = std::max(1, std::min((ngroups + LG_WARPS - 1) / LG_WARPS, sm_count() * 8));
-        learn_geo_kernel<<<gblocks, LG_THREADS, 0, st>>>(P, T, recs, rec_cnt, gcen, rec_cap, off, ngroups, expo, flags,
-                                                         net_list, net_count);
+        learn_geo_kernel<<<gblocks, LG_THREADS, 0, st>>>(P, T, recs, rec_cnt, gcen, rec_cap, off, ngroups, expo,
+                                                         expo + (size_t)EXP_F4 * total, flags, net_list, net_count);
         // the network's CTAs: enough for every listed record (the count is read on the device)
         const int tiles = (total + MT - 1) / MT;
         const int blocks = std::max(1, std::min(tiles, sm_count() * 6));
@@ -867,7 +871,8 @@ void learn_correct(const DevParams& P, const DevState& S, const TreeBufs& T, con
         lc.add(2);
     }
     const int blocks = std::max(1, std::min((ngroups + LA_WARPS - 1) / LA_WARPS, sm_count() * 8));
-    learn_apply_kernel<<<blocks, LA_THREADS, 0, st>>>(P, S, T, ctl, recs, rec_cnt, gcen, rec_cap, off, expo, flags);
+    learn_apply_kernel<<<blocks, LA_THREADS, 0, st>>>(P, S, T, ctl, recs, rec_cnt, gcen, rec_cap, off, expo,
+                                                      expo + (size_t)EXP_F4 * std::max(total, 0), flags);
     lc.add(1);
 }
 
