@@ -1690,7 +1690,10 @@ static bool frame_eligible(const GeonHandle* h) {
 }
 
 // geon_update through the frame kernel: one launch, then one read of the
-// control block and the frame's results.
+// control block and the frame's results.  FRAME_NOT_LAUNCHED (positive) when
+// the device cannot hold the cooperative grid: the caller then runs the frame
+// on the launch-per-phase path.
+constexpr int FRAME_NOT_LAUNCHED = 1;
 static int frame_update(GeonHandle* h, double dt, int32_t* substeps) {
     int r = ensure_tree(h);
     if (r) return r;
@@ -1730,6 +1733,10 @@ static int frame_update(GeonHandle* h, double dt, int32_t* substeps) {
     // duplicated top of the walk grows)
     C.split_level = 8;
     const cudaError_t e = frame_launch(rel, h->P, h->S, h->S2, h->T, h->d_root, h->ctl, C, A, h->frun, h->n, h->st, h->lc);
+    if (e == cudaErrorCooperativeLaunchTooLarge || e == cudaErrorNotSupported) {
+        cudaGetLastError();                   // nothing was launched: this device takes the launch-per-phase path
+        return FRAME_NOT_LAUNCHED;
+    }
     if (e != cudaSuccess) return cuda_check(h, e, "frame kernel launch");
     CK(cudaMemcpyAsync(h->frun_h, h->frun, sizeof(FrameRun), cudaMemcpyDeviceToHost, h->st));
     r = read_ctl(h);
@@ -1801,7 +1808,10 @@ int geon_update(GeonHandle* h, double dt, int32_t* substeps) {
         if (r) return r;
         h->forcesInit = true;
     }
-    if (frame_eligible(h)) return frame_update(h, dt, substeps);
+    if (frame_eligible(h)) {
+        r = frame_update(h, dt, substeps);
+        if (r != FRAME_NOT_LAUNCHED) return r;
+    }
     // frame-start planner scan (integrator.js:813-836)
     launch_frame_scan(h->P, h->S, h->ctl, h->n_cap, h->st, h->lc);
     CKL();
