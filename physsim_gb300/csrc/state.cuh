@@ -69,7 +69,7 @@ struct TreeBufs {
     // higher moments about each node's centre of mass (learned correction only; null otherwise)
     float4* int_m1; float4* int_m2; float4* int_m3;    // (Ixx, Ixy, Iyy, sum|q|), (Dx, Dy, Jxx, Jxy), (Jyy, -, -, -)
     float4* leaf_m1; float4* leaf_m2; float4* leaf_m3;
-    int mom_on;         // compute the moments in this build
+    int mom_on;         // compute the moments in this tree build
     int* roots;         // [nsys] root of each system (batched handles; null otherwise)
 };
 
