@@ -186,6 +186,8 @@ frame_kernel(DevParams P, DevState S, DevState S2, TreeBufs T, int* d_root, Fram
     T.sidx = T.idx_alt;
     auto sync = [&]() { return frame_barrier(R, expect, A.waitNs, ctl, &s_ok); };
     auto mark = [&](int i) { if (lead) R->stamp[i] = global_ns(); };
+    if (lead)
+        for (int i = 1; i < FRAME_STAMPS; i++) R->stamp[i] = 0ull;         // phases this frame does not reach stay 0
     mark(0);
 
     // frame start: planner maxima of the current forces
