@@ -325,19 +325,19 @@ static cudaError_t launch_frame_t(const DevParams& P, const DevState& S, const D
     constexpr size_t sort_smem = (size_t)FRAME_MAX_POINTS * sizeof(uint64_t);
     constexpr size_t smem = walk_smem > sort_smem ? walk_smem : sort_smem;
     static_assert(smem <= 200 * 1024, "frame kernel shared memory");
-    static int attr_dev = -1;
+    // per device: the shared-memory attribute and the resident blocks it allows
+    static int attr_dev = -1, per_sm = 0;
     int dev = 0;
     cudaGetDevice(&dev);
     if (attr_dev != dev) {
         cudaError_t e = cudaFuncSetAttribute(frame_kernel<REL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, frame_kernel<REL>, FR_THREADS, smem);
         if (e != cudaSuccess) return e;
         attr_dev = dev;
     }
     const int G = frame_blocks(n);
-    int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, frame_kernel<REL>, FR_THREADS, smem);
-    if (e != cudaSuccess) return e;
     if ((long long)per_sm * device_sms() < G) return cudaErrorCooperativeLaunchTooLarge;
+    cudaError_t e;
     DevParams p = P;
     DevState s = S, s2 = S2;
     TreeBufs t = T;
