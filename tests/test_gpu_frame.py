@@ -212,3 +212,22 @@ def test_frame_kernel_edge_frames(gpu_lib, dt, max_sub):
     finally:
         a.close()
         b.close()
+
+
+def test_frame_kernel_history_and_signal_delay(gpu_lib):
+    """Relativity samples the history every 64 frames, and the walk takes
+    signal-delayed sources once a particle has two samples: 140 frames of a
+    256-particle disk go through both inside the one-launch frame.  Same
+    substeps, counts and states as the split path."""
+    wl = W.small_disk(256, relativity=True, softening=8.0)
+    a, b = make(wl), make(wl, split=True)
+    try:
+        for f in range(140):
+            sa, sb = a.update(wl.dt), b.update(wl.dt)
+            assert sa == sb, (f, sa, sb)
+        assert a.count() == b.count()
+        assert_close(a.state(f64=True), b.state(f64=True))
+        assert a.stats()["sim_time"] == b.stats()["sim_time"]
+    finally:
+        a.close()
+        b.close()
