@@ -231,3 +231,23 @@ def test_frame_kernel_history_and_signal_delay(gpu_lib):
     finally:
         a.close()
         b.close()
+
+
+@pytest.mark.parametrize("path", ["frame", "split"])
+def test_planner_cyclotron_limit(gpu_lib, path):
+    """The cyclotron limit of the planner at an exact multiple (the case of
+    tests/test_oracle_kat.py): dt = 4 dtCyc takes 4 substeps, a dt one part
+    in 2^40 longer takes 5."""
+    bz = 50.25
+    dt4 = 4 * (0.7853981633974483 / bz)
+    fl = N.FLAG_SPLIT_FRAME if path == "split" else 0
+    p = N.make_params(toggles=N.GRAVITY | N.BARNES_HUT, flags=fl, softening=1.0, domain_w=1000, domain_h=1000,
+                      ext_bz=bz)
+    one = np.ones(1)
+    g_ = GeonSystem(p, 1)
+    try:
+        g_.upload_f64(np.array([500.0]), np.array([500.0]), 0 * one, 0 * one, one, one, 0 * one)
+        assert g_.update(dt4) == 4
+        assert g_.update(dt4 * (1 + 2.0 ** -40)) == 5
+    finally:
+        g_.close()

@@ -272,3 +272,18 @@ def test_yukawa_cutoff_tie(oracle_mod, d, inside):
         assert np.isclose(fx, yukawa_expect(d), rtol=1e-12, atol=0.0)
     else:
         assert fx == 0.0
+
+
+# integrator.js:866-869: the cyclotron limit dtCyc = (pi/4) / wc, wc = |q| |Bz| / m
+# (external Bz 50.25 on a unit charge and mass; no force, so dtSafe starts
+# at dtRemain).  dt = 4 dtCyc exactly (a power-of-two multiple): ceil gives 4;
+# one ulp-scale step longer gives 5.
+CYC_BZ = 50.25
+CYC_DT = 4 * (0.7853981633974483 / CYC_BZ)
+
+
+@pytest.mark.parametrize("dt,expect", [(CYC_DT, 4), (CYC_DT * (1 + 2.0 ** -40), 5)])
+def test_planner_cyclotron_limit(oracle_mod, dt, expect):
+    p = N.make_params(toggles=N.GRAVITY, softening=1.0, domain_w=1000, domain_h=1000, ext_bz=CYC_BZ)
+    o = sim(p, [500.0], [500.0], q=[1.0])
+    assert o.update(dt) == expect
