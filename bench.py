@@ -71,7 +71,8 @@ def parse():
     ap.add_argument("--learn-samples", type=int, default=4_000_000, help="resampled training records")
     ap.add_argument("--learn-steps", type=int, default=20000)
     ap.add_argument("--learn-batch", type=int, default=65536)
-    ap.add_argument("--learn-train-n", type=int, default=262144, help="particles of the training snapshot")
+    ap.add_argument("--learn-train-n", type=int, default=1 << 20,
+                    help="particles of the training snapshots (another seed of the same distribution)")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the other configurations (small disk, torus full force set, theta sweep)")
