@@ -41,8 +41,8 @@ UNIT = "particle-substeps/s"
 # tidal torque 16, Yukawa 16.
 FLOP_PER_INTERACTION_GCY = 58
 # DRAM bytes of one walk launch at N = 1M by theta (ncu captures of this workload;
-# at 0.2 the walk with record emission of the learned correction)
-WALK_TRAFFIC_BYTES = {0.1: 767.4e6, 0.2: 1409.2e6}
+# at 0.2 and 0.3 the walk with record emission of the learned correction)
+WALK_TRAFFIC_BYTES = {0.1: 767.4e6, 0.2: 1409.2e6, 0.3: 1043.5e6}
 # The theta the native arm's bisection finds for the seeded N = 1M disk (plain
 # Barnes-Hut RMS force error 8.3e-4 <= 1e-3); the reference arm runs the
 # same theta, since calibrating on the host cores would take hours.
