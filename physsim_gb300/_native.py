@@ -55,7 +55,7 @@ LEARN_OUTPUTS = 6
 LEARN_TARGETS = 18
 DIRECT_NOALLOC_MAX_K = 16384
 BATCH_MAX_SYSTEMS = 512
-BATCH_TUNE_MODES = 10
+BATCH_TUNE_MODES = 12
 
 OUT_ROWS = 25
 OUT_NAMES = ["fx", "fy", "Bz", "Bgz", "dBzdx", "dBzdy", "dBgzdx", "dBgzdy", "tidal", "frameDrag",
@@ -188,7 +188,7 @@ SIGNATURES = {
     "geon_batch_substeps": [_handle_t, _P(C.c_int32), C.c_int32],
     "geon_batch_set_mode": [_handle_t, C.c_int32, C.c_int32],
     "geon_batch_autotune": [_handle_t, C.c_double, C.c_int32, _P(C.c_int32), _P(C.c_double)],
-    "geon_batch_set_shape": [_handle_t, C.c_int32, C.c_int32, C.c_int32],
+    "geon_batch_set_shape": [_handle_t, C.c_int32, C.c_int32, C.c_int32, C.c_int32],
     "geon_batch_tune_mode": [C.c_int32, _P(C.c_int32)],
     "geon_heatmap": [_handle_t, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_uint32, C.c_int32,
                      _P(C.c_float), _P(C.c_float), _P(C.c_float)],

@@ -82,6 +82,8 @@ struct Batch {
     int walk_split = 0;             // walk shape (geon_batch_set_shape): four warps per group
     int split_level = 6;
     int walk_ctas = 0;              // resident walk CTAs per SM (0: as many as fit)
+    int walk_chunk = 0;             // > 0: persistent walk CTAs take this many walk blocks at a time
+    unsigned* walk_queue = nullptr; // [2] their counters (next block, CTAs done)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     long long graph_head = 0, graph_body = 0, graph_tail = 0;   // kernels per part of the graph
@@ -2180,6 +2182,8 @@ static ForceCtx batch_ctx(GeonHandle* h, bool all) {
     C.walk_split = B.walk_split;
     C.split_level = B.split_level;
     C.walk_ctas = B.walk_ctas;
+    C.walk_chunk = B.walk_chunk;
+    C.walk_queue = B.walk_queue;
     return C;
 }
 
@@ -2399,6 +2403,7 @@ int geon_create_batch(const GeonParams* params, int32_t n_systems, const int32_t
     DevArena& A = B->A;
     B->sys = A.alloc<int>(total);
     B->roots = A.alloc<int>(n_systems);
+    B->walk_queue = A.alloc<unsigned>(2);
     int* d_off = A.alloc<int>(n_systems + 1);
     int* d_pad = A.alloc<int>(n_systems);
     BatchDev& D = B->dev;
@@ -2427,6 +2432,7 @@ int geon_create_batch(const GeonParams* params, int32_t n_systems, const int32_t
     if (e == cudaSuccess) e = cudaMemset(D.plan, 0, (size_t)n_systems * sizeof(SysPlan));
     if (e == cudaSuccess) e = cudaMemset(D.sys_dt, 0, (size_t)n_systems * sizeof(double));
     if (e == cudaSuccess) e = cudaMemset(B->roots, 0xFF, (size_t)n_systems * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(B->walk_queue, 0, 2 * sizeof(unsigned));
     if (e != cudaSuccess) { g_err = std::string("batch setup: ") + cudaGetErrorString(e); geon_destroy(h); return GEON_ERR_CUDA; }
     h->S.sys = B->sys;
     h->S2.sys = B->sys;
@@ -2455,40 +2461,50 @@ int geon_batch_set_mode(GeonHandle* h, int32_t use_graph, int32_t simple_walk) {
     return GEON_OK;
 }
 
-int geon_batch_set_shape(GeonHandle* h, int32_t warps_per_group, int32_t split_level, int32_t ctas_per_sm) {
+int geon_batch_set_shape(GeonHandle* h, int32_t warps_per_group, int32_t split_level, int32_t ctas_per_sm,
+                         int32_t queue_chunk) {
     if (!h) return GEON_ERR_ARG;
     if (!h->batch) return set_err(h, GEON_ERR_ARG, "not a batched handle");
     if ((warps_per_group != 1 && warps_per_group != 4) || split_level < 0 || split_level > KEY_LEVELS ||
-        ctas_per_sm < 0 || ctas_per_sm > 32)
-        return set_err(h, GEON_ERR_ARG, "walk shape: warps_per_group 1 or 4, split_level 0..31, ctas_per_sm 0..32");
+        ctas_per_sm < 0 || ctas_per_sm > 32 || queue_chunk < 0 || queue_chunk > 4096)
+        return set_err(h, GEON_ERR_ARG, "walk shape: warps_per_group 1 or 4, split_level 0..31, ctas_per_sm 0..32, "
+                                        "queue_chunk 0..4096");
     Batch& B = *h->batch;
     B.walk_split = warps_per_group == 4 ? 1 : 0;
     B.split_level = split_level;
     B.walk_ctas = ctas_per_sm;
+    B.walk_chunk = queue_chunk;
+    if (queue_chunk > 0) {
+        walk_queue_setup();
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_check(h, e, "work-queue walk setup");
+    }
     batch_drop_graph(B);
     return GEON_OK;
 }
 
 // The autotuner's candidates: use_graph, simple_walk, warps per group, split
-// level, walk CTAs per SM.  0-3 are the graph / launch and grouped / simple
-// modes; 4-6 cap the grouped walk's resident CTAs; 7-9 split each group's
-// walk over four warps at three depths.
-static const int32_t TUNE_MODES[GEON_BATCH_TUNE_MODES][5] = {
-    { 0, 0, 1, 6, 0 }, { 1, 0, 1, 6, 0 }, { 0, 1, 1, 6, 0 }, { 1, 1, 1, 6, 0 },
-    { 1, 0, 1, 6, 5 }, { 1, 0, 1, 6, 4 }, { 1, 0, 1, 6, 3 },
-    { 1, 0, 4, 4, 0 }, { 1, 0, 4, 6, 0 }, { 1, 0, 4, 8, 0 },
+// level, walk CTAs per SM, work-queue chunk.  0-3 are the graph / launch and
+// grouped / simple modes; 4-6 cap the grouped walk's resident CTAs; 7-9 split
+// each group's walk over four warps at three depths; 10-11 run the grouped
+// walk as persistent CTAs taking 1 or 4 walk blocks at a time.
+static const int32_t TUNE_MODES[GEON_BATCH_TUNE_MODES][6] = {
+    { 0, 0, 1, 6, 0, 0 }, { 1, 0, 1, 6, 0, 0 }, { 0, 1, 1, 6, 0, 0 }, { 1, 1, 1, 6, 0, 0 },
+    { 1, 0, 1, 6, 5, 0 }, { 1, 0, 1, 6, 4, 0 }, { 1, 0, 1, 6, 3, 0 },
+    { 1, 0, 4, 4, 0, 0 }, { 1, 0, 4, 6, 0, 0 }, { 1, 0, 4, 8, 0, 0 },
+    { 1, 0, 1, 6, 0, 1 }, { 1, 0, 1, 6, 0, 4 },
 };
 
 int geon_batch_tune_mode(int32_t mode, int32_t* desc) {
     if (mode < 0 || mode >= GEON_BATCH_TUNE_MODES || !desc) return GEON_ERR_ARG;
-    for (int k = 0; k < 5; k++) desc[k] = TUNE_MODES[mode][k];
+    for (int k = 0; k < 6; k++) desc[k] = TUNE_MODES[mode][k];
     return GEON_OK;
 }
 
 static int batch_apply_mode(GeonHandle* h, int c) {
     const int32_t* m = TUNE_MODES[c];
     int r = geon_batch_set_mode(h, m[0], m[1]);
-    if (!r) r = geon_batch_set_shape(h, m[2], m[3], m[4]);
+    if (!r) r = geon_batch_set_shape(h, m[2], m[3], m[4], m[5]);
     return r;
 }
 

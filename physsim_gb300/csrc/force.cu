@@ -60,6 +60,72 @@ walkc_split_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ 
     walkc_body<MAGGM, REL, BRK, PER, NOPE, false, WC_WARPS>(P, S, T, d_root, ctl, C, blockIdx.x);
 }
 
+// The grouped walk from a work queue: persistent CTAs take walk blocks (four
+// groups of 32 targets each) C.walk_chunk at a time from C.walk_queue[0];
+// C.walk_queue[1] counts the CTAs that are done.  Both are zero before a
+// launch and after it.  Every group's walk is the same code on the same data
+// whichever CTA runs it, so the results do not depend on the order.
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+__global__ void __launch_bounds__(WC_THREADS, wc_min_blocks<MAGGM, REL, BRK, PER, NOPE>())
+walkc_queue_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C,
+                   int nblocks) {
+    __shared__ int s_base;
+    for (;;) {
+        if (threadIdx.x == 0) s_base = (int)atomicAdd(C.walk_queue, (unsigned)C.walk_chunk);
+        __syncthreads();
+        const int base = s_base;
+        __syncthreads();                                   // all have read it before thread 0 takes the next
+        if (base >= nblocks) break;
+        const int end = min(base + C.walk_chunk, nblocks);
+        for (int vb = base; vb < end; vb++) {
+            walkc_body<MAGGM, REL, BRK, PER, NOPE, false>(P, S, T, d_root, ctl, C, vb);
+            __syncthreads();
+        }
+    }
+    // the last CTA out leaves both counters at zero for the next launch (no
+    // other CTA takes blocks any more)
+    if (threadIdx.x == 0 && atomicAdd(C.walk_queue + 1, 1u) + 1u == gridDim.x) {
+        atomicExch(C.walk_queue, 0u);
+        atomicExch(C.walk_queue + 1, 0u);
+    }
+}
+
+// Resident CTAs per SM of the work-queue walk, looked up once per device.
+// The lookup is not a stream operation: walk_queue_setup() makes it outside
+// any graph capture (geon_batch_set_shape calls it).
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+static int& walk_queue_per_sm(int dev) {
+    static int cache[64] = { 0 };
+    return cache[dev >= 0 && dev < 64 ? dev : 0];
+}
+
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+static int walk_queue_prepare() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int& per_sm = walk_queue_per_sm<MAGGM, REL, BRK, PER, NOPE>(dev);
+    if (per_sm <= 0) {
+        constexpr size_t smem = wc_smem_bytes<MAGGM, REL, BRK, PER, NOPE>();
+        cudaFuncSetAttribute(walkc_queue_kernel<MAGGM, REL, BRK, PER, NOPE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        int v = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, walkc_queue_kernel<MAGGM, REL, BRK, PER, NOPE>, WC_THREADS, smem);
+        per_sm = std::max(v, 1);
+    }
+    return per_sm;
+}
+
+void walk_queue_setup() { walk_queue_prepare<false, false, false, 2, true>(); }
+
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+static void launch_walkc_queue(int blocks, const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root,
+                               FrameCtl* ctl, const ForceCtx& C, cudaStream_t st) {
+    constexpr size_t smem = wc_smem_bytes<MAGGM, REL, BRK, PER, NOPE>();
+    const int per_sm = walk_queue_prepare<MAGGM, REL, BRK, PER, NOPE>();
+    const int grid = std::max(1, std::min(blocks, per_sm * device_sms()));
+    walkc_queue_kernel<MAGGM, REL, BRK, PER, NOPE><<<grid, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C, blocks);
+}
+
 template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
 static void launch_walkc_split(int slots, const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root,
                                FrameCtl* ctl, const ForceCtx& C, cudaStream_t st) {
@@ -874,6 +940,10 @@ static void launch_force(bool bh, const DevParams& P, const DevState& S, const T
             if constexpr (PLAIN) {
                 if (lean && C.walk_split && torus) {
                     launch_walkc_split<false, false, false, 2, true>(slots, P, S, T, d_root, ctl, C, st);
+                    return;
+                }
+                if (lean && C.walk_chunk > 0 && C.walk_queue && torus) {
+                    launch_walkc_queue<false, false, false, 2, true>(blocks, P, S, T, d_root, ctl, C, st);
                     return;
                 }
                 if (lean) {

@@ -48,6 +48,11 @@ struct ForceCtx {
     // > 0 caps the resident walk CTAs per SM by padding their shared memory
     int walk_split;
     int walk_ctas;
+    // walk_chunk > 0: the grouped walk runs as persistent CTAs (as many as fit
+    // the GPU at once) that take walk blocks walk_chunk at a time from the
+    // counters walk_queue[2] (zero between launches); plain forces only
+    int walk_chunk;
+    unsigned* walk_queue;
 };
 
 // How the pairwise sum over n_cap targets is split: the number of source
@@ -76,6 +81,11 @@ int heatmap_slices(const DevParams& P, int G, bool useTree);
 
 // clear = false keeps the planner reductions and the interaction counter of
 // earlier passes (a force pass split over target chunks).
+// Prepares the work-queue walk (ForceCtx::walk_chunk) on the current device:
+// its shared-memory limit and resident CTAs per SM, looked up outside any
+// graph capture.
+void walk_queue_setup();
+
 void force_pass(const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root, FrameCtl* ctl,
                 const ForceCtx& C, bool bh, int n_cap, cudaStream_t st, LaunchCounter& lc, bool clear = true);
 

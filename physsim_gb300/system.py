@@ -351,17 +351,19 @@ class BatchSystem(GeonSystem):
     def set_mode(self, use_graph: bool = True, simple_walk: bool = False):
         self._ck(self.lib.geon_batch_set_mode(self._h, int(use_graph), int(simple_walk)))
 
-    def set_shape(self, warps_per_group: int = 1, split_level: int = 6, ctas_per_sm: int = 0):
-        self._ck(self.lib.geon_batch_set_shape(self._h, int(warps_per_group), int(split_level), int(ctas_per_sm)))
+    def set_shape(self, warps_per_group: int = 1, split_level: int = 6, ctas_per_sm: int = 0, queue_chunk: int = 0):
+        self._ck(self.lib.geon_batch_set_shape(self._h, int(warps_per_group), int(split_level), int(ctas_per_sm),
+                                               int(queue_chunk)))
 
     @staticmethod
     def tune_mode(mode: int) -> dict:
-        """Candidate `mode` of autotune: graph, simple walk, warps per group, split level, CTAs per SM."""
-        d = (C.c_int32 * 5)()
+        """Candidate `mode` of autotune: graph, simple walk, warps per group, split level, CTAs per SM,
+        work-queue chunk."""
+        d = (C.c_int32 * 6)()
         lib = N.load()
         N.check(lib, None, lib.geon_batch_tune_mode(int(mode), d))
         return {"use_graph": bool(d[0]), "simple_walk": bool(d[1]), "warps_per_group": int(d[2]),
-                "split_level": int(d[3]), "ctas_per_sm": int(d[4])}
+                "split_level": int(d[3]), "ctas_per_sm": int(d[4]), "queue_chunk": int(d[5])}
 
     def autotune(self, dt: float, frames: int = 2) -> tuple:
         """Times every candidate mode (tune_mode), keeps the fastest; returns

@@ -125,7 +125,7 @@ def test_autotune_restores_state_and_keeps_results(gpu_lib):
     for k in ("x", "y", "wx", "wy"):
         np.testing.assert_array_equal(st0[k], wl.state[k].astype(np.float32).astype(np.float64))
     b.set_mode(use_graph=BatchSystem.tune_mode(choice)["use_graph"], simple_walk=False)
-    b.set_shape(1, 6, 0)
+    b.set_shape(1, 6, 0, 0)
     b.update(wl.dt)
     b.update(wl.dt)
     got = b.state(f64=True)
@@ -146,15 +146,16 @@ def test_batched_rejects_unsupported(gpu_lib):
     b.close()
 
 
-@pytest.mark.parametrize("warps,ctas", [(1, 3), (4, 0)])
-def test_walk_shapes(gpu_lib, warps, ctas):
-    """The walk shapes the autotuner searches: a cap on resident walk CTAs runs
-    the same code (bit-identical frames); four warps per group of targets
-    change only the order of each target's sums (1e-6)."""
+@pytest.mark.parametrize("warps,ctas,chunk", [(1, 3, 0), (4, 0, 0), (1, 0, 1), (1, 0, 4)])
+def test_walk_shapes(gpu_lib, warps, ctas, chunk):
+    """The walk shapes the autotuner searches: a cap on resident walk CTAs and
+    the work-queue form run the same code per group (bit-identical frames);
+    four warps per group of targets change only the order of each target's
+    sums (1e-6)."""
     wl = small_ensemble(seed=46, n=10, lo=64, hi=3000)
     ref = batch_of(wl)
     b = batch_of(wl)
-    b.set_shape(warps, 6, ctas)
+    b.set_shape(warps, 6, ctas, chunk)
     try:
         for _ in range(2):
             assert np.array_equal(ref.update(wl.dt), b.update(wl.dt))
