@@ -414,6 +414,8 @@ def tune_name(m: dict) -> str:
     walk = "simple walk" if m["simple_walk"] else (
         "grouped walk" if m["warps_per_group"] == 1 else f"split walk (4 warps per group, level {m['split_level']})")
     cap = f", <= {m['ctas_per_sm']} CTAs/SM" if m["ctas_per_sm"] else ""
+    if m["ctas_per_sm"] == 7:
+        cap = ", 288-entry stack, 7 CTAs/SM"
     queue = f", work queue of {m['queue_chunk']} blocks" if m.get("queue_chunk") else ""
     return ("graph" if m["use_graph"] else "launches") + ", " + walk + cap + queue
 

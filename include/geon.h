@@ -396,7 +396,8 @@ int geon_batch_set_mode(GeonHandle* h, int32_t use_graph, int32_t simple_walk);
  * 32 targets; default) or 4 (the four warps of a CTA share one group's
  * subtrees below split_level; plain forces in the lean form, otherwise the
  * one-warp walk runs); ctas_per_sm > 0 caps the resident walk CTAs per SM by
- * padding their shared memory (0: as many as fit); queue_chunk > 0 runs the
+ * padding their shared memory (0: as many as fit; 7: the plain torus walk
+ * with a 288-entry stack, which fits seven); queue_chunk > 0 runs the
  * one-warp walk of plain forces on the torus as persistent CTAs taking
  * queue_chunk walk blocks at a time from a counter (0: one CTA per block). */
 int geon_batch_set_shape(GeonHandle* h, int32_t warps_per_group, int32_t split_level, int32_t ctas_per_sm,
@@ -406,7 +407,7 @@ int geon_batch_set_shape(GeonHandle* h, int32_t warps_per_group, int32_t split_l
  * modes (geon_batch_tune_mode), restores the state, and keeps the fastest;
  * `choice` receives its index, ms_per_frame[GEON_BATCH_TUNE_MODES] (may be
  * NULL) the time of each. */
-#define GEON_BATCH_TUNE_MODES 12
+#define GEON_BATCH_TUNE_MODES 13
 int geon_batch_autotune(GeonHandle* h, double dt, int32_t frames, int32_t* choice, double* ms_per_frame);
 
 /* Candidate `mode` of geon_batch_autotune as desc[6] = { use_graph,

@@ -55,7 +55,7 @@ LEARN_OUTPUTS = 6
 LEARN_TARGETS = 18
 DIRECT_NOALLOC_MAX_K = 16384
 BATCH_MAX_SYSTEMS = 512
-BATCH_TUNE_MODES = 12
+BATCH_TUNE_MODES = 13
 
 OUT_ROWS = 25
 OUT_NAMES = ["fx", "fy", "Bz", "Bgz", "dBzdx", "dBzdy", "dBgzdx", "dBgzdy", "tidal", "frameDrag",

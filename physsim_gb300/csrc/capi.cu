@@ -2487,12 +2487,14 @@ int geon_batch_set_shape(GeonHandle* h, int32_t warps_per_group, int32_t split_l
 // level, walk CTAs per SM, work-queue chunk.  0-3 are the graph / launch and
 // grouped / simple modes; 4-6 cap the grouped walk's resident CTAs; 7-9 split
 // each group's walk over four warps at three depths; 10-11 run the grouped
-// walk as persistent CTAs taking 1 or 4 walk blocks at a time.
+// walk as persistent CTAs taking 1 or 4 walk blocks at a time; 12 runs it
+// with the short stack at seven CTAs per SM.
 static const int32_t TUNE_MODES[GEON_BATCH_TUNE_MODES][6] = {
     { 0, 0, 1, 6, 0, 0 }, { 1, 0, 1, 6, 0, 0 }, { 0, 1, 1, 6, 0, 0 }, { 1, 1, 1, 6, 0, 0 },
     { 1, 0, 1, 6, 5, 0 }, { 1, 0, 1, 6, 4, 0 }, { 1, 0, 1, 6, 3, 0 },
     { 1, 0, 4, 4, 0, 0 }, { 1, 0, 4, 6, 0, 0 }, { 1, 0, 4, 8, 0, 0 },
     { 1, 0, 1, 6, 0, 1 }, { 1, 0, 1, 6, 0, 4 },
+    { 1, 0, 1, 6, 7, 0 },
 };
 
 int geon_batch_tune_mode(int32_t mode, int32_t* desc) {

@@ -60,6 +60,23 @@ walkc_split_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ 
     walkc_body<MAGGM, REL, BRK, PER, NOPE, false, WC_WARPS>(P, S, T, d_root, ctl, C, blockIdx.x);
 }
 
+// The short-stack walk (a batched walk shape): a 288-entry stack takes the
+// plain walk's shared memory to 31 KB per CTA and its registers to 72, so
+// seven CTAs fit an SM instead of six.  Only shallow walks gain: at small
+// opening angles the stack runs deep and the walk falls back to single pops.
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+__global__ void __launch_bounds__(WC_THREADS, 7)
+walkc_short_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
+    walkc_body<MAGGM, REL, BRK, PER, NOPE, false, 1, WC_STACK_SHORT>(P, S, T, d_root, ctl, C, blockIdx.x);
+}
+
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+static void launch_walkc_short(int blocks, const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root,
+                               FrameCtl* ctl, const ForceCtx& C, cudaStream_t st) {
+    constexpr size_t smem = wc_smem_bytes<MAGGM, REL, BRK, PER, NOPE, WC_WARPS, WC_STACK_SHORT>();
+    walkc_short_kernel<MAGGM, REL, BRK, PER, NOPE><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+}
+
 // The grouped walk from a work queue: persistent CTAs take walk blocks (four
 // groups of 32 targets each) C.walk_chunk at a time from C.walk_queue[0];
 // C.walk_queue[1] counts the CTAs that are done.  Both are zero before a
@@ -944,6 +961,10 @@ static void launch_force(bool bh, const DevParams& P, const DevState& S, const T
                 }
                 if (lean && C.walk_chunk > 0 && C.walk_queue && torus) {
                     launch_walkc_queue<false, false, false, 2, true>(blocks, P, S, T, d_root, ctl, C, st);
+                    return;
+                }
+                if (lean && C.walk_ctas == 7 && torus) {
+                    launch_walkc_short<false, false, false, 2, true>(blocks, P, S, T, d_root, ctl, C, st);
                     return;
                 }
                 if (lean) {

@@ -723,6 +723,7 @@ walk_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root,
 constexpr int WC_THREADS = 128;
 constexpr int WC_WARPS = WC_THREADS / 32;
 constexpr int WC_STACK = 448;
+constexpr int WC_STACK_SHORT = 288;   // the short-stack plain walk (seven CTAs per SM; a batched walk shape)
 constexpr int WC_RESERVE = 3 * KEY_LEVELS + 3 * 16 + 4;   // growth a depth-first tail can still need
 constexpr int WC_POOL_SHF = 64;    // the walks in shared-memory form (below)
 constexpr int WC_POOL_WIDE = 96;   // the others: fewer, fuller flushes
@@ -733,11 +734,12 @@ static_assert(WC_POOL_SHF >= WC_POP * LEAF_CAP && WC_POOL_SHF >= 32, "source poo
 static_assert(WC_POOL_WIDE >= WC_POOL_SHF && WC_POOL_WIDE <= 255, "pool indices are bytes");
 constexpr uint32_t AGG_REF = 0xffffffffu;
 
-template <bool NEEDC, int POOL>
+template <bool NEEDC, int POOL, int STACK = WC_STACK>
 struct WcSmem {
     static constexpr int kPool = POOL;
-    int stk_node[WC_STACK];
-    unsigned stk_mask[WC_STACK];
+    static constexpr int kStack = STACK;
+    int stk_node[STACK];
+    unsigned stk_mask[STACK];
     float4 a[POOL];                    // x (hi), y (hi), mass, charge
     float4 b[POOL];                    // x (lo), y (lo), vx, vy
     float4 c[NEEDC ? POOL : 1];        // angVel, magMoment, angMomentum, -
@@ -923,7 +925,7 @@ __host__ __device__ constexpr int wc_min_blocks() {
 // sums are then added in warp order by warp 0, which writes the target.
 // The interaction list of every target is the one of the plain walk; only
 // the order of the sums differs.
-template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, bool EMIT, int SPLIT = 1>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, bool EMIT, int SPLIT = 1, int STACK = WC_STACK>
 __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S, const TreeBufs& T,
                                            const int* d_root, FrameCtl* ctl, const ForceCtx& C, int vb) {
     static_assert(SPLIT == 1 || ((SPLIT == WC_WARPS || SPLIT == 2 * WC_WARPS) && !EMIT),
@@ -933,7 +935,7 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
     // shared-memory form (six or four CTAs per SM); its rows hold ACC_SH_THREADS columns
     constexpr bool SHF = NWARPS == WC_WARPS && wc_sh<MAGGM, REL, BRK, PER, NOPE>();
     using AccT = Acc<MAGGM, BRK, SHF>;
-    using WS = WcSmem<NEEDC, SHF ? WC_POOL_SHF : WC_POOL_WIDE>;
+    using WS = WcSmem<NEEDC, SHF ? WC_POOL_SHF : WC_POOL_WIDE, STACK>;
     unsigned char* wc_smem = geon_dsmem + AccT::SH_BYTES;
     WS* Wall = reinterpret_cast<WS*>(wc_smem);
     float* s_age = reinterpret_cast<float*>(Wall + NWARPS);
@@ -979,9 +981,9 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
     __syncwarp();
     while (top > 0) {
         // wide pops while the stack has room; single pops (depth first) near the limit
-        int k = min(min(WC_POP, top), (WC_STACK - WC_RESERVE - top) / 3);
+        int k = min(min(WC_POP, top), (STACK - WC_RESERVE - top) / 3);
         if (k < 1) k = 1;
-        if (top + 3 > WC_STACK) { if (lane == 0) atomicOr(&ctl->err, ERR_STACK_OVERFLOW); break; }
+        if (top + 3 > STACK) { if (lane == 0) atomicOr(&ctl->err, ERR_STACK_OVERFLOW); break; }
         int node = -1;
         unsigned mask = 0;
         if ((int)lane < k) { node = W.stk_node[top - k + lane]; mask = W.stk_mask[top - k + lane]; }
@@ -1194,12 +1196,14 @@ walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root
 // Dynamic shared memory of one walk CTA: accumulator rows (six-CTA form),
 // the four warps' stacks and source pools, and the history tables when
 // relativity is on.
-template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, int NWARPS = WC_WARPS>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, int NWARPS = WC_WARPS, int STACK = WC_STACK>
 constexpr size_t wc_smem_bytes() {
     constexpr bool SHF = NWARPS == WC_WARPS && wc_sh<MAGGM, REL, BRK, PER, NOPE>();
-    return Acc<MAGGM, BRK, SHF>::SH_BYTES + sizeof(WcSmem<MAGGM || REL, SHF ? WC_POOL_SHF : WC_POOL_WIDE>) * NWARPS +
+    return Acc<MAGGM, BRK, SHF>::SH_BYTES + sizeof(WcSmem<MAGGM || REL, SHF ? WC_POOL_SHF : WC_POOL_WIDE, STACK>) * NWARPS +
            (REL ? 2 * HIST_LEN * sizeof(float) : 0);
 }
+static_assert(7 * (wc_smem_bytes<false, false, false, 2, true, WC_WARPS, WC_STACK_SHORT>() + 1024) <= 228 * 1024,
+              "seven short-stack torus plain walk CTAs per SM must fit in shared memory");
 static_assert(6 * (wc_smem_bytes<false, false, false, false, true>() + 1024) <= 228 * 1024,
               "six plain walk CTAs per SM must fit in shared memory");
 static_assert(6 * (wc_smem_bytes<false, false, false, true, true>() + 1024) <= 228 * 1024,

@@ -146,11 +146,12 @@ def test_batched_rejects_unsupported(gpu_lib):
     b.close()
 
 
-@pytest.mark.parametrize("warps,ctas,chunk", [(1, 3, 0), (4, 0, 0), (1, 0, 1), (1, 0, 4)])
+@pytest.mark.parametrize("warps,ctas,chunk", [(1, 3, 0), (4, 0, 0), (1, 0, 1), (1, 0, 4), (1, 7, 0)])
 def test_walk_shapes(gpu_lib, warps, ctas, chunk):
     """The walk shapes the autotuner searches: a cap on resident walk CTAs and
     the work-queue form run the same code per group (bit-identical frames);
-    four warps per group of targets change only the order of each target's
+    four warps per group of targets, and the short stack (which pops fewer
+    nodes at a time near its limit), change only the order of each target's
     sums (1e-6)."""
     wl = small_ensemble(seed=46, n=10, lo=64, hi=3000)
     ref = batch_of(wl)
@@ -164,7 +165,7 @@ def test_walk_shapes(gpu_lib, warps, ctas, chunk):
         ref.close()
         b.close()
     for k in ("x", "y", "wx", "wy"):
-        if warps == 1:
+        if warps == 1 and ctas != 7:
             np.testing.assert_array_equal(sb[k], sr[k])
         else:
             d = np.linalg.norm(sb[k] - sr[k]) / max(np.linalg.norm(sr[k]), 1e-30)
