@@ -287,3 +287,31 @@ def test_planner_cyclotron_limit(oracle_mod, dt, expect):
     p = N.make_params(toggles=N.GRAVITY, softening=1.0, domain_w=1000, domain_h=1000, ext_bz=CYC_BZ)
     o = sim(p, [500.0], [500.0], q=[1.0])
     assert o.update(dt) == expect
+
+
+@pytest.mark.parametrize("order,dropped,level", [("forward", 5, 67), ("reversed", 0, 69)])
+def test_relative_depth_guard_drops_deep_insert(oracle_mod, order, dropped, level):
+    """quadtree.js:207-234: the insert's depth count starts at 0 for every
+    (node, point) pair popped from its work stack, and a point that is still
+    descending after 49 steps is left out of the tree (the loop ends without
+    storing it).  Six points one FP64 ulp apart near (0.001, 0.002), root box
+    [-150, 250]^2: the first five build a chain of divided nodes by the
+    re-insert cascade (each pop descends one or two levels) until level 67
+    separates them (level 69 for the last five, inserted in reverse); the
+    sixth, inserted from the root, is still descending at step 49 and is
+    dropped.  So the leaves hold five points at that level, the root's
+    aggregate mass is 5, and the dropped point is whichever comes last in
+    insertion order."""
+    p = N.make_params(domain_w=100, domain_h=100)
+    xs = [0.001]
+    for _ in range(5):
+        xs.append(float(np.nextafter(xs[-1], 1.0)))
+    idx = list(range(6)) if order == "forward" else list(range(5, -1, -1))
+    o = sim(p, [xs[i] for i in idx], [0.002] * 6)
+    npts, nn = o.build_tree()
+    assert npts == 6 and nn == 1 + 4 * level
+    lop, bx, by, bw, lv = o.leaves(npts)
+    gone = [idx[k] for k in range(6) if lop[k] < 0]
+    assert gone == [dropped]
+    assert set(lv[lop[lop >= 0]]) == {level}
+    assert o.tree_nodes()["mass"][0] == 5.0
