@@ -788,10 +788,16 @@ __device__ __forceinline__ void eval_entry(const DevParams& P, const DevState& S
     float rx, ry, svx = b.z, svy = b.w, sAng = c.x, sMu = c.y, sL = c.z;
     SPos sp{ a.x, b.x, a.y, b.y };
     bool dl = false;
-    if (ref != AGG_REF) {
+    if (!REL) {
+        // self and own ghosts (forces.js:648-649); an aggregate's index field
+        // (REF_INDEX_MASK) lies above every particle index, so the one test
+        // covers points and aggregates alike
+        if ((int)ref_index(ref) == t.idx) return;
+        displacement_p<PER>(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
+    } else if (ref != AGG_REF) {
         const int j = (int)ref_index(ref);
         if (j == t.idx) return;                                       // self and own ghosts (forces.js:648-649)
-        if (REL) {                                                    // forces.js:652-672
+        {                                                             // forces.js:652-672
             Delayed d;
             if (!delayed_state(P, S, C, s_age, s_segdt, j, t, d)) return;
             const uint32_t code = ref_code(ref);
@@ -807,8 +813,6 @@ __device__ __forceinline__ void eval_entry(const DevParams& P, const DevState& S
             sMu = MAG_MOMENT_K * a.w * sAng * rj2;
             sL = INERTIA_K * a.z * sAng * rj2;
             dl = true;
-        } else {
-            displacement_p<PER>(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
         }
     } else {
         displacement_p<PER>(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
