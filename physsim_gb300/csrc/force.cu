@@ -38,43 +38,43 @@ static size_t walk_dyn_smem(size_t smem, const ForceCtx& C) {
     return std::min(std::max(smem, want), WC_SMEM_LIMIT);
 }
 
-template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE = false, bool EMIT = false>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE = false, bool EMIT = false, bool YUK = true>
 static void launch_walkc(int blocks, const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root,
                          FrameCtl* ctl, const ForceCtx& C, cudaStream_t st) {
     constexpr size_t smem = wc_smem_bytes<MAGGM, REL, BRK, PER, NOPE>();
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK, PER, NOPE, EMIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)WC_SMEM_LIMIT);
+        cudaFuncSetAttribute(walkc_kernel<MAGGM, REL, BRK, PER, NOPE, EMIT, YUK>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WC_SMEM_LIMIT);
         attr = true;
     }
-    walkc_kernel<MAGGM, REL, BRK, PER, NOPE, EMIT><<<blocks, WC_THREADS, walk_dyn_smem(smem, C), st>>>(P, S, T, d_root,
-                                                                                                     ctl, C);
+    walkc_kernel<MAGGM, REL, BRK, PER, NOPE, EMIT, YUK><<<blocks, WC_THREADS, walk_dyn_smem(smem, C), st>>>(
+        P, S, T, d_root, ctl, C);
 }
 
 // The split walk: one CTA per group of 32 targets, its four warps sharing the
 // group's subtrees (walkc_body with SPLIT = WC_WARPS).
-template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, bool YUK = true>
 __global__ void __launch_bounds__(WC_THREADS, wc_min_blocks<MAGGM, REL, BRK, PER, NOPE>())
 walkc_split_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
-    walkc_body<MAGGM, REL, BRK, PER, NOPE, false, WC_WARPS>(P, S, T, d_root, ctl, C, blockIdx.x);
+    walkc_body<MAGGM, REL, BRK, PER, NOPE, false, WC_WARPS, WC_STACK, YUK>(P, S, T, d_root, ctl, C, blockIdx.x);
 }
 
 // The short-stack walk (a batched walk shape): a 288-entry stack takes the
 // plain walk's shared memory to 31 KB per CTA and its registers to 72, so
 // seven CTAs fit an SM instead of six.  Only shallow walks gain: at small
 // opening angles the stack runs deep and the walk falls back to single pops.
-template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, bool YUK = true>
 __global__ void __launch_bounds__(WC_THREADS, 7)
 walkc_short_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
-    walkc_body<MAGGM, REL, BRK, PER, NOPE, false, 1, WC_STACK_SHORT>(P, S, T, d_root, ctl, C, blockIdx.x);
+    walkc_body<MAGGM, REL, BRK, PER, NOPE, false, 1, WC_STACK_SHORT, YUK>(P, S, T, d_root, ctl, C, blockIdx.x);
 }
 
-template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, bool YUK = true>
 static void launch_walkc_short(int blocks, const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root,
                                FrameCtl* ctl, const ForceCtx& C, cudaStream_t st) {
     constexpr size_t smem = wc_smem_bytes<MAGGM, REL, BRK, PER, NOPE, WC_WARPS, WC_STACK_SHORT>();
-    walkc_short_kernel<MAGGM, REL, BRK, PER, NOPE><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
+    walkc_short_kernel<MAGGM, REL, BRK, PER, NOPE, YUK><<<blocks, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C);
 }
 
 // The grouped walk from a work queue: persistent CTAs take walk blocks (four
@@ -82,7 +82,7 @@ static void launch_walkc_short(int blocks, const DevParams& P, const DevState& S
 // C.walk_queue[1] counts the CTAs that are done.  Both are zero before a
 // launch and after it.  Every group's walk is the same code on the same data
 // whichever CTA runs it, so the results do not depend on the order.
-template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, bool YUK = true>
 __global__ void __launch_bounds__(WC_THREADS, wc_min_blocks<MAGGM, REL, BRK, PER, NOPE>())
 walkc_queue_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C,
                    int nblocks) {
@@ -95,7 +95,7 @@ walkc_queue_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ 
         if (base >= nblocks) break;
         const int end = min(base + C.walk_chunk, nblocks);
         for (int vb = base; vb < end; vb++) {
-            walkc_body<MAGGM, REL, BRK, PER, NOPE, false>(P, S, T, d_root, ctl, C, vb);
+            walkc_body<MAGGM, REL, BRK, PER, NOPE, false, 1, WC_STACK, YUK>(P, S, T, d_root, ctl, C, vb);
             __syncthreads();
         }
     }
@@ -110,52 +110,67 @@ walkc_queue_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ 
 // Resident CTAs per SM of the work-queue walk, looked up once per device.
 // The lookup is not a stream operation: walk_queue_setup() makes it outside
 // any graph capture (geon_batch_set_shape calls it).
-template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, bool YUK>
 static int& walk_queue_per_sm(int dev) {
     static int cache[64] = { 0 };
     return cache[dev >= 0 && dev < 64 ? dev : 0];
 }
 
-template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, bool YUK>
 static int walk_queue_prepare() {
     int dev = 0;
     cudaGetDevice(&dev);
-    int& per_sm = walk_queue_per_sm<MAGGM, REL, BRK, PER, NOPE>(dev);
+    int& per_sm = walk_queue_per_sm<MAGGM, REL, BRK, PER, NOPE, YUK>(dev);
     if (per_sm <= 0) {
         constexpr size_t smem = wc_smem_bytes<MAGGM, REL, BRK, PER, NOPE>();
-        cudaFuncSetAttribute(walkc_queue_kernel<MAGGM, REL, BRK, PER, NOPE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
+        cudaFuncSetAttribute(walkc_queue_kernel<MAGGM, REL, BRK, PER, NOPE, YUK>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int v = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, walkc_queue_kernel<MAGGM, REL, BRK, PER, NOPE>, WC_THREADS, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, walkc_queue_kernel<MAGGM, REL, BRK, PER, NOPE, YUK>, WC_THREADS,
+                                                      smem);
         per_sm = std::max(v, 1);
     }
     return per_sm;
 }
 
-void walk_queue_setup() { walk_queue_prepare<false, false, false, 2, true>(); }
+void walk_queue_setup() {
+    walk_queue_prepare<false, false, false, 2, true, true>();
+    walk_queue_prepare<false, false, false, 2, true, false>();
+}
 
-template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, bool YUK = true>
 static void launch_walkc_queue(int blocks, const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root,
                                FrameCtl* ctl, const ForceCtx& C, cudaStream_t st) {
     constexpr size_t smem = wc_smem_bytes<MAGGM, REL, BRK, PER, NOPE>();
-    const int per_sm = walk_queue_prepare<MAGGM, REL, BRK, PER, NOPE>();
+    const int per_sm = walk_queue_prepare<MAGGM, REL, BRK, PER, NOPE, YUK>();
     const int grid = std::max(1, std::min(blocks, per_sm * device_sms()));
-    walkc_queue_kernel<MAGGM, REL, BRK, PER, NOPE><<<grid, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C, blocks);
+    walkc_queue_kernel<MAGGM, REL, BRK, PER, NOPE, YUK><<<grid, WC_THREADS, smem, st>>>(P, S, T, d_root, ctl, C, blocks);
 }
 
-template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, bool YUK = true>
 static void launch_walkc_split(int slots, const DevParams& P, const DevState& S, const TreeBufs& T, const int* d_root,
                                FrameCtl* ctl, const ForceCtx& C, cudaStream_t st) {
     constexpr size_t smem = wc_smem_bytes<MAGGM, REL, BRK, PER, NOPE>();
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(walkc_split_kernel<MAGGM, REL, BRK, PER, NOPE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)WC_SMEM_LIMIT);
+        cudaFuncSetAttribute(walkc_split_kernel<MAGGM, REL, BRK, PER, NOPE, YUK>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WC_SMEM_LIMIT);
         attr = true;
     }
     const int blocks = std::max(1, (slots + 31) / 32);
-    walkc_split_kernel<MAGGM, REL, BRK, PER, NOPE><<<blocks, WC_THREADS, walk_dyn_smem(smem, C), st>>>(P, S, T, d_root,
-                                                                                                     ctl, C);
+    walkc_split_kernel<MAGGM, REL, BRK, PER, NOPE, YUK><<<blocks, WC_THREADS, walk_dyn_smem(smem, C), st>>>(
+        P, S, T, d_root, ctl, C);
+}
+
+// The plain torus walk without energy sums in the shape the batch chose:
+// four warps per group, a work queue, the short stack, or one warp per group.
+template <bool YUK>
+static void launch_lean_torus(int slots, int blocks, const DevParams& P, const DevState& S, const TreeBufs& T,
+                              const int* d_root, FrameCtl* ctl, const ForceCtx& C, cudaStream_t st) {
+    if (C.walk_split) launch_walkc_split<false, false, false, 2, true, YUK>(slots, P, S, T, d_root, ctl, C, st);
+    else if (C.walk_chunk > 0 && C.walk_queue) launch_walkc_queue<false, false, false, 2, true, YUK>(blocks, P, S, T, d_root, ctl, C, st);
+    else if (C.walk_ctas == 7) launch_walkc_short<false, false, false, 2, true, YUK>(blocks, P, S, T, d_root, ctl, C, st);
+    else launch_walkc<false, false, false, 2, true, false, YUK>(blocks, P, S, T, d_root, ctl, C, st);
 }
 
 // ---- pairwise O(N^2) sum (forces.js:94-125) -------------------------------------------------
@@ -955,21 +970,14 @@ static void launch_force(bool bh, const DevParams& P, const DevState& S, const T
             // force set with relativity carry the torus wrap alone
             const bool torus = P.topology == GEON_TORUS;
             if constexpr (PLAIN) {
-                if (lean && C.walk_split && torus) {
-                    launch_walkc_split<false, false, false, 2, true>(slots, P, S, T, d_root, ctl, C, st);
-                    return;
-                }
-                if (lean && C.walk_chunk > 0 && C.walk_queue && torus) {
-                    launch_walkc_queue<false, false, false, 2, true>(blocks, P, S, T, d_root, ctl, C, st);
-                    return;
-                }
-                if (lean && C.walk_ctas == 7 && torus) {
-                    launch_walkc_short<false, false, false, 2, true>(blocks, P, S, T, d_root, ctl, C, st);
+                if (lean && torus) {
+                    // without the Yukawa term its cutoff guard and force leave the loop
+                    if (P.yukOn) launch_lean_torus<true>(slots, blocks, P, S, T, d_root, ctl, C, st);
+                    else launch_lean_torus<false>(slots, blocks, P, S, T, d_root, ctl, C, st);
                     return;
                 }
                 if (lean) {
-                    if (torus) launch_walkc<false, false, false, 2, true>(blocks, P, S, T, d_root, ctl, C, st);
-                    else launch_walkc<false, false, false, 1, true>(blocks, P, S, T, d_root, ctl, C, st);
+                    launch_walkc<false, false, false, 1, true>(blocks, P, S, T, d_root, ctl, C, st);
                     return;
                 }
             }

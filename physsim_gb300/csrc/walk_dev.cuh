@@ -776,7 +776,9 @@ __device__ __forceinline__ int warp_max_i(int v) {
     return v;
 }
 
-template <bool MAGGM, bool REL, bool BRK, int PER, class ACC, class WS>
+// YUK false: the Yukawa term is off at compile time (the lean torus walks
+// carry no cutoff guard or Yukawa force code when the term is off).
+template <bool MAGGM, bool REL, bool BRK, int PER, bool YUK, class ACC, class WS>
 __device__ __forceinline__ void eval_entry(const DevParams& P, const DevState& S, const ForceCtx& C,
                                            const float* s_age, const float* s_segdt, const WS& W,
                                            int e, const Tgt& t, ACC& A, unsigned& inter, bool pe) {
@@ -817,12 +819,12 @@ __device__ __forceinline__ void eval_entry(const DevParams& P, const DevState& S
     } else {
         displacement_p<PER>(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
     }
-    const bool yk = yukawa_in<PER>(P, rx, ry, sp, t);
+    const bool yk = YUK && yukawa_in<PER>(P, rx, ry, sp, t);
     pair_force<MAGGM, BRK>(P, t, rx, ry, svx, svy, a.z, a.w, sAng, sMu, sL, dl, yk, pe, A);
     inter++;
 }
 
-template <bool MAGGM, bool REL, bool BRK, int PER, class ACC, class WS>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool YUK, class ACC, class WS>
 __device__ __forceinline__ void flush_pool(const DevParams& P, const DevState& S, const ForceCtx& C,
                                            const float* s_age, const float* s_segdt, WS& W,
                                            int& nfull, int& lcnt, int& npool, const Tgt& t, ACC& A,
@@ -841,7 +843,7 @@ __device__ __forceinline__ void flush_pool(const DevParams& P, const DevState& S
         for (int i = 0; i < total; i++) {
             const int l0 = i - nfull;
             const int e0 = l0 < 0 ? W.full[i] : (l0 < lcnt ? W.lst[l0][lane] : -1);
-            if (e0 >= 0) eval_entry<MAGGM, REL, BRK, PER>(P, S, C, s_age, s_segdt, W, e0, t, A, inter, pe);
+            if (e0 >= 0) eval_entry<MAGGM, REL, BRK, PER, YUK>(P, S, C, s_age, s_segdt, W, e0, t, A, inter, pe);
             if (i & 1) A.tick();
         }
     } else {
@@ -850,8 +852,8 @@ __device__ __forceinline__ void flush_pool(const DevParams& P, const DevState& S
             const int l0 = i - nfull, l1 = i + 1 - nfull;
             const int e0 = l0 < 0 ? W.full[i] : (l0 < lcnt ? W.lst[l0][lane] : -1);
             const int e1 = (i + 1 >= total) ? -1 : (l1 < 0 ? W.full[i + 1] : (l1 < lcnt ? W.lst[l1][lane] : -1));
-            if (e0 >= 0) eval_entry<MAGGM, REL, BRK, PER>(P, S, C, s_age, s_segdt, W, e0, t, A, inter, pe);
-            if (e1 >= 0) eval_entry<MAGGM, REL, BRK, PER>(P, S, C, s_age, s_segdt, W, e1, t, A, inter, pe);
+            if (e0 >= 0) eval_entry<MAGGM, REL, BRK, PER, YUK>(P, S, C, s_age, s_segdt, W, e0, t, A, inter, pe);
+            if (e1 >= 0) eval_entry<MAGGM, REL, BRK, PER, YUK>(P, S, C, s_age, s_segdt, W, e1, t, A, inter, pe);
             A.tick();
         }
     }
@@ -929,7 +931,8 @@ __host__ __device__ constexpr int wc_min_blocks() {
 // sums are then added in warp order by warp 0, which writes the target.
 // The interaction list of every target is the one of the plain walk; only
 // the order of the sums differs.
-template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, bool EMIT, int SPLIT = 1, int STACK = WC_STACK>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE, bool EMIT, int SPLIT = 1, int STACK = WC_STACK,
+          bool YUK = true>
 __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S, const TreeBufs& T,
                                            const int* d_root, FrameCtl* ctl, const ForceCtx& C, int vb) {
     static_assert(SPLIT == 1 || ((SPLIT == WC_WARPS || SPLIT == 2 * WC_WARPS) && !EMIT),
@@ -1083,7 +1086,7 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
         int incl = warp_incl_scan_i(myEnt);
         const int tot = __shfl_sync(0xffffffffu, incl, 31);
         if (npool + tot > WS::kPool)
-            flush_pool<MAGGM, REL, BRK, PER>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
+            flush_pool<MAGGM, REL, BRK, PER, YUK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
         const int e0 = npool + incl - myEnt;
         if (myAcc) {                                                  // forces.js:682-685
             const float4 nb = T.int_b[node];
@@ -1128,7 +1131,7 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
             for (int b0 = 0; b0 < bcount; b0 += 32) {
                 const int chunk = min(32, bcount - b0);
                 if (npool + chunk > WS::kPool)
-                    flush_pool<MAGGM, REL, BRK, PER>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
+                    flush_pool<MAGGM, REL, BRK, PER, YUK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
                 if ((int)lane < chunk) stage_point<NEEDC>(T, W, npool + lane, bstart + b0 + lane);
                 __syncwarp();
                 list_entries<NEEDC>(W, bmask, active, npool, chunk, nfull, lcnt);
@@ -1154,7 +1157,7 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
         top += chTot;
         __syncwarp();
     }
-    flush_pool<MAGGM, REL, BRK, PER>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
+    flush_pool<MAGGM, REL, BRK, PER, YUK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
     if constexpr (SPLIT > 1) {
         // partial sums of warps 1.. through their (now unused) stacks; warp 0 adds them in order
         constexpr int NQ = AccT::NQ;
@@ -1191,10 +1194,10 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
     finalize_target<MAGGM, BRK>(P, S, C, ctl, t, valid, A, inter, sysId);
 }
 
-template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE = false, bool EMIT = false>
+template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE = false, bool EMIT = false, bool YUK = true>
 __global__ void __launch_bounds__(WC_THREADS, wc_min_blocks<MAGGM, REL, BRK, PER, NOPE>())
 walkc_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root, FrameCtl* ctl, ForceCtx C) {
-    walkc_body<MAGGM, REL, BRK, PER, NOPE, EMIT>(P, S, T, d_root, ctl, C, blockIdx.x);
+    walkc_body<MAGGM, REL, BRK, PER, NOPE, EMIT, 1, WC_STACK, YUK>(P, S, T, d_root, ctl, C, blockIdx.x);
 }
 
 // Dynamic shared memory of one walk CTA: accumulator rows (six-CTA form),
