@@ -716,10 +716,11 @@ walk_kernel(DevParams P, DevState S, TreeBufs T, const int* __restrict__ d_root,
 //    it, no per-particle test is needed; only the remaining ("mixed") nodes
 //    get the per-lane test, from shuffled registers, with a ballot;
 //  * accepted aggregates and the points of reached leaves are staged in a
-//    per-warp pool in shared memory.  Entries every particle needs go to a
-//    list evaluated with broadcast reads; entries only some particles need go
-//    to per-lane index lists, evaluated transposed so that no lane idles on
-//    another lane's sources.
+//    per-warp pool in shared memory.  Entries every particle needs fill the
+//    pool from the bottom, in order, and are evaluated by position with
+//    broadcast reads; entries only some particles need fill it from the top
+//    and go to per-lane index lists, evaluated transposed so that no lane
+//    idles on another lane's sources.
 constexpr int WC_THREADS = 128;
 constexpr int WC_WARPS = WC_THREADS / 32;
 constexpr int WC_STACK = 448;
@@ -744,7 +745,6 @@ struct WcSmem {
     float4 b[POOL];                    // x (lo), y (lo), vx, vy
     float4 c[NEEDC ? POOL : 1];        // angVel, magMoment, angMomentum, -
     uint32_t ref[POOL];                // particle ref, AGG_REF for aggregates
-    uint8_t full[POOL];                // pool indices every lane evaluates
     uint8_t lst[POOL][32];             // per-lane lists (column = lane) of partial entries
     // read at each node classification, kept here rather than in registers
     float gbox[4];                     // the warp's target box: centre x, y, half-widths x, y
@@ -827,12 +827,13 @@ __device__ __forceinline__ void eval_entry(const DevParams& P, const DevState& S
 template <bool MAGGM, bool REL, bool BRK, int PER, bool YUK, class ACC, class WS>
 __device__ __forceinline__ void flush_pool(const DevParams& P, const DevState& S, const ForceCtx& C,
                                            const float* s_age, const float* s_segdt, WS& W,
-                                           int& nfull, int& lcnt, int& npool, const Tgt& t, ACC& A,
+                                           int& nfull, int& lcnt, int& npart, const Tgt& t, ACC& A,
                                            unsigned& inter, bool pe) {
     __syncwarp();
     const unsigned lane = threadIdx.x & 31;
     const int total = nfull + warp_max_i(lcnt);
-    // full entries first (broadcast reads), then this lane's own list
+    // full entries first (pool slots 0 .. nfull - 1, broadcast reads), then
+    // this lane's own list
     if (MAGGM) {
         // one entry per iteration: the dipole / 1PN pair force (with the
         // light-cone solve when relativity is on) is large enough that a
@@ -842,7 +843,7 @@ __device__ __forceinline__ void flush_pool(const DevParams& P, const DevState& S
         // faster with two)
         for (int i = 0; i < total; i++) {
             const int l0 = i - nfull;
-            const int e0 = l0 < 0 ? W.full[i] : (l0 < lcnt ? W.lst[l0][lane] : -1);
+            const int e0 = l0 < 0 ? i : (l0 < lcnt ? W.lst[l0][lane] : -1);
             if (e0 >= 0) eval_entry<MAGGM, REL, BRK, PER, YUK>(P, S, C, s_age, s_segdt, W, e0, t, A, inter, pe);
             if (i & 1) A.tick();
         }
@@ -850,15 +851,15 @@ __device__ __forceinline__ void flush_pool(const DevParams& P, const DevState& S
         // two independent entries per iteration for instruction-level parallelism
         for (int i = 0; i < total; i += 2) {
             const int l0 = i - nfull, l1 = i + 1 - nfull;
-            const int e0 = l0 < 0 ? W.full[i] : (l0 < lcnt ? W.lst[l0][lane] : -1);
-            const int e1 = (i + 1 >= total) ? -1 : (l1 < 0 ? W.full[i + 1] : (l1 < lcnt ? W.lst[l1][lane] : -1));
+            const int e0 = l0 < 0 ? i : (l0 < lcnt ? W.lst[l0][lane] : -1);
+            const int e1 = (i + 1 >= total) ? -1 : (l1 < 0 ? i + 1 : (l1 < lcnt ? W.lst[l1][lane] : -1));
             if (e0 >= 0) eval_entry<MAGGM, REL, BRK, PER, YUK>(P, S, C, s_age, s_segdt, W, e0, t, A, inter, pe);
             if (e1 >= 0) eval_entry<MAGGM, REL, BRK, PER, YUK>(P, S, C, s_age, s_segdt, W, e1, t, A, inter, pe);
             A.tick();
         }
     }
     __syncwarp();
-    nfull = 0; lcnt = 0; npool = 0;
+    nfull = 0; lcnt = 0; npart = 0;
 }
 
 template <bool NEEDC, class WS>
@@ -883,16 +884,12 @@ __device__ __forceinline__ bool accept_exact(const DevParams& P, double tx, doub
     return size * size < P.thetaSqD * (dx * dx + dy * dy);
 }
 
-// Adds entries [e0, e0+cnt) with lane mask m to the full list or the per-lane lists.
-template <bool NEEDC, class WS>
-__device__ __forceinline__ void list_entries(WS& W, unsigned m, unsigned active, int e0, int cnt,
-                                             int& nfull, int& lcnt) {
+// Appends the pool slots first .. first + cnt - 1 to the lists of the lanes in m.
+template <class WS>
+__device__ __forceinline__ void list_add(WS& W, unsigned m, int first, int cnt, int& lcnt) {
     const unsigned lane = threadIdx.x & 31;
-    if (m == active) {
-        if ((int)lane < cnt) W.full[nfull + lane] = (uint8_t)(e0 + lane);
-        nfull += cnt;
-    } else if ((m >> lane) & 1u) {
-        for (int q = 0; q < cnt; q++) W.lst[lcnt + q][lane] = (uint8_t)(e0 + q);
+    if ((m >> lane) & 1u) {
+        for (int q = 0; q < cnt; q++) W.lst[lcnt + q][lane] = (uint8_t)(first + q);
         lcnt += cnt;
     }
 }
@@ -902,8 +899,9 @@ __device__ __forceinline__ void list_entries(WS& W, unsigned m, unsigned active,
 // evaluation loop.  EMIT: record the accepted (cell, group) pairs for the
 // learned correction.  The plain walk without energy sums keeps its
 // compensated sums, group box and node counts in shared memory and runs six
-// CTAs per SM (80 registers; the periodic form spills 32 bytes there and is
-// still 2 % faster than at five); the other forms keep them in registers.
+// CTAs per SM (80 registers; the form with the topology chosen at run time
+// spills 32-52 bytes there and was still 2 % faster than at five); the other
+// forms keep them in registers.
 template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
 __host__ __device__ constexpr bool wc_six() { return !MAGGM && !REL && !BRK && NOPE; }
 // The walks with dipole / 1PN terms and without breakdown rows take the same
@@ -978,7 +976,7 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
     const bool treeOk = (ctl->err & (ERR_NODE_OVERFLOW | ERR_BAD_INDEX)) == 0;
     const int nInt0 = ctl->nInternal, nLeaf0 = ctl->nLeaves, nValid0 = ctl->nValid;
     if (SHF && lane == 0) { W.counts[0] = nInt0; W.counts[1] = nLeaf0; W.counts[2] = nValid0; }
-    int top = 0, npool = 0, nfull = 0, lcnt = 0;
+    int top = 0, npart = 0, nfull = 0, lcnt = 0;   // pool: nfull slots from the bottom, npart from the top
     int rcnt = 0;                                                     // EMIT: records of this warp
     const int grp = SPLIT > 1 ? vb : vb * WC_WARPS + warp;
     if (root != ROOT_NONE && treeOk) {
@@ -1082,12 +1080,23 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
         const unsigned leafMask = kind == 1 ? mask : 0u;
         const bool bucket = leafMask && lm.y > LEAF_CAP;
         const int myPts = (leafMask && !bucket) ? lm.y : 0;
+        // a lane holds one node: its entries (an aggregate, or a leaf's
+        // points) are all taken by every lane or all by some.  Entries every
+        // lane takes fill the pool from the bottom, in lane order, and are
+        // evaluated by position; the others fill it from the top, each lane's
+        // block in ascending slots, and then go, source by source, to the
+        // lists of the lanes that take them
+        const bool accFull = myAcc != 0 && myAcc == active;
+        const bool ptsFull = myPts > 0 && leafMask == active;
+        const bool isFull = accFull || ptsFull;
         const int myEnt = (myAcc ? 1 : 0) + myPts;
-        int incl = warp_incl_scan_i(myEnt);
-        const int tot = __shfl_sync(0xffffffffu, incl, 31);
-        if (npool + tot > WS::kPool)
-            flush_pool<MAGGM, REL, BRK, PER, YUK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
-        const int e0 = npool + incl - myEnt;
+        const int myFull = isFull ? myEnt : 0;
+        const int incl = warp_incl_scan_i(myEnt);
+        const int fincl = warp_incl_scan_i(myFull);
+        const int tot = __shfl_sync(0xffffffffu, incl, 31), ftot = __shfl_sync(0xffffffffu, fincl, 31);
+        if (nfull + npart + tot > WS::kPool)
+            flush_pool<MAGGM, REL, BRK, PER, YUK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npart, t, A, inter, pe);
+        const int e0 = isFull ? nfull + fincl - myFull : WS::kPool - (npart + incl - fincl);
         if (myAcc) {                                                  // forces.js:682-685
             const float4 nb = T.int_b[node];
             W.a[e0] = na;
@@ -1095,47 +1104,34 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
             if (NEEDC) W.c[e0] = make_float4(0.f, nb.z, nb.w, 0.f);
             W.ref[e0] = AGG_REF;
         }
-        const int p0 = e0 + (myAcc ? 1 : 0);
-        for (int q = 0; q < myPts; q++) stage_point<NEEDC>(T, W, p0 + q, lm.x + q);   // forces.js:643-679
-        npool += tot;
+        for (int q = 0; q < myPts; q++) stage_point<NEEDC>(T, W, e0 + q, lm.x + q);   // forces.js:643-679
+        nfull += ftot;
+        npart += tot - ftot;
         __syncwarp();
-        // route the new entries: those every particle needs go to the full
-        // list, placed in parallel by a prefix sum; the others go, source by
-        // source, to the per-lane lists of the particles that need them
-        {
-            const bool accFull = myAcc != 0 && myAcc == active;
-            const bool ptsFull = myPts > 0 && leafMask == active;
-            const int myFull = (accFull ? 1 : 0) + (ptsFull ? myPts : 0);
-            const int fincl = warp_incl_scan_i(myFull);
-            int fp = nfull + fincl - myFull;
-            if (accFull) W.full[fp++] = (uint8_t)e0;
-            if (ptsFull)
-                for (int q = 0; q < myPts; q++) W.full[fp++] = (uint8_t)(p0 + q);
-            nfull += __shfl_sync(0xffffffffu, fincl, 31);
-            for (unsigned gm = __ballot_sync(0xffffffffu, myAcc != 0 && !accFull); gm; gm &= gm - 1) {
-                const int jj = __ffs(gm) - 1;
-                list_entries<NEEDC>(W, __shfl_sync(0xffffffffu, myAcc, jj), active, __shfl_sync(0xffffffffu, e0, jj), 1,
-                                    nfull, lcnt);
-            }
-            for (unsigned gm = __ballot_sync(0xffffffffu, myPts > 0 && !ptsFull); gm; gm &= gm - 1) {
-                const int jj = __ffs(gm) - 1;
-                list_entries<NEEDC>(W, __shfl_sync(0xffffffffu, leafMask, jj), active, __shfl_sync(0xffffffffu, p0, jj),
-                                    __shfl_sync(0xffffffffu, myPts, jj), nfull, lcnt);
-            }
+        for (unsigned gm = __ballot_sync(0xffffffffu, myAcc != 0 && !accFull); gm; gm &= gm - 1) {
+            const int jj = __ffs(gm) - 1;
+            list_add(W, __shfl_sync(0xffffffffu, myAcc, jj), __shfl_sync(0xffffffffu, e0, jj), 1, lcnt);
+        }
+        for (unsigned gm = __ballot_sync(0xffffffffu, myPts > 0 && !ptsFull); gm; gm &= gm - 1) {
+            const int jj = __ffs(gm) - 1;
+            list_add(W, __shfl_sync(0xffffffffu, leafMask, jj), __shfl_sync(0xffffffffu, e0, jj),
+                     __shfl_sync(0xffffffffu, myPts, jj), lcnt);
         }
         // leaves holding more than LEAF_CAP points (level-31 buckets)
         for (unsigned bk = __ballot_sync(0xffffffffu, bucket); bk; bk &= bk - 1) {
             const int jj = __ffs(bk) - 1;
             const int bstart = __shfl_sync(0xffffffffu, lm.x, jj), bcount = __shfl_sync(0xffffffffu, lm.y, jj);
             const unsigned bmask = __shfl_sync(0xffffffffu, leafMask, jj);
+            const bool bfull = bmask == active;
             for (int b0 = 0; b0 < bcount; b0 += 32) {
                 const int chunk = min(32, bcount - b0);
-                if (npool + chunk > WS::kPool)
-                    flush_pool<MAGGM, REL, BRK, PER, YUK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
-                if ((int)lane < chunk) stage_point<NEEDC>(T, W, npool + lane, bstart + b0 + lane);
+                if (nfull + npart + chunk > WS::kPool)
+                    flush_pool<MAGGM, REL, BRK, PER, YUK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npart, t, A, inter, pe);
+                const int first = bfull ? nfull : WS::kPool - npart - chunk;
+                if ((int)lane < chunk) stage_point<NEEDC>(T, W, first + lane, bstart + b0 + lane);
                 __syncwarp();
-                list_entries<NEEDC>(W, bmask, active, npool, chunk, nfull, lcnt);
-                npool += chunk;
+                if (bfull) nfull += chunk;
+                else { list_add(W, bmask, first, chunk, lcnt); npart += chunk; }
             }
         }
         // children of nodes some lanes open (forces.js:686-692)
@@ -1157,7 +1153,7 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
         top += chTot;
         __syncwarp();
     }
-    flush_pool<MAGGM, REL, BRK, PER, YUK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npool, t, A, inter, pe);
+    flush_pool<MAGGM, REL, BRK, PER, YUK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npart, t, A, inter, pe);
     if constexpr (SPLIT > 1) {
         // partial sums of warps 1.. through their (now unused) stacks; warp 0 adds them in order
         constexpr int NQ = AccT::NQ;
