@@ -733,6 +733,7 @@ constexpr int WC_POP = 16;
 // aggregate per lane) and a bucket chunk 32 points, each after a flush
 static_assert(WC_POOL_SHF >= WC_POP * LEAF_CAP && WC_POOL_SHF >= 32, "source pool smaller than one step's staging");
 static_assert(WC_POOL_WIDE >= WC_POOL_SHF && WC_POOL_WIDE <= 255, "pool indices are bytes");
+static_assert(WC_POP * LEAF_CAP < 256, "a pop step's entry counts share one prefix sum, 8 bits apiece");
 constexpr uint32_t AGG_REF = 0xffffffffu;
 
 template <bool NEEDC, int POOL, int STACK = WC_STACK>
@@ -790,18 +791,20 @@ __device__ __forceinline__ void eval_entry(const DevParams& P, const DevState& S
     float rx, ry, svx = b.z, svy = b.w, sAng = c.x, sMu = c.y, sL = c.z;
     SPos sp{ a.x, b.x, a.y, b.y };
     bool dl = false;
+    // inter counted this entry when the pool was flushed: an entry that is
+    // not evaluated takes it back
     if (!REL) {
         // self and own ghosts (forces.js:648-649); an aggregate's index field
         // (REF_INDEX_MASK) lies above every particle index, so the one test
         // covers points and aggregates alike
-        if ((int)ref_index(ref) == t.idx) return;
+        if ((int)ref_index(ref) == t.idx) { inter--; return; }
         displacement_p<PER>(P, t.x, t.y, a.x, b.x - t.xlo, a.y, b.y - t.ylo, rx, ry);
     } else if (ref != AGG_REF) {
         const int j = (int)ref_index(ref);
-        if (j == t.idx) return;                                       // self and own ghosts (forces.js:648-649)
+        if (j == t.idx) { inter--; return; }                         // self and own ghosts (forces.js:648-649)
         {                                                             // forces.js:652-672
             Delayed d;
-            if (!delayed_state(P, S, C, s_age, s_segdt, j, t, d)) return;
+            if (!delayed_state(P, S, C, s_age, s_segdt, j, t, d)) { inter--; return; }
             const uint32_t code = ref_code(ref);
             float xj = 0.f, yj = 0.f;
             if (code != CODE_IDENTITY && (code_mx(code) || code_my(code) || P.topology != GEON_TORUS)) {
@@ -821,7 +824,6 @@ __device__ __forceinline__ void eval_entry(const DevParams& P, const DevState& S
     }
     const bool yk = YUK && yukawa_in<PER>(P, rx, ry, sp, t);
     pair_force<MAGGM, BRK>(P, t, rx, ry, svx, svy, a.z, a.w, sAng, sMu, sL, dl, yk, pe, A);
-    inter++;
 }
 
 template <bool MAGGM, bool REL, bool BRK, int PER, bool YUK, class ACC, class WS>
@@ -832,6 +834,7 @@ __device__ __forceinline__ void flush_pool(const DevParams& P, const DevState& S
     __syncwarp();
     const unsigned lane = threadIdx.x & 31;
     const int total = nfull + warp_max_i(lcnt);
+    inter += (unsigned)(nfull + lcnt);                               // the entries this lane evaluates
     // full entries first (pool slots 0 .. nfull - 1, broadcast reads), then
     // this lane's own list
     if (MAGGM) {
@@ -899,9 +902,8 @@ __device__ __forceinline__ void list_add(WS& W, unsigned m, int first, int cnt, 
 // evaluation loop.  EMIT: record the accepted (cell, group) pairs for the
 // learned correction.  The plain walk without energy sums keeps its
 // compensated sums, group box and node counts in shared memory and runs six
-// CTAs per SM (80 registers; the form with the topology chosen at run time
-// spills 32-52 bytes there and was still 2 % faster than at five); the other
-// forms keep them in registers.
+// CTAs per SM (80 registers, no spills); the other forms keep them in
+// registers.
 template <bool MAGGM, bool REL, bool BRK, int PER, bool NOPE>
 __host__ __device__ constexpr bool wc_six() { return !MAGGM && !REL && !BRK && NOPE; }
 // The walks with dipole / 1PN terms and without breakdown rows take the same
@@ -1091,9 +1093,11 @@ __device__ __forceinline__ void walkc_body(const DevParams& P, const DevState& S
         const bool isFull = accFull || ptsFull;
         const int myEnt = (myAcc ? 1 : 0) + myPts;
         const int myFull = isFull ? myEnt : 0;
-        const int incl = warp_incl_scan_i(myEnt);
-        const int fincl = warp_incl_scan_i(myFull);
-        const int tot = __shfl_sync(0xffffffffu, incl, 31), ftot = __shfl_sync(0xffffffffu, fincl, 31);
+        // one prefix sum for both counts, 8 bits apiece (each totals at most 64)
+        const int sc = warp_incl_scan_i(myEnt | (myFull << 8));
+        const int scTot = __shfl_sync(0xffffffffu, sc, 31);
+        const int incl = sc & 0xff, fincl = sc >> 8;
+        const int tot = scTot & 0xff, ftot = scTot >> 8;
         if (nfull + npart + tot > WS::kPool)
             flush_pool<MAGGM, REL, BRK, PER, YUK>(P, S, C, s_age, s_segdt, W, nfull, lcnt, npart, t, A, inter, pe);
         const int e0 = isFull ? nfull + fincl - myFull : WS::kPool - (npart + incl - fincl);
