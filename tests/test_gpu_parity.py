@@ -137,6 +137,59 @@ def test_near_coincident_points_forces(gpu_lib, oracle_mod):
     assert e["norm"] <= FORCE_TOL, e
 
 
+def _cell_aligned(start, n=6, ulp=2.0 ** -25, lo=-150.0, width=400.0):
+    """n consecutive FP32 values from start (spacing ulp) inside one level-31
+    cell of a root box [lo, lo + width]: the first run whose first value sits
+    in the lowest tenth of its cell (n ulps span 0.8 of a cell here)."""
+    cw = width / 2 ** 31
+    x = start
+    for _ in range(64):
+        if ((x - lo) / cw) % 1.0 < 0.1:
+            return x + np.arange(n) * ulp
+        x += ulp
+    raise AssertionError("no aligned run")
+
+
+def test_large_bucket_leaves_forces(gpu_lib, oracle_mod):
+    """Two 6 x 6 lattices of adjacent FP32 positions, each inside one level-31
+    cell (1.86e-7 wide in the 400-wide root box), with 120 points around each
+    within 0.02 and 250 across the box: the GPU tree keeps each lattice in one
+    bucket leaf of 36 points, which a walk stages in chunks of 32 and 4 (the
+    source pool flushing between them when it holds more than 32 entries),
+    reached by every lane of the lattice's own warp and by some lanes of the
+    warps around it.  The reference separates the points at level 33.  The
+    forces on all points agree within the force bar (softening 1 makes the
+    pairs inside a lattice negligible, so the deeper split does not show)."""
+    p = N.make_params(toggles=N.GRAVITY | N.COULOMB | N.BARNES_HUT, domain_w=100, domain_h=100, softening=1.0)
+    rng = np.random.default_rng(21)
+    xs, ys = [], []
+    for x0, y0, cx, cy in ((0.25, 0.3125, 0.25, 0.3125), (0.375, 0.28125, 0.375, 0.28125)):
+        lx, ly = _cell_aligned(x0), _cell_aligned(y0)
+        gx, gy = np.meshgrid(lx, ly)
+        xs.append(gx.ravel()); ys.append(gy.ravel())
+        r = 0.02 * np.sqrt(rng.uniform(0, 1, 120)); a = rng.uniform(0, 2 * np.pi, 120)
+        xs.append(cx + 0.01 + r * np.cos(a)); ys.append(cy + 0.01 + r * np.sin(a))
+    xs.append(rng.uniform(5, 95, 250)); ys.append(rng.uniform(5, 95, 250))
+    xs, ys = (np.asarray(np.concatenate(v), np.float32).astype(np.float64) for v in (xs, ys))
+    n = xs.size
+    z = np.zeros(n)
+    q = np.asarray(rng.integers(-5, 6, n) * 0.1, np.float32).astype(np.float64)
+    m = np.asarray(rng.lognormal(0, 0.5, n), np.float32).astype(np.float64)
+    wl = W.Workload("large_buckets", p, {"x": xs, "y": ys, "wx": z, "wy": z, "mass": m, "charge": q,
+                                         "angw": z}, 1 / 60, 1)
+    g, o = load_both(wl)
+    info = g.build_tree()
+    assert info["n_bucket"] >= 2 and info["max_level"] == 31
+    lop, *_ = g.leaves(info)
+    assert np.bincount(lop[lop >= 0]).max() == 36
+    g.compute_forces()
+    o.compute_forces()
+    fg, fo = g.forces(), o.forces()
+    e = vec_err(fg["fx"], fg["fy"], fo["fx"], fo["fy"])
+    g.close()
+    assert e["norm"] <= FORCE_TOL, e
+
+
 # ---- forces ---------------------------------------------------------------------------
 GC_KEYS = ("tidal", "pe", "grav_x", "coul_x")
 FULL_KEYS = ("Bz", "Bgz", "dBzdx", "dBzdy", "dBgzdx", "dBgzdy", "tidal", "frameDrag", "f1pn_x", "f1pn_y", "pe")
