@@ -160,6 +160,7 @@ struct GeonHandle {
     uint2* recs = nullptr;          // (cell, group) records: rec_cap per group of 32 walk slots
     int* rec_cnt = nullptr;         // [rec_groups] records of each group in the last walk
     unsigned* rec_max = nullptr;    // largest count of the last walk (counters: learn_arena)
+    unsigned* apply_queue = nullptr;  // the correction's group counter (learn_arena)
     unsigned long long* rec_total = nullptr;
     long long rec_total_h = 0;      // records of the last walk
     int rec_cap = 0;
@@ -593,9 +594,11 @@ static int ensure_recs(GeonHandle* h, int cap) {
     if (!h->rec_max) {
         unsigned* m = h->learn_arena.alloc<unsigned>(1);
         unsigned long long* t = h->learn_arena.alloc<unsigned long long>(1);
+        unsigned* q = h->learn_arena.alloc<unsigned>(1);
         if (h->learn_arena.failed) return set_err(h, GEON_ERR_NOMEM, "record counter allocation failed");
         h->rec_max = m;
         h->rec_total = t;
+        h->apply_queue = q;
     }
     if (groups > h->rec_groups) {
         cudaStreamSynchronize(h->st);
@@ -690,7 +693,7 @@ static int learn_correct_records(GeonHandle* h, const float* yext) {
     learn_record_offsets(h->rec_cnt, h->rec_cap, ngroups, 1, h->rec_off, h->rec_off + ngroups, h->rec_scan, h->st, h->lc);
     learn_correct(h->P, h->S, h->T, h->ctl, h->learn_w, h->recs, h->rec_cnt, h->gcen, h->rec_cap, ngroups, h->rec_off,
                   (int)h->rec_total_h, yext, h->rec_exp, h->rec_flags, h->rec_net, h->rec_net + h->rec_exp_cap,
-                  &h->ctl->err, h->st, h->lc);
+                  h->apply_queue, &h->ctl->err, h->st, h->lc);
     return GEON_OK;
 }
 

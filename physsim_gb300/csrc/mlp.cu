@@ -508,16 +508,24 @@ constexpr int LA_WARPS = LA_THREADS / 32;
 // wide groups, near the cutoff) are staged 32 at a time in shared memory
 // (coalesced loads, all in flight together) and read back in order as
 // broadcasts by every lane.  Everything a record needs is in its phase-A
-// output: no tree node is read here.  The summation order is fixed.
+// output: no tree node is read here.  The summation order is fixed.  Warps
+// take groups one at a time from *queue (zero at launch), so a warp that
+// drew groups with many records does not hold up the end of the launch;
+// which warp applies a group does not change its sums.
 __global__ void __launch_bounds__(LA_THREADS)
 learn_apply_kernel(DevParams P, DevState S, TreeBufs T, const FrameCtl* __restrict__ ctl, const uint2* __restrict__ recs,
                    const int* __restrict__ rec_cnt, const float4* __restrict__ gcen, int rec_cap, const int* __restrict__ off,
-                   const float4* __restrict__ expo, const float4* __restrict__ cms, const uint2* __restrict__ flags) {
+                   const float4* __restrict__ expo, const float4* __restrict__ cms, const uint2* __restrict__ flags,
+                   unsigned* __restrict__ queue) {
     __shared__ float4 st[LA_WARPS][32][5];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int n = ctl->n;
     const int ngroups = (n + 31) / 32;
-    for (int g = blockIdx.x * LA_WARPS + w; g < ngroups; g += gridDim.x * LA_WARPS) {
+    for (;;) {
+        int g = 0;
+        if (lane == 0) g = (int)atomicAdd(queue, 1u);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= ngroups) break;
         const int k = g * 32 + lane;
         int ti = k < n ? T.tgt[k] : -1;
         if (ti >= n) ti = -1;
@@ -850,8 +858,8 @@ void mlp_forward(const float* W, const float* X, int n, float* Y, int* err, cuda
 
 void learn_correct(const DevParams& P, const DevState& S, const TreeBufs& T, const FrameCtl* ctl, const float* W,
                    const uint2* recs, const int* rec_cnt, const float4* gcen, int rec_cap, int ngroups, const int* off,
-                   int total, const float* yext, float4* expo, uint2* flags, int* net_list, int* net_count, int* err,
-                   cudaStream_t st, LaunchCounter& lc) {
+                   int total, const float* yext, float4* expo, uint2* flags, int* net_list, int* net_count,
+                   unsigned* group_queue, int* err, cudaStream_t st, LaunchCounter& lc) {
     static bool a0 = false, a1 = false;
     allow_smem(learn_net_kernel<false>, NET_SMEM, a0);
     allow_smem(learn_net_kernel<true>, NET_SMEM, a1);
@@ -871,8 +879,9 @@ void learn_correct(const DevParams& P, const DevState& S, const TreeBufs& T, con
         lc.add(2);
     }
     const int blocks = std::max(1, std::min((ngroups + LA_WARPS - 1) / LA_WARPS, sm_count() * 8));
+    cudaMemsetAsync(group_queue, 0, sizeof(unsigned), st);
     learn_apply_kernel<<<blocks, LA_THREADS, 0, st>>>(P, S, T, ctl, recs, rec_cnt, gcen, rec_cap, off, expo,
-                                                      expo + (size_t)EXP_F4 * std::max(total, 0), flags);
+                                                      expo + (size_t)EXP_F4 * std::max(total, 0), flags, group_queue);
     lc.add(1);
 }
 

@@ -19,13 +19,13 @@ void mlp_forward(const float* W, const float* X, int n, float* Y, int* err, cuda
 // rec_cnt, gcen, rec_cap; learn.cuh) to S.force of the ngroups groups'
 // targets.  off[ngroups] is the exclusive prefix of the groups' counts and
 // total their sum; expo (total x 16 floats), flags (total), net_list
-// (total) and net_count (1) are scratch.  With yext the network is not run:
-// a record e (in group order) it applies to takes its outputs from
-// yext[e * 6 ...] instead.
+// (total), net_count (1) and group_queue (1) are scratch.  With yext the
+// network is not run: a record e (in group order) it applies to takes its
+// outputs from yext[e * 6 ...] instead.
 void learn_correct(const DevParams& P, const DevState& S, const TreeBufs& T, const FrameCtl* ctl, const float* W,
                    const uint2* recs, const int* rec_cnt, const float4* gcen, int rec_cap, int ngroups, const int* off,
-                   int total, const float* yext, float4* expo, uint2* flags, int* net_list, int* net_count, int* err,
-                   cudaStream_t st, LaunchCounter& lc);
+                   int total, const float* yext, float4* expo, uint2* flags, int* net_list, int* net_count,
+                   unsigned* group_queue, int* err, cudaStream_t st, LaunchCounter& lc);
 
 // Accumulates into `grad` (MLP_NPARAM floats, zeroed by the caller) the
 // gradient of  L = (1/B) sum_s wt_s sum_c (y_sc - y*_sc)^T A_sc (y_sc - y*_sc)
