@@ -372,10 +372,15 @@ __global__ void __launch_bounds__(LG_THREADS)
 learn_geo_kernel(DevParams P, TreeBufs T, const uint2* __restrict__ recs, const int* __restrict__ rec_cnt,
                  const float4* __restrict__ gcen, int rec_cap, const int* __restrict__ off, int ngroups,
                  float4* __restrict__ expo, float4* __restrict__ cms, uint2* __restrict__ flags, int* __restrict__ net_list,
-                 int* __restrict__ net_count) {
+                 int* __restrict__ net_count, unsigned* __restrict__ queue) {
     const int lane = threadIdx.x & 31;
-    // one warp per group: its records r = lane, lane + 32, ...
-    for (int g = blockIdx.x * LG_WARPS + (threadIdx.x >> 5); g < ngroups; g += gridDim.x * LG_WARPS) {
+    // one warp per group, taken from *queue (zero at launch): its records
+    // r = lane, lane + 32, ...; every record's outputs go to its own slots
+    for (;;) {
+        int g = 0;
+        if (lane == 0) g = (int)atomicAdd(queue, 1u);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= ngroups) break;
         const int cnt = min(rec_cnt[g], rec_cap);
         const int base = off[g];
         const float4 gc = gcen[g];
@@ -867,8 +872,10 @@ void learn_correct(const DevParams& P, const DevState& S, const TreeBufs& T, con
     if (total > 0) {
         cudaMemsetAsync(net_count, 0, sizeof(int), st);
         const int gblocks = std::max(1, std::min((ngroups + LG_WARPS - 1) / LG_WARPS, sm_count() * 8));
+        cudaMemsetAsync(group_queue, 0, sizeof(unsigned), st);
         learn_geo_kernel<<<gblocks, LG_THREADS, 0, st>>>(P, T, recs, rec_cnt, gcen, rec_cap, off, ngroups, expo,
-                                                         expo + (size_t)EXP_F4 * total, flags, net_list, net_count);
+                                                         expo + (size_t)EXP_F4 * total, flags, net_list, net_count,
+                                                         group_queue);
         // the network's CTAs: enough for every listed record (the count is read on the device)
         const int tiles = (total + MT - 1) / MT;
         const int blocks = std::max(1, std::min(tiles, sm_count() * 6));
