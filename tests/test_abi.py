@@ -61,3 +61,25 @@ def test_create_rejects_bad_arguments(gpu_lib):
     p = N.make_params(toggles=N.GRAVITY | N.HIGGS)
     assert gpu_lib.geon_create(ctypes.byref(p), 16, ctypes.byref(h)) == N.GEON_ERR_UNSUPPORTED
     assert b"Higgs" in gpu_lib.geon_last_error(None)
+
+
+def test_batch_tune_modes_table(gpu_lib):
+    """The autotuner's candidates (a host table, no device work): the header's
+    count, every shape geon_batch_set_shape accepts, the short-stack walk at
+    seven CTAs per SM among them, and GEON_ERR_ARG past the end."""
+    from physsim_gb300 import _native as N
+    from physsim_gb300.system import BatchSystem
+    text = HEADER.read_text()
+    assert int(re.search(r"#define GEON_BATCH_TUNE_MODES (\d+)", text).group(1)) == N.BATCH_TUNE_MODES == 13
+    modes = [BatchSystem.tune_mode(m) for m in range(N.BATCH_TUNE_MODES)]
+    for d in modes:
+        assert d["use_graph"] in (0, 1) and d["simple_walk"] in (0, 1)
+        assert d["warps_per_group"] in (1, 4) and d["ctas_per_sm"] in (0, 3, 4, 5, 7)
+        assert d["queue_chunk"] in (0, 1, 4)
+        # one shape at a time: split walk, CTA cap, or work queue
+        assert sum([d["warps_per_group"] > 1, d["ctas_per_sm"] > 0, d["queue_chunk"] > 0]) <= 1
+    assert any(d["ctas_per_sm"] == 7 for d in modes)
+    assert len({tuple(sorted(d.items())) for d in modes}) == len(modes)
+    desc = (ctypes.c_int32 * 6)()
+    assert gpu_lib.geon_batch_tune_mode(N.BATCH_TUNE_MODES, desc) == N.GEON_ERR_ARG
+    assert gpu_lib.geon_batch_tune_mode(-1, desc) == N.GEON_ERR_ARG
