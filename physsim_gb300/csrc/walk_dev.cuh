@@ -455,7 +455,8 @@ template <bool MAGGM, bool BRK, class ACC>
 __device__ __forceinline__ void finalize_target(const DevParams& P, const DevState& S, const ForceCtx& C,
                                                 FrameCtl* ctl, const Tgt& t, bool valid, ACC& A,
                                                 unsigned inter32, int sysId = -1) {
-    unsigned long long inter = inter32;
+    // padding lanes evaluate the warp's shared entries too: only real targets count
+    unsigned long long inter = valid ? inter32 : 0ull;
     A.flush();
     double aSq = 0.0, wc = 0.0;
     if (valid) {

@@ -190,6 +190,28 @@ def test_large_bucket_leaves_forces(gpu_lib, oracle_mod):
     assert e["norm"] <= FORCE_TOL, e
 
 
+@pytest.mark.parametrize("theta", [0.4999999, 0.5, 0.5000001])
+def test_opening_test_tie(gpu_lib, oracle_mod, theta):
+    """The exact tie of the opening test (size^2 = theta^2 d^2 at theta 0.5,
+    test_oracle_kat.TIE_X): the FP32 test falls in its guard band and the
+    FP64 re-test opens the node, as the reference's strict comparison does;
+    the interaction counts and forces match the oracle at, below and above
+    the tie."""
+    from tests.test_oracle_kat import TIE_X, TIE_Y, TIE_M
+    p = N.make_params(toggles=N.GRAVITY | N.BARNES_HUT, domain_w=100, domain_h=100, theta=theta)
+    z = np.zeros(6)
+    wl = W.Workload("opening_tie", p, {"x": np.array(TIE_X), "y": np.array(TIE_Y), "wx": z, "wy": z,
+                                       "mass": np.array(TIE_M), "charge": z, "angw": z}, 1 / 60, 1)
+    g, o = load_both(wl)
+    g.compute_forces()
+    o.compute_forces()
+    assert g.interactions() == o.interactions() == (26 if theta > 0.5 else 30)
+    fg, fo = g.forces(), o.forces()
+    e = vec_err(fg["fx"], fg["fy"], fo["fx"], fo["fy"])
+    g.close()
+    assert e["norm"] <= FORCE_TOL, e
+
+
 # ---- forces ---------------------------------------------------------------------------
 GC_KEYS = ("tidal", "pe", "grav_x", "coul_x")
 FULL_KEYS = ("Bz", "Bgz", "dBzdx", "dBzdy", "dBgzdx", "dBgzdy", "tidal", "frameDrag", "f1pn_x", "f1pn_y", "pe")

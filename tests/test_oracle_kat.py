@@ -315,3 +315,24 @@ def test_relative_depth_guard_drops_deep_insert(oracle_mod, order, dropped, leve
     assert gone == [dropped]
     assert set(lv[lop[lop >= 0]]) == {level}
     assert o.tree_nodes()["mass"][0] == 5.0
+
+
+# An exact tie of the opening test (forces.js:680, size^2 < theta^2 d^2, strict):
+# a cluster of total mass 8 centred at (6.25, 6.25), the centre of the
+# level-5 cell [0, 12.5]^2 of the root box [-150, 250]^2 (size 12.5), and a
+# target 25 away on the x axis, so at theta 0.5 both sides are 156.25.
+TIE_X = [5.25, 7.25, 5.25, 7.25, 6.25, 31.25]
+TIE_Y = [5.25, 5.25, 7.25, 7.25, 6.25, 6.25]
+TIE_M = [1.0, 1.0, 1.0, 1.0, 4.0, 1.0]
+
+
+@pytest.mark.parametrize("theta,inter", [(0.4999999, 30), (0.5, 30), (0.5000001, 26)])
+def test_opening_test_tie_opens(oracle_mod, theta, inter):
+    """At the tie the node is opened: the target takes the cluster's five
+    points from four level-6 leaves instead of one aggregate (4 more
+    interactions); just above the tie it takes the aggregate.  Every other
+    decision of the six walks is far from a tie."""
+    p = N.make_params(toggles=N.GRAVITY | N.BARNES_HUT, domain_w=100, domain_h=100, theta=theta)
+    o = sim(p, TIE_X, TIE_Y, m=np.array(TIE_M))
+    o.compute_forces()
+    assert o.interactions() == inter
