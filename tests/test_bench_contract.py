@@ -24,3 +24,15 @@ def test_reference_arm_prints_one_contract_line(oracle_mod):
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_tuner_table_names_are_distinct(gpu_lib):
+    """Every autotuner candidate gets its own name in the bench line (a host
+    lookup in the library; no device work)."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    from physsim_gb300 import _native as N
+    from physsim_gb300.system import BatchSystem
+    names = [bench.tune_name(BatchSystem.tune_mode(m)) for m in range(N.BATCH_TUNE_MODES)]
+    assert len(set(names)) == len(names), names
+    assert "graph, grouped walk, 288-entry stack, 7 CTAs/SM" in names
